@@ -1,0 +1,157 @@
+/*
+ * pgx -- GB300-native batch evaluation for pagmo (C ABI).
+ *
+ * This is the drop-in boundary of the library: plain C types only (pointers,
+ * sizes, status codes), no CUDA or C++ types in any signature, so that the
+ * pagmo adaptor headers (include/pagmo_gb300/), a ctypes/cffi binding or a
+ * pybind11 module of pygmo can bind it directly.
+ *
+ * Each entry point names the reference interface it replaces, as a path in
+ * the pagmo 2.19.1 source tree.
+ *
+ * Conventions
+ *  - Decision vectors are row-major: n_dvs rows of nx doubles, exactly the
+ *    layout pagmo::bfe receives (src/problem.cpp:383-392). Fitness vectors are
+ *    n_dvs doubles (all three problems are single-objective, nf = 1).
+ *    Gradients are dense, n_dvs rows of nx doubles: for nf = 1 this is the
+ *    layout of problem::gradient (src/problem.cpp:456-467, dense sparsity).
+ *  - Problems: PGX_RASTRIGIN (param = dim >= 1), PGX_ROSENBROCK (param =
+ *    dim >= 2), PGX_LENNARD_JONES (param = atoms >= 3, nx = 3*atoms - 6).
+ *  - Every function returns PGX_OK (0) or an error status; the message of the
+ *    calling thread's last error is pgx_last_error(). PGX_ERR_INVALID maps to
+ *    pagmo's std::invalid_argument. There is no CPU fallback: without a usable
+ *    GB300 every compute entry point fails with PGX_ERR_CUDA/PGX_ERR_NODEVICE.
+ *  - Host-buffer entry points are synchronous. *_device entry points take
+ *    device pointers and a cudaStream_t passed as void* (NULL = the context's
+ *    own stream) and are asynchronous on that stream.
+ *  - A context is bound to one device. Calls on one context are serialised
+ *    by an internal lock, so island threads may share it.
+ */
+#ifndef PGX_H
+#define PGX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGX_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define PGX_API __attribute__((visibility("default")))
+#else
+#define PGX_API
+#endif
+
+/* status codes */
+#define PGX_OK 0
+#define PGX_ERR_INVALID 1  /* bad argument (pagmo: std::invalid_argument) */
+#define PGX_ERR_CUDA 2     /* a CUDA runtime call failed */
+#define PGX_ERR_TIMEOUT 3  /* a bounded device-side wait gave up */
+#define PGX_ERR_CAPACITY 4 /* a size exceeds a fixed capacity */
+#define PGX_ERR_NODEVICE 5 /* no CUDA device could be opened */
+
+/* problem kinds (the reference UDPs) */
+#define PGX_RASTRIGIN 1     /* src/problems/rastrigin.cpp */
+#define PGX_ROSENBROCK 2    /* src/problems/rosenbrock.cpp */
+#define PGX_LENNARD_JONES 3 /* src/problems/lennard_jones.cpp */
+
+typedef struct pgx_context pgx_context;
+typedef struct pgx_epoch pgx_epoch;
+
+/* ------------------------------------------------------------------ runtime */
+
+/* ABI version of the loaded library (PGX_ABI_VERSION at build time). */
+PGX_API int pgx_abi_version(void);
+
+/* Message of the calling thread's most recent failing call ("" if none). */
+PGX_API const char *pgx_last_error(void);
+
+/* Opens a context on CUDA device `device`: a non-blocking stream, grow-only
+   device and pinned staging buffers, cached graphs. */
+PGX_API int pgx_context_create(int device, pgx_context **out);
+PGX_API void pgx_context_destroy(pgx_context *ctx);
+
+/* Number of kernels this library launched on `ctx` since creation (for the
+   benchmark's launch accounting). */
+PGX_API uint64_t pgx_context_launch_count(const pgx_context *ctx);
+
+/* ------------------------------------------------------------ problem facts */
+
+/* Decision-vector size for (kind, param): rastrigin::get_bounds
+   (src/problems/rastrigin.cpp:80-85), rosenbrock (:72-75), lennard_jones
+   (src/problems/lennard_jones.cpp:99-113); validates param as the UDP
+   constructors do (rastrigin.cpp:46-52, rosenbrock.cpp:43-49,
+   lennard_jones.cpp:51-63). */
+PGX_API int pgx_problem_nx(int kind, uint64_t param, uint64_t *nx);
+
+/* Box bounds, nx doubles each (same sources as above). */
+PGX_API int pgx_problem_bounds(int kind, uint64_t param, double *lb, double *ub);
+
+/* --------------------------------------------------------- batch evaluation */
+
+/* Batch fitness, host buffers. Replaces the fitness loop that
+   bfe{thread_bfe{}} / member_bfe run for one problem
+   (src/batch_evaluators/thread_bfe.cpp:64-144, member_bfe.cpp:40-45,
+   src/problem.cpp:413-425) with one GPU pass. dvs: n_dvs*nx, fvs: n_dvs.
+   Does not touch any fevals counter (pagmo::bfe adds n_dvs itself,
+   src/bfe.cpp:106-107). */
+PGX_API int pgx_batch_fitness(pgx_context *ctx, int kind, uint64_t param, const double *dvs, uint64_t n_dvs, double *fvs);
+
+/* Batch fitness + gradient, host buffers: fvs (nullable) n_dvs, grads
+   n_dvs*nx. Row i of grads equals problem::gradient(dv_i) of the reference
+   (src/problems/rastrigin.cpp:98-107, src/problems/rosenbrock.cpp:83-92);
+   for lennard_jones, which has no reference gradient, it is dE/dx over the
+   3*atoms-6 free coordinates (minus the forces), with the pair loop
+   recomputed. */
+PGX_API int pgx_batch_gradient(pgx_context *ctx, int kind, uint64_t param, const double *dvs, uint64_t n_dvs, double *fvs,
+                       double *grads);
+
+/* Device-resident variant of both calls: d_grads NULL = fitness only,
+   d_fvs may be NULL when d_grads is not. Asynchronous on `stream`. */
+PGX_API int pgx_batch_eval_device(pgx_context *ctx, int kind, uint64_t param, const double *d_dvs, uint64_t n_dvs,
+                          double *d_fvs, double *d_grads, void *stream);
+
+/* --------------------------------------------------- NSGA-II survival (MO) */
+
+/* fast_non_dominated_sorting (src/utils/multi_objective.cpp:200-257) over n
+   points of m objectives, row-major host buffer. Outputs (host):
+     rank[n], dom_count[n]                    -- bit-exact with the reference
+     front_offsets[n+1], front_indices[n]     -- fronts in the reference's order
+     *n_fronts
+   Errors as the reference: n < 2 -> PGX_ERR_INVALID. m may be 0. */
+PGX_API int pgx_fnds(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, int32_t *rank, int32_t *dom_count,
+             int32_t *front_offsets, int32_t *front_indices, int32_t *n_fronts);
+
+/* The dom_list member of fnds_return_type, flattened: dl_offsets[n+1] and
+   dl_indices[capacity] (each list ascending, as the reference builds it).
+   Returns PGX_ERR_CAPACITY and the needed size in *dl_total when capacity
+   is too small (dl_indices may then be NULL). */
+PGX_API int pgx_fnds_dom_list(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, int64_t *dl_offsets,
+                      int32_t *dl_indices, uint64_t capacity, uint64_t *dl_total);
+
+/* crowding_distance of one non-dominated front (src/utils/multi_objective.cpp:280-315).
+   n >= 2 and m >= 2 or PGX_ERR_INVALID. Ties between equal objective values
+   are broken by position in the input (the reference's std::sort leaves tie
+   order unspecified); untied points are bit-exact with the reference. */
+PGX_API int pgx_crowding_distance(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, double *out);
+
+/* NSGA-II survival block (src/algorithms/nsga2.cpp:183-206): fnds, then the
+   crowding distance of every point within its front (fronts of one or two
+   points get +inf). crowding[n]; the fnds outputs as in pgx_fnds. */
+PGX_API int pgx_nsga2_survival(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, int32_t *rank,
+                       int32_t *dom_count, int32_t *front_offsets, int32_t *front_indices, int32_t *n_fronts,
+                       double *crowding);
+
+/* Device-resident survival: all pointers are device memory; d_n_fronts is a
+   device int32. Asynchronous on `stream`. */
+PGX_API int pgx_nsga2_survival_device(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, int32_t *d_rank,
+                              int32_t *d_dom_count, int32_t *d_front_offsets, int32_t *d_front_indices,
+                              int32_t *d_n_fronts, double *d_crowding, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,250 @@
+"""CPU oracle for the batch-evaluation path -- TEST INFRASTRUCTURE ONLY.
+
+Loads oracle/_ref/liboracle.so (the C++ restatement in oracle.cpp) and, when
+it has been built from the reference sources in this container,
+oracle/_ref/libpagmo_ref.so (the unmodified reference compiled by
+oracle/Makefile). Only tests/, __graft_entry__.smoke() and the CPU leg of
+bench.py use this module, as the checker; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_ref"
+ORACLE_SO = OUT / "liboracle.so"
+REF_SO = OUT / "libpagmo_ref.so"
+REF_ROOT = Path(os.environ.get("PGX_REFERENCE_ROOT", "/root/reference"))
+
+_vp, _u64 = C.c_void_p, C.c_uint64
+
+
+def build(reference: bool | None = None) -> None:
+    """Compile the oracle (always) and the reference library (when its sources exist)."""
+    r = subprocess.run(["make", "-s", "-C", str(HERE), "oracle"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    if reference is None:
+        reference = (REF_ROOT / "src" / "problem.cpp").exists()
+    if reference:
+        r = subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "ref", f"REF_ROOT={REF_ROOT}"],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference build failed:\n{r.stdout}\n{r.stderr}")
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class _Oracle:
+    def __init__(self, path: Path):
+        self.h = C.CDLL(str(path))
+        h = self.h
+        for name in ("orc_rastrigin_fitness", "orc_rosenbrock_fitness"):
+            getattr(h, name).restype = C.c_double
+            getattr(h, name).argtypes = [_vp, _u64]
+        h.orc_lj_fitness.restype = C.c_double
+        h.orc_lj_fitness.argtypes = [_vp, _u64]
+        for name in ("orc_rastrigin_fitness_ld", "orc_rosenbrock_fitness_ld", "orc_lj_fitness_ld"):
+            getattr(h, name).restype = C.c_double
+            getattr(h, name).argtypes = [_vp, _u64, _vp]
+        h.orc_last_error.restype = C.c_char_p
+        for name in ("orc_batch_fitness", "orc_batch_gradient"):
+            getattr(h, name).argtypes = [C.c_int, _u64, _vp, _u64, _u64, _vp, C.c_int]
+        for name in ("orc_batch_fitness_ld", "orc_batch_gradient_ld"):
+            getattr(h, name).argtypes = [C.c_int, _u64, _vp, _u64, _u64, _vp, _vp, C.c_int]
+        h.orc_pareto_dominance.argtypes = [_vp, _vp, _u64]
+        h.orc_fnds.argtypes = [_vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u64]
+        h.orc_crowding.argtypes = [_vp, _u64, _u64, _vp]
+        h.orc_nsga2_crowding.argtypes = [_vp, _u64, _u64, _vp, _vp, _u64, _vp]
+
+    def _chk(self, st):
+        if st != 0:
+            raise ValueError(self.h.orc_last_error().decode())
+
+    # batch evaluation -------------------------------------------------------
+    def batch_fitness(self, kind, param, dvs, threads=0):
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        n, nx = x.shape
+        f = np.empty(n)
+        self._chk(self.h.orc_batch_fitness(kind, param, _p(x), n, nx, _p(f), threads))
+        return f
+
+    def batch_gradient(self, kind, param, dvs, threads=0):
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        n, nx = x.shape
+        g = np.empty((n, nx))
+        self._chk(self.h.orc_batch_gradient(kind, param, _p(x), n, nx, _p(g), threads))
+        return g
+
+    def batch_fitness_ld(self, kind, param, dvs, threads=0):
+        """(value, condition scale) per row, long double."""
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        n, nx = x.shape
+        f = np.empty(n)
+        s = np.empty(n)
+        self._chk(self.h.orc_batch_fitness_ld(kind, param, _p(x), n, nx, _p(f), _p(s), threads))
+        return f, s
+
+    def batch_gradient_ld(self, kind, param, dvs, threads=0):
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        n, nx = x.shape
+        g = np.empty((n, nx))
+        s = np.empty((n, nx))
+        self._chk(self.h.orc_batch_gradient_ld(kind, param, _p(x), n, nx, _p(g), _p(s), threads))
+        return g, s
+
+    # multi-objective ---------------------------------------------------------
+    def pareto_dominance(self, a, b):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        return bool(self.h.orc_pareto_dominance(_p(a), _p(b), a.size))
+
+    def fnds(self, pts, dom_list=True):
+        p = np.ascontiguousarray(pts, dtype=np.float64)
+        n, m = p.shape
+        rank = np.empty(n, np.uint64)
+        dc = np.empty(n, np.uint64)
+        off = np.empty(n + 1, np.uint64)
+        idx = np.empty(n, np.uint64)
+        nf = C.c_uint64()
+        cap = n * (n - 1) // 2 if dom_list else 0
+        dlo = np.empty(n + 1, np.uint64) if dom_list else None
+        dli = np.empty(max(cap, 1), np.uint64) if dom_list else None
+        self._chk(self.h.orc_fnds(_p(p), n, m, _p(rank), _p(dc), _p(off), _p(idx), C.addressof(nf), _p(dlo),
+                                  _p(dli), cap))
+        k = nf.value
+        out = {"rank": rank.astype(np.int64), "dom_count": dc.astype(np.int64),
+               "front_offsets": off[:k + 1].astype(np.int64), "front_indices": idx.astype(np.int64)}
+        if dom_list:
+            out["dl_offsets"] = dlo.astype(np.int64)
+            out["dl_indices"] = dli[:int(dlo[n])].astype(np.int64)
+        return out
+
+    def crowding(self, pts):
+        p = np.ascontiguousarray(pts, dtype=np.float64)
+        n, m = p.shape
+        out = np.empty(n)
+        self._chk(self.h.orc_crowding(_p(p), n, m, _p(out)))
+        return out
+
+    def nsga2_crowding(self, pts, front_offsets, front_indices):
+        p = np.ascontiguousarray(pts, dtype=np.float64)
+        n, m = p.shape
+        off = np.ascontiguousarray(front_offsets, dtype=np.uint64)
+        idx = np.ascontiguousarray(front_indices, dtype=np.uint64)
+        out = np.empty(n)
+        self._chk(self.h.orc_nsga2_crowding(_p(p), n, m, _p(off), _p(idx), off.size - 1, _p(out)))
+        return out
+
+
+class _Reference:
+    """The reference's own compiled sources (only where they were built)."""
+
+    def __init__(self, path: Path):
+        self.h = C.CDLL(str(path))
+        h = self.h
+        h.ref_last_error.restype = C.c_char_p
+        h.ref_thread_bfe.argtypes = [C.c_int, _u64, _vp, _u64, _u64, _vp, _vp]
+        h.ref_fitness_rows.argtypes = [C.c_int, _u64, _vp, _u64, _u64, _vp]
+        h.ref_gradient_rows.argtypes = [C.c_int, _u64, _vp, _u64, _u64, _vp]
+        h.ref_bounds.argtypes = [C.c_int, _u64, _vp, _vp]
+        h.ref_fnds.argtypes = [_vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u64]
+        h.ref_crowding.argtypes = [_vp, _u64, _u64, _vp]
+        h.ref_pareto_dominance.argtypes = [_vp, _vp, _u64, _vp]
+
+    def _chk(self, st):
+        if st == 1:
+            raise ValueError(self.h.ref_last_error().decode())
+        if st != 0:
+            raise RuntimeError(self.h.ref_last_error().decode())
+
+    def thread_bfe(self, kind, param, dvs):
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        n, nx = x.shape
+        f = np.empty(n)
+        fe = C.c_uint64()
+        self._chk(self.h.ref_thread_bfe(kind, param, _p(x), n, nx, _p(f), C.byref(fe)))
+        return f, fe.value
+
+    def fitness_rows(self, kind, param, dvs):
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        n, nx = x.shape
+        f = np.empty(n)
+        self._chk(self.h.ref_fitness_rows(kind, param, _p(x), n, nx, _p(f)))
+        return f
+
+    def gradient_rows(self, kind, param, dvs):
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        n, nx = x.shape
+        g = np.empty((n, nx))
+        self._chk(self.h.ref_gradient_rows(kind, param, _p(x), n, nx, _p(g)))
+        return g
+
+    def bounds(self, kind, param, nx):
+        lb = np.empty(nx)
+        ub = np.empty(nx)
+        self._chk(self.h.ref_bounds(kind, param, _p(lb), _p(ub)))
+        return lb, ub
+
+    def fnds(self, pts):
+        p = np.ascontiguousarray(pts, dtype=np.float64)
+        n, m = p.shape
+        rank = np.empty(n, np.uint64)
+        dc = np.empty(n, np.uint64)
+        off = np.empty(n + 1, np.uint64)
+        idx = np.empty(n, np.uint64)
+        nf = C.c_uint64()
+        cap = n * (n - 1) // 2
+        dlo = np.empty(n + 1, np.uint64)
+        dli = np.empty(max(cap, 1), np.uint64)
+        self._chk(self.h.ref_fnds(_p(p), n, m, _p(rank), _p(dc), _p(off), _p(idx), C.addressof(nf), _p(dlo),
+                                  _p(dli), cap))
+        k = nf.value
+        return {"rank": rank.astype(np.int64), "dom_count": dc.astype(np.int64),
+                "front_offsets": off[:k + 1].astype(np.int64), "front_indices": idx.astype(np.int64),
+                "dl_offsets": dlo.astype(np.int64), "dl_indices": dli[:int(dlo[n])].astype(np.int64)}
+
+    def crowding(self, pts):
+        p = np.ascontiguousarray(pts, dtype=np.float64)
+        n, m = p.shape
+        out = np.empty(n)
+        self._chk(self.h.ref_crowding(_p(p), n, m, _p(out)))
+        return out
+
+    def pareto_dominance(self, a, b):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        r = C.c_int()
+        self._chk(self.h.ref_pareto_dominance(_p(a), _p(b), a.size, C.byref(r)))
+        return bool(r.value)
+
+
+_oracle = None
+_reference = None
+
+
+def oracle() -> _Oracle:
+    global _oracle
+    if _oracle is None:
+        if not ORACLE_SO.exists():
+            build(reference=False)
+        _oracle = _Oracle(ORACLE_SO)
+    return _oracle
+
+
+def reference() -> _Reference | None:
+    """The compiled reference, or None where it was not built (e.g. a machine without its sources)."""
+    global _reference
+    if _reference is None and REF_SO.exists():
+        try:
+            _reference = _Reference(REF_SO)
+        except OSError:
+            return None
+    return _reference

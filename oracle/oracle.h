@@ -1,0 +1,84 @@
+/*
+ * CPU oracle for the pagmo batch-evaluation path (TEST INFRASTRUCTURE ONLY).
+ *
+ * This is a plain C++ restatement of the reference algorithms that the GPU
+ * library replaces. It is the checker: only the test suite, the smoke check
+ * and the CPU leg of the benchmark call it. The product library never links,
+ * loads or falls back to it.
+ *
+ * Parity pin: tests/test_oracle.py checks every function here against the
+ * golden vectors in tests/golden/ (produced by the reference's own sources,
+ * compiled unmodified by oracle/Makefile) and against the known answers in
+ * the reference's tests (tests/lennard_jones.cpp:59-60, tests/rastrigin.cpp:56-57,
+ * tests/rosenbrock.cpp:70-79, tests/multi_objective.cpp:81-182).
+ *
+ * Two families:
+ *  - "mirror" functions repeat the reference's double arithmetic in the same
+ *    order, so they reproduce its results bit for bit (same libm);
+ *  - "_ld" functions evaluate the same formulas in long double and also return
+ *    a condition scale (the sum of the absolute values of the summed terms),
+ *    used to state relative errors that survive cancellation.
+ *
+ * Problem kinds: 1 = rastrigin (param = dim), 2 = rosenbrock (param = dim),
+ * 3 = lennard_jones (param = atoms, dim = 3*atoms-6).
+ * Status codes: 0 ok, 1 invalid argument (message via orc_last_error()).
+ */
+#ifndef PGX_ORACLE_H
+#define PGX_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+const char *orc_last_error(void);
+
+/* ---- mirrors of the reference arithmetic (double) ---- */
+double orc_rastrigin_fitness(const double *x, uint64_t n);
+void orc_rastrigin_gradient(const double *x, uint64_t n, double *g);
+double orc_rosenbrock_fitness(const double *x, uint64_t n);
+void orc_rosenbrock_gradient(const double *x, uint64_t n, double *g);
+double orc_lj_fitness(const double *x, uint64_t atoms);
+
+/* ---- long-double oracle with condition scales ---- */
+double orc_rastrigin_fitness_ld(const double *x, uint64_t n, double *scale);
+void orc_rastrigin_gradient_ld(const double *x, uint64_t n, double *g, double *gscale);
+double orc_rosenbrock_fitness_ld(const double *x, uint64_t n, double *scale);
+void orc_rosenbrock_gradient_ld(const double *x, uint64_t n, double *g, double *gscale);
+double orc_lj_fitness_ld(const double *x, uint64_t atoms, double *scale);
+void orc_lj_gradient_ld(const double *x, uint64_t atoms, double *g, double *gscale);
+
+/* ---- batch runners over row-major dvs (n rows of nx) ---- */
+/* Mirror of bfe{thread_bfe{}}: static partition over nthreads std::threads,
+   each row copied into a temporary vector and evaluated by the mirror fitness
+   (thread_bfe.cpp:94-123). nthreads <= 0 -> hardware_concurrency. */
+int orc_batch_fitness(int kind, uint64_t param, const double *dvs, uint64_t n, uint64_t nx, double *f, int nthreads);
+/* Mirror gradients per row (rastrigin/rosenbrock: the reference's gradient();
+   lennard_jones: the long-double formula rounded to double). */
+int orc_batch_gradient(int kind, uint64_t param, const double *dvs, uint64_t n, uint64_t nx, double *g, int nthreads);
+/* Long-double fitness (+scale) and gradient (+component scales) per row. */
+int orc_batch_fitness_ld(int kind, uint64_t param, const double *dvs, uint64_t n, uint64_t nx, double *f,
+                         double *scale, int nthreads);
+int orc_batch_gradient_ld(int kind, uint64_t param, const double *dvs, uint64_t n, uint64_t nx, double *g,
+                          double *gscale, int nthreads);
+
+/* ---- multi-objective survival ---- */
+int orc_pareto_dominance(const double *a, const double *b, uint64_t m);
+/* fast_non_dominated_sorting (multi_objective.cpp:200-257). Fronts are
+   flattened: front_offsets[0..n_fronts], front_indices[0..n). dom_list is
+   flattened the same way (dl_offsets[0..n], dl_indices) when dl_offsets is
+   non-null; dl_capacity bounds dl_indices. */
+int orc_fnds(const double *pts, uint64_t n, uint64_t m, uint64_t *rank, uint64_t *dom_count,
+             uint64_t *front_offsets, uint64_t *front_indices, uint64_t *n_fronts, uint64_t *dl_offsets,
+             uint64_t *dl_indices, uint64_t dl_capacity);
+/* crowding_distance of one front (multi_objective.cpp:280-315). */
+int orc_crowding(const double *pts, uint64_t n, uint64_t m, double *out);
+/* NSGA-II survival glue (nsga2.cpp:183-206): crowding per front for all points,
+   fronts of size 1 or 2 get +inf. Needs the fronts from orc_fnds. */
+int orc_nsga2_crowding(const double *pts, uint64_t n, uint64_t m, const uint64_t *front_offsets,
+                       const uint64_t *front_indices, uint64_t n_fronts, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,183 @@
+// C entry points over the reference's own compiled sources (pagmo 2.19.1),
+// used only by the test suite and by the CPU leg of the benchmark to run the
+// unmodified reference implementation of the batch-evaluation path.
+//
+// Every function catches exceptions and returns a status (0 = ok, 1 = the
+// reference threw std::invalid_argument, 2 = any other exception); the
+// message of the last error is available from ref_last_error().
+#include <cstdint>
+#include <cstring>
+#include <exception>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <pagmo/batch_evaluators/thread_bfe.hpp>
+#include <pagmo/bfe.hpp>
+#include <pagmo/problem.hpp>
+#include <pagmo/problems/lennard_jones.hpp>
+#include <pagmo/problems/rastrigin.hpp>
+#include <pagmo/problems/rosenbrock.hpp>
+#include <pagmo/utils/multi_objective.hpp>
+
+namespace
+{
+thread_local std::string g_err;
+
+pagmo::problem make_problem(int kind, std::uint64_t param)
+{
+    switch (kind) {
+        case 1:
+            return pagmo::problem{pagmo::rastrigin{static_cast<unsigned>(param)}};
+        case 2:
+            return pagmo::problem{pagmo::rosenbrock{static_cast<pagmo::vector_double::size_type>(param)}};
+        case 3:
+            return pagmo::problem{pagmo::lennard_jones{static_cast<unsigned>(param)}};
+        default:
+            throw std::invalid_argument("unknown problem kind " + std::to_string(kind));
+    }
+}
+
+template <typename F>
+int guard(F &&f)
+{
+    try {
+        f();
+        return 0;
+    } catch (const std::invalid_argument &e) {
+        g_err = e.what();
+        return 1;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return 2;
+    }
+}
+
+std::vector<pagmo::vector_double> rows(const double *p, std::uint64_t n, std::uint64_t m)
+{
+    std::vector<pagmo::vector_double> out(n, pagmo::vector_double(m));
+    for (std::uint64_t i = 0; i < n; ++i)
+        for (std::uint64_t k = 0; k < m; ++k) out[i][k] = p[i * m + k];
+    return out;
+}
+} // namespace
+
+extern "C" {
+
+const char *ref_last_error(void)
+{
+    return g_err.c_str();
+}
+
+// bfe{thread_bfe{}}(problem{udp}, dvs): the reference's multi-threaded batch path.
+// fevals_out (nullable) receives the caller-side fevals counter after the call.
+int ref_thread_bfe(int kind, std::uint64_t param, const double *dvs, std::uint64_t n_dvs, std::uint64_t nx,
+                   double *fvs, std::uint64_t *fevals_out)
+{
+    return guard([&] {
+        auto p = make_problem(kind, param);
+        pagmo::bfe b{pagmo::thread_bfe{}};
+        pagmo::vector_double in(dvs, dvs + n_dvs * nx);
+        auto out = b(p, in);
+        std::memcpy(fvs, out.data(), out.size() * sizeof(double));
+        if (fevals_out) *fevals_out = p.get_fevals();
+    });
+}
+
+// Serial problem::fitness over rows (the per-call path).
+int ref_fitness_rows(int kind, std::uint64_t param, const double *dvs, std::uint64_t n_dvs, std::uint64_t nx,
+                     double *fvs)
+{
+    return guard([&] {
+        auto p = make_problem(kind, param);
+        pagmo::vector_double x(nx);
+        for (std::uint64_t i = 0; i < n_dvs; ++i) {
+            std::memcpy(x.data(), dvs + i * nx, nx * sizeof(double));
+            fvs[i] = p.fitness(x)[0];
+        }
+    });
+}
+
+// Serial problem::gradient over rows (rastrigin and rosenbrock provide one).
+int ref_gradient_rows(int kind, std::uint64_t param, const double *dvs, std::uint64_t n_dvs, std::uint64_t nx,
+                      double *grads)
+{
+    return guard([&] {
+        auto p = make_problem(kind, param);
+        pagmo::vector_double x(nx);
+        for (std::uint64_t i = 0; i < n_dvs; ++i) {
+            std::memcpy(x.data(), dvs + i * nx, nx * sizeof(double));
+            auto g = p.gradient(x);
+            std::memcpy(grads + i * nx, g.data(), nx * sizeof(double));
+        }
+    });
+}
+
+// problem::get_bounds of the reference UDP.
+int ref_bounds(int kind, std::uint64_t param, double *lb, double *ub)
+{
+    return guard([&] {
+        auto p = make_problem(kind, param);
+        auto b = p.get_bounds();
+        std::memcpy(lb, b.first.data(), b.first.size() * sizeof(double));
+        std::memcpy(ub, b.second.data(), b.second.size() * sizeof(double));
+    });
+}
+
+// fast_non_dominated_sorting over n points of m objectives (row-major). Outputs:
+// rank[n], dom_count[n], fronts flattened (front_offsets[n_fronts+1],
+// front_indices[n]), dom_list flattened (dl_offsets[n+1], dl_indices up to
+// dl_capacity entries; nullable).
+int ref_fnds(const double *pts, std::uint64_t n, std::uint64_t m, std::uint64_t *rank, std::uint64_t *dom_count,
+             std::uint64_t *front_offsets, std::uint64_t *front_indices, std::uint64_t *n_fronts,
+             std::uint64_t *dl_offsets, std::uint64_t *dl_indices, std::uint64_t dl_capacity)
+{
+    return guard([&] {
+        auto r = pagmo::fast_non_dominated_sorting(rows(pts, n, m));
+        const auto &fr = std::get<0>(r);
+        const auto &dl = std::get<1>(r);
+        const auto &dc = std::get<2>(r);
+        const auto &rk = std::get<3>(r);
+        for (std::uint64_t i = 0; i < n; ++i) {
+            rank[i] = rk[i];
+            dom_count[i] = dc[i];
+        }
+        std::uint64_t pos = 0;
+        front_offsets[0] = 0;
+        for (std::size_t f = 0; f < fr.size(); ++f) {
+            for (auto v : fr[f]) front_indices[pos++] = v;
+            front_offsets[f + 1] = pos;
+        }
+        *n_fronts = fr.size();
+        if (dl_offsets) {
+            std::uint64_t q = 0;
+            dl_offsets[0] = 0;
+            for (std::uint64_t i = 0; i < n; ++i) {
+                for (auto v : dl[i]) {
+                    if (q >= dl_capacity) throw std::overflow_error("dom_list capacity exceeded");
+                    dl_indices[q++] = v;
+                }
+                dl_offsets[i + 1] = q;
+            }
+        }
+    });
+}
+
+// crowding_distance over one front of n points with m objectives (row-major).
+int ref_crowding(const double *pts, std::uint64_t n, std::uint64_t m, double *out)
+{
+    return guard([&] {
+        auto r = pagmo::crowding_distance(rows(pts, n, m));
+        std::memcpy(out, r.data(), r.size() * sizeof(double));
+    });
+}
+
+// pareto_dominance(a, b) for two m-vectors: returns 0/1 in *out.
+int ref_pareto_dominance(const double *a, const double *b, std::uint64_t m, int *out)
+{
+    return guard([&] {
+        *out = pagmo::pareto_dominance(pagmo::vector_double(a, a + m), pagmo::vector_double(b, b + m)) ? 1 : 0;
+    });
+}
+
+} // extern "C"

@@ -1,0 +1,144 @@
+"""ctypes binding of the C ABI in include/pgx.h (libpgx.so, built in-tree).
+
+There is deliberately no fallback: if the library is missing or no GB300 can
+be opened, every call raises. Status codes map onto Python exceptions the way
+pagmo's C++ exceptions map in pygmo: PGX_ERR_INVALID -> ValueError (pagmo's
+std::invalid_argument), PGX_ERR_CAPACITY -> OverflowError, PGX_ERR_TIMEOUT ->
+TimeoutError, CUDA / no device -> RuntimeError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpgx.so"
+
+OK, ERR_INVALID, ERR_CUDA, ERR_TIMEOUT, ERR_CAPACITY, ERR_NODEVICE = 0, 1, 2, 3, 4, 5
+RASTRIGIN, ROSENBROCK, LENNARD_JONES = 1, 2, 3
+
+# Exported symbols and their signatures (kept in step with include/pgx.h).
+_vp, _u64, _i32, _d = C.c_void_p, C.c_uint64, C.c_int32, C.c_double
+SIGNATURES = {
+    "pgx_abi_version": (C.c_int, []),
+    "pgx_last_error": (C.c_char_p, []),
+    "pgx_context_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
+    "pgx_context_destroy": (None, [_vp]),
+    "pgx_context_launch_count": (_u64, [_vp]),
+    "pgx_problem_nx": (C.c_int, [C.c_int, _u64, C.POINTER(_u64)]),
+    "pgx_problem_bounds": (C.c_int, [C.c_int, _u64, _vp, _vp]),
+    "pgx_batch_fitness": (C.c_int, [_vp, C.c_int, _u64, _vp, _u64, _vp]),
+    "pgx_batch_gradient": (C.c_int, [_vp, C.c_int, _u64, _vp, _u64, _vp, _vp]),
+    "pgx_batch_eval_device": (C.c_int, [_vp, C.c_int, _u64, _vp, _u64, _vp, _vp, _vp]),
+    "pgx_fnds": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp]),
+    "pgx_fnds_dom_list": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _u64, C.POINTER(_u64)]),
+    "pgx_crowding_distance": (C.c_int, [_vp, _vp, _u64, _u64, _vp]),
+    "pgx_nsga2_survival": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "pgx_nsga2_survival_device": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+}
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def lib() -> C.CDLL:
+    """The loaded libpgx.so (raises if it has not been built)."""
+    global _lib
+    with _lib_lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise RuntimeError(
+                    f"libpgx.so not found at {LIB_PATH}; build it with `python -m pagmo2_gb300.build` "
+                    "(there is no CPU fallback)")
+            h = C.CDLL(str(LIB_PATH))
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(h, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = h
+        return _lib
+
+
+def last_error() -> str:
+    m = lib().pgx_last_error()
+    return m.decode() if m else ""
+
+
+def check(status: int) -> None:
+    if status == OK:
+        return
+    msg = last_error()
+    if status == ERR_INVALID:
+        raise ValueError(msg)
+    if status == ERR_CAPACITY:
+        raise OverflowError(msg)
+    if status == ERR_TIMEOUT:
+        raise TimeoutError(msg)
+    raise RuntimeError(msg or f"pgx status {status}")
+
+
+def ptr(a: np.ndarray | None) -> int | None:
+    if a is None:
+        return None
+    return a.ctypes.data
+
+
+class Context:
+    """A pgx context on one CUDA device (streams, staging buffers)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib().pgx_context_create(device, C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self) -> None:
+        if self.handle:
+            lib().pgx_context_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def launches(self) -> int:
+        return int(lib().pgx_context_launch_count(self.handle))
+
+
+_default: dict[int, Context] = {}
+_default_lock = threading.Lock()
+
+
+def default_context(device: int = 0) -> Context:
+    """One shared context per device, created on first use."""
+    with _default_lock:
+        ctx = _default.get(device)
+        if ctx is None:
+            ctx = Context(device)
+            _default[device] = ctx
+        return ctx
+
+
+def problem_nx(kind: int, param: int) -> int:
+    nx = C.c_uint64()
+    check(lib().pgx_problem_nx(kind, param, C.byref(nx)))
+    return int(nx.value)
+
+
+def problem_bounds(kind: int, param: int) -> tuple[np.ndarray, np.ndarray]:
+    nx = problem_nx(kind, param)
+    lb = np.empty(nx)
+    ub = np.empty(nx)
+    check(lib().pgx_problem_bounds(kind, param, ptr(lb), ptr(ub)))
+    return lb, ub

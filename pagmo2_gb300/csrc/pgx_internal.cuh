@@ -1,0 +1,135 @@
+// Internal declarations shared by the pgx translation units: error state,
+// the context object, device helpers and the kernel launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/pgx.h"
+
+namespace pgx
+{
+
+// ------------------------------------------------------------------ errors
+
+void set_error(const std::string &msg);
+const char *get_error();
+
+// Returns PGX_ERR_CUDA (and records the message) when `e` is an error.
+int cuda_status(cudaError_t e, const char *what);
+
+#define PGX_CUDA(call)                                                                                                 \
+    do {                                                                                                               \
+        cudaError_t pgx_e_ = (call);                                                                                   \
+        if (pgx_e_ != cudaSuccess) return ::pgx::cuda_status(pgx_e_, #call);                                           \
+    } while (0)
+
+#define PGX_CHECK(cond, code, msg)                                                                                     \
+    do {                                                                                                               \
+        if (!(cond)) {                                                                                                 \
+            ::pgx::set_error(msg);                                                                                     \
+            return (code);                                                                                             \
+        }                                                                                                              \
+    } while (0)
+
+#define PGX_TRY(expr)                                                                                                  \
+    do {                                                                                                               \
+        int pgx_s_ = (expr);                                                                                           \
+        if (pgx_s_ != PGX_OK) return pgx_s_;                                                                           \
+    } while (0)
+
+// --------------------------------------------------------- device buffers
+
+// Grow-only device allocation owned by a context.
+struct dbuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t need);
+    void release();
+    template <typename T>
+    T *as() const
+    {
+        return static_cast<T *>(ptr);
+    }
+};
+
+// Grow-only pinned host allocation owned by a context.
+struct hbuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t need);
+    void release();
+    template <typename T>
+    T *as() const
+    {
+        return static_cast<T *>(ptr);
+    }
+};
+
+} // namespace pgx
+
+// The context (opaque to callers of the C ABI).
+struct pgx_context {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr; // kernels
+    cudaStream_t h2d = nullptr;    // host-to-device copies of the host pipelines
+    cudaStream_t d2h = nullptr;    // device-to-host copies of the host pipelines
+    std::mutex lock;
+    uint64_t launches = 0;
+    // device buffers of the host-buffer calls
+    pgx::dbuf d_in, d_out, d_grad;
+    std::vector<cudaEvent_t> chunk_ev;
+    // survival scratch
+    pgx::dbuf s_points, s_keys, s_dommat, s_state, s_outs, s_crowd;
+};
+
+namespace pgx
+{
+
+// Scope guard: makes ctx->device current for the calling thread.
+int use_device(pgx_context *ctx);
+
+// ------------------------------------------------------------ problem facts
+
+int problem_nx(int kind, uint64_t param, uint64_t *nx);
+
+// -------------------------------------------------------------- launchers
+
+// Batch fitness (+ gradient when d_g != nullptr) for one problem on `stream`.
+// Returns the number of kernel launches issued through *launches.
+int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64_t n, double *d_f, double *d_g,
+                cudaStream_t stream, int num_sms, uint64_t *launches);
+
+// Survival: fnds (+ crowding when d_crowd != nullptr) on device buffers.
+struct survival_out {
+    int32_t *rank = nullptr;
+    int32_t *dom_count = nullptr;
+    int32_t *front_offsets = nullptr; // n + 1 entries
+    int32_t *front_indices = nullptr; // n entries
+    int32_t *n_fronts = nullptr;      // one int32
+    double *crowding = nullptr;       // n entries or nullptr
+};
+int launch_survival(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, const survival_out &out,
+                    cudaStream_t stream);
+
+// Single-front crowding distance on device buffers.
+int launch_crowding_single(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, double *d_out,
+                           cudaStream_t stream);
+
+// Reads the device status word of the last survival launch (after a stream
+// synchronisation): PGX_ERR_TIMEOUT when a grid barrier gave up.
+int survival_status(pgx_context *ctx);
+
+// dom_list support: builds the "dominates" bit matrix (row i: the points i
+// dominates) and per-row counts (device int64[n], owned by the context), then
+// writes each row's set bits, ascending, at the given CSR offsets.
+int build_dominates_rows(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, int64_t **d_row_count,
+                         cudaStream_t stream);
+int extract_dom_list(pgx_context *ctx, uint64_t n, const int64_t *d_offsets, int32_t *d_indices, cudaStream_t stream);
+
+} // namespace pgx

@@ -1,0 +1,106 @@
+"""GPU NSGA-II survival with the reference's signatures
+(src/utils/multi_objective.cpp:200-257, :280-315; src/algorithms/nsga2.cpp:183-206).
+
+``fast_non_dominated_sorting(points)`` returns the same 4-tuple as the
+reference's ``fnds_return_type`` (fronts, dom_list, dom_count, rank), with the
+fronts in the reference's order. ``crowding_distance(front)`` returns the
+crowding distances of one front. ``nsga2_survival(points)`` runs the survival
+block of one NSGA-II generation (fronts + per-front crowding) in one call.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+def _points(points) -> tuple[np.ndarray, int, int]:
+    if isinstance(points, np.ndarray) and points.ndim == 2:
+        a = np.ascontiguousarray(points, dtype=np.float64)
+        return a, a.shape[0], a.shape[1]
+    rows = [np.asarray(p, dtype=np.float64).reshape(-1) for p in points]
+    n = len(rows)
+    m = rows[0].size if n else 0
+    if any(r.size != m for r in rows):
+        raise ValueError("Different number of objectives found in input fitnesses. I cannot define dominance")
+    a = np.ascontiguousarray(np.stack(rows) if n else np.empty((0, 0)), dtype=np.float64).reshape(n, m)
+    return a, n, m
+
+
+def _fronts(off: np.ndarray, idx: np.ndarray, nf: int) -> list[list[int]]:
+    return [idx[off[f]:off[f + 1]].tolist() for f in range(nf)]
+
+
+def fnds_arrays(points, ctx: N.Context | None = None):
+    """Flat outputs: (rank[n] int32, dom_count[n] int32, front_offsets[nf+1], front_indices[n])."""
+    a, n, m = _points(points)
+    if n < 2:
+        raise ValueError(f"At least two points are needed for fast_non_dominated_sorting: {n} detected.")
+    ctx = ctx or N.default_context()
+    rank = np.empty(n, np.int32)
+    dc = np.empty(n, np.int32)
+    off = np.empty(n + 1, np.int32)
+    idx = np.empty(n, np.int32)
+    nf = C.c_int32()
+    N.check(N.lib().pgx_fnds(ctx.handle, N.ptr(a), n, m, N.ptr(rank), N.ptr(dc), N.ptr(off), N.ptr(idx),
+                             C.addressof(nf)))
+    return rank, dc, off[:nf.value + 1].copy(), idx
+
+
+def dom_list_arrays(points, ctx: N.Context | None = None):
+    """(offsets[n+1] int64, indices[total] int32) of the reference's dom_list."""
+    a, n, m = _points(points)
+    if n < 2:
+        raise ValueError(f"At least two points are needed for fast_non_dominated_sorting: {n} detected.")
+    ctx = ctx or N.default_context()
+    off = np.empty(n + 1, np.int64)
+    total = C.c_uint64()
+    st = N.lib().pgx_fnds_dom_list(ctx.handle, N.ptr(a), n, m, N.ptr(off), None, 0, C.byref(total))
+    if st not in (N.OK, N.ERR_CAPACITY):
+        N.check(st)
+    idx = np.empty(max(int(total.value), 1), np.int32)
+    N.check(N.lib().pgx_fnds_dom_list(ctx.handle, N.ptr(a), n, m, N.ptr(off), N.ptr(idx), idx.size,
+                                      C.byref(total)))
+    return off, idx[:int(total.value)]
+
+
+def fast_non_dominated_sorting(points, ctx: N.Context | None = None, with_dom_list: bool = True):
+    """(fronts, dom_list, dom_count, rank) as the reference returns them."""
+    rank, dc, off, idx = fnds_arrays(points, ctx)
+    fronts = _fronts(off, idx, off.size - 1)
+    dom_list = None
+    if with_dom_list:
+        doff, didx = dom_list_arrays(points, ctx)
+        dom_list = [didx[doff[i]:doff[i + 1]].tolist() for i in range(rank.size)]
+    return fronts, dom_list, dc.tolist(), rank.tolist()
+
+
+def crowding_distance(front, ctx: N.Context | None = None) -> np.ndarray:
+    a, n, m = _points(front)
+    if n < 2:
+        raise ValueError(f"A non dominated front must contain at least two points: {n} detected.")
+    if m < 2:
+        raise ValueError(f"Points in the non dominated front must contain at least two objectives: {m} detected.")
+    ctx = ctx or N.default_context()
+    out = np.empty(n)
+    N.check(N.lib().pgx_crowding_distance(ctx.handle, N.ptr(a), n, m, N.ptr(out)))
+    return out
+
+
+def nsga2_survival(points, ctx: N.Context | None = None):
+    """(rank, dom_count, front_offsets, front_indices, crowding) for one population."""
+    a, n, m = _points(points)
+    if n < 2:
+        raise ValueError(f"At least two points are needed for fast_non_dominated_sorting: {n} detected.")
+    ctx = ctx or N.default_context()
+    rank = np.empty(n, np.int32)
+    dc = np.empty(n, np.int32)
+    off = np.empty(n + 1, np.int32)
+    idx = np.empty(n, np.int32)
+    cd = np.empty(n)
+    nf = C.c_int32()
+    N.check(N.lib().pgx_nsga2_survival(ctx.handle, N.ptr(a), n, m, N.ptr(rank), N.ptr(dc), N.ptr(off), N.ptr(idx),
+                                       C.addressof(nf), N.ptr(cd)))
+    return rank, dc, off[:nf.value + 1].copy(), idx, cd

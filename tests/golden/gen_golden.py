@@ -1,0 +1,114 @@
+"""Generates the golden fixtures in this directory from the reference itself.
+
+The reference's hot-path sources are compiled unmodified by oracle/Makefile
+into oracle/_ref/libpagmo_ref.so (this needs the reference tree, so run it
+where that exists):
+
+    make -C oracle ref REF_ROOT=<pagmo2 source tree>
+    python tests/golden/gen_golden.py
+
+Outputs (numpy .npz, small):
+  fitness.npz  per case: the decision vectors, bfe{thread_bfe{}} fitness, and
+               problem::gradient rows (rastrigin, rosenbrock)
+  mo.npz       per case: the objective vectors, fast_non_dominated_sorting
+               (rank, dom_count, fronts, dom_list) and crowding_distance of
+               every front of three or more points
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parents[1]))
+
+import oracle  # noqa: E402
+from pagmo2_gb300 import workloads as W  # noqa: E402
+
+RAS, ROS, LJ = 1, 2, 3
+
+
+def fitness_cases():
+    cases = []
+    for dim, n, seed in ((1, 16, 101), (5, 32, 102), (50, 64, 103), (173, 8, 104)):
+        cases.append((f"rastrigin_{dim}", RAS, dim, W.uniform_batch(RAS, dim, n, seed)))
+    for dim, n, seed in ((2, 32, 201), (5, 16, 202), (37, 16, 203), (1000, 4, 204)):
+        cases.append((f"rosenbrock_{dim}", ROS, dim, W.uniform_batch(ROS, dim, n, seed)))
+    for atoms, n, seed in ((3, 16, 301), (4, 8, 302), (7, 8, 303), (33, 4, 304), (150, 2, 305)):
+        cases.append((f"lj_{atoms}", LJ, atoms, W.uniform_batch(LJ, atoms, n, seed)))
+    for atoms, n, seed in ((13, 4, 311), (38, 2, 312), (150, 2, 313)):
+        cases.append((f"ljlat_{atoms}", LJ, atoms, W.lj_lattice_batch(n, atoms, seed=seed)))
+    # near the optimum (cancellation in the gradients)
+    cases.append(("rosenbrock_near_opt", ROS, 64, 1.0 + 1e-3 * np.random.RandomState(205).standard_normal((8, 64))))
+    cases.append(("rastrigin_near_opt", RAS, 64, 1e-3 * np.random.RandomState(105).standard_normal((8, 64))))
+    # integer points: exact values in the reference
+    cases.append(("rastrigin_ints", RAS, 7, np.random.RandomState(106).randint(-5, 6, (8, 7)).astype(float)))
+    return cases
+
+
+def mo_cases():
+    cases = []
+    # tests/multi_objective.cpp fnds examples
+    cases.append(("ex11", np.array([[0, 7], [1, 5], [2, 3], [4, 2], [7, 1], [10, 0], [2, 6], [4, 4], [10, 2], [6, 6],
+                                    [9, 5]], float)))
+    cases.append(("ex4", np.array([[1, 2, 3], [-2, 3, 7], [-1, -2, -3], [0, 0, 0]], float)))
+    rs = np.random.RandomState(401)
+    cases.append(("rand2", rs.random_sample((200, 2))))
+    cases.append(("rand3", rs.random_sample((300, 3))))
+    cases.append(("rand5", rs.random_sample((150, 5))))
+    cases.append(("grid3", rs.randint(0, 4, (120, 3)).astype(float)))  # many ties and duplicates
+    cases.append(("nested", W.nsga2_points(600, 3, layers=10, seed=402)))
+    cases.append(("nested_nodup", W.nsga2_points(500, 3, layers=8, dup_frac=0.0, seed=403)))
+    p = rs.random_sample((60, 3))
+    p[3, 1] = np.nan
+    p[17, 0] = np.nan
+    p[17, 2] = np.nan
+    p[25] = np.nan
+    p[40, 2] = -0.0
+    p[41, 2] = 0.0
+    p[50, 0] = -np.inf
+    p[51, 1] = np.inf
+    cases.append(("special", p))
+    cases.append(("single_front", np.stack([np.linspace(0, 1, 64), 1 - np.linspace(0, 1, 64)], 1)))
+    return cases
+
+
+def main():
+    ref = oracle.reference()
+    if ref is None:
+        raise SystemExit("oracle/_ref/libpagmo_ref.so is missing: build it with `make -C oracle ref` first")
+    fit = {}
+    for name, kind, param, x in fitness_cases():
+        x = np.ascontiguousarray(x)
+        f, fe = ref.thread_bfe(kind, param, x)
+        assert fe == x.shape[0]
+        fit[f"{name}/kind"] = np.array([kind, param])
+        fit[f"{name}/x"] = x
+        fit[f"{name}/f"] = f
+        if kind != LJ:
+            fit[f"{name}/g"] = ref.gradient_rows(kind, param, x)
+    np.savez_compressed(HERE / "fitness.npz", **fit)
+
+    mo = {}
+    for name, p in mo_cases():
+        r = ref.fnds(p)
+        mo[f"{name}/points"] = p
+        for k, v in r.items():
+            mo[f"{name}/{k}"] = v
+        off, idx = r["front_offsets"], r["front_indices"]
+        cd = np.full(p.shape[0], np.nan)
+        for fi in range(off.size - 1):
+            members = idx[off[fi]:off[fi + 1]]
+            if members.size >= 3 and p.shape[1] >= 2:
+                cd[members] = ref.crowding(p[members])
+            elif members.size in (1, 2):
+                cd[members] = np.inf
+        mo[f"{name}/crowding"] = cd
+    np.savez_compressed(HERE / "mo.npz", **mo)
+    print("wrote", HERE / "fitness.npz", HERE / "mo.npz")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,239 @@
+"""GPU parity of batch fitness and gradient (through the C ABI) against the
+reference's golden vectors and the long-double oracle.
+
+Tolerance: |gpu - x| <= 1e-13 * scale per value, where scale is the
+first-order error bound of the reference's own evaluation (the sum of the
+absolute values of the summed terms, plus the rounded squares inside
+rosenbrock's t = x_i^2 - x_{i+1}); computed by the oracle in long double.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from pathlib import Path
+
+from pagmo2_gb300 import _native as N
+from pagmo2_gb300 import bfe as B
+from pagmo2_gb300 import problems as P
+from pagmo2_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+TOL = 1e-13
+
+
+def eval_gpu(ctx, kind, param, x, grad=True):
+    udp = P.from_kind(kind, param, ctx)
+    if grad:
+        return udp.batch_gradient(x)
+    return udp.batch_fitness(x), None
+
+
+def rel_err(got, want, scale):
+    return np.max(np.abs(got - want) / np.maximum(scale, np.finfo(float).tiny)) if got.size else 0.0
+
+
+def check_against_oracle(orc, ctx, kind, param, x, grad=True):
+    f, g = eval_gpu(ctx, kind, param, x, grad)
+    fl, fs = orc.batch_fitness_ld(kind, param, x)
+    assert rel_err(f, fl, fs) <= TOL, (kind, param, rel_err(f, fl, fs))
+    if grad:
+        gl, gs = orc.batch_gradient_ld(kind, param, x)
+        assert rel_err(g, gl, gs) <= TOL, (kind, param, rel_err(g, gl, gs))
+    return f, g
+
+
+# ------------------------------------------------------------ reference pins
+
+def test_golden_fitness_and_gradient(ctx, orc):
+    gold = np.load(GOLD / "fitness.npz")
+    names = sorted({k.split("/")[0] for k in gold.files})
+    for name in names:
+        kind, param = (int(v) for v in gold[f"{name}/kind"])
+        x = gold[f"{name}/x"]
+        f, g = eval_gpu(ctx, kind, param, x)
+        fl, fs = orc.batch_fitness_ld(kind, param, x)
+        assert rel_err(f, gold[f"{name}/f"], fs) <= TOL, (name, rel_err(f, gold[f"{name}/f"], fs))
+        # the fitness-only kernel agrees with the fused one
+        f_only = P.from_kind(kind, param, ctx).batch_fitness(x)
+        assert rel_err(f_only, f, fs) <= TOL, name
+        if f"{name}/g" in gold.files:
+            gl, gs = orc.batch_gradient_ld(kind, param, x)
+            assert rel_err(g, gold[f"{name}/g"], gs) <= TOL, (name, rel_err(g, gold[f"{name}/g"], gs))
+        else:
+            gl, gs = orc.batch_gradient_ld(kind, param, x)
+            assert rel_err(g, gl, gs) <= TOL, (name, rel_err(g, gl, gs))
+
+
+def test_reference_known_answers(ctx):
+    # tests/rastrigin.cpp:56-62 (exact), tests/rosenbrock.cpp:70-79, tests/lennard_jones.cpp:59-60
+    assert P.rastrigin(1, ctx).fitness([1.0]).tolist() == [1.0]
+    assert P.rastrigin(5, ctx).fitness([1.0] * 5).tolist() == [5.0]
+    for g in (P.rastrigin(1, ctx).gradient([1.0]), P.rastrigin(5, ctx).gradient([1.0] * 5)):
+        assert np.allclose(g, 2.0, rtol=1e-14, atol=0)
+    assert P.rosenbrock(2, ctx).fitness([1.0, 1.0]).tolist() == [0.0]
+    assert P.rosenbrock(5, ctx).fitness([1.0] * 5).tolist() == [0.0]
+    g2 = P.rosenbrock(2, ctx).gradient([0.1, 0.2])
+    assert abs(g2[0] + 9.4) < 1e-8 and abs(g2[1] - 38.0) < 1e-8
+    g5 = P.rosenbrock(5, ctx).gradient([0.1, 0.2, 0.3, 0.4, 0.5])
+    assert np.all(np.abs(g5 - np.array([-9.4, 15.6, 13.4, 6.4, 68.0])) < 1e-8)
+    lj = P.lennard_jones(3, ctx)
+    assert math.isclose(lj.fitness([1.12, -0.33, 2.34])[0], -1.7633355813175688, rel_tol=1e-15)
+    assert math.isclose(lj.fitness([1.23, -1.23, 0.33])[0], -1.833100934753864, rel_tol=1e-15)
+
+
+# ------------------------------------------------------------ seeded parity
+
+@pytest.mark.parametrize("dim", [1, 2, 3, 7, 8, 9, 16, 17, 31, 33, 48, 49, 50, 64, 255, 257, 1000])
+def test_rastrigin_dims(ctx, orc, dim):
+    check_against_oracle(orc, ctx, N.RASTRIGIN, dim, W.uniform_batch(N.RASTRIGIN, dim, 97, seed=dim))
+
+
+@pytest.mark.parametrize("dim", [2, 3, 5, 8, 9, 16, 17, 31, 32, 33, 47, 48, 49, 255, 256, 257, 1000, 1001])
+def test_rosenbrock_dims(ctx, orc, dim):
+    check_against_oracle(orc, ctx, N.ROSENBROCK, dim, W.uniform_batch(N.ROSENBROCK, dim, 67, seed=dim))
+
+
+@pytest.mark.parametrize("atoms", [3, 4, 5, 6, 7, 32, 33, 34, 64, 65, 150])
+def test_lennard_jones_atoms(ctx, orc, atoms):
+    n = 24 if atoms <= 64 else 6
+    check_against_oracle(orc, ctx, N.LENNARD_JONES, atoms, W.uniform_batch(N.LENNARD_JONES, atoms, n, seed=atoms))
+    check_against_oracle(orc, ctx, N.LENNARD_JONES, atoms, W.lj_lattice_batch(n // 2 + 1, atoms, seed=atoms))
+
+
+def test_config1_rastrigin_full(ctx, orc):
+    x = W.rastrigin_batch()  # 4096 x 50, the reference's CPU-runnable case
+    f, g = check_against_oracle(orc, ctx, N.RASTRIGIN, 50, x)
+    fr = orc.batch_fitness(N.RASTRIGIN, 50, x)
+    assert np.max(np.abs(f - fr) / np.abs(fr)) <= TOL
+
+
+def test_config2_rosenbrock_sampled_and_properties(ctx, orc):
+    x = W.rosenbrock_batch()  # 65536 x 1000
+    udp = P.rosenbrock(1000, ctx)
+    f, g = udp.batch_gradient(x)
+    f_only = udp.batch_fitness(x)
+    # size-independent: the fused and fitness-only kernels agree everywhere
+    assert np.max(np.abs(f - f_only) / f) <= 1e-14
+    assert np.all(np.isfinite(g))
+    rows = np.random.RandomState(0).choice(x.shape[0], 96, replace=False)
+    fl, fs = orc.batch_fitness_ld(N.ROSENBROCK, 1000, x[rows])
+    gl, gs = orc.batch_gradient_ld(N.ROSENBROCK, 1000, x[rows])
+    assert rel_err(f[rows], fl, fs) <= TOL and rel_err(g[rows], gl, gs) <= TOL
+    # the plain relative error on these inputs is within the bar too
+    assert np.max(np.abs(f[rows] - fl) / np.abs(fl)) <= TOL
+
+
+def test_config3_lj_sampled(ctx, orc):
+    x = W.lj_batch(2048, 150)
+    udp = P.lennard_jones(150, ctx)
+    f, g = udp.batch_gradient(x)
+    assert np.max(np.abs(f - udp.batch_fitness(x)) / np.abs(f)) <= 1e-13
+    rows = np.arange(0, 2048, 128)
+    fl, fs = orc.batch_fitness_ld(N.LENNARD_JONES, 150, x[rows])
+    gl, gs = orc.batch_gradient_ld(N.LENNARD_JONES, 150, x[rows])
+    assert rel_err(f[rows], fl, fs) <= TOL and rel_err(g[rows], gl, gs) <= TOL
+
+
+# --------------------------------------------------------- finite differences
+
+def estimate_gradient_h(fun, x, dx=1e-2):
+    """6th-order central differences (include/pagmo/utils/gradients_and_hessians.hpp:199-244)."""
+    g = np.empty_like(x)
+    for j in range(x.size):
+        h = max(abs(x[j]), 1.0) * dx
+        def at(k):
+            y = x.copy()
+            y[j] += k * h
+            return fun(y)
+        m1 = (at(1) - at(-1)) / 2.0
+        m2 = (at(2) - at(-2)) / 4.0
+        m3 = (at(3) - at(-3)) / 6.0
+        g[j] = ((15.0 * m1 - 6.0 * m2) + m3) / (10.0 * h)
+    return g
+
+
+def test_gradients_against_finite_differences(ctx, orc):
+    for kind, param, x, dx, tol in ((N.RASTRIGIN, 6, W.uniform_batch(1, 6, 1, 5)[0], 1e-3, 1e-6),
+                                    (N.ROSENBROCK, 6, W.uniform_batch(2, 6, 1, 6)[0], 1e-3, 1e-6),
+                                    (N.LENNARD_JONES, 8, W.lj_lattice_batch(1, 8, seed=7)[0], 1e-3, 1e-6)):
+        udp = P.from_kind(kind, param, ctx)
+        g = udp.gradient(x)
+        fd = estimate_gradient_h(lambda y: orc.batch_fitness_ld(kind, param, y[None, :])[0][0], x, dx)
+        assert np.max(np.abs(g - fd)) <= tol * max(1.0, np.max(np.abs(g))), (kind, np.max(np.abs(g - fd)))
+
+
+# ------------------------------------------------------------------ edge cases
+
+def test_empty_batch_and_single_row(ctx):
+    udp = P.rosenbrock(10, ctx)
+    assert udp.batch_fitness(np.empty(0)).shape == (0,)
+    f, g = udp.batch_gradient(np.empty((0, 10)))
+    assert f.shape == (0,) and g.shape == (0, 10)
+    assert udp.batch_fitness(np.ones(10)).tolist() == [0.0]
+
+
+def test_wrong_sizes_raise(ctx):
+    with pytest.raises(ValueError, match="is not an exact multiple of the dimension of the problem, 10"):
+        P.rosenbrock(10, ctx).batch_fitness(np.zeros(15))
+    with pytest.raises(ValueError):
+        P.rastrigin(3, ctx).fitness([1.0, 2.0])
+
+
+def test_lj_coinciding_atoms_give_inf(ctx, orc):
+    x = W.lj_lattice_batch(3, 6, seed=2)
+    x[1, 3:6] = 0.0  # atom 3 on top of atom 0
+    x[2, 0] = 0.0    # atom 1 on top of atom 0
+    f, g = P.lennard_jones(6, ctx).batch_gradient(x)
+    assert np.isfinite(f[0]) and f[1] == math.inf and f[2] == math.inf
+    assert orc.batch_fitness(N.LENNARD_JONES, 6, x)[1:].tolist() == [math.inf, math.inf]
+    assert np.all(np.isnan(g[1, 3:6]))
+
+
+def test_nonfinite_inputs_propagate(ctx, orc):
+    for kind, param in ((N.RASTRIGIN, 9), (N.ROSENBROCK, 9), (N.LENNARD_JONES, 5)):
+        nx = N.problem_nx(kind, param)
+        x = W.uniform_batch(kind, param, 3, seed=1)
+        x[0, 2] = math.nan
+        x[1, 1] = math.inf
+        f = P.from_kind(kind, param, ctx).batch_fitness(x)
+        fr = orc.batch_fitness(kind, param, x)
+        for a, b in zip(f, fr):
+            assert (math.isnan(a) and math.isnan(b)) or a == b or abs(a - b) <= 1e-13 * abs(b), (kind, a, b)
+
+
+def test_device_entry_point_matches_host(ctx):
+    torch = pytest.importorskip("torch")
+    x = W.rosenbrock_batch(512, 300)
+    udp = P.rosenbrock(300, ctx)
+    f, g = udp.batch_gradient(x)
+    dx = torch.from_numpy(x).cuda()
+    df = torch.empty(512, dtype=torch.float64, device="cuda")
+    dg = torch.empty((512, 300), dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    N.check(N.lib().pgx_batch_eval_device(ctx.handle, N.ROSENBROCK, 300, dx.data_ptr(), 512, df.data_ptr(),
+                                          dg.data_ptr(), s))
+    torch.cuda.synchronize()
+    assert np.array_equal(df.cpu().numpy(), f) and np.array_equal(dg.cpu().numpy(), g)
+
+
+# ------------------------------------------------------- bfe contract / fevals
+
+def test_bfe_fevals_and_equality_with_per_call(ctx):
+    # tests/thread_bfe.cpp:57-95: bfe output equals per-call fitness; fevals counted once
+    prob = B.problem(P.rosenbrock(2, ctx))
+    dvs = np.random.RandomState(5).uniform(-1, 1, 10000)
+    fvs = B.bfe()(prob, dvs)
+    assert prob.get_fevals() == 5000
+    for i in range(0, 10000, 997 * 2):
+        assert fvs[i // 2] == P.rosenbrock(2, ctx).fitness(dvs[i:i + 2])[0]
+
+
+def test_gpu_bfe_rejects_unknown_problems(ctx):
+    class other:
+        def get_name(self):
+            return "other"
+
+    with pytest.raises(ValueError, match="Cannot use a gpu_bfe on the problem 'other'"):
+        B.gpu_bfe()(other(), np.zeros(4))

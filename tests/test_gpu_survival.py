@@ -1,0 +1,138 @@
+"""GPU parity of NSGA-II survival (through the C ABI): fast non-dominated
+sorting bit-exact with the reference (ranks, domination counts, fronts in the
+reference's order, dom_list), crowding distance bit-exact on every point
+whose objective values are not tied inside its front; inside a tie group the
+reference's unstable std::sort fixes which duplicate gets which neighbour
+difference, so there the multiset of the group's values must match.
+"""
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from pagmo2_gb300 import multi_objective as MO
+from pagmo2_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def fronts_of(off, idx):
+    return [list(map(int, idx[a:b])) for a, b in zip(off[:-1], off[1:])]
+
+
+def check_crowding(pts, off, idx, got, want):
+    """Untied points bit-exact; tied groups equal as multisets."""
+    for a, b in zip(off[:-1], off[1:]):
+        members = np.asarray(idx[a:b])
+        if members.size < 3:
+            assert np.all(got[members] == math.inf)
+            continue
+        sub = pts[members]
+        tied = np.zeros(members.size, bool)
+        for k in range(pts.shape[1]):
+            col = sub[:, k]
+            _, inv, cnt = np.unique(col, return_inverse=True, return_counts=True, equal_nan=True)
+            tied |= cnt[inv] > 1
+            nan = np.isnan(col)
+            if nan.sum() > 1:
+                tied |= nan
+        u = members[~tied]
+        assert np.array_equal(got[u], want[u], equal_nan=True), "untied crowding differs"
+        t = members[tied]
+        if t.size:
+            g = np.sort(got[t])
+            w = np.sort(want[t])
+            assert np.allclose(g, w, rtol=1e-12, atol=0, equal_nan=True), "tie-group crowding multiset differs"
+
+
+def test_golden_fnds_and_crowding(ctx):
+    gold = np.load(GOLD / "mo.npz")
+    for name in sorted({k.split("/")[0] for k in gold.files}):
+        p = gold[f"{name}/points"]
+        rank, dc, off, idx, cd = MO.nsga2_survival(p, ctx)
+        assert np.array_equal(rank, gold[f"{name}/rank"]), name
+        assert np.array_equal(dc, gold[f"{name}/dom_count"]), name
+        assert fronts_of(off, idx) == fronts_of(gold[f"{name}/front_offsets"], gold[f"{name}/front_indices"]), name
+        doff, didx = MO.dom_list_arrays(p, ctx)
+        assert np.array_equal(doff, gold[f"{name}/dl_offsets"]), name
+        assert np.array_equal(didx, gold[f"{name}/dl_indices"]), name
+        check_crowding(p, off, idx, cd, gold[f"{name}/crowding"])
+
+
+def test_reference_fnds_examples(ctx):
+    # tests/multi_objective.cpp:81-145
+    ex = [[0, 7], [1, 5], [2, 3], [4, 2], [7, 1], [10, 0], [2, 6], [4, 4], [10, 2], [6, 6], [9, 5]]
+    fronts, dom_list, dom_count, rank = MO.fast_non_dominated_sorting(ex, ctx)
+    assert fronts == [[0, 1, 2, 3, 4, 5], [6, 7, 8], [9, 10]]
+    assert dom_list == [[], [6, 9, 10], [6, 7, 9, 10], [7, 8, 9, 10], [8, 10], [8], [9], [9, 10], [], [], []]
+    assert dom_count == [0, 0, 0, 0, 0, 0, 2, 2, 3, 5, 5]
+    assert rank == [0, 0, 0, 0, 0, 0, 1, 1, 1, 2, 2]
+    fronts, dom_list, dom_count, rank = MO.fast_non_dominated_sorting([[1, 2, 3], [-2, 3, 7], [-1, -2, -3],
+                                                                       [0, 0, 0]], ctx)
+    assert (fronts, dom_list, dom_count, rank) == ([[1, 2], [3], [0]], [[], [], [0, 3], [0]], [2, 0, 0, 1],
+                                                   [2, 0, 0, 1])
+    fronts, dom_list, dom_count, rank = MO.fast_non_dominated_sorting(np.zeros((4, 0)), ctx)
+    assert (fronts, dom_list, dom_count, rank) == ([[0, 1, 2, 3]], [[], [], [], []], [0, 0, 0, 0], [0, 0, 0, 0])
+    for bad in ([[0, 0, 0]], [[]], []):
+        with pytest.raises(ValueError):
+            MO.fast_non_dominated_sorting(bad, ctx)
+    for bad in ([[1, 3], [3, 42, 3], []], [[3, 4, 5], []]):
+        with pytest.raises(ValueError):
+            MO.fast_non_dominated_sorting(bad, ctx)
+
+
+def test_reference_crowding_examples(ctx):
+    # tests/multi_objective.cpp:147-182
+    inf = math.inf
+    assert MO.crowding_distance([[0, 0], [-1, 1], [2, -2]], ctx).tolist() == [2, inf, inf]
+    assert MO.crowding_distance([[0.25, 0.25], [-1, 1], [2, -2]], ctx).tolist() == [2, inf, inf]
+    assert MO.crowding_distance([[0, 0, 0], [-1, 1, 2], [2, -2, -2]], ctx).tolist() == [3, inf, inf]
+    assert MO.crowding_distance([[0.25, 0.25, 0.25], [-1, 1, 2], [2, -2, -2]], ctx).tolist() == [3, inf, inf]
+    assert MO.crowding_distance([[0, 0], [1, -1], [2, -2], [4, -4]], ctx).tolist() == [inf, 1.0, 1.5, inf]
+    assert MO.crowding_distance([[0, 0], [0, 0]], ctx).tolist() == [inf, inf]
+    for bad in ([], [[], []], [[1, 2]], [[1], [2]], [[2, 3], [3, 4], [2, 4, 5]]):
+        with pytest.raises(ValueError):
+            MO.crowding_distance(bad, ctx)
+
+
+def test_crowding_degenerate_objective_is_nan(ctx, orc):
+    # df == 0 with interior points: 0/0 as in the reference
+    p = np.array([[1.0, 0.0], [1.0, 0.5], [1.0, 1.0], [1.0, 2.0]])
+    got = MO.crowding_distance(p, ctx)
+    want = orc.crowding(p)
+    assert np.array_equal(got, want, equal_nan=True)
+
+
+def test_config4_nested_fronts_full(ctx, orc):
+    p = W.nsga2_points()  # 20000 x 3, 30 layers, 5 % duplicates
+    rank, dc, off, idx, cd = MO.nsga2_survival(p, ctx)
+    want = orc.fnds(p, dom_list=False)
+    assert np.array_equal(rank, want["rank"])
+    assert np.array_equal(dc, want["dom_count"])
+    assert np.array_equal(off, want["front_offsets"])
+    assert np.array_equal(idx, want["front_indices"])
+    wcd = orc.nsga2_crowding(p, want["front_offsets"], want["front_indices"])
+    check_crowding(p, off, idx, cd, wcd)
+
+
+@pytest.mark.parametrize("n,m,seed", [(2, 2, 1), (3, 1, 2), (33, 2, 3), (257, 4, 4), (1000, 3, 5), (700, 7, 6)])
+def test_random_sets(ctx, orc, n, m, seed):
+    rs = np.random.RandomState(seed)
+    p = rs.random_sample((n, m))
+    p[rs.randint(0, n, n // 10)] = p[rs.randint(0, n, n // 10)]  # duplicates
+    rank, dc, off, idx = MO.fnds_arrays(p, ctx)
+    want = orc.fnds(p)
+    assert np.array_equal(rank, want["rank"]) and np.array_equal(dc, want["dom_count"])
+    assert fronts_of(off, idx) == fronts_of(want["front_offsets"], want["front_indices"])
+    doff, didx = MO.dom_list_arrays(p, ctx)
+    assert np.array_equal(doff, want["dl_offsets"]) and np.array_equal(didx, want["dl_indices"])
+
+
+def test_single_objective_front_of_three_raises_in_survival(ctx):
+    # crowding_distance needs two objectives (multi_objective.cpp:290-294)
+    with pytest.raises(ValueError):
+        MO.nsga2_survival(np.array([[1.0], [1.0], [1.0]]), ctx)
+    rank, dc, off, idx, cd = MO.nsga2_survival(np.array([[1.0], [2.0], [3.0]]), ctx)
+    assert rank.tolist() == [0, 1, 2] and cd.tolist() == [math.inf] * 3
