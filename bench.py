@@ -1,0 +1,437 @@
+"""Benchmark of the batch-evaluation hot path.
+
+Headline workload: FP64 fitness + adjoint gradient of pagmo's rosenbrock UDP on
+65536 decision vectors of dimension 1000 (seeded uniform in [-5, 10]); one
+step = one batch. Prints one JSON line:
+
+  value  evals/s with the batch resident in HBM (CUDA events on the launching
+         stream around exactly --steps launches; inputs 524 MB > L2, so no
+         flush between steps)
+  e2e    the same metric through the public host-buffer entry point
+         (pgx_batch_gradient) from pinned host memory, uploads and downloads
+         inside the timed region
+  roofline  FP64 pipe of the rosenbrock kernel (peak measured in-run by a DFMA
+         probe; MEASURED_PEAKS.json has no FP64 figure) plus its HBM fraction
+  cpu_baseline  the reference's CPU path (compiled reference where present,
+         else the oracle's restatement of thread_bfe + gradient) on the host
+  secondary  the other kernels of the path (rastrigin, lennard_jones, NSGA-II
+         survival) measured the same way
+
+--impl reference times the reference's CPU implementation of the same step
+with every host thread. Multi-GPU (torchrun): every rank evaluates its own
+batch (replicas, weak scaling); value = all ranks' evals / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_ROWS, DIM = 65536, 1000
+METRIC = "FP64 fitness+grad evals/s"
+UNIT = "evals/s"
+
+# FP64 flops per rosenbrock element in the implemented formulation
+# (FMA = 2): fitness t, sum t^2, (2x-2)^2 accumulate; gradient 2x, 2x-2,
+# t_prev - 2x t, 200 b + c -> 5 FMA + 2 add/sub = 12.
+ROS_FG_FLOPS_PER_ELEM = 12
+ROS_F_FLOPS_PER_ELEM = 7
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="pgx", choices=["pgx", "reference"])
+    ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--rows", type=int, default=N_ROWS, help="batch rows (smaller cases for profiling)")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self._t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ helpers
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            pass
+    return {}
+
+
+def ncu_traffic(key: str):
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get(key)
+        except ValueError:
+            return None
+    return None
+
+
+def cpu_reference_step_fn(kind: int, param: int, x: np.ndarray, grad: bool, threads: int):
+    """A callable evaluating x with the reference's CPU path and its kind."""
+    import oracle
+
+    ref = oracle.reference()
+    orc = oracle.oracle()
+    if ref is not None:
+        os.environ["PGX_REF_THREADS"] = str(threads)
+
+        def step():
+            f, _ = ref.thread_bfe(kind, param, x)
+            g = orc.batch_gradient(kind, param, x, threads) if grad else None
+            return f, g
+        return step, "reference"
+
+    def step():
+        f = orc.batch_fitness(kind, param, x, threads)
+        g = orc.batch_gradient(kind, param, x, threads) if grad else None
+        return f, g
+    return step, "port"
+
+
+def time_cpu(step, budget_s: float = 8.0, max_reps: int = 20) -> float:
+    step()
+    ts = []
+    t_start = time.perf_counter()
+    while len(ts) < max_reps and (time.perf_counter() - t_start) < budget_s:
+        t0 = time.perf_counter()
+        step()
+        ts.append(time.perf_counter() - t0)
+    return float(np.median(ts))
+
+
+# ------------------------------------------------------------------ reference arm
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from pagmo2_gb300 import workloads as W
+
+    threads = os.cpu_count() or 1
+    x = W.rosenbrock_batch(N_ROWS, DIM)
+    # each step evaluates a bounded sample of the batch so the run stays short
+    sample = N_ROWS
+    step, kind = cpu_reference_step_fn(2, DIM, x[:sample], True, threads)
+    for _ in range(max(0, args.warmup)):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = (time.perf_counter() - t0) / max(1, args.steps)
+    v = sample / dt
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mt19937)",
+            "config": {"workload": f"rosenbrock fitness+gradient, {N_ROWS} x {DIM}, FP64", "batch": N_ROWS,
+                       "dim": DIM, "parallelism": "host threads"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": f"{sample} rows x {DIM} per step, fitness (thread_bfe) + gradient"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    ws, rank, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    from pagmo2_gb300 import _native as N
+    from pagmo2_gb300 import workloads as W
+
+    ctx = N.Context(local)
+    L = N.lib()
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+
+    # ---- headline: rosenbrock f+g, device resident
+    rows_n = args.rows
+    x = W.rosenbrock_batch(rows_n, DIM, seed=2 + rank)
+    dx = torch.from_numpy(x).cuda()
+    df = torch.empty(rows_n, dtype=torch.float64, device="cuda")
+    dg = torch.empty((rows_n, DIM), dtype=torch.float64, device="cuda")
+
+    def launch():
+        N.check(L.pgx_batch_eval_device(ctx.handle, N.ROSENBROCK, DIM, dx.data_ptr(), rows_n, df.data_ptr(),
+                                        dg.data_ptr(), sp))
+
+    for _ in range(max(3, args.warmup)):
+        launch()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = ctx.launches
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        launch()
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    gpu_launches = ctx.launches - launches0
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * rows_n / (ms * 1e-3)
+
+    # ---- FP64 / HBM roofline of the rosenbrock kernel
+    fp = C.c_double()
+    N.check(L.pgx_measure_fp64_peak(ctx.handle, C.byref(fp)))
+    fp64_peak_tflops = fp.value / 1e3
+    flops = rows_n * ((DIM - 1) * ROS_FG_FLOPS_PER_ELEM + 2)
+    achieved_tflops = flops / (ms * 1e-3) / 1e12
+    alg_bytes = rows_n * (DIM * 8 * 2 + 8)
+    peaks = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs")
+    hbm_src = "MEASURED_PEAKS.json hbm_gbs" if hbm_peak else "fallback 6800 GB/s"
+    hbm_peak = hbm_peak or 6800.0
+    achieved_gbs = alg_bytes / (ms * 1e-3) / 1e9
+    traffic = ncu_traffic("rosenbrock_fg_65536x1000")
+    roofline = {"bound": "fp64", "achieved": achieved_tflops, "peak": fp64_peak_tflops, "unit": "TFLOP/s",
+                "frac": achieved_tflops / fp64_peak_tflops, "traffic": traffic,
+                "kernel": "rosenbrock_kernel<32,true>",
+                "peak_source": "in-run DFMA throughput probe (pgx_measure_fp64_peak); no FP64 figure in "
+                               "MEASURED_PEAKS.json",
+                "algorithmic": f"{ROS_FG_FLOPS_PER_ELEM} flops/element (FMA=2), {alg_bytes} bytes per launch",
+                "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
+                        "peak_source": hbm_src}}
+
+    # ---- e2e through the public host-buffer entry point, pinned buffers
+    e2e, parity = None, None
+    if not args.no_e2e:
+        hx = torch.from_numpy(x).pin_memory()
+        hf = torch.empty(rows_n, dtype=torch.float64).pin_memory()
+        hg = torch.empty((rows_n, DIM), dtype=torch.float64).pin_memory()
+
+        def e2e_step():
+            N.check(L.pgx_batch_gradient(ctx.handle, N.ROSENBROCK, DIM, hx.data_ptr(), rows_n, hf.data_ptr(),
+                                         hg.data_ptr()))
+
+        for _ in range(2):
+            e2e_step()
+        e2e_steps = max(3, min(args.steps, 10))
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        if dist:
+            t = torch.tensor([e2e_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": ws * rows_n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": rows_n * DIM * 8,
+               "d2h_bytes_per_step": rows_n * DIM * 8 + rows_n * 8, "ms_per_step": e2e_s * 1e3,
+               "entry_point": "pgx_batch_gradient (host buffers, pinned)"}
+
+    # parity spot-check of this run's output against the oracle
+    if rank == 0 and e2e is not None:
+        try:
+            import oracle
+
+            rows = np.arange(0, rows_n, max(1, rows_n // 32))
+            fl, fs = oracle.oracle().batch_fitness_ld(N.ROSENBROCK, DIM, x[rows])
+            gl, gs = oracle.oracle().batch_gradient_ld(N.ROSENBROCK, DIM, x[rows])
+            fo = hf.numpy()[rows]
+            go = hg.numpy()[rows]
+            parity = {"rows_checked": int(rows.size),
+                      "max_rel_err_fitness": float(np.max(np.abs(fo - fl) / np.abs(fl))),
+                      "max_scaled_err_gradient": float(np.max(np.abs(go - gl) / gs))}
+        except Exception as e:  # the checker is optional; the number is not
+            parity = {"error": str(e)}
+
+    secondary = {}
+    if rank == 0 and not args.no_secondary:
+        secondary = run_secondary(ctx, L, N, W, stream, fp64_peak_tflops)
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        sample = 8192
+        step, kind = cpu_reference_step_fn(N.ROSENBROCK, DIM, x[:sample], True, threads)
+        dt = time_cpu(step)
+        cpu = {"value": sample / dt, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": f"{sample} of the {N_ROWS} rows, fitness (thread_bfe) + gradient, median of repeats"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic: seeded mt19937 uniform in [-5, 10] (rosenbrock bounds)",
+                "config": {"workload": f"rosenbrock fitness+gradient, {rows_n} x {DIM}, FP64", "batch": rows_n,
+                           "dim": DIM, "parallelism": "replicas" if ws > 1 else "single GPU",
+                           "l2": "inputs 524 MB > 129 MB L2 (no flush)"},
+                "e2e": e2e, "gpu_launches": gpu_launches, "clocks": clk, "roofline": roofline,
+                "cpu_baseline": cpu, "parity": parity, "secondary": secondary}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops) -> dict:
+    """The other kernels of the path, device resident, CUDA-event timed."""
+    import torch
+
+    out = {}
+    sp = stream.cuda_stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # 256 MB > L2
+
+    def timed(fn, reps=10, flush_l2=True):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            if flush_l2:
+                flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    def fitness_case(name, kind, param, x, grad):
+        n, nx = x.shape
+        dx = torch.from_numpy(x).cuda()
+        df = torch.empty(n, dtype=torch.float64, device="cuda")
+        dg = torch.empty((n, nx), dtype=torch.float64, device="cuda") if grad else None
+
+        def fn():
+            N.check(L.pgx_batch_eval_device(ctx.handle, kind, param, dx.data_ptr(), n, df.data_ptr(),
+                                            dg.data_ptr() if grad else None, sp))
+        ms = timed(fn)
+        bytes_ = n * nx * 8 * (2 if grad else 1) + n * 8
+        out[name] = {"evals_per_s": n / (ms * 1e-3), "ms": ms, "hbm_gbs": bytes_ / (ms * 1e-3) / 1e9}
+
+    fitness_case("rastrigin_fg_4096x50", N.RASTRIGIN, 50, W.rastrigin_batch(), True)
+    fitness_case("rastrigin_f_4096x50", N.RASTRIGIN, 50, W.rastrigin_batch(), False)
+    fitness_case("rastrigin_fg_1048576x50", N.RASTRIGIN, 50, W.rastrigin_batch(1 << 20, 50), True)
+    fitness_case("rosenbrock_f_65536x1000", N.ROSENBROCK, 1000, W.rosenbrock_batch(), False)
+    lj = W.lj_batch()
+    fitness_case("lj_fg_16384x150", N.LENNARD_JONES, 150, lj, True)
+    fitness_case("lj_f_16384x150", N.LENNARD_JONES, 150, lj, False)
+    pairs = 16384 * 150 * 149 // 2
+    for k in ("lj_fg_16384x150", "lj_f_16384x150"):
+        out[k]["pair_evals_per_s"] = pairs / (out[k]["ms"] * 1e-3)
+
+    # NSGA-II survival, device resident
+    p = W.nsga2_points()
+    n, m = p.shape
+    dp = torch.from_numpy(p).cuda()
+    i32 = lambda k: torch.empty(k, dtype=torch.int32, device="cuda")  # noqa: E731
+    rank, dc, off, idx, nf = i32(n), i32(n), i32(n + 1), i32(n), i32(1)
+    cd = torch.empty(n, dtype=torch.float64, device="cuda")
+
+    def surv():
+        N.check(L.pgx_nsga2_survival_device(ctx.handle, dp.data_ptr(), n, m, rank.data_ptr(), dc.data_ptr(),
+                                            off.data_ptr(), idx.data_ptr(), nf.data_ptr(), cd.data_ptr(), sp))
+    ms = timed(surv, reps=10, flush_l2=False)
+    out["nsga2_survival_20000x3"] = {"ms": ms, "fronts": int(nf.item()),
+                                     "pair_tests_per_s": n * n / (ms * 1e-3)}
+    return out
+
+
+if __name__ == "__main__":
+    main()

@@ -22,8 +22,8 @@
  *    pagmo's std::invalid_argument. There is no CPU fallback: without a usable
  *    GB300 every compute entry point fails with PGX_ERR_CUDA/PGX_ERR_NODEVICE.
  *  - Host-buffer entry points are synchronous. *_device entry points take
- *    device pointers and a cudaStream_t passed as void* (NULL = the context's
- *    own stream) and are asynchronous on that stream.
+ *    device pointers and a cudaStream_t passed as void* (NULL = the legacy
+ *    default stream, as in CUDA) and are asynchronous on that stream.
  *  - A context is bound to one device. Calls on one context are serialised
  *    by an internal lock, so island threads may share it.
  */
@@ -133,9 +133,11 @@ PGX_API int pgx_fnds_dom_list(pgx_context *ctx, const double *points, uint64_t n
                       int32_t *dl_indices, uint64_t capacity, uint64_t *dl_total);
 
 /* crowding_distance of one non-dominated front (src/utils/multi_objective.cpp:280-315).
-   n >= 2 and m >= 2 or PGX_ERR_INVALID. Ties between equal objective values
-   are broken by position in the input (the reference's std::sort leaves tie
-   order unspecified); untied points are bit-exact with the reference. */
+   n >= 2 and m >= 2 or PGX_ERR_INVALID. Equal objective values keep the
+   order they had along the previous objective (the first objective: input
+   order), which is what the reference's loop gives with a stable sort; the
+   reference's std::sort leaves the order of ties unspecified. Points whose
+   values are not tied are bit-exact with the reference. */
 PGX_API int pgx_crowding_distance(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, double *out);
 
 /* NSGA-II survival block (src/algorithms/nsga2.cpp:183-206): fnds, then the
@@ -150,6 +152,12 @@ PGX_API int pgx_nsga2_survival(pgx_context *ctx, const double *points, uint64_t 
 PGX_API int pgx_nsga2_survival_device(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, int32_t *d_rank,
                               int32_t *d_dom_count, int32_t *d_front_offsets, int32_t *d_front_indices,
                               int32_t *d_n_fronts, double *d_crowding, void *stream);
+
+/* ------------------------------------------------------------ measurement */
+
+/* FP64 FMA throughput of the device in GFLOP/s (FMA = 2 flops), measured by a
+   short DFMA-chain kernel: the denominator of the FP64 roofline. */
+PGX_API int pgx_measure_fp64_peak(pgx_context *ctx, double *gflops);
 
 #ifdef __cplusplus
 }

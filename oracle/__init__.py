@@ -63,6 +63,8 @@ class _Oracle:
         h.orc_fnds.argtypes = [_vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u64]
         h.orc_crowding.argtypes = [_vp, _u64, _u64, _vp]
         h.orc_nsga2_crowding.argtypes = [_vp, _u64, _u64, _vp, _vp, _u64, _vp]
+        h.orc_crowding_ex.argtypes = [_vp, _u64, _u64, C.c_int, _vp]
+        h.orc_nsga2_crowding_ex.argtypes = [_vp, _u64, _u64, _vp, _vp, _u64, C.c_int, _vp]
 
     def _chk(self, st):
         if st != 0:
@@ -127,20 +129,21 @@ class _Oracle:
             out["dl_indices"] = dli[:int(dlo[n])].astype(np.int64)
         return out
 
-    def crowding(self, pts):
+    def crowding(self, pts, stable=False):
+        """crowding_distance; stable=True keeps tied values in input order."""
         p = np.ascontiguousarray(pts, dtype=np.float64)
         n, m = p.shape
         out = np.empty(n)
-        self._chk(self.h.orc_crowding(_p(p), n, m, _p(out)))
+        self._chk(self.h.orc_crowding_ex(_p(p), n, m, int(stable), _p(out)))
         return out
 
-    def nsga2_crowding(self, pts, front_offsets, front_indices):
+    def nsga2_crowding(self, pts, front_offsets, front_indices, stable=False):
         p = np.ascontiguousarray(pts, dtype=np.float64)
         n, m = p.shape
         off = np.ascontiguousarray(front_offsets, dtype=np.uint64)
         idx = np.ascontiguousarray(front_indices, dtype=np.uint64)
         out = np.empty(n)
-        self._chk(self.h.orc_nsga2_crowding(_p(p), n, m, _p(off), _p(idx), off.size - 1, _p(out)))
+        self._chk(self.h.orc_nsga2_crowding_ex(_p(p), n, m, _p(off), _p(idx), off.size - 1, int(stable), _p(out)))
         return out
 
 

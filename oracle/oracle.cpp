@@ -497,6 +497,13 @@ int orc_fnds(const double *pts, uint64_t n, uint64_t m, uint64_t *rank, uint64_t
 // with the same standard library the order of tied values is the reference's.
 int orc_crowding(const double *pts, uint64_t n, uint64_t m, double *out)
 {
+    return orc_crowding_ex(pts, n, m, 0, out);
+}
+
+// stable != 0: std::stable_sort instead of std::sort, i.e. equal objective
+// values keep their order in the front (the GPU's documented tie rule).
+int orc_crowding_ex(const double *pts, uint64_t n, uint64_t m, int stable, double *out)
+{
     if (n < 2u) {
         g_err = "A non dominated front must contain at least two points: " + std::to_string(n) + " detected.";
         return 1;
@@ -510,8 +517,11 @@ int orc_crowding(const double *pts, uint64_t n, uint64_t m, double *out)
     std::iota(idx.begin(), idx.end(), uint64_t(0));
     std::fill(out, out + n, 0.);
     for (uint64_t i = 0; i < m; ++i) {
-        std::sort(idx.begin(), idx.end(),
-                  [i, m, pts](uint64_t a, uint64_t b) { return lt_f(pts[a * m + i], pts[b * m + i]); });
+        const auto cmp = [i, m, pts](uint64_t a, uint64_t b) { return lt_f(pts[a * m + i], pts[b * m + i]); };
+        if (stable)
+            std::stable_sort(idx.begin(), idx.end(), cmp);
+        else
+            std::sort(idx.begin(), idx.end(), cmp);
         out[idx[0]] = std::numeric_limits<double>::infinity();
         out[idx[n - 1u]] = std::numeric_limits<double>::infinity();
         const double df = pts[idx[n - 1u] * m + i] - pts[idx[0] * m + i];
@@ -526,6 +536,12 @@ int orc_crowding(const double *pts, uint64_t n, uint64_t m, double *out)
 int orc_nsga2_crowding(const double *pts, uint64_t n, uint64_t m, const uint64_t *front_offsets,
                        const uint64_t *front_indices, uint64_t n_fronts, double *out)
 {
+    return orc_nsga2_crowding_ex(pts, n, m, front_offsets, front_indices, n_fronts, 0, out);
+}
+
+int orc_nsga2_crowding_ex(const double *pts, uint64_t n, uint64_t m, const uint64_t *front_offsets,
+                          const uint64_t *front_indices, uint64_t n_fronts, int stable, double *out)
+{
     std::vector<double> buf, cd;
     for (uint64_t f = 0; f < n_fronts; ++f) {
         const uint64_t b = front_offsets[f], e = front_offsets[f + 1];
@@ -538,7 +554,7 @@ int orc_nsga2_crowding(const double *pts, uint64_t n, uint64_t m, const uint64_t
         cd.resize(k);
         for (uint64_t t = 0; t < k; ++t)
             std::memcpy(buf.data() + t * m, pts + front_indices[b + t] * m, m * sizeof(double));
-        const int st = orc_crowding(buf.data(), k, m, cd.data());
+        const int st = orc_crowding_ex(buf.data(), k, m, stable, cd.data());
         if (st) return st;
         for (uint64_t t = 0; t < k; ++t) out[front_indices[b + t]] = cd[t];
     }

@@ -77,6 +77,11 @@ int orc_crowding(const double *pts, uint64_t n, uint64_t m, double *out);
    fronts of size 1 or 2 get +inf. Needs the fronts from orc_fnds. */
 int orc_nsga2_crowding(const double *pts, uint64_t n, uint64_t m, const uint64_t *front_offsets,
                        const uint64_t *front_indices, uint64_t n_fronts, double *out);
+/* Same with stable != 0: ties between equal objective values keep their
+   order in the front (std::stable_sort), the tie rule of the GPU kernels. */
+int orc_crowding_ex(const double *pts, uint64_t n, uint64_t m, int stable, double *out);
+int orc_nsga2_crowding_ex(const double *pts, uint64_t n, uint64_t m, const uint64_t *front_offsets,
+                          const uint64_t *front_indices, uint64_t n_fronts, int stable, double *out);
 
 #ifdef __cplusplus
 }

@@ -6,13 +6,13 @@ plugin interface for the batch-fitness path:
 
   problems:         rastrigin, rosenbrock, lennard_jones (GPU UDPs with
                     batch_fitness, gradient and batch_gradient)
-  bfe:              gpu_bfe (the UDBFE) and a bfe/problem pair reproducing
+  batch_evaluators: gpu_bfe (the UDBFE) and a bfe/problem pair reproducing
                     pagmo's input/output checks and fevals accounting
   multi_objective:  fast_non_dominated_sorting, crowding_distance,
                     nsga2_survival
   workloads:        seeded synthetic inputs
 """
 from ._native import Context, default_context  # noqa: F401
-from .bfe import bfe, gpu_bfe, problem  # noqa: F401
+from .batch_evaluators import bfe, gpu_bfe, problem  # noqa: F401
 from .multi_objective import crowding_distance, fast_non_dominated_sorting, nsga2_survival  # noqa: F401
 from .problems import lennard_jones, rastrigin, rosenbrock  # noqa: F401

@@ -37,6 +37,7 @@ SIGNATURES = {
     "pgx_crowding_distance": (C.c_int, [_vp, _vp, _u64, _u64, _vp]),
     "pgx_nsga2_survival": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp]),
     "pgx_nsga2_survival_device": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "pgx_measure_fp64_peak": (C.c_int, [_vp, C.POINTER(C.c_double)]),
 }
 
 _lib = None

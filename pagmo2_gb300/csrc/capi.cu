@@ -218,7 +218,7 @@ int host_survival(pgx_context *ctx, const double *points, uint64_t n, uint64_t m
         PGX_CUDA(cudaMemcpyAsync(front_offsets, d.front_offsets, (n + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     if (crowding) PGX_CUDA(cudaMemcpyAsync(crowding, d.crowding, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     PGX_CUDA(cudaStreamSynchronize(s));
-    PGX_TRY(survival_status(ctx));
+    PGX_TRY(read_survival_status(ctx, n, m));
     if (n_fronts) *n_fronts = nf;
     if (crowding && m < 2u) {
         // crowding_distance throws for fewer than two objectives
@@ -300,7 +300,7 @@ void pgx_context_destroy(pgx_context *ctx)
         if (s) cudaStreamSynchronize(s);
     for (auto &ev : ctx->chunk_ev)
         if (ev) cudaEventDestroy(ev);
-    for (pgx::dbuf *b : {&ctx->d_in, &ctx->d_out, &ctx->d_grad, &ctx->s_points, &ctx->s_keys, &ctx->s_dommat,
+    for (pgx::dbuf *b : {&ctx->d_in, &ctx->d_out, &ctx->d_grad, &ctx->s_points,
                          &ctx->s_state, &ctx->s_outs, &ctx->s_crowd})
         b->release();
     for (cudaStream_t s : {ctx->stream, ctx->h2d, ctx->d2h})
@@ -368,7 +368,7 @@ int pgx_batch_eval_device(pgx_context *ctx, int kind, uint64_t param, const doub
     PGX_CHECK(d_dvs != nullptr, PGX_ERR_INVALID, "null decision vector buffer");
     std::lock_guard<std::mutex> g(ctx->lock);
     PGX_TRY(use_device(ctx));
-    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     uint64_t l = 0;
     PGX_TRY(launch_eval(kind, param, nx, d_dvs, n_dvs, d_fvs, d_grads, s, ctx->num_sms, &l));
     ctx->launches += l;
@@ -403,7 +403,7 @@ int pgx_nsga2_survival_device(pgx_context *ctx, const double *d_points, uint64_t
               "null output buffer");
     std::lock_guard<std::mutex> g(ctx->lock);
     PGX_TRY(use_device(ctx));
-    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     survival_out o;
     o.rank = d_rank;
     o.dom_count = d_dom_count;
@@ -465,7 +465,7 @@ int pgx_fnds_dom_list(pgx_context *ctx, const double *points, uint64_t n, uint64
     PGX_TRY(ctx->d_out.ensure((n + 1) * sizeof(int64_t)));
     PGX_TRY(ctx->d_grad.ensure(total * sizeof(int32_t)));
     PGX_CUDA(cudaMemcpyAsync(ctx->d_out.ptr, dl_offsets, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
-    PGX_TRY(extract_dom_list(ctx, n, ctx->d_out.as<int64_t>(), ctx->d_grad.as<int32_t>(), s));
+    PGX_TRY(extract_dom_list(ctx, n, m, ctx->d_out.as<int64_t>(), ctx->d_grad.as<int32_t>(), s));
     PGX_CUDA(cudaMemcpyAsync(dl_indices, ctx->d_grad.ptr, total * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     PGX_CUDA(cudaStreamSynchronize(s));
     return PGX_OK;

@@ -84,8 +84,8 @@ struct pgx_context {
     // device buffers of the host-buffer calls
     pgx::dbuf d_in, d_out, d_grad;
     std::vector<cudaEvent_t> chunk_ev;
-    // survival scratch
-    pgx::dbuf s_points, s_keys, s_dommat, s_state, s_outs, s_crowd;
+    // survival: inputs/outputs of host calls, the scratch of a pass, small outputs
+    pgx::dbuf s_points, s_state, s_outs, s_crowd;
 };
 
 namespace pgx
@@ -121,15 +121,17 @@ int launch_survival(pgx_context *ctx, const double *d_points, uint64_t n, uint64
 int launch_crowding_single(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, double *d_out,
                            cudaStream_t stream);
 
-// Reads the device status word of the last survival launch (after a stream
-// synchronisation): PGX_ERR_TIMEOUT when a grid barrier gave up.
-int survival_status(pgx_context *ctx);
+// Reads the device status word of the last survival pass of shape (n, m) on
+// this context (after a stream synchronisation): PGX_ERR_TIMEOUT when a grid
+// barrier gave up.
+int read_survival_status(pgx_context *ctx, uint64_t n, uint64_t m);
 
 // dom_list support: builds the "dominates" bit matrix (row i: the points i
 // dominates) and per-row counts (device int64[n], owned by the context), then
 // writes each row's set bits, ascending, at the given CSR offsets.
 int build_dominates_rows(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, int64_t **d_row_count,
                          cudaStream_t stream);
-int extract_dom_list(pgx_context *ctx, uint64_t n, const int64_t *d_offsets, int32_t *d_indices, cudaStream_t stream);
+int extract_dom_list(pgx_context *ctx, uint64_t n, uint64_t m, const int64_t *d_offsets, int32_t *d_indices,
+                     cudaStream_t stream);
 
 } // namespace pgx

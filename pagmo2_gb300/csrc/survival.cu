@@ -167,94 +167,119 @@ __device__ bool grid_sync(peel_state *st)
     return *reinterpret_cast<volatile int *>(&st->err) == 0;
 }
 
-__device__ __forceinline__ int warp_max(int v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
-    return v;
-}
+constexpr int kTile = 2048; // (key, index) pairs per shared-memory tile
 
-// Front peeling. masks[0..2*W8): the bit sets of the current and the next
-// front, alternating by iteration parity. rem[W8]: unassigned points.
+// Front peeling, one front per iteration, two grid barriers per front.
+//
+// Phase A: every unassigned point j whose row of Dt has no unassigned
+// dominator joins front k. Warps take 8-candidate slices of the rem bit set
+// and scan each candidate's row cooperatively (128 words per step, early
+// exit). A member's ordering key is the highest position, in front k-1, of
+// one of its dominators: a reverse scan over front k-1's positions (32 at a
+// time, ballot) stops at the first hit.
+// Phase C: the position of a member is the number of members with a smaller
+// (key, index), counted against shared-memory tiles; members are written to
+// front_indices, ranked, and cleared from rem.
 __global__ void __launch_bounds__(256) peel_kernel(const uint32_t *__restrict__ Dt, uint32_t n, uint32_t W,
-                                                   uint32_t W8, uint32_t *rem, uint32_t *masks, int32_t *pos,
-                                                   int32_t *list, int32_t *keyv, int32_t *rank, int32_t *front_offsets,
-                                                   int32_t *front_indices, peel_state *st)
+                                                   uint32_t W8, uint32_t *rem, int32_t *list, int32_t *keyv,
+                                                   int32_t *rank, int32_t *front_offsets, int32_t *front_indices,
+                                                   peel_state *st)
 {
+    extern __shared__ int32_t sh[]; // kTile keys, then kTile indices
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nthreads = gridDim.x * blockDim.x;
     const uint32_t gwarp = tid >> 5, nwarps = nthreads >> 5;
-    int offset = 0;
+    int off = 0, off_prev = 0, size_prev = 0;
     int k = 0;
     for (;; ++k) {
-        uint32_t *next = masks + static_cast<size_t>(k & 1) * W8;
-        uint32_t *cur = masks + static_cast<size_t>((k + 1) & 1) * W8;
         int *cnt = &st->counts[k & 1];
-        // Phase A: members of front k.
-        for (uint32_t j = gwarp; j < n; j += nwarps) {
-            if (!((__ldcg(rem + (j >> 5)) >> (j & 31u)) & 1u)) continue;
-            const uint32_t *row = Dt + static_cast<uint64_t>(j) * W8;
-            bool hit = false;
-            for (uint32_t b = 0; b < W; b += 32u) {
-                const uint32_t w = b + lane;
-                const uint32_t v = w < W ? (__ldg(row + w) & __ldcg(rem + w)) : 0u;
-                if (__any_sync(kFull, v != 0u)) {
-                    hit = true;
-                    break;
+        // ---- Phase A
+        const uint32_t tasks = W * 4u;
+        for (uint32_t t = gwarp; t < tasks; t += nwarps) {
+            const uint32_t w = t >> 2, sub = t & 3u;
+            uint32_t cand = (__ldcg(rem + w) >> (sub * 8u)) & 0xffu;
+            while (cand) {
+                const uint32_t b = static_cast<uint32_t>(__ffs(cand) - 1);
+                cand &= cand - 1u;
+                const uint32_t j = w * 32u + sub * 8u + b;
+                const uint32_t *row = Dt + static_cast<uint64_t>(j) * W8;
+                bool hit = false;
+                for (uint32_t base = 0; base < W; base += 128u) {
+                    uint32_t v = 0u;
+#pragma unroll
+                    for (uint32_t u = 0; u < 4u; ++u) {
+                        const uint32_t ww = base + u * 32u + lane;
+                        if (ww < W) v |= __ldg(row + ww) & __ldcg(rem + ww);
+                    }
+                    if (__any_sync(kFull, v != 0u)) {
+                        hit = true;
+                        break;
+                    }
                 }
-            }
-            if (!hit && lane == 0) {
-                const int s = atomicAdd(cnt, 1);
-                list[s] = static_cast<int32_t>(j);
-                atomicOr(next + (j >> 5), 1u << (j & 31u));
+                if (hit) continue;
+                int key = 0;
+                if (k > 0) {
+                    key = -1;
+                    for (int top = size_prev - 1; top >= 0; top -= 32) {
+                        const int p = top - static_cast<int>(lane);
+                        bool h = false;
+                        if (p >= 0) {
+                            const uint32_t d = static_cast<uint32_t>(__ldcg(front_indices + off_prev + p));
+                            h = (__ldg(row + (d >> 5)) >> (d & 31u)) & 1u;
+                        }
+                        const unsigned bal = __ballot_sync(kFull, h);
+                        if (bal) {
+                            key = top - (__ffs(bal) - 1);
+                            break;
+                        }
+                    }
+                }
+                if (lane == 0) {
+                    const int s = atomicAdd(cnt, 1);
+                    list[s] = static_cast<int32_t>(j);
+                    keyv[s] = key;
+                }
             }
         }
         if (!grid_sync(st)) return;
         const int L = *reinterpret_cast<volatile int *>(cnt);
         if (L == 0) break;
-        // Phase B: retire front k from rem; ordering key of each member.
-        for (uint32_t w = tid; w < W; w += nthreads) rem[w] = __ldcg(rem + w) & ~__ldcg(next + w);
-        if (k == 0) {
-            for (uint32_t s = tid; s < static_cast<uint32_t>(L); s += nthreads) keyv[s] = 0;
-        } else {
-            for (uint32_t s = gwarp; s < static_cast<uint32_t>(L); s += nwarps) {
-                const uint32_t q = static_cast<uint32_t>(__ldcg(list + s));
-                const uint32_t *row = Dt + static_cast<uint64_t>(q) * W8;
-                int best = -1;
-                for (uint32_t w = lane; w < W; w += 32u) {
-                    uint32_t bits = __ldg(row + w) & __ldcg(cur + w);
-                    while (bits) {
-                        const int t = __ffs(bits) - 1;
-                        bits &= bits - 1u;
-                        best = max(best, __ldcg(pos + w * 32u + t));
+        // ---- Phase C (the loop bound is uniform per block: __syncthreads is safe)
+        for (uint32_t s0 = blockIdx.x * blockDim.x; s0 < static_cast<uint32_t>(L); s0 += nthreads) {
+            const uint32_t s = s0 + threadIdx.x;
+            const bool act = s < static_cast<uint32_t>(L);
+            const int q = act ? __ldcg(list + s) : 0;
+            const int kq = act ? __ldcg(keyv + s) : 0;
+            int p = 0;
+            for (int t0 = 0; t0 < L; t0 += kTile) {
+                const int lim = min(kTile, L - t0);
+                __syncthreads();
+                for (int t = threadIdx.x; t < lim; t += blockDim.x) {
+                    sh[t] = __ldcg(keyv + t0 + t);
+                    sh[kTile + t] = __ldcg(list + t0 + t);
+                }
+                __syncthreads();
+                if (act) {
+                    for (int t = 0; t < lim; ++t) {
+                        const int kt = sh[t], qt = sh[kTile + t];
+                        p += (kt < kq) | ((kt == kq) & (qt < q));
                     }
                 }
-                best = warp_max(best);
-                if (lane == 0) keyv[s] = best;
+            }
+            if (act) {
+                front_indices[off + p] = q;
+                rank[q] = k;
+                atomicAnd(rem + (q >> 5), ~(1u << (q & 31)));
             }
         }
-        if (!grid_sync(st)) return;
-        // Phase C: position of each member = rank of (key, index) in the front.
-        for (uint32_t s = tid; s < static_cast<uint32_t>(L); s += nthreads) {
-            const int q = __ldcg(list + s);
-            const int kq = __ldcg(keyv + s);
-            int p = 0;
-            for (int t = 0; t < L; ++t) {
-                const int kt = __ldcg(keyv + t);
-                const int qt = __ldcg(list + t);
-                p += (kt < kq) || (kt == kq && qt < q);
-            }
-            front_indices[offset + p] = q;
-            rank[q] = k;
-            pos[q] = p;
-        }
-        for (uint32_t w = tid; w < W8; w += nthreads) cur[w] = 0u;
         if (tid == 0) {
             st->counts[(k + 1) & 1] = 0;
-            front_offsets[k + 1] = offset + L;
+            front_offsets[k + 1] = off + L;
         }
-        offset += L;
+        off_prev = off;
+        size_prev = L;
+        off += L;
         if (!grid_sync(st)) return;
     }
     if (tid == 0) {
@@ -263,37 +288,70 @@ __global__ void __launch_bounds__(256) peel_kernel(const uint32_t *__restrict__ 
     }
 }
 
-// Sorted position of every point of a front of size >= 3 along each objective;
-// sorted[k*n + off + p] = point. Ties keep front order.
-__global__ void crowding_rank_kernel(const long long *__restrict__ keys, uint32_t n, uint32_t m,
-                                     const int32_t *__restrict__ rank, const int32_t *__restrict__ pos,
-                                     const int32_t *__restrict__ front_offsets,
-                                     const int32_t *__restrict__ front_indices, int32_t *__restrict__ sorted,
-                                     int32_t *__restrict__ inv_pos)
+// Sorted position, along objective k, of every point of every front of
+// three or more points. The reference sorts one index vector objective after
+// objective (multi_objective.cpp:301-306), so ties along objective k keep the
+// order of objective k-1: the tie-break is the point's position in objective
+// k-1's order (its position in the front for k = 0), which is what a stable
+// sort of that vector yields. Tasks = (front, 256-point chunk), dealt
+// round-robin to blocks; each thread counts the front members before its
+// point against shared-memory tiles of (key, tie-break).
+// Writes sorted[k*n + off + p] = point and inv_pos[k*n + point] = p.
+__global__ void __launch_bounds__(256) crowding_rank_kernel(const long long *__restrict__ keys, uint32_t n, uint32_t k,
+                                                            const int32_t *__restrict__ front_offsets,
+                                                            const int32_t *__restrict__ front_indices,
+                                                            const int32_t *__restrict__ n_fronts,
+                                                            int32_t *__restrict__ sorted, int32_t *__restrict__ inv_pos)
 {
-    const uint64_t total = static_cast<uint64_t>(n) * m;
-    for (uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < total;
-         t += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
-        const uint32_t k = static_cast<uint32_t>(t / n), q = static_cast<uint32_t>(t - static_cast<uint64_t>(k) * n);
-        const int f = rank[q];
-        const int off = front_offsets[f], end = front_offsets[f + 1];
-        if (end - off < 3) continue;
-        const long long *kk = keys + static_cast<uint64_t>(k) * n;
-        const long long kq = kk[q];
-        const int pq = pos[q];
-        int p = 0;
-        for (int s = off; s < end; ++s) {
-            const long long v = kk[front_indices[s]];
-            p += (v < kq) || (v == kq && (s - off) < pq);
+    __shared__ long long tk[kTile];
+    __shared__ int32_t tt[kTile];
+    const int nf = *n_fronts;
+    const uint32_t G = gridDim.x;
+    const long long *kk = keys + static_cast<uint64_t>(k) * n;
+    const int32_t *prev = k > 0 ? inv_pos + static_cast<uint64_t>(k - 1) * n : nullptr;
+    uint64_t base = 0; // tasks dealt so far
+    for (int f = 0; f < nf; ++f) {
+        const int off = front_offsets[f], sz = front_offsets[f + 1] - off;
+        if (sz < 3) continue;
+        const uint32_t tasks = (static_cast<uint32_t>(sz) + 255u) / 256u;
+        // first task of this front owned by this block under round-robin dealing
+        uint32_t t = static_cast<uint32_t>((blockIdx.x + G - static_cast<uint32_t>(base % G)) % G);
+        for (; t < tasks; t += G) {
+            const int pq = static_cast<int>(t * 256u + threadIdx.x);
+            const bool act = pq < sz;
+            const int q = act ? front_indices[off + pq] : 0;
+            const long long kq = act ? kk[q] : 0;
+            const int tq = act ? (prev ? prev[q] : pq) : 0;
+            int p = 0;
+            for (int t0 = 0; t0 < sz; t0 += kTile) {
+                const int lim = min(kTile, sz - t0);
+                __syncthreads();
+                for (int s2 = threadIdx.x; s2 < lim; s2 += blockDim.x) {
+                    const int pt = front_indices[off + t0 + s2];
+                    tk[s2] = kk[pt];
+                    tt[s2] = prev ? prev[pt] : t0 + s2;
+                }
+                __syncthreads();
+                if (act) {
+                    for (int s2 = 0; s2 < lim; ++s2) {
+                        const long long v = tk[s2];
+                        p += (v < kq) | ((v == kq) & (tt[s2] < tq));
+                    }
+                }
+            }
+            if (act) {
+                sorted[static_cast<uint64_t>(k) * n + off + p] = q;
+                inv_pos[static_cast<uint64_t>(k) * n + q] = p;
+            }
         }
-        sorted[static_cast<uint64_t>(k) * n + off + p] = static_cast<int32_t>(q);
-        inv_pos[static_cast<uint64_t>(k) * n + q] = p;
+        base += tasks;
     }
 }
 
 // crowding_distance per point: ends of each objective get +inf (assignment),
-// interior points add (f[next] - f[prev]) / (f[last] - f[first]); fronts of
-// one or two points are +inf (nsga2.cpp:188-193).
+// interior points add (f[next] - f[prev]) / (f[last] - f[first]), objectives
+// in order (multi_objective.cpp:303-313); fronts of one or two points are
+// +inf (nsga2.cpp:188-193).
 __global__ void crowding_accumulate_kernel(const double *__restrict__ pts, uint32_t n, uint32_t m,
                                            const int32_t *__restrict__ rank, const int32_t *__restrict__ front_offsets,
                                            const int32_t *__restrict__ sorted, const int32_t *__restrict__ inv_pos,
@@ -323,17 +381,17 @@ __global__ void crowding_accumulate_kernel(const double *__restrict__ pts, uint3
 }
 
 // One front holding every point: rank 0, identity order.
-__global__ void single_front_kernel(uint32_t n, int32_t *rank, int32_t *pos, int32_t *front_offsets,
-                                    int32_t *front_indices)
+__global__ void single_front_kernel(uint32_t n, int32_t *rank, int32_t *front_offsets, int32_t *front_indices,
+                                    int32_t *n_fronts)
 {
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         rank[q] = 0;
-        pos[q] = static_cast<int32_t>(q);
         front_indices[q] = static_cast<int32_t>(q);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         front_offsets[0] = 0;
         front_offsets[1] = static_cast<int32_t>(n);
+        *n_fronts = 1;
     }
 }
 
@@ -472,49 +530,6 @@ int launch_dominates_rows(const long long *keys, uint32_t n, uint32_t m, uint32_
     return PGX_OK;
 }
 
-constexpr uint64_t kMaxPoints = 1u << 19; // 524288 points: a 32 GiB bit matrix
-
-// Scratch layout inside ctx->s_state (device): peel_state, rem, masks, pos,
-// list, keyv, sorted, inv_pos.
-struct scratch_view {
-    peel_state *st;
-    uint32_t *rem, *masks;
-    int32_t *pos, *list, *keyv, *sorted, *inv_pos;
-};
-
-size_t align256(size_t b)
-{
-    return (b + 255u) & ~static_cast<size_t>(255u);
-}
-
-int carve_scratch(pgx_context *ctx, uint64_t n, uint64_t m, uint32_t W8, scratch_view *v)
-{
-    const size_t mm = m > 0 ? m : 1;
-    const size_t b_st = align256(sizeof(peel_state));
-    const size_t b_rem = align256(W8 * 4u);
-    const size_t b_masks = align256(2u * W8 * 4u);
-    const size_t b_n = align256(n * 4u);
-    const size_t b_nm = align256(n * mm * 4u);
-    PGX_TRY(ctx->s_state.ensure(b_st + b_rem + b_masks + 3u * b_n + 2u * b_nm));
-    char *p = ctx->s_state.as<char>();
-    v->st = reinterpret_cast<peel_state *>(p);
-    p += b_st;
-    v->rem = reinterpret_cast<uint32_t *>(p);
-    p += b_rem;
-    v->masks = reinterpret_cast<uint32_t *>(p);
-    p += b_masks;
-    v->pos = reinterpret_cast<int32_t *>(p);
-    p += b_n;
-    v->list = reinterpret_cast<int32_t *>(p);
-    p += b_n;
-    v->keyv = reinterpret_cast<int32_t *>(p);
-    p += b_n;
-    v->sorted = reinterpret_cast<int32_t *>(p);
-    p += b_nm;
-    v->inv_pos = reinterpret_cast<int32_t *>(p);
-    return PGX_OK;
-}
-
 __global__ void init_rem_kernel(uint32_t *rem, uint32_t n, uint32_t W8)
 {
     for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < W8; w += gridDim.x * blockDim.x) {
@@ -528,87 +543,149 @@ __global__ void init_rem_kernel(uint32_t *rem, uint32_t n, uint32_t W8)
     }
 }
 
-} // namespace
+constexpr uint64_t kMaxPoints = 1u << 19; // 524288 points: a 32 GiB bit matrix
 
-int launch_survival(pgx_context *ctx, const double *d_points, uint64_t n64, uint64_t m64, const survival_out &out,
-                    cudaStream_t s)
+size_t align256(size_t b)
 {
-    PGX_CHECK(n64 >= 2u, PGX_ERR_INVALID,
-              "At least two points are needed for fast_non_dominated_sorting: " + std::to_string(n64) + " detected.");
-    PGX_CHECK(n64 <= kMaxPoints, PGX_ERR_CAPACITY, "fast_non_dominated_sorting: more than 524288 points");
-    PGX_CHECK(m64 <= 4096u, PGX_ERR_CAPACITY, "fast_non_dominated_sorting: more than 4096 objectives");
-    const uint32_t n = static_cast<uint32_t>(n64), m = static_cast<uint32_t>(m64);
+    return (b + 255u) & ~static_cast<size_t>(255u);
+}
+
+// Device scratch of one survival pass (global memory beyond the inputs and
+// outputs). Laid out back to back, each piece 256-byte aligned.
+struct survival_scratch {
+    long long *keys;   // m * n order keys (objective-major)
+    uint32_t *Dt;      // n * W8 dominated-by bit matrix
+    peel_state *st;    // barrier, counters, status
+    uint32_t *rem;     // W8 unassigned-point bit set
+    int32_t *list;     // n members of the front being built
+    int32_t *keyv;     // n their ordering keys
+    int32_t *sorted;   // m * n per-objective sorted front members
+    int32_t *inv_pos;  // m * n position of each point in its sorted front
+};
+
+size_t survival_scratch_bytes(uint64_t n, uint64_t m)
+{
+    const uint64_t mm = m > 0 ? m : 1;
+    const uint64_t W8 = (((n + 31u) / 32u) + 7u) & ~uint64_t(7);
+    return align256(n * mm * sizeof(long long)) + align256(n * W8 * 4u) + align256(sizeof(peel_state))
+           + align256(W8 * 4u) + 2u * align256(n * 4u) + 2u * align256(n * mm * 4u);
+}
+
+survival_scratch carve_survival_scratch(void *base, uint64_t n, uint64_t m)
+{
+    const uint64_t mm = m > 0 ? m : 1;
+    const uint64_t W8 = (((n + 31u) / 32u) + 7u) & ~uint64_t(7);
+    char *p = static_cast<char *>(base);
+    survival_scratch s{};
+    s.keys = reinterpret_cast<long long *>(p);
+    p += align256(n * mm * sizeof(long long));
+    s.Dt = reinterpret_cast<uint32_t *>(p);
+    p += align256(n * W8 * 4u);
+    s.st = reinterpret_cast<peel_state *>(p);
+    p += align256(sizeof(peel_state));
+    s.rem = reinterpret_cast<uint32_t *>(p);
+    p += align256(W8 * 4u);
+    s.list = reinterpret_cast<int32_t *>(p);
+    p += align256(n * 4u);
+    s.keyv = reinterpret_cast<int32_t *>(p);
+    p += align256(n * 4u);
+    s.sorted = reinterpret_cast<int32_t *>(p);
+    p += align256(n * mm * 4u);
+    s.inv_pos = reinterpret_cast<int32_t *>(p);
+    return s;
+}
+
+// The whole survival pass on `stream` over caller-provided scratch: clears
+// what must start at zero, builds keys and the bit matrix, peels the fronts
+// (cooperative launch) and, when out.crowding is set, computes the crowding
+// distances. *launches counts the kernels launched.
+int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n, uint32_t m,
+                 const survival_out &out, int num_sms, cudaStream_t s, uint64_t *launches)
+{
     const uint32_t W = (n + 31u) / 32u;
     const uint32_t W8 = (W + 7u) & ~7u;
-    const int sms = ctx->num_sms;
-
-    PGX_TRY(ctx->s_keys.ensure(static_cast<size_t>(n) * (m ? m : 1) * sizeof(long long)));
-    PGX_TRY(ctx->s_dommat.ensure(static_cast<size_t>(n) * W8 * sizeof(uint32_t)));
-    scratch_view v{};
-    PGX_TRY(carve_scratch(ctx, n, m, W8, &v));
-    long long *keys = ctx->s_keys.as<long long>();
-    uint32_t *Dt = ctx->s_dommat.as<uint32_t>();
-
     PGX_CUDA(cudaMemsetAsync(out.dom_count, 0, static_cast<size_t>(n) * sizeof(int32_t), s));
-    PGX_CUDA(cudaMemsetAsync(v.st, 0, sizeof(peel_state), s));
-    PGX_CUDA(cudaMemsetAsync(v.masks, 0, 2u * W8 * sizeof(uint32_t), s));
+    PGX_CUDA(cudaMemsetAsync(sc.st, 0, sizeof(peel_state), s));
     PGX_CUDA(cudaMemsetAsync(out.front_offsets, 0, (static_cast<size_t>(n) + 1u) * sizeof(int32_t), s));
-    init_rem_kernel<<<blocks_for(W8, 256, sms), 256, 0, s>>>(v.rem, n, W8);
+    init_rem_kernel<<<blocks_for(W8, 256, num_sms), 256, 0, s>>>(sc.rem, n, W8);
     PGX_CUDA(cudaGetLastError());
-    ++ctx->launches;
+    *launches += 1;
     if (m > 0) {
-        order_keys_kernel<<<blocks_for(static_cast<uint64_t>(n) * m, 256, sms), 256, 0, s>>>(d_points, n, m, keys);
+        order_keys_kernel<<<blocks_for(static_cast<uint64_t>(n) * m, 256, num_sms), 256, 0, s>>>(d_points, n, m,
+                                                                                                 sc.keys);
         PGX_CUDA(cudaGetLastError());
-        PGX_TRY(launch_dominance(keys, n, m, W, W8, Dt, out.dom_count, s));
-        ctx->launches += 2;
+        PGX_TRY(launch_dominance(sc.keys, n, m, W, W8, sc.Dt, out.dom_count, s));
+        *launches += 2;
     } else {
-        PGX_CUDA(cudaMemsetAsync(Dt, 0, static_cast<size_t>(n) * W8 * sizeof(uint32_t), s));
+        PGX_CUDA(cudaMemsetAsync(sc.Dt, 0, static_cast<size_t>(n) * W8 * sizeof(uint32_t), s));
     }
 
     // cooperative peel: every block resident at once (the grid barrier needs it)
+    const size_t smem = 2u * kTile * sizeof(int32_t);
     int occ = 0;
-    PGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, peel_kernel, 256, 0));
-    if (occ < 1) occ = 1;
+    PGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, peel_kernel, 256, smem));
+    PGX_CHECK(occ >= 1, PGX_ERR_CUDA, "peel kernel cannot be resident");
     if (occ > 2) occ = 2;
-    const int grid = sms * occ;
+    const int grid = num_sms * occ;
     {
-        const uint32_t *a0 = Dt;
+        const uint32_t *a0 = sc.Dt;
         uint32_t a1 = n, a2 = W, a3 = W8;
-        uint32_t *a4 = v.rem, *a5 = v.masks;
-        int32_t *a6 = v.pos, *a7 = v.list, *a8 = v.keyv, *a9 = out.rank, *a10 = out.front_offsets,
-                *a11 = out.front_indices;
-        peel_state *a12 = v.st;
-        void *args[] = {&a0, &a1, &a2, &a3, &a4, &a5, &a6, &a7, &a8, &a9, &a10, &a11, &a12};
+        uint32_t *a4 = sc.rem;
+        int32_t *a5 = sc.list, *a6 = sc.keyv, *a7 = out.rank, *a8 = out.front_offsets, *a9 = out.front_indices;
+        peel_state *a10 = sc.st;
+        void *args[] = {&a0, &a1, &a2, &a3, &a4, &a5, &a6, &a7, &a8, &a9, &a10};
         PGX_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(peel_kernel), dim3(grid), dim3(256), args,
-                                             0, s));
-        ++ctx->launches;
+                                             smem, s));
+        *launches += 1;
     }
-    PGX_CUDA(cudaMemcpyAsync(out.n_fronts, &v.st->n_fronts, sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+    PGX_CUDA(cudaMemcpyAsync(out.n_fronts, &sc.st->n_fronts, sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
 
     if (out.crowding) {
         if (m > 0) {
-            const uint64_t nm = static_cast<uint64_t>(n) * m;
-            crowding_rank_kernel<<<blocks_for(nm, 256, sms), 256, 0, s>>>(keys, n, m, out.rank, v.pos,
-                                                                          out.front_offsets, out.front_indices,
-                                                                          v.sorted, v.inv_pos);
-            PGX_CUDA(cudaGetLastError());
-            ++ctx->launches;
+            for (uint32_t k = 0; k < m; ++k) {
+                crowding_rank_kernel<<<num_sms * 4, 256, 0, s>>>(sc.keys, n, k, out.front_offsets,
+                                                                 out.front_indices, out.n_fronts, sc.sorted,
+                                                                 sc.inv_pos);
+                PGX_CUDA(cudaGetLastError());
+            }
+            *launches += m;
         }
-        crowding_accumulate_kernel<<<blocks_for(n, 256, sms), 256, 0, s>>>(d_points, n, m, out.rank,
-                                                                           out.front_offsets, v.sorted, v.inv_pos,
-                                                                           out.crowding);
+        crowding_accumulate_kernel<<<blocks_for(n, 256, num_sms), 256, 0, s>>>(
+            d_points, n, m, out.rank, out.front_offsets, sc.sorted, sc.inv_pos, out.crowding);
         PGX_CUDA(cudaGetLastError());
-        ++ctx->launches;
+        *launches += 1;
     }
     return PGX_OK;
 }
 
-int survival_status(pgx_context *ctx)
+int check_survival_shape(uint64_t n, uint64_t m)
 {
-    PGX_CHECK(ctx->s_state.ptr != nullptr, PGX_ERR_INVALID, "survival_status before any survival call");
+    PGX_CHECK(n >= 2u, PGX_ERR_INVALID,
+              "At least two points are needed for fast_non_dominated_sorting: " + std::to_string(n) + " detected.");
+    PGX_CHECK(n <= kMaxPoints, PGX_ERR_CAPACITY, "fast_non_dominated_sorting: more than 524288 points");
+    PGX_CHECK(m <= 4096u, PGX_ERR_CAPACITY, "fast_non_dominated_sorting: more than 4096 objectives");
+    return PGX_OK;
+}
+
+} // namespace
+
+int launch_survival(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, const survival_out &out,
+                    cudaStream_t s)
+{
+    PGX_TRY(check_survival_shape(n, m));
+    PGX_TRY(ctx->s_state.ensure(survival_scratch_bytes(n, m)));
+    const survival_scratch sc = carve_survival_scratch(ctx->s_state.ptr, n, m);
+    return run_survival(sc, d_points, static_cast<uint32_t>(n), static_cast<uint32_t>(m), out, ctx->num_sms, s,
+                        &ctx->launches);
+}
+
+// After a synchronisation: PGX_ERR_TIMEOUT when a grid barrier of the last
+// survival pass on this context gave up.
+int read_survival_status(pgx_context *ctx, uint64_t n, uint64_t m)
+{
+    const survival_scratch sc = carve_survival_scratch(ctx->s_state.ptr, n, m);
     int err = 0;
-    PGX_CUDA(cudaMemcpy(&err, &reinterpret_cast<peel_state *>(ctx->s_state.ptr)->err, sizeof(int),
-                        cudaMemcpyDeviceToHost));
+    PGX_CUDA(cudaMemcpy(&err, &sc.st->err, sizeof(int), cudaMemcpyDeviceToHost));
     PGX_CHECK(err == 0, PGX_ERR_TIMEOUT, "fast_non_dominated_sorting: a grid barrier timed out on the device");
     return PGX_OK;
 }
@@ -621,70 +698,70 @@ int launch_crowding_single(pgx_context *ctx, const double *d_points, uint64_t n6
     PGX_CHECK(m64 >= 2u, PGX_ERR_INVALID,
               "Points in the non dominated front must contain at least two objectives: " + std::to_string(m64)
                   + " detected.");
-    PGX_CHECK(n64 < (1ull << 30) && m64 <= 4096u, PGX_ERR_CAPACITY, "crowding_distance: input too large");
+    PGX_CHECK(n64 <= kMaxPoints && m64 <= 4096u, PGX_ERR_CAPACITY, "crowding_distance: input too large");
     const uint32_t n = static_cast<uint32_t>(n64), m = static_cast<uint32_t>(m64);
     const int sms = ctx->num_sms;
-    const uint32_t W8 = (((n + 31u) / 32u) + 7u) & ~7u;
-    PGX_TRY(ctx->s_keys.ensure(static_cast<size_t>(n) * m * sizeof(long long)));
-    scratch_view v{};
-    PGX_TRY(carve_scratch(ctx, n, m, W8, &v));
+    // keys, sorted and inv_pos come from the survival scratch layout (no bit matrix use)
+    PGX_TRY(ctx->s_state.ensure(survival_scratch_bytes(n, m)));
+    const survival_scratch sc = carve_survival_scratch(ctx->s_state.ptr, n, m);
     const size_t b_rank = align256(static_cast<size_t>(n) * 4u);
-    PGX_TRY(ctx->s_outs.ensure(b_rank + align256((static_cast<size_t>(n) + 1u) * 4u)));
+    const size_t b_off = align256(2u * 4u);
+    PGX_TRY(ctx->s_outs.ensure(2u * b_rank + b_off + 256u));
     int32_t *rank = ctx->s_outs.as<int32_t>();
-    int32_t *front_offsets = reinterpret_cast<int32_t *>(ctx->s_outs.as<char>() + b_rank);
-    int32_t *front_indices = v.list;
-    long long *keys = ctx->s_keys.as<long long>();
+    int32_t *front_indices = reinterpret_cast<int32_t *>(ctx->s_outs.as<char>() + b_rank);
+    int32_t *front_offsets = reinterpret_cast<int32_t *>(ctx->s_outs.as<char>() + 2u * b_rank);
+    int32_t *n_fronts = reinterpret_cast<int32_t *>(ctx->s_outs.as<char>() + 2u * b_rank + b_off);
     const uint64_t nm = static_cast<uint64_t>(n) * m;
-    single_front_kernel<<<blocks_for(n, 256, sms), 256, 0, s>>>(n, rank, v.pos, front_offsets, front_indices);
+    single_front_kernel<<<blocks_for(n, 256, sms), 256, 0, s>>>(n, rank, front_offsets, front_indices, n_fronts);
     PGX_CUDA(cudaGetLastError());
-    order_keys_kernel<<<blocks_for(nm, 256, sms), 256, 0, s>>>(d_points, n, m, keys);
+    order_keys_kernel<<<blocks_for(nm, 256, sms), 256, 0, s>>>(d_points, n, m, sc.keys);
     PGX_CUDA(cudaGetLastError());
-    crowding_rank_kernel<<<blocks_for(nm, 256, sms), 256, 0, s>>>(keys, n, m, rank, v.pos, front_offsets,
-                                                                  front_indices, v.sorted, v.inv_pos);
+    for (uint32_t k = 0; k < m; ++k) {
+        crowding_rank_kernel<<<sms * 4, 256, 0, s>>>(sc.keys, n, k, front_offsets, front_indices, n_fronts, sc.sorted,
+                                                     sc.inv_pos);
+        PGX_CUDA(cudaGetLastError());
+    }
+    crowding_accumulate_kernel<<<blocks_for(n, 256, sms), 256, 0, s>>>(d_points, n, m, rank, front_offsets, sc.sorted,
+                                                                       sc.inv_pos, d_out);
     PGX_CUDA(cudaGetLastError());
-    crowding_accumulate_kernel<<<blocks_for(n, 256, sms), 256, 0, s>>>(d_points, n, m, rank, front_offsets, v.sorted,
-                                                                       v.inv_pos, d_out);
-    PGX_CUDA(cudaGetLastError());
-    ctx->launches += 4;
+    ctx->launches += 3 + m;
     return PGX_OK;
 }
 
 int build_dominates_rows(pgx_context *ctx, const double *d_points, uint64_t n64, uint64_t m64, int64_t **d_row_count,
                          cudaStream_t s)
 {
-    PGX_CHECK(n64 >= 2u, PGX_ERR_INVALID,
-              "At least two points are needed for fast_non_dominated_sorting: " + std::to_string(n64) + " detected.");
-    PGX_CHECK(n64 <= kMaxPoints, PGX_ERR_CAPACITY, "fast_non_dominated_sorting: more than 524288 points");
-    PGX_CHECK(m64 <= 4096u, PGX_ERR_CAPACITY, "fast_non_dominated_sorting: more than 4096 objectives");
+    PGX_TRY(check_survival_shape(n64, m64));
     const uint32_t n = static_cast<uint32_t>(n64), m = static_cast<uint32_t>(m64);
     const uint32_t W = (n + 31u) / 32u;
     const uint32_t W8 = (W + 7u) & ~7u;
     const int sms = ctx->num_sms;
-    PGX_TRY(ctx->s_keys.ensure(static_cast<size_t>(n) * (m ? m : 1) * sizeof(long long)));
-    PGX_TRY(ctx->s_dommat.ensure(static_cast<size_t>(n) * W8 * sizeof(uint32_t)));
+    PGX_TRY(ctx->s_state.ensure(survival_scratch_bytes(n, m)));
+    const survival_scratch sc = carve_survival_scratch(ctx->s_state.ptr, n, m);
     PGX_TRY(ctx->s_outs.ensure(static_cast<size_t>(n) * sizeof(int64_t)));
     int64_t *cnt = ctx->s_outs.as<int64_t>();
     PGX_CUDA(cudaMemsetAsync(cnt, 0, static_cast<size_t>(n) * sizeof(int64_t), s));
     if (m > 0) {
-        long long *keys = ctx->s_keys.as<long long>();
-        order_keys_kernel<<<blocks_for(static_cast<uint64_t>(n) * m, 256, sms), 256, 0, s>>>(d_points, n, m, keys);
+        order_keys_kernel<<<blocks_for(static_cast<uint64_t>(n) * m, 256, sms), 256, 0, s>>>(d_points, n, m, sc.keys);
         PGX_CUDA(cudaGetLastError());
-        PGX_TRY(launch_dominates_rows(keys, n, m, W, W8, ctx->s_dommat.as<uint32_t>(), cnt, s));
+        PGX_TRY(launch_dominates_rows(sc.keys, n, m, W, W8, sc.Dt, cnt, s));
         ctx->launches += 2;
     } else {
-        PGX_CUDA(cudaMemsetAsync(ctx->s_dommat.ptr, 0, static_cast<size_t>(n) * W8 * sizeof(uint32_t), s));
+        PGX_CUDA(cudaMemsetAsync(sc.Dt, 0, static_cast<size_t>(n) * W8 * sizeof(uint32_t), s));
     }
     *d_row_count = cnt;
     return PGX_OK;
 }
 
-int extract_dom_list(pgx_context *ctx, uint64_t n64, const int64_t *d_offsets, int32_t *d_indices, cudaStream_t s)
+int extract_dom_list(pgx_context *ctx, uint64_t n64, uint64_t m64, const int64_t *d_offsets, int32_t *d_indices,
+                     cudaStream_t s)
 {
     const uint32_t n = static_cast<uint32_t>(n64);
     const uint32_t W = (n + 31u) / 32u;
     const uint32_t W8 = (W + 7u) & ~7u;
+    const survival_scratch sc = carve_survival_scratch(ctx->s_state.ptr, n64, m64);
     dom_list_extract_kernel<<<blocks_for(static_cast<uint64_t>(n) * 32u, 256, ctx->num_sms), 256, 0, s>>>(
-        ctx->s_dommat.as<uint32_t>(), n, W, W8, d_offsets, d_indices);
+        sc.Dt, n, W, W8, d_offsets, d_indices);
     PGX_CUDA(cudaGetLastError());
     ++ctx->launches;
     return PGX_OK;

@@ -14,7 +14,7 @@ import pytest
 from pathlib import Path
 
 from pagmo2_gb300 import _native as N
-from pagmo2_gb300 import bfe as B
+from pagmo2_gb300 import batch_evaluators as B
 from pagmo2_gb300 import problems as P
 from pagmo2_gb300 import workloads as W
 

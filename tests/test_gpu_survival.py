@@ -1,9 +1,11 @@
 """GPU parity of NSGA-II survival (through the C ABI): fast non-dominated
 sorting bit-exact with the reference (ranks, domination counts, fronts in the
-reference's order, dom_list), crowding distance bit-exact on every point
-whose objective values are not tied inside its front; inside a tie group the
-reference's unstable std::sort fixes which duplicate gets which neighbour
-difference, so there the multiset of the group's values must match.
+reference's order, dom_list); crowding distance bit-exact with the reference
+on every point whose objective values are not tied inside its front, and
+bit-exact everywhere with the oracle run with the GPU's tie rule (equal values
+keep their order in the front, i.e. a stable sort). The reference sorts with
+the unstable std::sort, so which of two equal values gets which neighbour
+difference is an artefact of libstdc++'s introsort, not of the algorithm.
 """
 import math
 from pathlib import Path
@@ -22,8 +24,10 @@ def fronts_of(off, idx):
     return [list(map(int, idx[a:b])) for a, b in zip(off[:-1], off[1:])]
 
 
-def check_crowding(pts, off, idx, got, want):
-    """Untied points bit-exact; tied groups equal as multisets."""
+def check_crowding(pts, off, idx, got, want, want_stable):
+    """All points bit-exact with the stable-tie oracle; untied points bit-exact
+    with the reference."""
+    assert np.array_equal(got, want_stable, equal_nan=True), "crowding differs from the stable-tie oracle"
     for a, b in zip(off[:-1], off[1:]):
         members = np.asarray(idx[a:b])
         if members.size < 3:
@@ -38,16 +42,13 @@ def check_crowding(pts, off, idx, got, want):
             nan = np.isnan(col)
             if nan.sum() > 1:
                 tied |= nan
+        # an untied point's sorted position, and the values (not identities)
+        # of its neighbours, do not depend on how ties elsewhere are ordered
         u = members[~tied]
-        assert np.array_equal(got[u], want[u], equal_nan=True), "untied crowding differs"
-        t = members[tied]
-        if t.size:
-            g = np.sort(got[t])
-            w = np.sort(want[t])
-            assert np.allclose(g, w, rtol=1e-12, atol=0, equal_nan=True), "tie-group crowding multiset differs"
+        assert np.array_equal(got[u], want[u], equal_nan=True), "untied crowding differs from the reference"
 
 
-def test_golden_fnds_and_crowding(ctx):
+def test_golden_fnds_and_crowding(ctx, orc):
     gold = np.load(GOLD / "mo.npz")
     for name in sorted({k.split("/")[0] for k in gold.files}):
         p = gold[f"{name}/points"]
@@ -58,7 +59,8 @@ def test_golden_fnds_and_crowding(ctx):
         doff, didx = MO.dom_list_arrays(p, ctx)
         assert np.array_equal(doff, gold[f"{name}/dl_offsets"]), name
         assert np.array_equal(didx, gold[f"{name}/dl_indices"]), name
-        check_crowding(p, off, idx, cd, gold[f"{name}/crowding"])
+        stable = orc.nsga2_crowding(p, off, idx, stable=True) if p.shape[1] >= 2 else cd
+        check_crowding(p, off, idx, cd, gold[f"{name}/crowding"], stable)
 
 
 def test_reference_fnds_examples(ctx):
@@ -114,7 +116,8 @@ def test_config4_nested_fronts_full(ctx, orc):
     assert np.array_equal(off, want["front_offsets"])
     assert np.array_equal(idx, want["front_indices"])
     wcd = orc.nsga2_crowding(p, want["front_offsets"], want["front_indices"])
-    check_crowding(p, off, idx, cd, wcd)
+    wst = orc.nsga2_crowding(p, want["front_offsets"], want["front_indices"], stable=True)
+    check_crowding(p, off, idx, cd, wcd, wst)
 
 
 @pytest.mark.parametrize("n,m,seed", [(2, 2, 1), (3, 1, 2), (33, 2, 3), (257, 4, 4), (1000, 3, 5), (700, 7, 6)])
