@@ -148,7 +148,9 @@ PGX_API int pgx_nsga2_survival(pgx_context *ctx, const double *points, uint64_t 
                        double *crowding);
 
 /* Device-resident survival: all pointers are device memory; d_n_fronts is a
-   device int32. Asynchronous on `stream`. */
+   device int32. Asynchronous on `stream`. The front peeling waits on grid
+   barriers with a bounded spin (about a second); if one gives up, the call
+   still returns and *d_n_fronts reads -1 once the stream has run. */
 PGX_API int pgx_nsga2_survival_device(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, int32_t *d_rank,
                               int32_t *d_dom_count, int32_t *d_front_offsets, int32_t *d_front_indices,
                               int32_t *d_n_fronts, double *d_crowding, void *stream);

@@ -153,7 +153,9 @@ __device__ bool grid_sync(peel_state *st)
             atomicAdd(&st->bar_gen, 1u);
         } else {
             unsigned long long spins = 0;
+            volatile int *verr = &st->err;
             while (*vgen == g0) {
+                if (*verr) break; // another block gave up: do not wait for it
                 if (++spins > kSpinLimit) {
                     atomicExch(&st->err, 1);
                     break;
@@ -242,7 +244,10 @@ __global__ void __launch_bounds__(256) peel_kernel(const uint32_t *__restrict__ 
                 }
             }
         }
-        if (!grid_sync(st)) return;
+        if (!grid_sync(st)) {
+            if (threadIdx.x == 0) atomicExch(&st->n_fronts, -1);
+            return;
+        }
         const int L = *reinterpret_cast<volatile int *>(cnt);
         if (L == 0) break;
         // ---- Phase C (the loop bound is uniform per block: __syncthreads is safe)
@@ -280,10 +285,14 @@ __global__ void __launch_bounds__(256) peel_kernel(const uint32_t *__restrict__ 
         off_prev = off;
         size_prev = L;
         off += L;
-        if (!grid_sync(st)) return;
+        if (!grid_sync(st)) {
+            if (threadIdx.x == 0) atomicExch(&st->n_fronts, -1);
+            return;
+        }
     }
     if (tid == 0) {
-        st->n_fronts = k;
+        // a barrier that gave up elsewhere leaves the fronts incomplete: report -1
+        st->n_fronts = *reinterpret_cast<volatile int *>(&st->err) ? -1 : k;
         front_offsets[0] = 0;
     }
 }
