@@ -155,6 +155,23 @@ PGX_API int pgx_nsga2_survival_device(pgx_context *ctx, const double *d_points, 
                               int32_t *d_dom_count, int32_t *d_front_offsets, int32_t *d_front_indices,
                               int32_t *d_n_fronts, double *d_crowding, void *stream);
 
+/* Allocation-free variant of pgx_nsga2_survival_device, for callers that
+   cannot call cudaMalloc when they evaluate (their device memory is already
+   held by another allocator, or they must not risk the device-wide
+   synchronisation cudaMalloc/cudaFree can cause). It has no counterpart in
+   the reference. Same arguments, outputs and asynchronous behaviour as
+   pgx_nsga2_survival_device, without a context: it runs on the current
+   device, and its scratch is a fixed device array inside the library, so
+   n <= 4096 and m <= 8, else PGX_ERR_CAPACITY. The first call on each device
+   looks up that array's device address (a one-time set-up); make that first
+   call before any stream capture. All calls share the array and it keeps the
+   last call's contents (each call re-initialises what it needs); calls whose
+   work overlaps on the GPU race on it and must be serialised by the caller. */
+PGX_API int pgx_nsga2_survival_device_noalloc(const double *d_points, uint64_t n, uint64_t m, int32_t *d_rank,
+                                              int32_t *d_dom_count, int32_t *d_front_offsets,
+                                              int32_t *d_front_indices, int32_t *d_n_fronts, double *d_crowding,
+                                              void *stream);
+
 /* ------------------------------------------------------------ measurement */
 
 /* FP64 FMA throughput of the device in GFLOP/s (FMA = 2 flops), measured by a

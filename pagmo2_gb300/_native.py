@@ -38,6 +38,7 @@ SIGNATURES = {
     "pgx_nsga2_survival": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp]),
     "pgx_nsga2_survival_device": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "pgx_measure_fp64_peak": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "pgx_nsga2_survival_device_noalloc": (C.c_int, [_vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None

@@ -777,3 +777,116 @@ int extract_dom_list(pgx_context *ctx, uint64_t n64, uint64_t m64, const int64_t
 }
 
 } // namespace pgx
+
+// ---------------------------------------------------------------------------
+// Allocation-free NSGA-II survival.
+//
+// Some callers cannot call cudaMalloc at the time they evaluate a population:
+// an application whose device memory is already claimed by another allocator
+// (a framework's caching allocator that reserved most of HBM up front), or a
+// latency-bound island thread that must not risk the implicit device-wide
+// synchronisation cudaMalloc and cudaFree can cause. pgx_nsga2_survival_device
+// grows context buffers on demand, so this variant instead takes its scratch
+// (order keys, the dominance bit matrix, peel state, per-objective orders)
+// from one array compiled into the library: g_noalloc_scratch, sized for at
+// most kNoAllocMaxPoints points and kNoAllocMaxObjectives objectives
+// (about 2.6 MB, held by every GPU that loads the library until the process
+// exits). Larger inputs are rejected with PGX_ERR_CAPACITY.
+//
+// Host code cannot use the array's name as a device address (it names a host
+// stand-in), so the first call on each device looks up its address with
+// cudaGetSymbolAddress, with that device current, and caches it; the kernels
+// then receive that pointer. All calls share the one array and it keeps the
+// last call's contents: every pass clears what must start at zero itself, and
+// calls whose work overlaps on the GPU (different streams, or different host
+// threads) race on the array and must be serialised by the caller.
+namespace pgx
+{
+namespace
+{
+
+constexpr uint64_t kNoAllocMaxPoints = 4096;
+constexpr uint64_t kNoAllocMaxObjectives = 8;
+constexpr int kNoAllocMaxDevices = 64;
+
+constexpr size_t noalloc_align(size_t b)
+{
+    return (b + 255u) & ~static_cast<size_t>(255u);
+}
+
+// Bytes of the survival scratch layout for the largest accepted shape.
+constexpr size_t noalloc_bytes(uint64_t n, uint64_t m)
+{
+    return noalloc_align(n * m * 8u) + noalloc_align(n * ((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u)
+           + noalloc_align(sizeof(peel_state)) + noalloc_align(((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u)
+           + 2u * noalloc_align(n * 4u) + 2u * noalloc_align(n * m * 4u);
+}
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[noalloc_bytes(kNoAllocMaxPoints,
+                                                                               kNoAllocMaxObjectives)];
+
+struct noalloc_device {
+    void *scratch = nullptr; // device address of g_noalloc_scratch on this device
+    int num_sms = 0;
+};
+
+std::mutex g_noalloc_lock;
+noalloc_device g_noalloc_devices[kNoAllocMaxDevices];
+
+// One-time set-up per device, run with that device current.
+int noalloc_setup(int device, noalloc_device *out)
+{
+    std::lock_guard<std::mutex> g(g_noalloc_lock);
+    noalloc_device &d = g_noalloc_devices[device];
+    if (d.scratch == nullptr) {
+        void *p = nullptr;
+        PGX_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        int sms = 0;
+        PGX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        d.num_sms = sms;
+        d.scratch = p;
+    }
+    *out = d;
+    return PGX_OK;
+}
+
+} // namespace
+} // namespace pgx
+
+extern "C" int pgx_nsga2_survival_device_noalloc(const double *d_points, uint64_t n, uint64_t m, int32_t *d_rank,
+                                                 int32_t *d_dom_count, int32_t *d_front_offsets,
+                                                 int32_t *d_front_indices, int32_t *d_n_fronts, double *d_crowding,
+                                                 void *stream)
+{
+    using namespace pgx;
+    PGX_CHECK(n >= 2u, PGX_ERR_INVALID,
+              "At least two points are needed for fast_non_dominated_sorting: " + std::to_string(n) + " detected.");
+    PGX_CHECK(n <= kNoAllocMaxPoints && m <= kNoAllocMaxObjectives, PGX_ERR_CAPACITY,
+              "pgx_nsga2_survival_device_noalloc: at most " + std::to_string(kNoAllocMaxPoints) + " points and "
+                  + std::to_string(kNoAllocMaxObjectives) + " objectives, got " + std::to_string(n) + " x "
+                  + std::to_string(m));
+    PGX_CHECK(d_crowding == nullptr || m >= 2u, PGX_ERR_INVALID,
+              "Points in the non dominated front must contain at least two objectives: " + std::to_string(m)
+                  + " detected.");
+    PGX_CHECK(d_points != nullptr || m == 0, PGX_ERR_INVALID, "null points buffer");
+    PGX_CHECK(d_rank && d_dom_count && d_front_offsets && d_front_indices && d_n_fronts, PGX_ERR_INVALID,
+              "null output buffer");
+    PGX_CHECK(survival_scratch_bytes(n, m) <= sizeof(g_noalloc_scratch), PGX_ERR_CAPACITY,
+              "pgx_nsga2_survival_device_noalloc: scratch layout exceeds the static array");
+    int device = 0;
+    PGX_CUDA(cudaGetDevice(&device));
+    PGX_CHECK(device >= 0 && device < kNoAllocMaxDevices, PGX_ERR_CAPACITY, "device ordinal too large");
+    noalloc_device nd;
+    PGX_TRY(noalloc_setup(device, &nd));
+    const survival_scratch sc = carve_survival_scratch(nd.scratch, n, m);
+    survival_out o;
+    o.rank = d_rank;
+    o.dom_count = d_dom_count;
+    o.front_offsets = d_front_offsets;
+    o.front_indices = d_front_indices;
+    o.n_fronts = d_n_fronts;
+    o.crowding = d_crowding;
+    uint64_t launches = 0;
+    return run_survival(sc, d_points, static_cast<uint32_t>(n), static_cast<uint32_t>(m), o, nd.num_sms,
+                        static_cast<cudaStream_t>(stream), &launches);
+}
