@@ -1,0 +1,496 @@
+// Device routines of the batch fitness/gradient path, shared by the
+// per-problem kernels (fitness.cu) and the fused archipelago kernel
+// (epoch.cu). Every routine evaluates whole rows with a fixed group of lanes
+// and FP64 arithmetic throughout.
+//
+// GB300's FP64 pipe retires two lanes per SM per clock, so these routines are
+// written for the fewest FP64 instructions per element; integer and shuffle
+// work is cheap by comparison.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+namespace pgx
+{
+namespace dev
+{
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// 2*pi and 10*(2*pi) as the reference rounds them (src/problems/rastrigin.cpp:65, :104).
+constexpr double kOmega = 2. * 3.1415926535897932384626433832795028841971693993;
+constexpr double k10Omega = 10.0 * kOmega;
+
+// Lanes of the calling thread's group of G consecutive lanes (G | 32).
+template <int G>
+__device__ __forceinline__ unsigned group_mask()
+{
+    if constexpr (G == 32) {
+        return kFull;
+    } else {
+        const unsigned lane = threadIdx.x & 31u;
+        return ((1u << G) - 1u) << (lane & ~static_cast<unsigned>(G - 1));
+    }
+}
+
+template <int G>
+__device__ __forceinline__ double group_sum(double v, unsigned mask)
+{
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, G);
+    return v;
+}
+
+__device__ __forceinline__ double flip_sign(double v, int flip)
+{
+    return __longlong_as_double(__double_as_longlong(v) ^ (static_cast<long long>(flip & 1) << 63));
+}
+
+// ------------------------------------------------------------ sin/cos(2 pi x)
+//
+// Method: exact argument reduction in units of the period, then polynomials.
+// With k = rint(4x) (one FMA against the 1.5*2^52 rounding constant, valid for
+// |x| < 2^49) and r = x - k/4 (exact: Sterbenz), 2 pi x = k pi/2 + 2 pi r with
+// |2 pi r| <= pi/4. sin(2 pi r) = r S(r^2) and cos(2 pi r) = 1 + r^2 C(r^2),
+// S and C near-minimax (Chebyshev interpolation) fits on r^2 in [0, 1/64],
+// |error| about 2e-16 including rounding; cos is exactly 1 at r = 0, so
+// integer x give cos = 1, sin = +-0 exactly. The quadrant k mod 4 swaps and
+// negates the pair with integer operations only. Callers route |x| >= 2^40,
+// infinities and NaN to CUDA's sincospi/cospi.
+constexpr double kRound52 = 0x1.8p52;
+
+__device__ __forceinline__ bool fast_trig_arg(double x)
+{
+    const unsigned e = (static_cast<unsigned>(__double2hiint(x)) >> 20) & 0x7ffu;
+    return e < 1023u + 40u;
+}
+
+__device__ __forceinline__ void sincos_2pi(double x, double &s, double &c)
+{
+    const double t = fma(x, 4.0, kRound52);
+    const int k = __double2loint(t);
+    const double r = fma(t - kRound52, -0.25, x);
+    const double z = r * r;
+    double ps = 0x1.e3f38399551bfp+1;
+    ps = fma(ps, z, -0x1.e30071afc3e59p+3);
+    ps = fma(ps, z, 0x1.50782fda12d96p+5);
+    ps = fma(ps, z, -0x1.32d2cce2e5b19p+6);
+    ps = fma(ps, z, 0x1.466bc677587f8p+6);
+    ps = fma(ps, z, -0x1.4abbce625be41p+5);
+    ps = fma(ps, z, 0x1.921fb54442d18p+2);
+    const double sr = r * ps;
+    double pc = 0x1.f4b536b457d9ep+2;
+    pc = fma(pc, z, -0x1.a6cc32d07dc98p+4);
+    pc = fma(pc, z, 0x1.e1f50093e4c8fp+5);
+    pc = fma(pc, z, -0x1.55d3c7e10153fp+6);
+    pc = fma(pc, z, 0x1.03c1f081b4b74p+6);
+    pc = fma(pc, z, -0x1.3bd3cc9be45dbp+4);
+    const double cr = fma(pc, z, 1.0);
+    const int q = k & 3;
+    const bool swap = (q & 1) != 0;
+    c = flip_sign(swap ? sr : cr, ((q + 1) >> 1) & 1); // negative in quadrants 1, 2
+    s = flip_sign(swap ? cr : sr, (q >> 1) & 1);       // negative in quadrants 2, 3
+}
+
+// cos(2 pi x) alone: half-period reduction k = rint(2x), r = x - k/2,
+// cos(2 pi x) = (-1)^k (1 + r^2 H(r^2)), H fitted on r^2 in [0, 1/16].
+__device__ __forceinline__ double cos_2pi(double x)
+{
+    const double t = fma(x, 2.0, kRound52);
+    const int k = __double2loint(t);
+    const double r = fma(t - kRound52, -0.5, x);
+    const double z = r * r;
+    double p = 0x1.179a329ef4140p-2;
+    p = fma(p, z, -0x1.b6a6feabe52e9p+0);
+    p = fma(p, z, 0x1.f9d2c1f3b2167p+2);
+    p = fma(p, z, -0x1.a6d1f12b0bef2p+4);
+    p = fma(p, z, 0x1.e1f5068620bcbp+5);
+    p = fma(p, z, -0x1.55d3c7e3c9051p+6);
+    p = fma(p, z, 0x1.03c1f081b5a9fp+6);
+    p = fma(p, z, -0x1.3bd3cc9be45dep+4);
+    return flip_sign(fma(p, z, 1.0), k & 1);
+}
+
+// ------------------------------------------------------------------ rastrigin
+//
+// f = sum_i (x_i^2 - 10 cos(2 pi x_i)) + 10 n  (src/problems/rastrigin.cpp:62-72),
+// accumulated as sum x^2 and sum cos apart; g_i = 2 x_i + 10 omega sin(2 pi x_i)
+// (:98-107). One group of G lanes per row, lanes strided over coordinates.
+template <int G, bool GRAD>
+__device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uint32_t nx, double *f_out,
+                                              double *__restrict__ gr)
+{
+    const unsigned sub = threadIdx.x & (G - 1);
+    const unsigned mask = group_mask<G>();
+    double sx = 0.0, sc = 0.0;
+    for (uint32_t i = sub; i < nx; i += G) {
+        const double xi = __ldg(xr + i);
+        double s, c;
+        if (fast_trig_arg(xi)) {
+            if (GRAD)
+                sincos_2pi(xi, s, c);
+            else
+                c = cos_2pi(xi);
+        } else {
+            if (GRAD)
+                sincospi(xi + xi, &s, &c);
+            else
+                c = cospi(xi + xi);
+        }
+        sx = fma(xi, xi, sx);
+        sc += c;
+        if (GRAD) gr[i] = fma(k10Omega, s, xi + xi);
+    }
+    sx = group_sum<G>(sx, mask);
+    sc = group_sum<G>(sc, mask);
+    if (sub == 0 && f_out) *f_out = fma(-10.0, sc, sx) + 10.0 * static_cast<double>(nx);
+}
+
+// ----------------------------------------------------------------- rosenbrock
+//
+// With t_i = x_{i+1} - x_i^2 and c_i = 2 x_i - 2 (src/problems/rosenbrock.cpp:59-66, 83-92):
+//   f   = 100 sum t_i^2 + sum (x_i - 1)^2        (i < n-1)
+//   g_i = 200 (t_{i-1} - 2 x_i t_i) + c_i        (i < n-1, t_{-1} = 0)
+//   g_{n-1} = 200 t_{n-2}
+// Fitness + gradient: 7 FP64 instructions per element (t, sum t^2, 2x, 2x-2,
+// sum (2x-2)^2, t_{i-1} - 2x t, 200 b + c); fitness only: 4.
+
+// Scalar variant: one group of G lanes per row, element i in lane i mod G;
+// x_{i+1} from the next lane (the last lane takes the next chunk's head),
+// t_{i-1} from the previous lane.
+template <int G, bool GRAD>
+__device__ __forceinline__ void rosenbrock_row(const double *__restrict__ xr, uint32_t nx, double *f_out,
+                                               double *__restrict__ gr)
+{
+    const unsigned sub = threadIdx.x & (G - 1);
+    const unsigned mask = group_mask<G>();
+    double acc_t = 0.0, acc_u = 0.0, t_carry = 0.0;
+    double x_cur = sub < nx ? __ldg(xr + sub) : 0.0;
+    for (uint32_t base = 0; base < nx; base += G) {
+        const uint32_t i = base + sub;
+        const double x_nxt = (i + G < nx) ? __ldg(xr + i + G) : 0.0;
+        double xn = __shfl_down_sync(mask, x_cur, 1, G);
+        const double head = __shfl_sync(mask, x_nxt, 0, G);
+        if (sub == G - 1) xn = head;
+        const bool has_next = i + 1u < nx;
+        const double t = has_next ? fma(-x_cur, x_cur, xn) : 0.0;
+        if (GRAD) {
+            double t_prev = __shfl_up_sync(mask, t, 1, G);
+            if (sub == 0) t_prev = t_carry;
+            t_carry = __shfl_sync(mask, t, G - 1, G);
+            if (i < nx) {
+                const double w = x_cur + x_cur;
+                const double c = w - 2.0;
+                double gi;
+                if (has_next) {
+                    acc_t = fma(t, t, acc_t);
+                    acc_u = fma(c, c, acc_u);
+                    gi = fma(200.0, fma(-w, t, t_prev), c);
+                } else {
+                    gi = 200.0 * t_prev;
+                }
+                gr[i] = gi;
+            }
+        } else if (has_next) {
+            const double u = x_cur - 1.0;
+            acc_t = fma(t, t, acc_t);
+            acc_u = fma(u, u, acc_u);
+        }
+        x_cur = x_nxt;
+    }
+    acc_t = group_sum<G>(acc_t, mask);
+    acc_u = group_sum<G>(acc_u, mask);
+    // with the gradient the second sum is over c^2 = 4 (x-1)^2
+    if (sub == 0 && f_out) *f_out = GRAD ? fma(100.0, acc_t, 0.25 * acc_u) : fma(100.0, acc_t, acc_u);
+}
+
+// Vector variant: one warp per row, each lane owning 4 consecutive elements
+// (two 16-byte loads), so a warp step covers 128 elements with a quarter of
+// the loads and shuffles of the scalar variant. Needs nx % 4 == 0 and a
+// 16-byte aligned row start.
+template <bool GRAD>
+__device__ __forceinline__ void rosenbrock_row_v4(const double *__restrict__ xr, uint32_t nx, double *f_out,
+                                                  double *__restrict__ gr)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t slots = nx >> 2;
+    const double2 *x2 = reinterpret_cast<const double2 *>(xr);
+    double acc_t = 0.0, acc_u = 0.0, t_carry = 0.0;
+    double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
+    if (lane < slots) {
+        a = __ldg(x2 + 2u * lane);
+        b = __ldg(x2 + 2u * lane + 1u);
+    }
+    for (uint32_t base = 0; base < slots; base += 32u) {
+        const uint32_t s = base + lane;
+        const bool act = s < slots;
+        const uint32_t sn = s + 32u;
+        double2 na = make_double2(0.0, 0.0), nb = make_double2(0.0, 0.0);
+        if (sn < slots) {
+            na = __ldg(x2 + 2u * sn);
+            nb = __ldg(x2 + 2u * sn + 1u);
+        }
+        const double x0 = a.x, x1 = a.y, x2v = b.x, x3 = b.y;
+        double xn = __shfl_down_sync(kFull, x0, 1);
+        const double head = __shfl_sync(kFull, na.x, 0);
+        if (lane == 31u) xn = head;
+        const bool last_has_next = s + 1u < slots;
+        const double t0 = fma(-x0, x0, x1);
+        const double t1 = fma(-x1, x1, x2v);
+        const double t2 = fma(-x2v, x2v, x3);
+        const double t3 = last_has_next ? fma(-x3, x3, xn) : 0.0;
+        if (GRAD) {
+            double tp = __shfl_up_sync(kFull, t3, 1);
+            if (lane == 0) tp = t_carry;
+            t_carry = __shfl_sync(kFull, t3, 31);
+            if (act) {
+                const double w0 = x0 + x0, w1 = x1 + x1, w2 = x2v + x2v, w3 = x3 + x3;
+                const double c0 = w0 - 2.0, c1 = w1 - 2.0, c2 = w2 - 2.0, c3 = w3 - 2.0;
+                acc_t = fma(t0, t0, acc_t);
+                acc_t = fma(t1, t1, acc_t);
+                acc_t = fma(t2, t2, acc_t);
+                acc_u = fma(c0, c0, acc_u);
+                acc_u = fma(c1, c1, acc_u);
+                acc_u = fma(c2, c2, acc_u);
+                double2 g01, g23;
+                g01.x = fma(200.0, fma(-w0, t0, tp), c0);
+                g01.y = fma(200.0, fma(-w1, t1, t0), c1);
+                g23.x = fma(200.0, fma(-w2, t2, t1), c2);
+                if (last_has_next) {
+                    acc_t = fma(t3, t3, acc_t);
+                    acc_u = fma(c3, c3, acc_u);
+                    g23.y = fma(200.0, fma(-w3, t3, t2), c3);
+                } else {
+                    g23.y = 200.0 * t2;
+                }
+                double2 *g2 = reinterpret_cast<double2 *>(gr);
+                g2[2u * s] = g01;
+                g2[2u * s + 1u] = g23;
+            }
+        } else if (act) {
+            const double u0 = x0 - 1.0, u1 = x1 - 1.0, u2 = x2v - 1.0;
+            acc_t = fma(t0, t0, acc_t);
+            acc_t = fma(t1, t1, acc_t);
+            acc_t = fma(t2, t2, acc_t);
+            acc_u = fma(u0, u0, acc_u);
+            acc_u = fma(u1, u1, acc_u);
+            acc_u = fma(u2, u2, acc_u);
+            if (last_has_next) {
+                const double u3 = x3 - 1.0;
+                acc_t = fma(t3, t3, acc_t);
+                acc_u = fma(u3, u3, acc_u);
+            }
+        }
+        a = na;
+        b = nb;
+    }
+    acc_t = group_sum<32>(acc_t, kFull);
+    acc_u = group_sum<32>(acc_u, kFull);
+    if (lane == 0 && f_out) *f_out = GRAD ? fma(100.0, acc_t, 0.25 * acc_u) : fma(100.0, acc_t, acc_u);
+}
+
+// ------------------------------------------------------------- lennard_jones
+//
+// E = 4 sum_{i<j} (s^2 - s), s = r_ij^-6 (src/problems/lennard_jones.cpp:72-91);
+// dE/dr_i = -24 sum_j s (2 s - 1) / r^2 (r_i - r_j). One warp per cluster.
+// Coordinates are decoded into shared memory (structure of arrays) with the
+// reference's pinned-atom convention (:132-151): atom 0 at the origin, atom 1
+// at (0, 0, x0), atom 2 at (0, x1, x2), atom k >= 3 at x[3(k-2) .. 3(k-2)+2];
+// in the flattened 3N layout P[p] = x[p-6] for p >= 7, P[5] = x[0], else 0.
+// The i<j pairs are walked as a half ring, pair (i, i+k mod N) for
+// k = 1..N/2 (k = N/2 only for i < N/2 when N is even), so every lane does
+// the same number of pairs. A zero distance makes the reference overwrite
+// its sum with DBL_MAX and end at +inf (:81-82, :89); a NaN term keeps NaN.
+
+// 1/d: the hardware approximation refined by one cubic Newton step
+// (y1 = y0 (1 + e + e^2), e = 1 - d y0). d = +inf gives 0 (not NaN).
+__device__ __forceinline__ double lj_rcp(double d)
+{
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(d));
+    const double e = fma(-d, y, 1.0);
+    const double r = fma(y, fma(e, e, e), y);
+    return (__double_as_longlong(y) << 1) == 0 ? y : r;
+}
+
+__device__ __forceinline__ void lj_decode(const double *__restrict__ xr, uint32_t na, double *px, double *py,
+                                          double *pz, double *gx, double *gy, double *gz, bool zero_g)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint32_t p = lane; p < 3u * na; p += 32u) {
+        double v = 0.0;
+        if (p == 5u)
+            v = __ldg(xr);
+        else if (p >= 7u)
+            v = __ldg(xr + (p - 6u));
+        const uint32_t at = p / 3u, cc = p - 3u * at;
+        (cc == 0u ? px : (cc == 1u ? py : pz))[at] = v;
+        if (zero_g) (cc == 0u ? gx : (cc == 1u ? gy : gz))[at] = 0.0;
+    }
+    __syncwarp();
+}
+
+// Writes -24 * G[atom(v)][coord(v)] for every free coordinate v.
+__device__ __forceinline__ void lj_store_gradient(uint32_t nx, const double *gx, const double *gy, const double *gz,
+                                                  double *__restrict__ gr)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint32_t v = lane; v < nx; v += 32u) {
+        uint32_t at, cc;
+        if (v < 3u) {
+            at = v == 0u ? 1u : 2u;
+            cc = v == 1u ? 1u : 2u;
+        } else {
+            at = v / 3u + 2u;
+            cc = v - 3u * (v / 3u);
+        }
+        gr[v] = -24.0 * (cc == 0u ? gx : (cc == 1u ? gy : gz))[at];
+    }
+}
+
+// Register variant (N <= 32*MA): lane l owns atoms l, l+32, ..., whose
+// positions and force sums stay in registers; only the reaction on the
+// partner atom goes through shared memory. Per pair, fitness + gradient:
+// 21 FP64 instructions (3 differences, r^2, reciprocal, r^-6, s^2-s, the
+// energy sum, the force coefficient, 3 own and 3 reaction FMAs); fitness only: 13.
+template <int MA, bool GRAD>
+__device__ __forceinline__ void lj_cluster_reg(const double *__restrict__ xr, uint32_t na, uint32_t nx, double *sm,
+                                               double *f_out, double *__restrict__ gr)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    double *px = sm, *py = px + na, *pz = py + na;
+    double *gx = pz + na, *gy = gx + na, *gz = gy + na;
+    lj_decode(xr, na, px, py, pz, gx, gy, gz, GRAD);
+    double ox[MA], oy[MA], oz[MA], fx[MA], fy[MA], fz[MA];
+#pragma unroll
+    for (int m = 0; m < MA; ++m) {
+        const uint32_t i = 32u * m + lane;
+        ox[m] = i < na ? px[i] : 0.0;
+        oy[m] = i < na ? py[i] : 0.0;
+        oz[m] = i < na ? pz[i] : 0.0;
+        fx[m] = fy[m] = fz[m] = 0.0;
+    }
+    double e = 0.0;
+    int zero = 0;
+    const bool even = (na & 1u) == 0u;
+    const uint32_t kmax = na / 2u;
+    for (uint32_t k = 1u; k <= kmax; ++k) {
+        const uint32_t ilim = (even && k == kmax) ? kmax : na;
+#pragma unroll
+        for (int m = 0; m < MA; ++m) {
+            const uint32_t i = 32u * m + lane;
+            if (i < ilim) {
+                uint32_t j = i + k;
+                if (j >= na) j -= na;
+                const double dx = ox[m] - px[j], dy = oy[m] - py[j], dz = oz[m] - pz[j];
+                const double d = fma(dx, dx, fma(dy, dy, dz * dz));
+                const double inv = lj_rcp(d);
+                const double s = inv * inv * inv;
+                const double term = fma(s, s, -s);
+                if (__double_as_longlong(d) != 0)
+                    e += term;
+                else
+                    zero = 1;
+                if (GRAD) {
+                    const double coef = fma(s, s, term) * inv; // (2 s^2 - s) / r^2
+                    fx[m] = fma(coef, dx, fx[m]);
+                    fy[m] = fma(coef, dy, fy[m]);
+                    fz[m] = fma(coef, dz, fz[m]);
+                    gx[j] = fma(-coef, dx, gx[j]);
+                    gy[j] = fma(-coef, dy, gy[j]);
+                    gz[j] = fma(-coef, dz, gz[j]);
+                }
+            }
+        }
+        // the partners of one step are distinct; the next step may revisit them
+        if (GRAD) __syncwarp();
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(kFull, e, o);
+    zero = __any_sync(kFull, zero);
+    if (lane == 0 && f_out) *f_out = zero ? (isnan(e) ? e : HUGE_VAL) : 4.0 * e;
+    if (GRAD) {
+#pragma unroll
+        for (int m = 0; m < MA; ++m) {
+            const uint32_t i = 32u * m + lane;
+            if (i < na) {
+                gx[i] += fx[m];
+                gy[i] += fy[m];
+                gz[i] += fz[m];
+            }
+        }
+        __syncwarp();
+        lj_store_gradient(nx, gx, gy, gz, gr);
+    }
+    __syncwarp();
+}
+
+// Shared-memory variant for any N: both sides of each pair go through shared
+// memory, in two conflict-free phases (the lanes of one step hold distinct i
+// and distinct j).
+template <bool GRAD>
+__device__ __forceinline__ void lj_cluster_smem(const double *__restrict__ xr, uint32_t na, uint32_t nx, double *sm,
+                                                double *f_out, double *__restrict__ gr)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    double *px = sm, *py = px + na, *pz = py + na;
+    double *gx = pz + na, *gy = gx + na, *gz = gy + na;
+    lj_decode(xr, na, px, py, pz, gx, gy, gz, GRAD);
+    double e = 0.0;
+    int zero = 0;
+    const bool even = (na & 1u) == 0u;
+    const uint32_t kmax = na / 2u;
+    for (uint32_t k = 1u; k <= kmax; ++k) {
+        const uint32_t ilim = (even && k == kmax) ? kmax : na;
+        for (uint32_t i0 = 0u; i0 < ilim; i0 += 32u) {
+            const uint32_t i = i0 + lane;
+            const bool act = i < ilim;
+            uint32_t j = i + k;
+            if (j >= na) j -= na;
+            double dx = 0.0, dy = 0.0, dz = 0.0, coef = 0.0;
+            if (act) {
+                dx = px[i] - px[j];
+                dy = py[i] - py[j];
+                dz = pz[i] - pz[j];
+                const double d = fma(dx, dx, fma(dy, dy, dz * dz));
+                const double inv = lj_rcp(d);
+                const double s = inv * inv * inv;
+                const double term = fma(s, s, -s);
+                if (__double_as_longlong(d) != 0)
+                    e += term;
+                else
+                    zero = 1;
+                if (GRAD) coef = fma(s, s, term) * inv;
+            }
+            if (GRAD) {
+                if (act) {
+                    gx[i] = fma(coef, dx, gx[i]);
+                    gy[i] = fma(coef, dy, gy[i]);
+                    gz[i] = fma(coef, dz, gz[i]);
+                }
+                __syncwarp();
+                if (act) {
+                    gx[j] = fma(-coef, dx, gx[j]);
+                    gy[j] = fma(-coef, dy, gy[j]);
+                    gz[j] = fma(-coef, dz, gz[j]);
+                }
+                __syncwarp();
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(kFull, e, o);
+    zero = __any_sync(kFull, zero);
+    if (lane == 0 && f_out) *f_out = zero ? (isnan(e) ? e : HUGE_VAL) : 4.0 * e;
+    if (GRAD) {
+        __syncwarp();
+        lj_store_gradient(nx, gx, gy, gz, gr);
+    }
+    __syncwarp();
+}
+
+} // namespace dev
+} // namespace pgx
