@@ -52,8 +52,8 @@ ROS_F_FLOPS_PER_ELEM = 7
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="pgx", choices=["pgx", "reference"])
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -380,11 +380,11 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops) -> dict:
         torch.cuda.synchronize()
         ts = []
         for _ in range(reps):
-            if flush_l2:
-                flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             with torch.cuda.stream(stream):
+                if flush_l2:
+                    flush.zero_()  # same stream: finishes before e0
                 e0.record(stream)
                 fn()
                 e1.record(stream)

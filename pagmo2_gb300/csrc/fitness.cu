@@ -101,6 +101,23 @@ int launch_rows(int kind, bool grad, const double *x, uint64_t n, uint32_t nx, d
                 : launch_simple(rosenbrock_kernel<G, false>, pb, x, n, nx, f, g, s, num_sms);
 }
 
+} // namespace
+
+// Lanes per row for the strided row kernels: the widest group (coalesced
+// loads, fewest sequential steps) that keeps at least 94% of its lanes busy;
+// the FP64 pipe spends a full warp instruction on partly idle warps.
+int lanes_per_row(uint32_t nx)
+{
+    for (uint32_t g = 32; g >= 2; g >>= 1) {
+        const uint32_t steps = (nx + g - 1) / g;
+        if (nx >= g && 100u * nx >= 94u * g * steps) return static_cast<int>(g);
+    }
+    return nx >= 2 ? 2 : 1;
+}
+
+namespace
+{
+
 template <typename K>
 int launch_lj(K kernel, bool grad, const double *x, uint64_t n, uint32_t na, uint32_t nx, double *f, double *g,
               cudaStream_t s, int num_sms)
@@ -143,12 +160,14 @@ int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64
         st = grad ? launch_simple(rosenbrock_v4_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
                   : launch_simple(rosenbrock_v4_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
     } else if (kind == PGX_RASTRIGIN || kind == PGX_ROSENBROCK) {
-        if (nx <= 48)
-            st = launch_rows<8>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);
-        else if (nx <= 256)
-            st = launch_rows<16>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);
-        else
-            st = launch_rows<32>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);
+        switch (lanes_per_row(nx32)) {
+            case 32: st = launch_rows<32>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;
+            case 16: st = launch_rows<16>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;
+            case 8: st = launch_rows<8>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;
+            case 4: st = launch_rows<4>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;
+            case 2: st = launch_rows<2>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;
+            default: st = launch_rows<1>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;
+        }
     } else if (kind == PGX_LENNARD_JONES) {
         const uint32_t na = static_cast<uint32_t>(param);
         const size_t per_warp = static_cast<size_t>(grad ? 6u : 3u) * na * sizeof(double);

@@ -44,9 +44,17 @@ __device__ __forceinline__ double group_sum(double v, unsigned mask)
     return v;
 }
 
-__device__ __forceinline__ double flip_sign(double v, int flip)
+// +1.0 or -1.0, and a constant with its sign flipped, built with integer
+// operations so that signs cost no FP64 instruction: callers fold them into
+// the FMA that consumes the value.
+__device__ __forceinline__ double unit_sign(int neg)
 {
-    return __longlong_as_double(__double_as_longlong(v) ^ (static_cast<long long>(flip & 1) << 63));
+    return __longlong_as_double(0x3ff0000000000000LL | (static_cast<long long>(neg & 1) << 63));
+}
+
+__device__ __forceinline__ double signed_const(double v, int neg)
+{
+    return __longlong_as_double(__double_as_longlong(v) ^ (static_cast<long long>(neg & 1) << 63));
 }
 
 // ------------------------------------------------------------ sin/cos(2 pi x)
@@ -57,9 +65,10 @@ __device__ __forceinline__ double flip_sign(double v, int flip)
 // |2 pi r| <= pi/4. sin(2 pi r) = r S(r^2) and cos(2 pi r) = 1 + r^2 C(r^2),
 // S and C near-minimax (Chebyshev interpolation) fits on r^2 in [0, 1/64],
 // |error| about 2e-16 including rounding; cos is exactly 1 at r = 0, so
-// integer x give cos = 1, sin = +-0 exactly. The quadrant k mod 4 swaps and
-// negates the pair with integer operations only. Callers route |x| >= 2^40,
-// infinities and NaN to CUDA's sincospi/cospi.
+// integer x give cos = 1, sin = +-0 exactly. The quadrant k mod 4 swaps the
+// pair and decides the signs, returned as flags (s_neg, c_neg) for the
+// caller's FMA. Callers route |x| >= 2^40, infinities and NaN to CUDA's
+// sincospi/cospi.
 constexpr double kRound52 = 0x1.8p52;
 
 __device__ __forceinline__ bool fast_trig_arg(double x)
@@ -68,7 +77,7 @@ __device__ __forceinline__ bool fast_trig_arg(double x)
     return e < 1023u + 40u;
 }
 
-__device__ __forceinline__ void sincos_2pi(double x, double &s, double &c)
+__device__ __forceinline__ void sincos_2pi(double x, double &s, int &s_neg, double &c, int &c_neg)
 {
     const double t = fma(x, 4.0, kRound52);
     const int k = __double2loint(t);
@@ -91,13 +100,16 @@ __device__ __forceinline__ void sincos_2pi(double x, double &s, double &c)
     const double cr = fma(pc, z, 1.0);
     const int q = k & 3;
     const bool swap = (q & 1) != 0;
-    c = flip_sign(swap ? sr : cr, ((q + 1) >> 1) & 1); // negative in quadrants 1, 2
-    s = flip_sign(swap ? cr : sr, (q >> 1) & 1);       // negative in quadrants 2, 3
+    c = swap ? sr : cr;
+    s = swap ? cr : sr;
+    c_neg = ((q + 1) >> 1) & 1; // negative in quadrants 1, 2
+    s_neg = (q >> 1) & 1;       // negative in quadrants 2, 3
 }
 
 // cos(2 pi x) alone: half-period reduction k = rint(2x), r = x - k/2,
 // cos(2 pi x) = (-1)^k (1 + r^2 H(r^2)), H fitted on r^2 in [0, 1/16].
-__device__ __forceinline__ double cos_2pi(double x)
+// Returns the magnitude; *neg = k mod 2.
+__device__ __forceinline__ double cos_2pi(double x, int &neg)
 {
     const double t = fma(x, 2.0, kRound52);
     const int k = __double2loint(t);
@@ -111,7 +123,8 @@ __device__ __forceinline__ double cos_2pi(double x)
     p = fma(p, z, -0x1.55d3c7e3c9051p+6);
     p = fma(p, z, 0x1.03c1f081b5a9fp+6);
     p = fma(p, z, -0x1.3bd3cc9be45dep+4);
-    return flip_sign(fma(p, z, 1.0), k & 1);
+    neg = k & 1;
+    return fma(p, z, 1.0);
 }
 
 // ------------------------------------------------------------------ rastrigin
@@ -119,6 +132,7 @@ __device__ __forceinline__ double cos_2pi(double x)
 // f = sum_i (x_i^2 - 10 cos(2 pi x_i)) + 10 n  (src/problems/rastrigin.cpp:62-72),
 // accumulated as sum x^2 and sum cos apart; g_i = 2 x_i + 10 omega sin(2 pi x_i)
 // (:98-107). One group of G lanes per row, lanes strided over coordinates.
+// FP64 instructions per element: fitness + gradient 21, fitness only 14.
 template <int G, bool GRAD>
 __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uint32_t nx, double *f_out,
                                               double *__restrict__ gr)
@@ -128,12 +142,13 @@ __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uin
     double sx = 0.0, sc = 0.0;
     for (uint32_t i = sub; i < nx; i += G) {
         const double xi = __ldg(xr + i);
-        double s, c;
+        double s = 0.0, c;
+        int s_neg = 0, c_neg = 0;
         if (fast_trig_arg(xi)) {
             if (GRAD)
-                sincos_2pi(xi, s, c);
+                sincos_2pi(xi, s, s_neg, c, c_neg);
             else
-                c = cos_2pi(xi);
+                c = cos_2pi(xi, c_neg);
         } else {
             if (GRAD)
                 sincospi(xi + xi, &s, &c);
@@ -141,8 +156,8 @@ __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uin
                 c = cospi(xi + xi);
         }
         sx = fma(xi, xi, sx);
-        sc += c;
-        if (GRAD) gr[i] = fma(k10Omega, s, xi + xi);
+        sc = fma(c, unit_sign(c_neg), sc);
+        if (GRAD) gr[i] = fma(signed_const(k10Omega, s_neg), s, xi + xi);
     }
     sx = group_sum<G>(sx, mask);
     sc = group_sum<G>(sc, mask);
@@ -156,7 +171,8 @@ __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uin
 //   g_i = 200 (t_{i-1} - 2 x_i t_i) + c_i        (i < n-1, t_{-1} = 0)
 //   g_{n-1} = 200 t_{n-2}
 // Fitness + gradient: 7 FP64 instructions per element (t, sum t^2, 2x, 2x-2,
-// sum (2x-2)^2, t_{i-1} - 2x t, 200 b + c); fitness only: 4.
+// sum (2x-2)^2, t_{i-1} - 2x t, 200 b + c), 6 in the vector variant where 2x
+// is an integer exponent increment; fitness only: 4.
 
 // Scalar variant: one group of G lanes per row, element i in lane i mod G;
 // x_{i+1} from the next lane (the last lane takes the next chunk's head),
@@ -207,6 +223,19 @@ __device__ __forceinline__ void rosenbrock_row(const double *__restrict__ xr, ui
     if (sub == 0 && f_out) *f_out = GRAD ? fma(100.0, acc_t, 0.25 * acc_u) : fma(100.0, acc_t, acc_u);
 }
 
+// 2x by incrementing the exponent field: exact for normal x whose double is
+// finite (biased exponent 1..0x7fd); an integer add instead of an FP64 one.
+__device__ __forceinline__ bool doubling_ok(double x)
+{
+    const unsigned e = (static_cast<unsigned>(__double2hiint(x)) >> 20) & 0x7ffu;
+    return e - 1u < 0x7fdu;
+}
+
+__device__ __forceinline__ double twice_normal(double x)
+{
+    return __hiloint2double(__double2hiint(x) + 0x00100000, __double2loint(x));
+}
+
 // Vector variant: one warp per row, each lane owning 4 consecutive elements
 // (two 16-byte loads), so a warp step covers 128 elements with a quarter of
 // the loads and shuffles of the scalar variant. Needs nx % 4 == 0 and a
@@ -246,8 +275,22 @@ __device__ __forceinline__ void rosenbrock_row_v4(const double *__restrict__ xr,
             double tp = __shfl_up_sync(kFull, t3, 1);
             if (lane == 0) tp = t_carry;
             t_carry = __shfl_sync(kFull, t3, 31);
+            // 2x exactly by an exponent increment when every element of the
+            // warp is a normal number whose double is finite, else by an add
+            const bool ok = !act || (doubling_ok(x0) && doubling_ok(x1) && doubling_ok(x2v) && doubling_ok(x3));
+            double w0, w1, w2, w3;
+            if (__all_sync(kFull, ok)) {
+                w0 = twice_normal(x0);
+                w1 = twice_normal(x1);
+                w2 = twice_normal(x2v);
+                w3 = twice_normal(x3);
+            } else {
+                w0 = x0 + x0;
+                w1 = x1 + x1;
+                w2 = x2v + x2v;
+                w3 = x3 + x3;
+            }
             if (act) {
-                const double w0 = x0 + x0, w1 = x1 + x1, w2 = x2v + x2v, w3 = x3 + x3;
                 const double c0 = w0 - 2.0, c1 = w1 - 2.0, c2 = w2 - 2.0, c3 = w3 - 2.0;
                 acc_t = fma(t0, t0, acc_t);
                 acc_t = fma(t1, t1, acc_t);

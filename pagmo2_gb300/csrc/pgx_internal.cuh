@@ -100,6 +100,9 @@ int problem_nx(int kind, uint64_t param, uint64_t *nx);
 
 // -------------------------------------------------------------- launchers
 
+// Lanes per row (1..32) used by the strided rastrigin/rosenbrock row kernels.
+int lanes_per_row(uint32_t nx);
+
 // Batch fitness (+ gradient when d_g != nullptr) for one problem on `stream`.
 // Returns the number of kernel launches issued through *launches.
 int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64_t n, double *d_f, double *d_g,

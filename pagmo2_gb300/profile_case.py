@@ -1,0 +1,85 @@
+"""Runs one kernel of the path on a chosen workload, for profilers.
+
+    python -m pagmo2_gb300.profile_case --case rosenbrock_fg --rows 16384
+    ncu --set full --clock-control none -k regex:rosenbrock -s 2 -c 1 \
+        python -m pagmo2_gb300.profile_case --case rosenbrock_fg --rows 16384
+
+Inputs are seeded synthetic batches resident on the device; --warmup launches
+are followed by --launches timed ones (CUDA events; numbers printed under a
+profiler are not benchmark values). Cases:
+
+  rastrigin_fg / rastrigin_f    dim 50
+  rosenbrock_fg / rosenbrock_f  dim 1000
+  lj_fg / lj_f                  150 atoms
+  survival                      NSGA-II survival of --rows nested-front points x 3
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[1]
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--case", required=True)
+    ap.add_argument("--rows", type=int, default=16384)
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--launches", type=int, default=3)
+    a = ap.parse_args()
+
+    import torch
+
+    from pagmo2_gb300 import _native as N
+    from pagmo2_gb300 import workloads as W
+
+    ctx = N.Context(0)
+    L = N.lib()
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    n = a.rows
+    if a.case == "survival":
+        p = W.nsga2_points(n, 3, layers=30)
+        dp = torch.from_numpy(p).cuda()
+        i32 = lambda k: torch.empty(k, dtype=torch.int32, device="cuda")  # noqa: E731
+        rank, dc, off, idx, nf = i32(n), i32(n), i32(n + 1), i32(n), i32(1)
+        cd = torch.empty(n, dtype=torch.float64, device="cuda")
+
+        def run():
+            N.check(L.pgx_nsga2_survival_device(ctx.handle, dp.data_ptr(), n, 3, rank.data_ptr(), dc.data_ptr(),
+                                                off.data_ptr(), idx.data_ptr(), nf.data_ptr(), cd.data_ptr(), sp))
+    else:
+        name, mode = a.case.rsplit("_", 1)
+        kind, param, x = {
+            "rastrigin": (N.RASTRIGIN, 50, lambda: W.rastrigin_batch(n, 50)),
+            "rosenbrock": (N.ROSENBROCK, 1000, lambda: W.rosenbrock_batch(n, 1000)),
+            "lj": (N.LENNARD_JONES, 150, lambda: W.lj_batch(n, 150)),
+        }[name]
+        x = x()
+        dx = torch.from_numpy(x).cuda()
+        df = torch.empty(n, dtype=torch.float64, device="cuda")
+        dg = torch.empty_like(dx) if mode == "fg" else None
+
+        def run():
+            N.check(L.pgx_batch_eval_device(ctx.handle, kind, param, dx.data_ptr(), n, df.data_ptr(),
+                                            dg.data_ptr() if dg is not None else None, sp))
+    for _ in range(a.warmup):
+        run()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.launches):
+        run()
+    e1.record(stream)
+    e1.synchronize()
+    print(f"{a.case} rows={n}: {e0.elapsed_time(e1) / a.launches:.4f} ms per launch")
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
