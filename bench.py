@@ -430,7 +430,88 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops) -> dict:
     ms = timed(surv, reps=10, flush_l2=False)
     out["nsga2_survival_20000x3"] = {"ms": ms, "fronts": int(nf.item()),
                                      "pair_tests_per_s": n * n / (ms * 1e-3)}
+    out["archipelago_64_islands"] = run_archipelago(ctx, L, N, W, stream)
     return out
+
+
+def run_archipelago(ctx, L, N, W, stream) -> dict:
+    """Mixed archipelago epoch (64 islands, fitness + gradient): the fused,
+    graph-captured epoch against one plain batch call per island."""
+    import torch
+
+    from pagmo2_gb300 import archipelago as A
+
+    reqs = W.archipelago(64)
+    shapes = [(r.kind, r.param, r.n, True) for r in reqs]
+    batches = [r.dvs for r in reqs]
+    rows = sum(r.n for r in reqs)
+    t0 = time.perf_counter()
+    ep = A.Epoch(shapes, ctx)
+    plan_s = time.perf_counter() - t0
+    sp = stream.cuda_stream
+
+    # device resident: the fused kernel alone vs one kernel launch per island
+    ep.run(batches)  # fills the plan's device input buffer
+    dx = [torch.from_numpy(b).cuda() for b in batches]
+    df = [torch.empty(r.n, dtype=torch.float64, device="cuda") for r in reqs]
+    dg = [torch.empty_like(d) for d in dx]
+
+    def plain_device():
+        for r, x, f, g in zip(reqs, dx, df, dg):
+            N.check(L.pgx_batch_eval_device(ctx.handle, r.kind, r.param, x.data_ptr(), r.n, f.data_ptr(),
+                                            g.data_ptr(), sp))
+
+    def fused_device():
+        ep.launch_device(sp)
+
+    def ev_time(fn, reps=10):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    ms_plain_dev = ev_time(plain_device)
+    ms_fused_dev = ev_time(fused_device)
+
+    # end to end from host buffers
+    def wall(fn, reps=5):
+        fn()
+        t = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        return (time.perf_counter() - t) / reps * 1e3
+
+    # outputs preallocated and reused by both paths (no first-touch page faults)
+    outs_plain = ep.outputs()
+    outs_fused = [ep.outputs() for _ in range(3)]
+    ms_plain_e2e = wall(lambda: A.run_plain(shapes, batches, ctx, outs_plain))
+    ms_fused_e2e = wall(lambda: ep.run(batches, outs_fused[0]))
+
+    # pipelined: epoch e+1 is packed and launched while epoch e runs
+    def pipelined(epochs=6):
+        ep.submit(batches, outs_fused[0])
+        for e in range(1, epochs):
+            ep.submit(batches, outs_fused[e % 3])
+            ep.collect()
+        ep.collect()
+
+    ms_pipe = wall(lambda: pipelined(), reps=2) / 6
+    ep.close()
+    return {"islands": 64, "rows": rows, "plan_s": plan_s,
+            "device_ms_plain": ms_plain_dev, "device_ms_fused": ms_fused_dev,
+            "device_speedup": ms_plain_dev / ms_fused_dev,
+            "e2e_ms_plain": ms_plain_e2e, "e2e_ms_fused": ms_fused_e2e, "e2e_speedup": ms_plain_e2e / ms_fused_e2e,
+            "e2e_ms_fused_pipelined": ms_pipe, "e2e_speedup_pipelined": ms_plain_e2e / ms_pipe,
+            "evals_per_s_fused_pipelined": rows / (ms_pipe * 1e-3)}
 
 
 if __name__ == "__main__":

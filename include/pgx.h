@@ -172,6 +172,56 @@ PGX_API int pgx_nsga2_survival_device_noalloc(const double *d_points, uint64_t n
                                               int32_t *d_front_indices, int32_t *d_n_fronts, double *d_crowding,
                                               void *stream);
 
+/* ------------------------------------------------- archipelago epochs */
+
+/* One island's request in a migration epoch: a batch of one problem. */
+typedef struct pgx_request {
+    int kind;           /* PGX_RASTRIGIN, PGX_ROSENBROCK or PGX_LENNARD_JONES */
+    uint64_t param;     /* dim, or atoms for lennard_jones */
+    uint64_t n_dvs;     /* rows */
+    const double *dvs;  /* host, n_dvs * nx, row-major */
+    double *fvs;        /* host, n_dvs (may be NULL when grads is set) */
+    double *grads;      /* host, n_dvs * nx, or NULL for fitness only */
+} pgx_request;
+
+/* Plans a migration epoch for a fixed list of request shapes (the pointers
+   are ignored here). The islands' rows are packed into one device buffer
+   and cut into warp-sized tiles, costliest first; lanes per row and tile
+   sizes come from an autotuner that times the candidates on this device
+   once per (problem, dimension) and caches the choice. Host-to-device copy,
+   one persistent fused kernel over all tiles and device-to-host copies are
+   captured in CUDA graphs, one per pinned staging set (three sets, three
+   streams), so consecutive epochs overlap. Replaces the island-by-island
+   bfe calls of an archipelago epoch (src/archipelago.cpp:325-330 ->
+   src/island.cpp:428-655 -> src/bfe.cpp:91-110). */
+PGX_API int pgx_epoch_create(pgx_context *ctx, const pgx_request *reqs, int n_reqs, pgx_epoch **out);
+
+/* One synchronous epoch: packs every request's dvs into the next staging
+   set, replays its graph, waits, unpacks fvs/grads. Shapes must match the
+   plan (PGX_ERR_INVALID otherwise). */
+PGX_API int pgx_epoch_run(pgx_epoch *ep, const pgx_request *reqs);
+
+/* Asynchronous pair over the staging sets: submit packs and launches
+   one epoch and returns; collect waits for the oldest submitted epoch and
+   unpacks it into the pointers given at its submit. At most three in flight. */
+PGX_API int pgx_epoch_submit(pgx_epoch *ep, const pgx_request *reqs);
+PGX_API int pgx_epoch_collect(pgx_epoch *ep);
+
+/* Device-resident replay of the fused kernel alone on the plan's device
+   buffers of staging set 0 (inputs as last copied), asynchronous on
+   `stream` (NULL: the plan's stream). For measurement. */
+PGX_API int pgx_epoch_launch_device(pgx_epoch *ep, void *stream);
+
+/* Number of tiles and the lanes per row the autotuner chose for request i. */
+PGX_API int pgx_epoch_info(const pgx_epoch *ep, int i, int *lanes_per_row, uint64_t *n_tiles);
+
+PGX_API void pgx_epoch_destroy(pgx_epoch *ep);
+
+/* The island-by-island baseline: one plain host-buffer batch call per
+   request, in order (pgx_batch_gradient, or pgx_batch_fitness when grads is
+   NULL). */
+PGX_API int pgx_requests_run_plain(pgx_context *ctx, const pgx_request *reqs, int n_reqs);
+
 /* ------------------------------------------------------------ measurement */
 
 /* FP64 FMA throughput of the device in GFLOP/s (FMA = 2 flops), measured by a

@@ -39,7 +39,21 @@ SIGNATURES = {
     "pgx_nsga2_survival_device": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "pgx_measure_fp64_peak": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "pgx_nsga2_survival_device_noalloc": (C.c_int, [_vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "pgx_epoch_create": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(_vp)]),
+    "pgx_epoch_run": (C.c_int, [_vp, _vp]),
+    "pgx_epoch_submit": (C.c_int, [_vp, _vp]),
+    "pgx_epoch_collect": (C.c_int, [_vp]),
+    "pgx_epoch_launch_device": (C.c_int, [_vp, _vp]),
+    "pgx_epoch_info": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(_u64)]),
+    "pgx_epoch_destroy": (None, [_vp]),
+    "pgx_requests_run_plain": (C.c_int, [_vp, _vp, C.c_int]),
 }
+
+
+class pgx_request(C.Structure):
+    """struct pgx_request of include/pgx.h."""
+    _fields_ = [("kind", C.c_int), ("param", C.c_uint64), ("n_dvs", C.c_uint64), ("dvs", C.c_void_p),
+                ("fvs", C.c_void_p), ("grads", C.c_void_p)]
 
 _lib = None
 _lib_lock = threading.Lock()

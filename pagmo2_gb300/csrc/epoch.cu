@@ -1,0 +1,656 @@
+// Archipelago migration epochs: every island's batch request of one epoch is
+// evaluated by one persistent fused kernel, captured in a CUDA graph together
+// with its staging copies.
+//
+// In the reference, islands evolve asynchronously and each of their
+// algorithms calls bfe::operator() on its own (src/archipelago.cpp:325-330,
+// src/island.cpp:428-655, src/bfe.cpp:91-110): one evaluation per island
+// call, each a few small kernels on a GPU backend. Here the requests of an
+// epoch are packed into one buffer and cut into tiles (rows of one request,
+// sized from the autotuner's per-row cost; one cluster for lennard_jones);
+// tiles are sorted costliest first and handed to warps through an atomic
+// counter, so small islands fill the gaps left by big ones.
+#include "fitness_dev.cuh"
+#include "pgx_internal.cuh"
+
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace pgx
+{
+namespace
+{
+
+using namespace dev;
+
+enum : uint8_t { kRows = 0, kRows4 = 1, kLJReg = 2, kLJFlat = 3 };
+
+// One warp's unit of work: `rows` consecutive rows of one request.
+struct tile_desc {
+    const double *x;
+    double *f;
+    double *g; // null: fitness only
+    uint32_t rows, nx, param;
+    uint8_t kind, lanes, variant, ma;
+};
+
+constexpr int kWarpsPerBlock = 4;
+constexpr int kSets = 3; // pinned staging sets: packing of later epochs never waits for the GPU
+
+template <int G, bool GRAD>
+__device__ __forceinline__ void tile_rows(const tile_desc &d)
+{
+    const unsigned grp = (threadIdx.x & 31u) / G;
+    constexpr unsigned per = 32u / G;
+    for (uint32_t base = 0; base < d.rows; base += per) {
+        const uint32_t r = base + grp;
+        if (r < d.rows) {
+            const double *xr = d.x + static_cast<uint64_t>(r) * d.nx;
+            double *gr = GRAD ? d.g + static_cast<uint64_t>(r) * d.nx : nullptr;
+            double *fo = d.f + r;
+            if (d.kind == PGX_RASTRIGIN)
+                rastrigin_row<G, GRAD>(xr, d.nx, fo, gr);
+            else
+                rosenbrock_row<G, GRAD>(xr, d.nx, fo, gr);
+        }
+    }
+}
+
+
+template <bool GRAD>
+__device__ __forceinline__ void run_tile(const tile_desc &d, double *sm)
+{
+    switch (d.variant) {
+        case kRows:
+            switch (d.lanes) {
+                case 32: tile_rows<32, GRAD>(d); break;
+                case 16: tile_rows<16, GRAD>(d); break;
+                case 8: tile_rows<8, GRAD>(d); break;
+                case 4: tile_rows<4, GRAD>(d); break;
+                case 2: tile_rows<2, GRAD>(d); break;
+                default: tile_rows<1, GRAD>(d); break;
+            }
+            break;
+        case kRows4:
+            for (uint32_t r = 0; r < d.rows; ++r)
+                rosenbrock_row_v4<GRAD>(d.x + static_cast<uint64_t>(r) * d.nx, d.nx, d.f + r,
+                                        GRAD ? d.g + static_cast<uint64_t>(r) * d.nx : nullptr);
+            break;
+        case kLJReg: // at most 32 atoms: one atom per lane
+            for (uint32_t r = 0; r < d.rows; ++r)
+                lj_cluster_reg<1, GRAD>(d.x + static_cast<uint64_t>(r) * d.nx, d.param, d.nx, sm, d.f + r,
+                                        GRAD ? d.g + static_cast<uint64_t>(r) * d.nx : nullptr);
+            break;
+        default:
+            for (uint32_t r = 0; r < d.rows; ++r)
+                lj_cluster_flat<GRAD>(d.x + static_cast<uint64_t>(r) * d.nx, d.param, d.nx, sm, d.f + r,
+                                      GRAD ? d.g + static_cast<uint64_t>(r) * d.nx : nullptr);
+            break;
+    }
+}
+
+// Persistent: every warp takes the next tile from the counter until none is left.
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 4)
+    epoch_kernel(const tile_desc *__restrict__ tiles, uint32_t n_tiles, unsigned *next, uint32_t sm_per_warp)
+{
+    extern __shared__ double smem[];
+    const unsigned lane = threadIdx.x & 31u;
+    double *sm = smem + static_cast<size_t>(threadIdx.x >> 5) * sm_per_warp;
+    for (;;) {
+        unsigned t = 0;
+        if (lane == 0) t = atomicAdd(next, 1u);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= n_tiles) break;
+        const tile_desc d = tiles[t];
+        if (d.g)
+            run_tile<true>(d, sm);
+        else
+            run_tile<false>(d, sm);
+    }
+}
+
+// ------------------------------------------------------------------ autotuner
+
+// Per (problem, dimension, gradient, device) choice of the row variant and its
+// measured cost per row at full-device throughput. Kept in memory and in a
+// text cache next to the library ("autotune.txt", one "key lanes ns" line per
+// entry); PGX_AUTOTUNE_CACHE overrides the path, "off" disables the file.
+struct tune_entry {
+    int lanes; // rastrigin/rosenbrock: 1..32 lanes per row, 0 = 4-wide rosenbrock rows; lennard_jones: 32
+    double ns_per_row;
+};
+
+std::mutex g_tune_lock;
+std::map<std::string, tune_entry> g_tune;
+bool g_tune_loaded = false;
+
+std::string tune_path()
+{
+    if (const char *p = std::getenv("PGX_AUTOTUNE_CACHE")) return p;
+    Dl_info info{};
+    if (dladdr(reinterpret_cast<void *>(&tune_path), &info) && info.dli_fname) {
+        std::string s(info.dli_fname);
+        const auto slash = s.rfind('/');
+        if (slash != std::string::npos) return s.substr(0, slash + 1) + "autotune.txt";
+    }
+    return "";
+}
+
+void tune_load()
+{
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const std::string p = tune_path();
+    if (p.empty() || p == "off") return;
+    std::ifstream in(p);
+    std::string key;
+    tune_entry e{};
+    while (in >> key >> e.lanes >> e.ns_per_row) g_tune[key] = e;
+}
+
+void tune_store(const std::string &key, const tune_entry &e)
+{
+    const std::string p = tune_path();
+    if (p.empty() || p == "off") return;
+    std::ofstream out(p, std::ios::app);
+    if (out) out << key << ' ' << e.lanes << ' ' << e.ns_per_row << '\n';
+}
+
+__global__ void fill_uniform_kernel(double *x, uint64_t n, uint64_t nx, const double *lb, const double *ub)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n * nx;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        uint64_t h = (i + 1) * 0x9E3779B97F4A7C15ull;
+        h ^= h >> 31;
+        h *= 0xBF58476D1CE4E5B9ull;
+        h ^= h >> 29;
+        const double u = static_cast<double>(h >> 11) * 0x1.0p-53;
+        const uint64_t c = i % nx;
+        x[i] = lb[c] + (ub[c] - lb[c]) * u;
+    }
+}
+
+int time_variant(pgx_context *ctx, int kind, uint64_t param, uint64_t nx, const double *dx, uint64_t rows, double *df,
+                 double *dg, int lanes, double *ms_out)
+{
+    cudaStream_t s = ctx->stream;
+    auto launch = [&]() -> int {
+        if (kind == PGX_LENNARD_JONES) return launch_eval(kind, param, nx, dx, rows, df, dg, s, ctx->num_sms, nullptr);
+        return launch_rows_variant(kind, nx, dx, rows, df, dg, lanes, s, ctx->num_sms);
+    };
+    cudaEvent_t e0, e1;
+    PGX_CUDA(cudaEventCreate(&e0));
+    PGX_CUDA(cudaEventCreate(&e1));
+    PGX_TRY(launch());
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+        PGX_CUDA(cudaEventRecord(e0, s));
+        PGX_TRY(launch());
+        PGX_CUDA(cudaEventRecord(e1, s));
+        PGX_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        PGX_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        best = std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->launches += 4;
+    *ms_out = best;
+    return PGX_OK;
+}
+
+// Chooses (and caches) the row variant for one request shape by timing the
+// candidates on a synthetic batch (uniform in the problem's bounds).
+int tune(pgx_context *ctx, int kind, uint64_t param, uint64_t nx, bool grad, tune_entry *out)
+{
+    cudaDeviceProp prop{};
+    PGX_CUDA(cudaGetDeviceProperties(&prop, ctx->device));
+    std::ostringstream ks;
+    ks << kind << ':' << param << ':' << nx << ':' << (grad ? 1 : 0) << ':' << prop.multiProcessorCount << ':'
+       << prop.major << prop.minor;
+    const std::string key = ks.str();
+    {
+        std::lock_guard<std::mutex> g(g_tune_lock);
+        tune_load();
+        const auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            *out = it->second;
+            return PGX_OK;
+        }
+    }
+    uint64_t rows = kind == PGX_LENNARD_JONES ? 2048u : 8192u;
+    const uint64_t cap = (uint64_t(64) << 20) / (nx * sizeof(double));
+    rows = std::max<uint64_t>(64u, std::min(rows, cap));
+    std::vector<double> lb(nx), ub(nx);
+    PGX_TRY(pgx_problem_bounds(kind, param, lb.data(), ub.data()));
+    double *dx = nullptr, *df = nullptr, *dg = nullptr, *dlb = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(dx);
+        cudaFree(df);
+        cudaFree(dg);
+        cudaFree(dlb);
+    };
+    int st = PGX_OK;
+    do {
+        cudaError_t e = cudaMalloc(&dx, rows * nx * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&df, rows * sizeof(double));
+        if (e == cudaSuccess && grad) e = cudaMalloc(&dg, rows * nx * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&dlb, 2 * nx * sizeof(double));
+        if (e == cudaSuccess) e = cudaMemcpy(dlb, lb.data(), nx * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(dlb + nx, ub.data(), nx * sizeof(double), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            st = cuda_status(e, "autotuner buffers");
+            break;
+        }
+        fill_uniform_kernel<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(dx, rows, nx, dlb, dlb + nx);
+        ++ctx->launches;
+        std::vector<int> cands;
+        if (kind == PGX_LENNARD_JONES) {
+            cands.push_back(32);
+        } else {
+            cands.push_back(lanes_per_row(static_cast<uint32_t>(nx)));
+            for (int g : {32, 16, 8, 4})
+                if (static_cast<uint64_t>(g) <= nx && std::find(cands.begin(), cands.end(), g) == cands.end())
+                    cands.push_back(g);
+            if (kind == PGX_ROSENBROCK && nx % 4 == 0 && nx >= 128) cands.push_back(0);
+        }
+        tune_entry best{cands[0], 1e30};
+        for (int lanes : cands) {
+            double ms = 0;
+            st = time_variant(ctx, kind, param, nx, dx, rows, df, dg, lanes, &ms);
+            if (st != PGX_OK) break;
+            const double ns = ms * 1e6 / static_cast<double>(rows);
+            if (ns < best.ns_per_row) best = tune_entry{lanes, ns};
+        }
+        if (st != PGX_OK) break;
+        *out = best;
+        std::lock_guard<std::mutex> g(g_tune_lock);
+        g_tune[key] = best;
+        tune_store(key, best);
+    } while (false);
+    cudaStreamSynchronize(ctx->stream);
+    cleanup();
+    return st;
+}
+
+// ------------------------------------------------------------------ host copies
+
+// Copies a list of (dst, src, bytes) with up to 16 threads when it is large.
+struct copy_item {
+    void *dst;
+    const void *src;
+    size_t bytes;
+};
+
+void parallel_copy(const std::vector<copy_item> &items)
+{
+    size_t total = 0;
+    for (const auto &c : items) total += c.bytes;
+    unsigned hw = std::thread::hardware_concurrency();
+    const unsigned nt = total < (size_t(8) << 20) ? 1u : std::min(16u, hw ? hw : 1u);
+    if (nt <= 1) {
+        for (const auto &c : items)
+            if (c.bytes) std::memcpy(c.dst, c.src, c.bytes);
+        return;
+    }
+    // cut into pieces of at most 2 MiB so the threads stay balanced
+    std::vector<copy_item> pieces;
+    for (const auto &c : items) {
+        for (size_t off = 0; off < c.bytes; off += (size_t(2) << 20)) {
+            const size_t b = std::min(c.bytes - off, size_t(2) << 20);
+            pieces.push_back({static_cast<char *>(c.dst) + off, static_cast<const char *>(c.src) + off, b});
+        }
+    }
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nt; ++t) {
+        pool.emplace_back([&pieces, t, nt]() {
+            for (size_t i = t; i < pieces.size(); i += nt) std::memcpy(pieces[i].dst, pieces[i].src, pieces[i].bytes);
+        });
+    }
+    for (auto &th : pool) th.join();
+}
+
+struct req_plan {
+    int kind;
+    uint64_t param, n, nx;
+    bool grad;
+    uint64_t off_x, off_f, off_g; // in doubles
+    tune_entry tune;
+    uint64_t tiles;
+};
+
+} // namespace
+} // namespace pgx
+
+using namespace pgx;
+
+struct pgx_epoch {
+    pgx_context *ctx = nullptr;
+    std::vector<req_plan> reqs;
+    uint64_t total_x = 0, total_f = 0, total_g = 0;
+    uint32_t n_tiles = 0;
+    int grid = 0;
+    uint32_t sm_per_warp = 0;
+    size_t smem = 0;
+    struct set_t {
+        dbuf d_x, d_f, d_g, d_tiles, d_next;
+        hbuf h_x, h_f, h_g;
+        cudaStream_t stream = nullptr;
+        cudaGraphExec_t graph = nullptr;
+        cudaEvent_t done = nullptr;
+        std::vector<pgx_request> pending;
+        bool in_flight = false;
+    } sets[kSets];
+    int next_set = 0;
+    std::deque<int> fifo;
+};
+
+namespace pgx
+{
+namespace
+{
+
+int check_shapes(const pgx_epoch *ep, const pgx_request *reqs)
+{
+    PGX_CHECK(reqs != nullptr || ep->reqs.empty(), PGX_ERR_INVALID, "null request list");
+    for (size_t i = 0; i < ep->reqs.size(); ++i) {
+        const req_plan &p = ep->reqs[i];
+        const pgx_request &r = reqs[i];
+        PGX_CHECK(r.kind == p.kind && r.param == p.param && r.n_dvs == p.n && (r.grads != nullptr) == p.grad,
+                  PGX_ERR_INVALID, "request " + std::to_string(i) + " does not match the epoch plan");
+        PGX_CHECK(r.n_dvs == 0 || (r.dvs != nullptr && (r.fvs != nullptr || r.grads != nullptr)), PGX_ERR_INVALID,
+                  "request " + std::to_string(i) + ": null buffer");
+    }
+    return PGX_OK;
+}
+
+int capture_set(pgx_epoch *ep, int si)
+{
+    auto &S = ep->sets[si];
+    cudaStream_t s = S.stream;
+    PGX_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    if (ep->total_x) cudaMemcpyAsync(S.d_x.ptr, S.h_x.ptr, ep->total_x * sizeof(double), cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(S.d_next.ptr, 0, sizeof(unsigned), s);
+    if (ep->n_tiles)
+        epoch_kernel<<<ep->grid, kWarpsPerBlock * 32, ep->smem, s>>>(S.d_tiles.as<tile_desc>(), ep->n_tiles,
+                                                                     S.d_next.as<unsigned>(), ep->sm_per_warp);
+    if (ep->total_f) cudaMemcpyAsync(S.h_f.ptr, S.d_f.ptr, ep->total_f * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (ep->total_g) cudaMemcpyAsync(S.h_g.ptr, S.d_g.ptr, ep->total_g * sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (ce != cudaSuccess) return cuda_status(ce, "cudaStreamEndCapture");
+    const cudaError_t ie = cudaGraphInstantiate(&S.graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return cuda_status(ie, "cudaGraphInstantiate");
+    return PGX_OK;
+}
+
+int build_plan(pgx_epoch *ep, const pgx_request *reqs, int n_reqs)
+{
+    pgx_context *ctx = ep->ctx;
+    uint32_t max_atoms_smem = 0;
+    for (int i = 0; i < n_reqs; ++i) {
+        const pgx_request &r = reqs[i];
+        req_plan p{};
+        p.kind = r.kind;
+        p.param = r.param;
+        p.n = r.n_dvs;
+        PGX_TRY(problem_nx(r.kind, r.param, &p.nx));
+        PGX_CHECK(p.nx < (1ull << 31), PGX_ERR_CAPACITY, "decision vector dimension exceeds 2^31-1");
+        p.grad = r.grads != nullptr;
+        p.off_x = ep->total_x;
+        p.off_f = ep->total_f;
+        p.off_g = ep->total_g;
+        // rows start 32-byte aligned so the 4-wide variant can use 16-byte loads
+        const uint64_t rowpad = 4;
+        ep->total_x += (p.n * p.nx + rowpad - 1) / rowpad * rowpad;
+        ep->total_f += p.n;
+        if (p.grad) ep->total_g += (p.n * p.nx + rowpad - 1) / rowpad * rowpad;
+        if (p.n) PGX_TRY(tune(ctx, p.kind, p.param, p.nx, p.grad, &p.tune));
+        if (p.kind == PGX_LENNARD_JONES) {
+            max_atoms_smem = std::max<uint32_t>(max_atoms_smem, static_cast<uint32_t>(p.param));
+            PGX_CHECK(6u * p.param * sizeof(double) * kWarpsPerBlock <= 200u * 1024u, PGX_ERR_CAPACITY,
+                      "lennard_jones: too many atoms for the fused epoch kernel");
+        }
+        ep->reqs.push_back(p);
+    }
+    ep->sm_per_warp = 6u * max_atoms_smem;
+    ep->smem = static_cast<size_t>(ep->sm_per_warp) * kWarpsPerBlock * sizeof(double);
+    PGX_CUDA(cudaFuncSetAttribute(epoch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(std::max<size_t>(ep->smem, 48u * 1024u))));
+    int occ = 0;
+    PGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, epoch_kernel, kWarpsPerBlock * 32, ep->smem));
+    PGX_CHECK(occ >= 1, PGX_ERR_CUDA, "epoch kernel cannot be resident");
+    const int max_grid = ctx->num_sms * occ;
+    const double warps = static_cast<double>(max_grid) * kWarpsPerBlock;
+
+    // tiles: cost-proportional sizes, about 8 tiles per warp on average
+    double total_ns = 0;
+    for (const auto &p : ep->reqs) total_ns += p.tune.ns_per_row * static_cast<double>(p.n);
+    const double target_ns = total_ns / (warps * 8.0);
+    struct tile_plan {
+        int req;
+        uint64_t row0;
+        uint32_t rows;
+        double cost;
+    };
+    std::vector<tile_plan> tp;
+    for (size_t i = 0; i < ep->reqs.size(); ++i) {
+        req_plan &p = ep->reqs[i];
+        if (p.n == 0) continue;
+        uint64_t per = 1, rows = 1;
+        if (p.kind != PGX_LENNARD_JONES) {
+            per = p.tune.lanes == 0 ? 1u : 32u / static_cast<uint64_t>(p.tune.lanes);
+            const double want = p.tune.ns_per_row > 0 ? target_ns / p.tune.ns_per_row : 1.0;
+            rows = std::max<uint64_t>(per, static_cast<uint64_t>(want) / per * per);
+            rows = std::min<uint64_t>(rows, 1024u);
+        }
+        for (uint64_t r0 = 0; r0 < p.n; r0 += rows) {
+            const uint32_t nr = static_cast<uint32_t>(std::min<uint64_t>(rows, p.n - r0));
+            tp.push_back({static_cast<int>(i), r0, nr, p.tune.ns_per_row * nr});
+            ++p.tiles;
+        }
+    }
+    std::stable_sort(tp.begin(), tp.end(), [](const tile_plan &a, const tile_plan &b) { return a.cost > b.cost; });
+    PGX_CHECK(tp.size() < (1ull << 31), PGX_ERR_CAPACITY, "too many tiles");
+    ep->n_tiles = static_cast<uint32_t>(tp.size());
+    ep->grid = std::max(1, std::min(max_grid, static_cast<int>((tp.size() + kWarpsPerBlock - 1) / kWarpsPerBlock)));
+
+    for (int si = 0; si < kSets; ++si) {
+        auto &S = ep->sets[si];
+        PGX_CUDA(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
+        PGX_CUDA(cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming));
+        PGX_TRY(S.d_x.ensure(std::max<uint64_t>(ep->total_x, 1) * sizeof(double)));
+        PGX_TRY(S.d_f.ensure(std::max<uint64_t>(ep->total_f, 1) * sizeof(double)));
+        PGX_TRY(S.d_g.ensure(std::max<uint64_t>(ep->total_g, 1) * sizeof(double)));
+        PGX_TRY(S.d_next.ensure(sizeof(unsigned)));
+        PGX_TRY(S.d_tiles.ensure(std::max<size_t>(tp.size(), 1) * sizeof(tile_desc)));
+        PGX_TRY(S.h_x.ensure(std::max<uint64_t>(ep->total_x, 1) * sizeof(double)));
+        PGX_TRY(S.h_f.ensure(std::max<uint64_t>(ep->total_f, 1) * sizeof(double)));
+        PGX_TRY(S.h_g.ensure(std::max<uint64_t>(ep->total_g, 1) * sizeof(double)));
+        std::vector<tile_desc> td(tp.size());
+        for (size_t t = 0; t < tp.size(); ++t) {
+            const req_plan &p = ep->reqs[tp[t].req];
+            tile_desc d{};
+            d.x = S.d_x.as<double>() + p.off_x + tp[t].row0 * p.nx;
+            d.f = S.d_f.as<double>() + p.off_f + tp[t].row0;
+            d.g = p.grad ? S.d_g.as<double>() + p.off_g + tp[t].row0 * p.nx : nullptr;
+            d.rows = tp[t].rows;
+            d.nx = static_cast<uint32_t>(p.nx);
+            d.param = static_cast<uint32_t>(p.param);
+            d.kind = static_cast<uint8_t>(p.kind);
+            if (p.kind == PGX_LENNARD_JONES) {
+                d.variant = d.param <= 32u ? kLJReg : kLJFlat;
+                d.ma = 1;
+                d.lanes = 32;
+            } else if (p.tune.lanes == 0) {
+                d.variant = kRows4;
+                d.lanes = 32;
+            } else {
+                d.variant = kRows;
+                d.lanes = static_cast<uint8_t>(p.tune.lanes);
+            }
+            td[t] = d;
+        }
+        if (!td.empty())
+            PGX_CUDA(cudaMemcpy(S.d_tiles.ptr, td.data(), td.size() * sizeof(tile_desc), cudaMemcpyHostToDevice));
+        PGX_TRY(capture_set(ep, si));
+    }
+    return PGX_OK;
+}
+
+int submit(pgx_epoch *ep, const pgx_request *reqs)
+{
+    PGX_TRY(check_shapes(ep, reqs));
+    const int si = ep->next_set;
+    auto &S = ep->sets[si];
+    PGX_CHECK(!S.in_flight, PGX_ERR_INVALID, "every staging set is in flight: collect an epoch first");
+    std::vector<copy_item> items;
+    for (size_t i = 0; i < ep->reqs.size(); ++i) {
+        const req_plan &p = ep->reqs[i];
+        if (p.n) items.push_back({S.h_x.as<double>() + p.off_x, reqs[i].dvs, p.n * p.nx * sizeof(double)});
+    }
+    parallel_copy(items);
+    PGX_TRY(use_device(ep->ctx));
+    PGX_CUDA(cudaGraphLaunch(S.graph, S.stream));
+    PGX_CUDA(cudaEventRecord(S.done, S.stream));
+    if (ep->n_tiles) ep->ctx->launches += 1;
+    S.pending.assign(reqs, reqs + ep->reqs.size());
+    S.in_flight = true;
+    ep->fifo.push_back(si);
+    ep->next_set = (ep->next_set + 1) % kSets;
+    return PGX_OK;
+}
+
+int collect(pgx_epoch *ep)
+{
+    PGX_CHECK(!ep->fifo.empty(), PGX_ERR_INVALID, "no epoch in flight");
+    const int si = ep->fifo.front();
+    auto &S = ep->sets[si];
+    const cudaError_t e = cudaEventSynchronize(S.done);
+    ep->fifo.pop_front();
+    S.in_flight = false;
+    if (e != cudaSuccess) return cuda_status(e, "epoch");
+    std::vector<copy_item> items;
+    for (size_t i = 0; i < ep->reqs.size(); ++i) {
+        const req_plan &p = ep->reqs[i];
+        const pgx_request &r = S.pending[i];
+        if (!p.n) continue;
+        if (r.fvs) items.push_back({r.fvs, S.h_f.as<double>() + p.off_f, p.n * sizeof(double)});
+        if (r.grads) items.push_back({r.grads, S.h_g.as<double>() + p.off_g, p.n * p.nx * sizeof(double)});
+    }
+    parallel_copy(items);
+    return PGX_OK;
+}
+
+} // namespace
+} // namespace pgx
+
+extern "C" {
+
+int pgx_epoch_create(pgx_context *ctx, const pgx_request *reqs, int n_reqs, pgx_epoch **out)
+{
+    PGX_CHECK(ctx != nullptr && out != nullptr, PGX_ERR_INVALID, "null argument");
+    PGX_CHECK(n_reqs >= 0 && (n_reqs == 0 || reqs != nullptr), PGX_ERR_INVALID, "bad request list");
+    *out = nullptr;
+    std::lock_guard<std::mutex> g(ctx->lock);
+    PGX_TRY(use_device(ctx));
+    auto *ep = new pgx_epoch();
+    ep->ctx = ctx;
+    const int st = build_plan(ep, reqs, n_reqs);
+    if (st != PGX_OK) {
+        pgx_epoch_destroy(ep);
+        return st;
+    }
+    *out = ep;
+    return PGX_OK;
+}
+
+int pgx_epoch_submit(pgx_epoch *ep, const pgx_request *reqs)
+{
+    PGX_CHECK(ep != nullptr, PGX_ERR_INVALID, "null epoch");
+    std::lock_guard<std::mutex> g(ep->ctx->lock);
+    return submit(ep, reqs);
+}
+
+int pgx_epoch_collect(pgx_epoch *ep)
+{
+    PGX_CHECK(ep != nullptr, PGX_ERR_INVALID, "null epoch");
+    return collect(ep);
+}
+
+int pgx_epoch_run(pgx_epoch *ep, const pgx_request *reqs)
+{
+    PGX_CHECK(ep != nullptr, PGX_ERR_INVALID, "null epoch");
+    PGX_CHECK(ep->fifo.empty(), PGX_ERR_INVALID, "epochs in flight: collect them first");
+    PGX_TRY(pgx_epoch_submit(ep, reqs));
+    return collect(ep);
+}
+
+int pgx_epoch_launch_device(pgx_epoch *ep, void *stream)
+{
+    PGX_CHECK(ep != nullptr, PGX_ERR_INVALID, "null epoch");
+    std::lock_guard<std::mutex> g(ep->ctx->lock);
+    PGX_TRY(use_device(ep->ctx));
+    auto &S = ep->sets[0];
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : S.stream;
+    PGX_CUDA(cudaMemsetAsync(S.d_next.ptr, 0, sizeof(unsigned), s));
+    if (ep->n_tiles) {
+        epoch_kernel<<<ep->grid, kWarpsPerBlock * 32, ep->smem, s>>>(S.d_tiles.as<tile_desc>(), ep->n_tiles,
+                                                                     S.d_next.as<unsigned>(), ep->sm_per_warp);
+        PGX_CUDA(cudaGetLastError());
+        ep->ctx->launches += 1;
+    }
+    return PGX_OK;
+}
+
+int pgx_epoch_info(const pgx_epoch *ep, int i, int *lanes, uint64_t *n_tiles)
+{
+    PGX_CHECK(ep != nullptr && i >= 0 && static_cast<size_t>(i) < ep->reqs.size(), PGX_ERR_INVALID, "bad index");
+    if (lanes) *lanes = ep->reqs[i].tune.lanes;
+    if (n_tiles) *n_tiles = ep->reqs[i].tiles;
+    return PGX_OK;
+}
+
+void pgx_epoch_destroy(pgx_epoch *ep)
+{
+    if (!ep) return;
+    if (ep->ctx) cudaSetDevice(ep->ctx->device);
+    for (auto &S : ep->sets) {
+        if (S.stream) cudaStreamSynchronize(S.stream);
+        if (S.graph) cudaGraphExecDestroy(S.graph);
+        if (S.done) cudaEventDestroy(S.done);
+        if (S.stream) cudaStreamDestroy(S.stream);
+        for (pgx::dbuf *b : {&S.d_x, &S.d_f, &S.d_g, &S.d_tiles, &S.d_next}) b->release();
+        for (pgx::hbuf *b : {&S.h_x, &S.h_f, &S.h_g}) b->release();
+    }
+    delete ep;
+}
+
+int pgx_requests_run_plain(pgx_context *ctx, const pgx_request *reqs, int n_reqs)
+{
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    PGX_CHECK(n_reqs >= 0 && (n_reqs == 0 || reqs != nullptr), PGX_ERR_INVALID, "bad request list");
+    for (int i = 0; i < n_reqs; ++i) {
+        const pgx_request &r = reqs[i];
+        if (r.grads)
+            PGX_TRY(pgx_batch_gradient(ctx, r.kind, r.param, r.dvs, r.n_dvs, r.fvs, r.grads));
+        else
+            PGX_TRY(pgx_batch_fitness(ctx, r.kind, r.param, r.dvs, r.n_dvs, r.fvs));
+    }
+    return PGX_OK;
+}
+
+} // extern "C"

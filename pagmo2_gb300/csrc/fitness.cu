@@ -54,6 +54,18 @@ __global__ void __launch_bounds__(128) lj_reg_kernel(const double *__restrict__ 
 }
 
 template <bool GRAD>
+__global__ void __launch_bounds__(128) lj_flat_kernel(const double *__restrict__ x, uint64_t n, uint32_t na,
+                                                      uint32_t nx, double *__restrict__ f, double *__restrict__ g)
+{
+    extern __shared__ double smem[];
+    const unsigned warp = threadIdx.x >> 5;
+    const unsigned wpb = blockDim.x >> 5;
+    double *sm = smem + static_cast<size_t>(warp) * (GRAD ? 6u : 3u) * na;
+    for (uint64_t c = static_cast<uint64_t>(blockIdx.x) * wpb + warp; c < n; c += static_cast<uint64_t>(gridDim.x) * wpb)
+        lj_cluster_flat<GRAD>(x + c * nx, na, nx, sm, f ? f + c : nullptr, GRAD ? g + c * nx : nullptr);
+}
+
+template <bool GRAD>
 __global__ void __launch_bounds__(128) lj_smem_kernel(const double *__restrict__ x, uint64_t n, uint32_t na,
                                                       uint32_t nx, double *__restrict__ f, double *__restrict__ g)
 {
@@ -115,6 +127,14 @@ int lanes_per_row(uint32_t nx)
     return nx >= 2 ? 2 : 1;
 }
 
+// lennard_jones: the flattened pair walk when the register variant (lane l
+// owns atoms l, l+32, ...) would leave more than 5% of its lanes idle.
+bool lj_use_flat(uint32_t na)
+{
+    const uint32_t ma = (na + 31u) / 32u;
+    return na >= 33u && 100u * na < 95u * 32u * ma;
+}
+
 namespace
 {
 
@@ -173,6 +193,12 @@ int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64
         const size_t per_warp = static_cast<size_t>(grad ? 6u : 3u) * na * sizeof(double);
         PGX_CHECK(per_warp <= 200u * 1024u, PGX_ERR_CAPACITY,
                   "lennard_jones: too many atoms for one cluster per warp");
+        if (lj_use_flat(na)) {
+            st = grad ? launch_lj(lj_flat_kernel<true>, true, d_x, n, na, nx32, d_f, d_g, stream, num_sms)
+                      : launch_lj(lj_flat_kernel<false>, false, d_x, n, na, nx32, d_f, d_g, stream, num_sms);
+            if (st == PGX_OK && launches) ++*launches;
+            return st;
+        }
         switch ((na + 31u) / 32u) {
             case 1: st = launch_lj_reg<1>(grad, d_x, n, na, nx32, d_f, d_g, stream, num_sms); break;
             case 2: st = launch_lj_reg<2>(grad, d_x, n, na, nx32, d_f, d_g, stream, num_sms); break;
@@ -192,6 +218,31 @@ int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64
     }
     if (st == PGX_OK && launches) ++*launches;
     return st;
+}
+
+// Same as launch_eval for rastrigin/rosenbrock with the variant forced:
+// lanes = 1..32 strided rows with that many lanes per row, lanes = 0 the
+// 4-wide rosenbrock rows. Used by the autotuner.
+int launch_rows_variant(int kind, uint64_t nx, const double *d_x, uint64_t n, double *d_f, double *d_g, int lanes,
+                        cudaStream_t stream, int num_sms)
+{
+    if (n == 0) return PGX_OK;
+    const bool grad = d_g != nullptr;
+    const uint32_t nx32 = static_cast<uint32_t>(nx);
+    if (lanes == 0) {
+        PGX_CHECK(kind == PGX_ROSENBROCK && nx % 4 == 0 && reinterpret_cast<uintptr_t>(d_x) % 16 == 0,
+                  PGX_ERR_INVALID, "4-wide rows need rosenbrock, nx % 4 == 0 and aligned rows");
+        return grad ? launch_simple(rosenbrock_v4_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
+                    : launch_simple(rosenbrock_v4_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
+    }
+    switch (lanes) {
+        case 32: return launch_rows<32>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);
+        case 16: return launch_rows<16>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);
+        case 8: return launch_rows<8>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);
+        case 4: return launch_rows<4>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);
+        case 2: return launch_rows<2>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);
+        default: return launch_rows<1>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);
+    }
 }
 
 } // namespace pgx

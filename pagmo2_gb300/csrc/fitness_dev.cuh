@@ -471,6 +471,79 @@ __device__ __forceinline__ void lj_cluster_reg(const double *__restrict__ xr, ui
     __syncwarp();
 }
 
+// Flattened variant (N >= 33): the half-ring pairs (k, i) are enumerated in
+// one sequence and the 32 lanes take 32 consecutive pairs per step, so every
+// lane is busy (the register variant idles the lanes beyond N in its last
+// chunk). A step spans at most two values of k; since N >= 33, its lanes
+// still hold distinct i and distinct j, so both sides of the pairs are
+// accumulated in shared memory in two conflict-free phases.
+template <bool GRAD>
+__device__ __forceinline__ void lj_cluster_flat(const double *__restrict__ xr, uint32_t na, uint32_t nx, double *sm,
+                                                double *f_out, double *__restrict__ gr)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    double *px = sm, *py = px + na, *pz = py + na;
+    double *gx = pz + na, *gy = gx + na, *gz = gy + na;
+    lj_decode(xr, na, px, py, pz, gx, gy, gz, GRAD);
+    const bool even = (na & 1u) == 0u;
+    const uint32_t kmax = na / 2u;
+    const uint32_t pairs = na * (na - 1u) / 2u;
+    double e = 0.0;
+    int zero = 0;
+    uint32_t k = 1u, i = lane; // pair number q0 + lane, q0 = 0
+    for (uint32_t q0 = 0; q0 < pairs; q0 += 32u) {
+        const bool act = q0 + lane < pairs;
+        uint32_t j = i + k;
+        if (j >= na) j -= na;
+        double dx = 0.0, dy = 0.0, dz = 0.0, coef = 0.0;
+        if (act) {
+            dx = px[i] - px[j];
+            dy = py[i] - py[j];
+            dz = pz[i] - pz[j];
+            const double d = fma(dx, dx, fma(dy, dy, dz * dz));
+            const double inv = lj_rcp(d);
+            const double s = inv * inv * inv;
+            const double term = fma(s, s, -s);
+            if (__double_as_longlong(d) != 0)
+                e += term;
+            else
+                zero = 1;
+            if (GRAD) coef = fma(s, s, term) * inv;
+        }
+        if (GRAD) {
+            if (act) {
+                gx[i] = fma(coef, dx, gx[i]);
+                gy[i] = fma(coef, dy, gy[i]);
+                gz[i] = fma(coef, dz, gz[i]);
+            }
+            __syncwarp();
+            if (act) {
+                gx[j] = fma(-coef, dx, gx[j]);
+                gy[j] = fma(-coef, dy, gy[j]);
+                gz[j] = fma(-coef, dz, gz[j]);
+            }
+            __syncwarp();
+        }
+        // advance this lane's pair by 32 in the (k, i) sequence
+        i += 32u;
+        for (;;) {
+            const uint32_t ilim = (even && k == kmax) ? kmax : na;
+            if (i < ilim || k >= kmax) break;
+            i -= ilim;
+            ++k;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(kFull, e, o);
+    zero = __any_sync(kFull, zero);
+    if (lane == 0 && f_out) *f_out = zero ? (isnan(e) ? e : HUGE_VAL) : 4.0 * e;
+    if (GRAD) {
+        __syncwarp();
+        lj_store_gradient(nx, gx, gy, gz, gr);
+    }
+    __syncwarp();
+}
+
 // Shared-memory variant for any N: both sides of each pair go through shared
 // memory, in two conflict-free phases (the lanes of one step hold distinct i
 // and distinct j).

@@ -103,6 +103,14 @@ int problem_nx(int kind, uint64_t param, uint64_t *nx);
 // Lanes per row (1..32) used by the strided rastrigin/rosenbrock row kernels.
 int lanes_per_row(uint32_t nx);
 
+// Whether lennard_jones clusters of na atoms use the flattened pair walk.
+bool lj_use_flat(uint32_t na);
+
+// rastrigin/rosenbrock with a forced row variant (lanes 1..32, or 0 for the
+// 4-wide rosenbrock rows); for the autotuner.
+int launch_rows_variant(int kind, uint64_t nx, const double *d_x, uint64_t n, double *d_f, double *d_g, int lanes,
+                        cudaStream_t stream, int num_sms);
+
 // Batch fitness (+ gradient when d_g != nullptr) for one problem on `stream`.
 // Returns the number of kernel launches issued through *launches.
 int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64_t n, double *d_f, double *d_g,

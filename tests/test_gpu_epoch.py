@@ -1,0 +1,102 @@
+"""The fused archipelago epoch (through the C ABI) against the island-by-island
+path and the long-double oracle, including two epochs in flight."""
+import numpy as np
+import pytest
+
+from pagmo2_gb300 import _native as N
+from pagmo2_gb300 import archipelago as A
+from pagmo2_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-13
+
+
+def shapes_and_batches(islands=18, seed=5, grad_every=1):
+    reqs = W.archipelago(islands, seed=seed, pop_hi=1024)
+    shapes = [(r.kind, r.param, r.n, i % grad_every == 0) for i, r in enumerate(reqs)]
+    return shapes, [r.dvs for r in reqs]
+
+
+def check(orc, shapes, batches, outs):
+    for (k, p, n, g), x, (f, gr) in zip(shapes, batches, outs):
+        rows = np.unique(np.linspace(0, n - 1, min(n, 6)).astype(int))
+        fl, fs = orc.batch_fitness_ld(k, p, x[rows])
+        assert np.max(np.abs(f[rows] - fl) / fs) <= TOL, (k, p)
+        if g:
+            gl, gs = orc.batch_gradient_ld(k, p, x[rows])
+            assert np.max(np.abs(gr[rows] - gl) / np.maximum(gs, 1e-300)) <= TOL, (k, p)
+
+
+def test_epoch_matches_plain_and_oracle(ctx, orc):
+    shapes, batches = shapes_and_batches(grad_every=3)  # some islands fitness only
+    ep = A.Epoch(shapes, ctx)
+    try:
+        fused = ep.run(batches)
+        plain = A.run_plain(shapes, batches, ctx)
+        check(orc, shapes, batches, fused)
+        for (k, p, n, g), x, (f1, g1), (f2, g2) in zip(shapes, batches, fused, plain):
+            fl, fs = orc.batch_fitness_ld(k, p, x)
+            assert np.max(np.abs(f1 - f2) / fs) <= 2 * TOL
+        for i in range(len(shapes)):
+            lanes, tiles = ep.info(i)
+            assert tiles >= 1 and lanes in (0, 1, 2, 4, 8, 16, 32)
+    finally:
+        ep.close()
+
+
+def test_epochs_in_flight(ctx, orc):
+    shapes, b1 = shapes_and_batches(islands=9, seed=7)
+    b2 = [W.uniform_batch(k, p, n, seed=100 + i) for i, (k, p, n, g) in enumerate(shapes)]
+    b3 = [W.uniform_batch(k, p, n, seed=200 + i) for i, (k, p, n, g) in enumerate(shapes)]
+    ep = A.Epoch(shapes, ctx)
+    try:
+        o1 = ep.submit(b1)
+        o2 = ep.submit(b2)
+        o3 = ep.submit(b3)
+        with pytest.raises(ValueError):
+            ep.submit(b1)  # every staging set busy
+        r1 = ep.collect()
+        r2 = ep.collect()
+        r3 = ep.collect()
+        assert r1 is o1 and r2 is o2 and r3 is o3
+        check(orc, shapes, b1, r1)
+        check(orc, shapes, b2, r2)
+        check(orc, shapes, b3, r3)
+        # repeat run gives identical results (deterministic tiles and order)
+        again = ep.run(b1)
+        for (f1, g1), (f2, g2) in zip(r1, again):
+            assert np.array_equal(f1, f2) and (g1 is None or np.array_equal(g1, g2))
+    finally:
+        ep.close()
+
+
+def test_epoch_shape_mismatch_is_rejected(ctx):
+    shapes, batches = shapes_and_batches(islands=3, seed=9)
+    ep = A.Epoch(shapes, ctx)
+    try:
+        bad = (N.pgx_request * 3)()
+        for i, (k, p, n, g) in enumerate(shapes):
+            bad[i].kind, bad[i].param, bad[i].n_dvs = k, p, n + 1
+        with pytest.raises(ValueError, match="does not match the epoch plan"):
+            N.check(N.lib().pgx_epoch_run(ep.handle, bad))
+    finally:
+        ep.close()
+
+
+def test_collector_threads_on_gpu(ctx, orc):
+    import threading
+
+    shapes, batches = shapes_and_batches(islands=6, seed=11)
+    col = A.Collector(shapes, deadline_s=5.0, ctx=ctx)
+    out = {}
+
+    def island(i):
+        out[i] = col.evaluate(i, batches[i])
+
+    ts = [threading.Thread(target=island, args=(i,)) for i in range(6)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join(timeout=60)
+    assert col.epochs_run == 1 and sorted(out) == list(range(6))
+    check(orc, shapes, batches, [out[i] for i in range(6)])
