@@ -1,0 +1,89 @@
+// gpu_bfe: a user-defined batch fitness evaluator (UDBFE) for pagmo::bfe
+// that evaluates pagmo's own rastrigin, rosenbrock and lennard_jones UDPs,
+// and the GPU UDPs of gpu_problems.hpp, on a GB300.
+//
+// A UDBFE is a callable vector_double(const problem &, const vector_double &)
+// (include/pagmo/bfe.hpp:68-108). Like every UDBFE it leaves the fevals
+// counter alone: pagmo::bfe::operator() checks the output and adds the
+// number of evaluated vectors itself (src/bfe.cpp:91-110,
+// src/batch_evaluators/member_bfe.cpp:42-44). Any other problem is rejected
+// with std::invalid_argument (there is no CPU fallback).
+#ifndef PAGMO_GB300_GPU_BFE_HPP
+#define PAGMO_GB300_GPU_BFE_HPP
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+#include <pagmo/problem.hpp>
+#include <pagmo/problems/lennard_jones.hpp>
+#include <pagmo/problems/rastrigin.hpp>
+#include <pagmo/problems/rosenbrock.hpp>
+#include <pagmo/threading.hpp>
+#include <pagmo/types.hpp>
+
+#include "gpu_problems.hpp"
+#include "pgx.hpp"
+
+namespace pagmo_gb300
+{
+
+class gpu_bfe
+{
+public:
+    explicit gpu_bfe(int device = 0) : m_device(device) {}
+
+    pagmo::vector_double operator()(const pagmo::problem &p, const pagmo::vector_double &dvs) const
+    {
+        if (const auto *g = p.extract<gpu_rastrigin>()) return g->batch_fitness(dvs);
+        if (const auto *g = p.extract<gpu_rosenbrock>()) return g->batch_fitness(dvs);
+        if (const auto *g = p.extract<gpu_lennard_jones>()) return g->batch_fitness(dvs);
+        int kind = 0;
+        std::uint64_t param = p.get_nx();
+        if (p.extract<pagmo::rastrigin>()) {
+            kind = PGX_RASTRIGIN;
+        } else if (p.extract<pagmo::rosenbrock>()) {
+            kind = PGX_ROSENBROCK;
+        } else if (p.extract<pagmo::lennard_jones>()) {
+            kind = PGX_LENNARD_JONES;
+            param = (p.get_nx() + 6u) / 3u;
+        } else {
+            throw std::invalid_argument("Cannot use a gpu_bfe on the problem '" + p.get_name()
+                                        + "': only rastrigin, rosenbrock and lennard_jones are evaluated on the GPU");
+        }
+        const std::uint64_t n = dvs.size() / p.get_nx(); // pagmo::bfe checked divisibility
+        pagmo::vector_double fvs(n);
+        if (n) check(pgx_batch_fitness(device_context(m_device), kind, param, dvs.data(), n, fvs.data()));
+        return fvs;
+    }
+
+    std::string get_name() const
+    {
+        return "GB300 batch fitness evaluator";
+    }
+
+    std::string get_extra_info() const
+    {
+        return "\tDevice: " + std::to_string(m_device) + "\n";
+    }
+
+    // callable from concurrent island threads: the library serialises work
+    // per device, and the object itself is never modified
+    pagmo::thread_safety get_thread_safety() const
+    {
+        return pagmo::thread_safety::basic;
+    }
+
+    template <typename Archive>
+    void serialize(Archive &ar, unsigned)
+    {
+        ar &m_device;
+    }
+
+private:
+    int m_device = 0;
+};
+
+} // namespace pagmo_gb300
+
+#endif

@@ -1,0 +1,159 @@
+// GPU-backed user-defined problems for pagmo: the rastrigin, rosenbrock and
+// lennard_jones UDPs (src/problems/{rastrigin,rosenbrock,lennard_jones}.cpp)
+// with the same dimensions, bounds, names and constructor errors, whose
+// evaluations run on a GB300 through libpgx.
+//
+// Besides fitness/get_bounds (the UDP minimum, include/pagmo/problem.hpp:436-448)
+// they provide batch_fitness, which member_bfe and default_bfe pick
+// (src/batch_evaluators/default_bfe.cpp:53-58), gradient
+// (src/problem.cpp:456-467; dense, nf = 1) and the batch extension
+// batch_gradient. Thread safety is constant: evaluations only read the object.
+#ifndef PAGMO_GB300_GPU_PROBLEMS_HPP
+#define PAGMO_GB300_GPU_PROBLEMS_HPP
+
+#include <cstdint>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include <pagmo/threading.hpp>
+#include <pagmo/types.hpp>
+
+#include "pgx.hpp"
+
+namespace pagmo_gb300
+{
+
+namespace detail
+{
+
+template <int Kind>
+class gpu_udp
+{
+public:
+    gpu_udp() = default;
+    explicit gpu_udp(std::uint64_t param, int device = 0) : m_param(param), m_device(device)
+    {
+        check(pgx_problem_nx(Kind, param, &m_nx)); // the reference constructors' checks and messages
+    }
+
+    pagmo::vector_double fitness(const pagmo::vector_double &x) const
+    {
+        return batch_fitness(x);
+    }
+
+    pagmo::vector_double batch_fitness(const pagmo::vector_double &dvs) const
+    {
+        const std::uint64_t n = rows(dvs);
+        pagmo::vector_double f(n);
+        if (n) check(pgx_batch_fitness(device_context(m_device), Kind, m_param, dvs.data(), n, f.data()));
+        return f;
+    }
+
+    pagmo::vector_double gradient(const pagmo::vector_double &x) const
+    {
+        return batch_gradient(x).second;
+    }
+
+    // (fitness, gradient) of a whole batch in one GPU pass: n fitness values
+    // and n * nx gradient entries, row-major.
+    std::pair<pagmo::vector_double, pagmo::vector_double> batch_gradient(const pagmo::vector_double &dvs) const
+    {
+        const std::uint64_t n = rows(dvs);
+        std::pair<pagmo::vector_double, pagmo::vector_double> out{pagmo::vector_double(n),
+                                                                  pagmo::vector_double(n * m_nx)};
+        if (n)
+            check(pgx_batch_gradient(device_context(m_device), Kind, m_param, dvs.data(), n, out.first.data(),
+                                     out.second.data()));
+        return out;
+    }
+
+    std::pair<pagmo::vector_double, pagmo::vector_double> get_bounds() const
+    {
+        std::pair<pagmo::vector_double, pagmo::vector_double> b{pagmo::vector_double(m_nx),
+                                                                pagmo::vector_double(m_nx)};
+        check(pgx_problem_bounds(Kind, m_param, b.first.data(), b.second.data()));
+        return b;
+    }
+
+    pagmo::thread_safety get_thread_safety() const
+    {
+        return pagmo::thread_safety::constant;
+    }
+
+    std::uint64_t param() const
+    {
+        return m_param;
+    }
+
+    template <typename Archive>
+    void serialize(Archive &ar, unsigned)
+    {
+        ar &m_param;
+        ar &m_nx;
+        ar &m_device;
+    }
+
+protected:
+    std::uint64_t rows(const pagmo::vector_double &dvs) const
+    {
+        if (m_nx == 0 || dvs.size() % m_nx)
+            throw std::invalid_argument("Invalid argument for a batch fitness evaluation: the length of the vector "
+                                        "representing the decision vectors, "
+                                        + std::to_string(dvs.size())
+                                        + ", is not an exact multiple of the dimension of the problem, "
+                                        + std::to_string(m_nx));
+        return dvs.size() / m_nx;
+    }
+
+    std::uint64_t m_param = 0;
+    std::uint64_t m_nx = 0;
+    int m_device = 0;
+};
+
+} // namespace detail
+
+// rastrigin{dim}: f = 10 n + sum (x_i^2 - 10 cos(2 pi x_i)) on [-5.12, 5.12]^n.
+class gpu_rastrigin : public detail::gpu_udp<PGX_RASTRIGIN>
+{
+public:
+    explicit gpu_rastrigin(unsigned dim = 1u, int device = 0) : gpu_udp(dim, device) {}
+    std::string get_name() const
+    {
+        return "Rastrigin Function";
+    }
+    pagmo::vector_double best_known() const
+    {
+        return pagmo::vector_double(m_nx, 0.);
+    }
+};
+
+// rosenbrock{dim}: f = sum 100 (x_i^2 - x_{i+1})^2 + (x_i - 1)^2 on [-5, 10]^n.
+class gpu_rosenbrock : public detail::gpu_udp<PGX_ROSENBROCK>
+{
+public:
+    explicit gpu_rosenbrock(pagmo::vector_double::size_type dim = 2u, int device = 0) : gpu_udp(dim, device) {}
+    std::string get_name() const
+    {
+        return "Multidimensional Rosenbrock Function";
+    }
+    pagmo::vector_double best_known() const
+    {
+        return pagmo::vector_double(m_nx, 1.);
+    }
+};
+
+// lennard_jones{atoms}: 4 sum_{i<j} (r^-12 - r^-6), three coordinates pinned.
+class gpu_lennard_jones : public detail::gpu_udp<PGX_LENNARD_JONES>
+{
+public:
+    explicit gpu_lennard_jones(unsigned atoms = 3u, int device = 0) : gpu_udp(atoms, device) {}
+    std::string get_name() const
+    {
+        return "Lennard Jones Cluster (" + std::to_string(m_param) + " atoms)";
+    }
+};
+
+} // namespace pagmo_gb300
+
+#endif

@@ -1,0 +1,123 @@
+// Host-side checks of the pagmo adaptors (include/pagmo_gb300/) against the
+// reference's own type machinery: the GPU UDPs are UDPs with batch_fitness
+// and gradient, gpu_bfe is a UDBFE, errors are pagmo's, and without a GPU
+// every evaluation fails loudly instead of falling back to the CPU.
+// Exit status 0 = all checks passed; with PGX_TEST_HAVE_GPU=1 the
+// evaluations are also compared with the reference's own results.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <pagmo/batch_evaluators/thread_bfe.hpp>
+#include <pagmo/bfe.hpp>
+#include <pagmo/problem.hpp>
+#include <pagmo/problems/null_problem.hpp>
+#include <pagmo/problems/rastrigin.hpp>
+#include <pagmo/problems/rosenbrock.hpp>
+#include <pagmo/utils/multi_objective.hpp>
+
+#include <pagmo_gb300/gpu_bfe.hpp>
+#include <pagmo_gb300/gpu_problems.hpp>
+#include <pagmo_gb300/multi_objective.hpp>
+
+using namespace pagmo_gb300;
+
+static int failures = 0;
+#define CHECK(c)                                                                                                      \
+    do {                                                                                                               \
+        if (!(c)) {                                                                                                    \
+            std::fprintf(stderr, "FAILED %s:%d: %s\n", __FILE__, __LINE__, #c);                                        \
+            ++failures;                                                                                                \
+        }                                                                                                              \
+    } while (0)
+
+template <typename E, typename F>
+bool throws_with(F &&f, const std::string &needle)
+{
+    try {
+        f();
+    } catch (const E &e) {
+        return std::string(e.what()).find(needle) != std::string::npos;
+    } catch (...) {
+        return false;
+    }
+    return false;
+}
+
+static_assert(pagmo::is_udbfe<gpu_bfe>::value, "gpu_bfe must be a UDBFE");
+static_assert(pagmo::is_udp<gpu_rastrigin>::value, "gpu_rastrigin must be a UDP");
+static_assert(pagmo::is_udp<gpu_rosenbrock>::value, "gpu_rosenbrock must be a UDP");
+static_assert(pagmo::is_udp<gpu_lennard_jones>::value, "gpu_lennard_jones must be a UDP");
+static_assert(pagmo::has_batch_fitness<gpu_rosenbrock>::value, "batch_fitness hook");
+static_assert(pagmo::has_gradient<gpu_rosenbrock>::value, "gradient hook");
+static_assert(pagmo::has_gradient<gpu_lennard_jones>::value, "gradient hook");
+
+int main()
+{
+    const bool gpu = std::getenv("PGX_TEST_HAVE_GPU") && std::string(std::getenv("PGX_TEST_HAVE_GPU")) == "1";
+
+    // problem facade: dims, bounds, hooks, thread safety
+    pagmo::problem p{gpu_rosenbrock{10u}};
+    CHECK(p.get_nx() == 10u && p.get_nf() == 1u);
+    CHECK(p.has_batch_fitness() && p.has_gradient());
+    CHECK(p.get_thread_safety() == pagmo::thread_safety::constant);
+    CHECK(p.get_bounds() == pagmo::problem{pagmo::rosenbrock{10u}}.get_bounds());
+    CHECK(pagmo::problem{gpu_rastrigin{7u}}.get_bounds() == pagmo::problem{pagmo::rastrigin{7u}}.get_bounds());
+    CHECK(pagmo::problem{gpu_lennard_jones{5u}}.get_nx() == 9u);
+    CHECK(pagmo::problem{gpu_lennard_jones{5u}}.get_name().find("Jones") != std::string::npos);
+
+    // constructor errors are the reference's
+    CHECK(throws_with<std::invalid_argument>([] { gpu_rastrigin{0u}; }, "must have minimum 1 dimension"));
+    CHECK(throws_with<std::invalid_argument>([] { gpu_rosenbrock{1u}; }, "must have minimum 2 dimensions"));
+    CHECK(throws_with<std::invalid_argument>([] { gpu_lennard_jones{2u}; }, "greater than 2"));
+
+    // the UDBFE wrapped by pagmo::bfe
+    pagmo::bfe b{gpu_bfe{}};
+    CHECK(b.get_name() == "GB300 batch fitness evaluator");
+    CHECK(b.get_thread_safety() == pagmo::thread_safety::basic);
+    CHECK(b.is<gpu_bfe>());
+    CHECK(throws_with<std::invalid_argument>([&b] { b(pagmo::problem{pagmo::null_problem{}}, {0.5, 0.5}); },
+                                             "Cannot use a gpu_bfe on the problem"));
+    // pagmo::bfe's own input check runs before the UDBFE
+    CHECK(throws_with<std::invalid_argument>([&b] { b(pagmo::problem{pagmo::rosenbrock{4u}}, {1., 2., 3.}); },
+                                             "is not an exact multiple"));
+
+    // multi-objective: argument errors before any device work
+    CHECK(throws_with<std::invalid_argument>([] { fast_non_dominated_sorting({{1., 2.}}); },
+                                             "At least two points"));
+    CHECK(throws_with<std::invalid_argument>([] { crowding_distance({{1.}, {2.}}); }, "at least two objectives"));
+
+    std::vector<double> dvs(40);
+    for (size_t i = 0; i < dvs.size(); ++i) dvs[i] = -2.0 + 0.1 * static_cast<double>(i);
+    if (!gpu) {
+        // no device: evaluations fail loudly, never on the CPU
+        pagmo::problem pr{pagmo::rosenbrock{4u}};
+        CHECK(throws_with<std::runtime_error>([&] { b(pr, dvs); }, ""));
+        CHECK(pr.get_fevals() == 0u);
+        CHECK(throws_with<std::runtime_error>([&] { pagmo::problem{gpu_rosenbrock{4u}}.fitness({1., 1., 1., 1.}); },
+                                              ""));
+    } else {
+        // with a device: bfe{gpu_bfe} against bfe{thread_bfe}, fevals counted once
+        pagmo::problem pr{pagmo::rosenbrock{4u}};
+        const auto f_gpu = b(pr, dvs);
+        CHECK(pr.get_fevals() == 10u);
+        const auto f_ref = pagmo::bfe{pagmo::thread_bfe{}}(pagmo::problem{pagmo::rosenbrock{4u}}, dvs);
+        for (size_t i = 0; i < f_ref.size(); ++i) CHECK(std::abs(f_gpu[i] - f_ref[i]) <= 1e-13 * std::abs(f_ref[i]));
+        pagmo::problem pg{gpu_rosenbrock{4u}};
+        CHECK(pg.gradient({.1, .2, .3, .4}).size() == 4u);
+        auto r = fast_non_dominated_sorting({{0, 7}, {1, 5}, {2, 3}, {4, 2}, {7, 1}, {10, 0}, {2, 6}, {4, 4}, {10, 2},
+                                             {6, 6}, {9, 5}});
+        auto w = pagmo::fast_non_dominated_sorting({{0, 7}, {1, 5}, {2, 3}, {4, 2}, {7, 1}, {10, 0}, {2, 6}, {4, 4},
+                                                    {10, 2}, {6, 6}, {9, 5}});
+        CHECK(r == w);
+    }
+    if (failures) {
+        std::fprintf(stderr, "%d check(s) failed\n", failures);
+        return 1;
+    }
+    std::printf("adaptor checks passed (%s)\n", gpu ? "with GPU" : "no GPU");
+    return 0;
+}
