@@ -19,8 +19,9 @@
 //     processed, so the order is by (max position of q's dominators in front k,
 //     q).
 //  4. crowding_rank / crowding_accumulate: for each front and objective the
-//     sorted position of every point (ties broken by position in the front),
-//     then the reference's neighbour differences over the objective range, in
+//     sorted position of every point (ties keep the previous objective's
+//     order, as a stable sort in the reference's loop would), then the
+//     reference's neighbour differences over the objective range, in
 //     objective order per point.
 #include "pgx_internal.cuh"
 
@@ -33,7 +34,7 @@ namespace
 {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr unsigned long long kSpinLimit = 1ull << 22; // x 256 ns sleep: about one second
+constexpr unsigned long long kSpinLimit = 1ull << 24; // x (64 ns sleep + a poll): a second or more
 
 __device__ __forceinline__ long long order_key(double v)
 {
@@ -160,7 +161,7 @@ __device__ bool grid_sync(peel_state *st)
                     atomicExch(&st->err, 1);
                     break;
                 }
-                __nanosleep(256);
+                __nanosleep(64);
             }
         }
         __threadfence();
@@ -174,20 +175,27 @@ constexpr int kTile = 2048; // (key, index) pairs per shared-memory tile
 // Front peeling, one front per iteration, two grid barriers per front.
 //
 // Phase A: every unassigned point j whose row of Dt has no unassigned
-// dominator joins front k. Warps take 8-candidate slices of the rem bit set
-// and scan each candidate's row cooperatively (128 words per step, early
+// dominator joins front k. Warps take 4-candidate slices of the rem bit set
+// and scan each candidate's row cooperatively (256 words per step, early
 // exit). A member's ordering key is the highest position, in front k-1, of
-// one of its dominators: a reverse scan over front k-1's positions (32 at a
-// time, ballot) stops at the first hit.
+// one of its dominators: a reverse scan over front k-1's positions (staged in
+// shared memory; 128 at a time, ballots) stops at the first hit.
 // Phase C: the position of a member is the number of members with a smaller
 // (key, index), counted against shared-memory tiles; members are written to
 // front_indices, ranked, and cleared from rem.
-__global__ void __launch_bounds__(256) peel_kernel(const uint32_t *__restrict__ Dt, uint32_t n, uint32_t W,
-                                                   uint32_t W8, uint32_t *rem, int32_t *list, int32_t *keyv,
-                                                   int32_t *rank, int32_t *front_offsets, int32_t *front_indices,
-                                                   peel_state *st)
+constexpr int kPeelThreads = 1024; // one block per SM: few arrivals per grid barrier
+constexpr int kLocalMembers = 1024; // members a block collects before one global append
+constexpr int kRemWords = 4096;     // rem staged in shared memory up to 131072 points
+
+__global__ void __launch_bounds__(kPeelThreads) peel_kernel(const uint32_t *__restrict__ Dt, uint32_t n, uint32_t W,
+                                                            uint32_t W8, uint32_t *rem, int32_t *list, int32_t *keyv,
+                                                            int32_t *rank, int32_t *front_offsets,
+                                                            int32_t *front_indices, peel_state *st)
 {
     extern __shared__ int32_t sh[]; // kTile keys, then kTile indices
+    __shared__ int32_t s_list[kLocalMembers], s_key[kLocalMembers];
+    __shared__ uint32_t s_rem[kRemWords];
+    __shared__ int s_cnt, s_base;
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nthreads = gridDim.x * blockDim.x;
@@ -196,23 +204,33 @@ __global__ void __launch_bounds__(256) peel_kernel(const uint32_t *__restrict__ 
     int k = 0;
     for (;; ++k) {
         int *cnt = &st->counts[k & 1];
-        // ---- Phase A
-        const uint32_t tasks = W * 4u;
+        // front k-1's members, by position, in shared memory when they fit
+        const bool prev_in_smem = size_prev <= 2 * kTile;
+        if (k > 0 && prev_in_smem)
+            for (int t = threadIdx.x; t < size_prev; t += blockDim.x) sh[t] = __ldcg(front_indices + off_prev + t);
+        // the unassigned set, read by every row scan of this phase
+        const bool rem_in_smem = W <= static_cast<uint32_t>(kRemWords);
+        if (rem_in_smem)
+            for (uint32_t w = threadIdx.x; w < W; w += blockDim.x) s_rem[w] = __ldcg(rem + w);
+        if (threadIdx.x == 0) s_cnt = 0;
+        __syncthreads();
+        // ---- Phase A (tasks: 4-candidate slices of the rem bit set)
+        const uint32_t tasks = W * 8u;
         for (uint32_t t = gwarp; t < tasks; t += nwarps) {
-            const uint32_t w = t >> 2, sub = t & 3u;
-            uint32_t cand = (__ldcg(rem + w) >> (sub * 8u)) & 0xffu;
+            const uint32_t w = t >> 3, sub = t & 7u;
+            uint32_t cand = (__ldcg(rem + w) >> (sub * 4u)) & 0xfu;
             while (cand) {
                 const uint32_t b = static_cast<uint32_t>(__ffs(cand) - 1);
                 cand &= cand - 1u;
-                const uint32_t j = w * 32u + sub * 8u + b;
+                const uint32_t j = w * 32u + sub * 4u + b;
                 const uint32_t *row = Dt + static_cast<uint64_t>(j) * W8;
                 bool hit = false;
-                for (uint32_t base = 0; base < W; base += 128u) {
+                for (uint32_t base = 0; base < W; base += 256u) { // 8 independent loads per lane
                     uint32_t v = 0u;
 #pragma unroll
-                    for (uint32_t u = 0; u < 4u; ++u) {
+                    for (uint32_t u = 0; u < 8u; ++u) {
                         const uint32_t ww = base + u * 32u + lane;
-                        if (ww < W) v |= __ldg(row + ww) & __ldcg(rem + ww);
+                        if (ww < W) v |= __ldg(row + ww) & (rem_in_smem ? s_rem[ww] : __ldcg(rem + ww));
                     }
                     if (__any_sync(kFull, v != 0u)) {
                         hit = true;
@@ -223,26 +241,46 @@ __global__ void __launch_bounds__(256) peel_kernel(const uint32_t *__restrict__ 
                 int key = 0;
                 if (k > 0) {
                     key = -1;
-                    for (int top = size_prev - 1; top >= 0; top -= 32) {
-                        const int p = top - static_cast<int>(lane);
-                        bool h = false;
-                        if (p >= 0) {
-                            const uint32_t d = static_cast<uint32_t>(__ldcg(front_indices + off_prev + p));
-                            h = (__ldg(row + (d >> 5)) >> (d & 31u)) & 1u;
+                    for (int top = size_prev - 1; top >= 0 && key < 0; top -= 128) { // 4 x 32 positions per step
+                        unsigned bal[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const int p = top - 32 * u - static_cast<int>(lane);
+                            bool h = false;
+                            if (p >= 0) {
+                                const uint32_t d = static_cast<uint32_t>(
+                                    prev_in_smem ? sh[p] : __ldcg(front_indices + off_prev + p));
+                                h = (__ldg(row + (d >> 5)) >> (d & 31u)) & 1u;
+                            }
+                            bal[u] = __ballot_sync(kFull, h);
                         }
-                        const unsigned bal = __ballot_sync(kFull, h);
-                        if (bal) {
-                            key = top - (__ffs(bal) - 1);
-                            break;
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            if (key < 0 && bal[u]) key = top - 32 * u - (__ffs(bal[u]) - 1);
                         }
                     }
                 }
                 if (lane == 0) {
-                    const int s = atomicAdd(cnt, 1);
-                    list[s] = static_cast<int32_t>(j);
-                    keyv[s] = key;
+                    const int ls = atomicAdd(&s_cnt, 1);
+                    if (ls < kLocalMembers) {
+                        s_list[ls] = static_cast<int32_t>(j);
+                        s_key[ls] = key;
+                    } else {
+                        const int s = atomicAdd(cnt, 1);
+                        list[s] = static_cast<int32_t>(j);
+                        keyv[s] = key;
+                    }
                 }
             }
+        }
+        // one global append per block
+        __syncthreads();
+        const int local = min(s_cnt, kLocalMembers);
+        if (threadIdx.x == 0) s_base = local ? atomicAdd(cnt, local) : 0;
+        __syncthreads();
+        for (int t = threadIdx.x; t < local; t += blockDim.x) {
+            list[s_base + t] = s_list[t];
+            keyv[s_base + t] = s_key[t];
         }
         if (!grid_sync(st)) {
             if (threadIdx.x == 0) atomicExch(&st->n_fronts, -1);
@@ -250,7 +288,33 @@ __global__ void __launch_bounds__(256) peel_kernel(const uint32_t *__restrict__ 
         }
         const int L = *reinterpret_cast<volatile int *>(cnt);
         if (L == 0) break;
-        // ---- Phase C (the loop bound is uniform per block: __syncthreads is safe)
+        // ---- Phase C
+        if (L <= kTile) {
+            // the whole front in shared memory; one warp per member, lanes
+            // splitting the comparisons
+            for (int t = threadIdx.x; t < L; t += blockDim.x) {
+                sh[t] = __ldcg(keyv + t);
+                sh[kTile + t] = __ldcg(list + t);
+            }
+            __syncthreads();
+            for (uint32_t s = gwarp; s < static_cast<uint32_t>(L); s += nwarps) {
+                const int q = sh[kTile + s], kq = sh[s];
+                int p = 0;
+                for (int t = static_cast<int>(lane); t < L; t += 32) {
+                    const int kt = sh[t], qt = sh[kTile + t];
+                    p += (kt < kq) | ((kt == kq) & (qt < q));
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(kFull, p, o);
+                if (lane == 0) {
+                    front_indices[off + p] = q;
+                    rank[q] = k;
+                    atomicAnd(rem + (q >> 5), ~(1u << (q & 31)));
+                }
+            }
+        } else {
+        // large fronts: one thread per member against shared-memory tiles (the
+        // loop bound is uniform per block, so __syncthreads is safe)
         for (uint32_t s0 = blockIdx.x * blockDim.x; s0 < static_cast<uint32_t>(L); s0 += nthreads) {
             const uint32_t s = s0 + threadIdx.x;
             const bool act = s < static_cast<uint32_t>(L);
@@ -277,6 +341,7 @@ __global__ void __launch_bounds__(256) peel_kernel(const uint32_t *__restrict__ 
                 rank[q] = k;
                 atomicAnd(rem + (q >> 5), ~(1u << (q & 31)));
             }
+        }
         }
         if (tid == 0) {
             st->counts[(k + 1) & 1] = 0;
@@ -632,9 +697,9 @@ int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n,
     // cooperative peel: every block resident at once (the grid barrier needs it)
     const size_t smem = 2u * kTile * sizeof(int32_t);
     int occ = 0;
-    PGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, peel_kernel, 256, smem));
+    PGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, peel_kernel, kPeelThreads, smem));
     PGX_CHECK(occ >= 1, PGX_ERR_CUDA, "peel kernel cannot be resident");
-    if (occ > 2) occ = 2;
+    if (occ > 1) occ = 1;
     const int grid = num_sms * occ;
     {
         const uint32_t *a0 = sc.Dt;
@@ -643,7 +708,7 @@ int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n,
         int32_t *a5 = sc.list, *a6 = sc.keyv, *a7 = out.rank, *a8 = out.front_offsets, *a9 = out.front_indices;
         peel_state *a10 = sc.st;
         void *args[] = {&a0, &a1, &a2, &a3, &a4, &a5, &a6, &a7, &a8, &a9, &a10};
-        PGX_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(peel_kernel), dim3(grid), dim3(256), args,
+        PGX_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(peel_kernel), dim3(grid), dim3(kPeelThreads), args,
                                              smem, s));
         *launches += 1;
     }

@@ -12,6 +12,7 @@ profiler are not benchmark values). Cases:
   rosenbrock_fg / rosenbrock_f  dim 1000
   lj_fg / lj_f                  150 atoms
   survival                      NSGA-II survival of --rows nested-front points x 3
+  archipelago                   the fused kernel of a 64-island mixed epoch (--rows unused)
 """
 from __future__ import annotations
 
@@ -42,7 +43,16 @@ def main() -> None:
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     n = a.rows
-    if a.case == "survival":
+    if a.case == "archipelago":
+        from pagmo2_gb300 import archipelago as A
+
+        reqs = W.archipelago(64)
+        ep = A.Epoch([(r.kind, r.param, r.n, True) for r in reqs], ctx)
+        ep.run([r.dvs for r in reqs])
+
+        def run():
+            ep.launch_device(sp)
+    elif a.case == "survival":
         p = W.nsga2_points(n, 3, layers=30)
         dp = torch.from_numpy(p).cuda()
         i32 = lambda k: torch.empty(k, dtype=torch.int32, device="cuda")  # noqa: E731
