@@ -155,6 +155,9 @@ class _Reference:
         h = self.h
         h.ref_last_error.restype = C.c_char_p
         h.ref_thread_bfe.argtypes = [C.c_int, _u64, _vp, _u64, _u64, _vp, _vp]
+        h.ref_load_dvs.argtypes = [_vp, _u64]
+        h.ref_thread_bfe_loaded.argtypes = [C.c_int, _u64, _vp]
+        h.ref_gradient_loaded.argtypes = [C.c_int, _u64, _vp, C.c_int]
         h.ref_fitness_rows.argtypes = [C.c_int, _u64, _vp, _u64, _u64, _vp]
         h.ref_gradient_rows.argtypes = [C.c_int, _u64, _vp, _u64, _u64, _vp]
         h.ref_bounds.argtypes = [C.c_int, _u64, _vp, _vp]
@@ -175,6 +178,23 @@ class _Reference:
         fe = C.c_uint64()
         self._chk(self.h.ref_thread_bfe(kind, param, _p(x), n, nx, _p(f), C.byref(fe)))
         return f, fe.value
+
+    def load(self, dvs):
+        """Holds dvs as one vector_double inside the reference library (the form a
+        pagmo algorithm hands its bfe); returns (n, nx) for the *_loaded calls."""
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        self._chk(self.h.ref_load_dvs(_p(x), x.size))
+        return x.shape
+
+    def thread_bfe_loaded(self, kind, param, out):
+        """bfe{thread_bfe{}} over the loaded rows into out (n fitness values)."""
+        self._chk(self.h.ref_thread_bfe_loaded(kind, param, _p(out)))
+        return out
+
+    def gradient_loaded(self, kind, param, out, threads):
+        """problem::gradient over the loaded rows on `threads` threads into out (n, nx)."""
+        self._chk(self.h.ref_gradient_loaded(kind, param, _p(out), int(threads)))
+        return out
 
     def fitness_rows(self, kind, param, dvs):
         x = np.ascontiguousarray(dvs, dtype=np.float64)

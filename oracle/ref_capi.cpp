@@ -10,6 +10,7 @@
 #include <exception>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <pagmo/batch_evaluators/thread_bfe.hpp>
@@ -81,6 +82,59 @@ int ref_thread_bfe(int kind, std::uint64_t param, const double *dvs, std::uint64
         auto out = b(p, in);
         std::memcpy(fvs, out.data(), out.size() * sizeof(double));
         if (fevals_out) *fevals_out = p.get_fevals();
+    });
+}
+
+// The decision vectors as the vector_double a pagmo algorithm hands its bfe,
+// loaded once so that timing the evaluation does not time building it.
+namespace
+{
+pagmo::vector_double g_loaded;
+}
+
+int ref_load_dvs(const double *dvs, std::uint64_t n_total)
+{
+    return guard([&] { g_loaded.assign(dvs, dvs + n_total); });
+}
+
+// bfe{thread_bfe{}}(problem{udp}, loaded dvs).
+int ref_thread_bfe_loaded(int kind, std::uint64_t param, double *fvs)
+{
+    return guard([&] {
+        auto p = make_problem(kind, param);
+        pagmo::bfe b{pagmo::thread_bfe{}};
+        auto out = b(p, g_loaded);
+        std::memcpy(fvs, out.data(), out.size() * sizeof(double));
+    });
+}
+
+// problem::gradient over the loaded rows on `threads` std::threads (pagmo has
+// no batch gradient: this is the per-row API a user would parallelise).
+int ref_gradient_loaded(int kind, std::uint64_t param, double *grads, int threads)
+{
+    return guard([&] {
+        auto p = make_problem(kind, param);
+        const std::uint64_t nx = p.get_nx(), n = g_loaded.size() / nx;
+        const std::uint64_t nt = static_cast<std::uint64_t>(threads > 0 ? threads : 1);
+        std::vector<std::thread> pool;
+        std::vector<std::exception_ptr> errs(nt);
+        for (std::uint64_t t = 0; t < nt; ++t) {
+            pool.emplace_back([&, t]() {
+                try {
+                    pagmo::vector_double x(nx);
+                    for (std::uint64_t i = t * n / nt; i < (t + 1) * n / nt; ++i) {
+                        std::memcpy(x.data(), g_loaded.data() + i * nx, nx * sizeof(double));
+                        const auto g = p.gradient(x);
+                        std::memcpy(grads + i * nx, g.data(), nx * sizeof(double));
+                    }
+                } catch (...) {
+                    errs[t] = std::current_exception();
+                }
+            });
+        }
+        for (auto &th : pool) th.join();
+        for (auto &e : errs)
+            if (e) std::rethrow_exception(e);
     });
 }
 
