@@ -304,7 +304,7 @@ def main():
     traffic = ncu_traffic("rosenbrock_fg_65536x1000")
     roofline = {"bound": "fp64", "achieved": achieved_tflops, "peak": fp64_peak_tflops, "unit": "TFLOP/s",
                 "frac": achieved_tflops / fp64_peak_tflops, "traffic": traffic,
-                "kernel": "rosenbrock_kernel<32,true>",
+                "kernel": "rosenbrock_v4_kernel<true>",
                 "peak_source": "in-run DFMA throughput probe (pgx_measure_fp64_peak); no FP64 figure in "
                                "MEASURED_PEAKS.json",
                 "algorithmic": f"{ROS_FG_FLOPS_PER_ELEM} flops/element (FMA=2), {alg_bytes} bytes per launch",

@@ -42,6 +42,14 @@ def _p(a):
     return None if a is None else a.ctypes.data
 
 
+def _pts2d(pts):
+    """n x m float64 C array from an n x m array or a list of n equal-length lists."""
+    p = np.ascontiguousarray(pts, dtype=np.float64)
+    if p.ndim != 2:
+        p = p.reshape(len(pts), -1) if p.size else np.zeros((len(pts), 0))
+    return p
+
+
 class _Oracle:
     def __init__(self, path: Path):
         self.h = C.CDLL(str(path))
@@ -65,10 +73,25 @@ class _Oracle:
         h.orc_nsga2_crowding.argtypes = [_vp, _u64, _u64, _vp, _vp, _u64, _vp]
         h.orc_crowding_ex.argtypes = [_vp, _u64, _u64, C.c_int, _vp]
         h.orc_nsga2_crowding_ex.argtypes = [_vp, _u64, _u64, _vp, _vp, _u64, C.c_int, _vp]
+        h.orc_sort_last_error.restype = C.c_char_p
+        for name in ("orc_std_sort_keys", "orc_introsort_keys", "orc_introsort_chunked_keys", "orc_heap_sort_keys",
+                     "orc_std_partial_sort_full"):
+            getattr(h, name).argtypes = [_vp, _vp, _u64]
+            getattr(h, name).restype = None
+        h.orc_quicksort_adversary.argtypes = [_u64, _vp]
+        h.orc_depth_limit_hits.restype = _u64
+        h.orc_depth_limit_hits.argtypes = []
+        h.orc_quicksort_adversary.restype = None
+        h.orc_select_best_n_mo.argtypes = [_vp, _u64, _u64, _u64, _vp, _vp]
+        h.orc_sort_population_mo.argtypes = [_vp, _u64, _u64, _vp]
 
     def _chk(self, st):
         if st != 0:
             raise ValueError(self.h.orc_last_error().decode())
+
+    def _chk_sort(self, st):
+        if st != 0:
+            raise ValueError(self.h.orc_sort_last_error().decode())
 
     # batch evaluation -------------------------------------------------------
     def batch_fitness(self, kind, param, dvs, threads=0):
@@ -146,6 +169,43 @@ class _Oracle:
         self._chk(self.h.orc_nsga2_crowding_ex(_p(p), n, m, _p(off), _p(idx), off.size - 1, int(stable), _p(out)))
         return out
 
+    # orderings -----------------------------------------------------------------
+    def sort_keys(self, keys, values=None, method="std"):
+        """(keys, values) sorted by key: method "std" (std::sort), "intro" (the
+        restated introsort), "chunked" (its 32-wide chunked partition), "heap"
+        (restated heapsort) or "std_heap" (std::partial_sort over the whole range)."""
+        k = np.array(keys, dtype=np.int64)
+        v = np.arange(k.size, dtype=np.int32) if values is None else np.array(values, dtype=np.int32)
+        fn = {"std": self.h.orc_std_sort_keys, "intro": self.h.orc_introsort_keys,
+              "chunked": self.h.orc_introsort_chunked_keys, "heap": self.h.orc_heap_sort_keys,
+              "std_heap": self.h.orc_std_partial_sort_full}[method]
+        fn(_p(k), _p(v), k.size)
+        return k, v
+
+    def depth_limit_hits(self):
+        """Ranges handed to heapsort so far by the restated introsorts (this thread)."""
+        return int(self.h.orc_depth_limit_hits())
+
+    def quicksort_adversary(self, n):
+        out = np.empty(n, np.int64)
+        self.h.orc_quicksort_adversary(n, _p(out))
+        return out
+
+    def select_best_n_mo(self, pts, N):
+        p = _pts2d(pts)
+        n, m = p.shape
+        out = np.empty(max(n, 1), np.uint64)
+        cnt = C.c_uint64()
+        self._chk_sort(self.h.orc_select_best_n_mo(_p(p), n, m, N, _p(out), C.addressof(cnt)))
+        return out[:cnt.value].astype(np.int64)
+
+    def sort_population_mo(self, pts):
+        p = _pts2d(pts)
+        n, m = p.shape
+        out = np.empty(max(n, 1), np.uint64)
+        self._chk_sort(self.h.orc_sort_population_mo(_p(p), n, m, _p(out)))
+        return out[:n].astype(np.int64)
+
 
 class _Reference:
     """The reference's own compiled sources (only where they were built)."""
@@ -164,6 +224,8 @@ class _Reference:
         h.ref_fnds.argtypes = [_vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _u64]
         h.ref_crowding.argtypes = [_vp, _u64, _u64, _vp]
         h.ref_pareto_dominance.argtypes = [_vp, _vp, _u64, _vp]
+        h.ref_select_best_n_mo.argtypes = [_vp, _u64, _u64, _u64, _vp, _vp]
+        h.ref_sort_population_mo.argtypes = [_vp, _u64, _u64, _vp]
 
     def _chk(self, st):
         if st == 1:
@@ -240,6 +302,21 @@ class _Reference:
         out = np.empty(n)
         self._chk(self.h.ref_crowding(_p(p), n, m, _p(out)))
         return out
+
+    def select_best_n_mo(self, pts, N):
+        p = _pts2d(pts)
+        n, m = p.shape
+        out = np.empty(max(n, 1), np.uint64)
+        cnt = C.c_uint64()
+        self._chk(self.h.ref_select_best_n_mo(_p(p), n, m, N, _p(out), C.addressof(cnt)))
+        return out[:cnt.value].astype(np.int64)
+
+    def sort_population_mo(self, pts):
+        p = _pts2d(pts)
+        n, m = p.shape
+        out = np.empty(max(n, 1), np.uint64)
+        self._chk(self.h.ref_sort_population_mo(_p(p), n, m, _p(out)))
+        return out[:n].astype(np.int64)
 
     def pareto_dominance(self, a, b):
         a = np.ascontiguousarray(a, dtype=np.float64)

@@ -83,6 +83,25 @@ int orc_crowding_ex(const double *pts, uint64_t n, uint64_t m, int stable, doubl
 int orc_nsga2_crowding_ex(const double *pts, uint64_t n, uint64_t m, const uint64_t *front_offsets,
                           const uint64_t *front_indices, uint64_t n_fronts, int stable, double *out);
 
+/* ---- orderings (sorting.cpp) ----
+   (key, value) pairs sorted by key in place: with std::sort (the reference's
+   order of ties), with the restated libstdc++ introsort, with the same
+   introsort partitioned in 32-wide chunks (the GPU's formulation), and with
+   std::partial_sort(first, last, last) / the restated heapsort. */
+const char *orc_sort_last_error(void);
+uint64_t orc_depth_limit_hits(void);
+void orc_std_sort_keys(long long *k, int32_t *v, uint64_t n);
+void orc_introsort_keys(long long *k, int32_t *v, uint64_t n);
+void orc_introsort_chunked_keys(long long *k, int32_t *v, uint64_t n);
+void orc_heap_sort_keys(long long *k, int32_t *v, uint64_t n);
+void orc_std_partial_sort_full(long long *k, int32_t *v, uint64_t n);
+/* McIlroy's quicksort adversary against std::sort: n keys. */
+void orc_quicksort_adversary(uint64_t n, long long *out);
+/* select_best_N_mo (multi_objective.cpp:344-396) and sort_population_mo
+   (:425-465). Errors: 1 with the message in orc_sort_last_error(). */
+int orc_select_best_n_mo(const double *pts, uint64_t n, uint64_t m, uint64_t N, uint64_t *out, uint64_t *n_out);
+int orc_sort_population_mo(const double *pts, uint64_t n, uint64_t m, uint64_t *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -226,6 +226,26 @@ int ref_crowding(const double *pts, std::uint64_t n, std::uint64_t m, double *ou
     });
 }
 
+// select_best_N_mo over n points of m objectives: out[*n_out] indices.
+int ref_select_best_n_mo(const double *pts, std::uint64_t n, std::uint64_t m, std::uint64_t N, std::uint64_t *out,
+                         std::uint64_t *n_out)
+{
+    return guard([&] {
+        const auto r = pagmo::select_best_N_mo(rows(pts, n, m), N);
+        for (std::size_t i = 0; i < r.size(); ++i) out[i] = r[i];
+        *n_out = r.size();
+    });
+}
+
+// sort_population_mo over n points of m objectives: out[n].
+int ref_sort_population_mo(const double *pts, std::uint64_t n, std::uint64_t m, std::uint64_t *out)
+{
+    return guard([&] {
+        const auto r = pagmo::sort_population_mo(rows(pts, n, m));
+        for (std::size_t i = 0; i < r.size(); ++i) out[i] = r[i];
+    });
+}
+
 // pareto_dominance(a, b) for two m-vectors: returns 0/1 in *out.
 int ref_pareto_dominance(const double *a, const double *b, std::uint64_t m, int *out)
 {
