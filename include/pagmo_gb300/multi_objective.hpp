@@ -1,14 +1,16 @@
 // NSGA-II survival on a GB300 with pagmo's signatures:
-// fast_non_dominated_sorting and crowding_distance
-// (include/pagmo/utils/multi_objective.hpp:72,75; src/utils/multi_objective.cpp:200-315),
-// and the survival block of nsga2::evolve (src/algorithms/nsga2.cpp:183-206)
-// in one call. Ranks, domination counts, the fronts (in the reference's
-// order) and dom_list are identical to the reference's; crowding distances
-// too, except that equal objective values are ordered as a stable sort would
-// order them (the reference's std::sort leaves that order unspecified).
+// fast_non_dominated_sorting, crowding_distance, select_best_N_mo and
+// sort_population_mo (include/pagmo/utils/multi_objective.hpp:72-81;
+// src/utils/multi_objective.cpp:200-465), and the survival block of
+// nsga2::evolve (src/algorithms/nsga2.cpp:183-206) in one call. Every output
+// is identical to the reference's: ranks, domination counts, the fronts in the
+// reference's order, dom_list, crowding distances and index lists, including
+// the order of ties, which the device sorts leave as the reference's std::sort
+// (GNU libstdc++) leaves them.
 #ifndef PAGMO_GB300_MULTI_OBJECTIVE_HPP
 #define PAGMO_GB300_MULTI_OBJECTIVE_HPP
 
+#include <cstddef>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -92,6 +94,38 @@ inline pagmo::vector_double crowding_distance(const std::vector<pagmo::vector_do
     pagmo::vector_double out(n);
     check(pgx_crowding_distance(device_context(device), flat.data(), n, m, out.data()));
     return out;
+}
+
+// select_best_N_mo: the best N individuals (whole fronts, then the critical
+// front by descending crowding distance).
+inline std::vector<pagmo::pop_size_t> select_best_N_mo(const std::vector<pagmo::vector_double> &points,
+                                                       pagmo::pop_size_t N, int device = 0)
+{
+    const std::uint64_t n = points.size();
+    if (N == 0u || n == 0u) return {};
+    if (n == 1u) return {0u};
+    std::uint64_t m = 0;
+    const auto flat = detail::flatten(points, m);
+    std::vector<std::int32_t> out(N < n ? N : n);
+    std::uint64_t cnt = 0;
+    check(pgx_select_best_n_mo(device_context(device), flat.empty() ? nullptr : flat.data(), n, m, N, out.data(),
+                               &cnt));
+    return std::vector<pagmo::pop_size_t>(out.begin(), out.begin() + static_cast<std::ptrdiff_t>(cnt));
+}
+
+// sort_population_mo: the individuals ordered by (non-domination rank,
+// descending crowding distance).
+inline std::vector<pagmo::pop_size_t> sort_population_mo(const std::vector<pagmo::vector_double> &points,
+                                                         int device = 0)
+{
+    const std::uint64_t n = points.size();
+    if (n == 0u) return {};
+    if (n == 1u) return {0u};
+    std::uint64_t m = 0;
+    const auto flat = detail::flatten(points, m);
+    std::vector<std::int32_t> out(n);
+    check(pgx_sort_population_mo(device_context(device), flat.empty() ? nullptr : flat.data(), n, m, out.data()));
+    return std::vector<pagmo::pop_size_t>(out.begin(), out.end());
 }
 
 // The survival block of one NSGA-II generation: non-domination ranks, the

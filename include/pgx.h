@@ -133,11 +133,9 @@ PGX_API int pgx_fnds_dom_list(pgx_context *ctx, const double *points, uint64_t n
                       int32_t *dl_indices, uint64_t capacity, uint64_t *dl_total);
 
 /* crowding_distance of one non-dominated front (src/utils/multi_objective.cpp:280-315).
-   n >= 2 and m >= 2 or PGX_ERR_INVALID. Equal objective values keep the
-   order they had along the previous objective (the first objective: input
-   order), which is what the reference's loop gives with a stable sort; the
-   reference's std::sort leaves the order of ties unspecified. Points whose
-   values are not tied are bit-exact with the reference. */
+   n >= 2 and m >= 2 or PGX_ERR_INVALID. Bit-exact with the reference,
+   including tied objective values: the per-objective sorts leave ties in the
+   order the reference's std::sort (GNU libstdc++ introsort) leaves them. */
 PGX_API int pgx_crowding_distance(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, double *out);
 
 /* NSGA-II survival block (src/algorithms/nsga2.cpp:183-206): fnds, then the
@@ -146,6 +144,37 @@ PGX_API int pgx_crowding_distance(pgx_context *ctx, const double *points, uint64
 PGX_API int pgx_nsga2_survival(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, int32_t *rank,
                        int32_t *dom_count, int32_t *front_offsets, int32_t *front_indices, int32_t *n_fronts,
                        double *crowding);
+
+/* select_best_N_mo (src/utils/multi_objective.cpp:344-396): the indices of
+   the best N of n points of m objectives (whole fronts while they fit, then the
+   critical front by descending crowding distance), min(N, n) of them in out,
+   that count in *n_out. Bit-exact with the reference, ties included. Errors as
+   the reference: a critical front with m < 2 -> PGX_ERR_INVALID. */
+PGX_API int pgx_select_best_n_mo(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, uint64_t N,
+                                 int32_t *out, uint64_t *n_out);
+
+/* sort_population_mo (src/utils/multi_objective.cpp:425-465): out[n], the
+   points ordered by (non-domination rank, descending crowding distance; a
+   front of one point counts 0). Bit-exact with the reference, ties included.
+   A front of two or more points with m < 2 -> PGX_ERR_INVALID. */
+PGX_API int pgx_sort_population_mo(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, int32_t *out);
+
+/* Device-resident variants, asynchronous on `stream`: d_out holds min(N, n)
+   (resp. n) indices. d_status (nullable device int32) reads, once the stream
+   has run: 0 ok, 1 the reference would have thrown (crowding over fewer than
+   two objectives; d_out is then incomplete), -1 a grid barrier gave up, 2 an
+   internal error of the device sort. */
+PGX_API int pgx_select_best_n_mo_device(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, uint64_t N,
+                                        int32_t *d_out, int32_t *d_status, void *stream);
+PGX_API int pgx_sort_population_mo_device(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m,
+                                          int32_t *d_out, int32_t *d_status, void *stream);
+
+/* Sorts (keys[i], values[i]) by key in place (host buffers) on the GPU,
+   leaving equal keys in the order std::sort (GNU libstdc++ introsort) leaves
+   them -- the order behind the three functions above. No counterpart in the
+   reference; exported so callers (and tests) can reproduce std::sort's tie
+   order. n <= 2^30. */
+PGX_API int pgx_std_sort_i64(pgx_context *ctx, int64_t *keys, int32_t *values, uint64_t n);
 
 /* Device-resident survival: all pointers are device memory; d_n_fronts is a
    device int32. Asynchronous on `stream`. The front peeling waits on grid

@@ -35,6 +35,11 @@ SIGNATURES = {
     "pgx_fnds": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp]),
     "pgx_fnds_dom_list": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _u64, C.POINTER(_u64)]),
     "pgx_crowding_distance": (C.c_int, [_vp, _vp, _u64, _u64, _vp]),
+    "pgx_select_best_n_mo": (C.c_int, [_vp, _vp, _u64, _u64, _u64, _vp, C.POINTER(_u64)]),
+    "pgx_sort_population_mo": (C.c_int, [_vp, _vp, _u64, _u64, _vp]),
+    "pgx_select_best_n_mo_device": (C.c_int, [_vp, _vp, _u64, _u64, _u64, _vp, _vp, _vp]),
+    "pgx_sort_population_mo_device": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp]),
+    "pgx_std_sort_i64": (C.c_int, [_vp, _vp, _vp, _u64]),
     "pgx_nsga2_survival": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp]),
     "pgx_nsga2_survival_device": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "pgx_measure_fp64_peak": (C.c_int, [_vp, C.POINTER(C.c_double)]),

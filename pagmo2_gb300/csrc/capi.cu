@@ -433,6 +433,102 @@ int pgx_crowding_distance(pgx_context *ctx, const double *points, uint64_t n, ui
     PGX_TRY(launch_crowding_single(ctx, dp, n, m, dout, s));
     PGX_CUDA(cudaMemcpyAsync(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     PGX_CUDA(cudaStreamSynchronize(s));
+    return read_mo_status(ctx, n, m);
+}
+
+int pgx_select_best_n_mo(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, uint64_t N, int32_t *out,
+                         uint64_t *n_out)
+{
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    PGX_CHECK(n_out != nullptr, PGX_ERR_INVALID, "null count pointer");
+    const uint64_t cnt = N < n ? N : n;
+    *n_out = 0;
+    PGX_CHECK(out != nullptr || cnt == 0, PGX_ERR_INVALID, "null output buffer");
+    PGX_CHECK(points != nullptr || n * m == 0, PGX_ERR_INVALID, "null points buffer");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    PGX_TRY(use_device(ctx));
+    const size_t bp = (n * m * sizeof(double) + 255u) & ~size_t(255);
+    PGX_TRY(ctx->s_crowd.ensure(bp + n * sizeof(int32_t) + 256));
+    double *dp = ctx->s_crowd.as<double>();
+    int32_t *dout = reinterpret_cast<int32_t *>(ctx->s_crowd.as<char>() + bp);
+    cudaStream_t s = ctx->stream;
+    if (n * m) PGX_CUDA(cudaMemcpyAsync(dp, points, n * m * sizeof(double), cudaMemcpyHostToDevice, s));
+    PGX_TRY(launch_select_best(ctx, dp, n, m, N, dout, nullptr, s));
+    if (cnt) PGX_CUDA(cudaMemcpyAsync(out, dout, cnt * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    PGX_CUDA(cudaStreamSynchronize(s));
+    if (n >= 2 && N > 0 && N < n) PGX_TRY(read_mo_status(ctx, n, m));
+    *n_out = cnt;
+    return PGX_OK;
+}
+
+int pgx_sort_population_mo(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, int32_t *out)
+{
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    PGX_CHECK(out != nullptr || n == 0, PGX_ERR_INVALID, "null output buffer");
+    PGX_CHECK(points != nullptr || n * m == 0, PGX_ERR_INVALID, "null points buffer");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    PGX_TRY(use_device(ctx));
+    const size_t bp = (n * m * sizeof(double) + 255u) & ~size_t(255);
+    PGX_TRY(ctx->s_crowd.ensure(bp + n * sizeof(int32_t) + 256));
+    double *dp = ctx->s_crowd.as<double>();
+    int32_t *dout = reinterpret_cast<int32_t *>(ctx->s_crowd.as<char>() + bp);
+    cudaStream_t s = ctx->stream;
+    if (n * m) PGX_CUDA(cudaMemcpyAsync(dp, points, n * m * sizeof(double), cudaMemcpyHostToDevice, s));
+    PGX_TRY(launch_sort_population(ctx, dp, n, m, dout, nullptr, s));
+    if (n) PGX_CUDA(cudaMemcpyAsync(out, dout, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    PGX_CUDA(cudaStreamSynchronize(s));
+    if (n >= 2) PGX_TRY(read_mo_status(ctx, n, m));
+    return PGX_OK;
+}
+
+int pgx_select_best_n_mo_device(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, uint64_t N,
+                                int32_t *d_out, int32_t *d_status, void *stream)
+{
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    PGX_CHECK(d_out != nullptr || N == 0 || n == 0, PGX_ERR_INVALID, "null output buffer");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    PGX_TRY(use_device(ctx));
+    return launch_select_best(ctx, d_points, n, m, N, d_out, d_status, static_cast<cudaStream_t>(stream));
+}
+
+int pgx_sort_population_mo_device(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, int32_t *d_out,
+                                  int32_t *d_status, void *stream)
+{
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    PGX_CHECK(d_out != nullptr || n == 0, PGX_ERR_INVALID, "null output buffer");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    PGX_TRY(use_device(ctx));
+    return launch_sort_population(ctx, d_points, n, m, d_out, d_status, static_cast<cudaStream_t>(stream));
+}
+
+int pgx_std_sort_i64(pgx_context *ctx, int64_t *keys, int32_t *values, uint64_t n)
+{
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    PGX_CHECK((keys != nullptr && values != nullptr) || n == 0, PGX_ERR_INVALID, "null buffer");
+    if (n < 2) return PGX_OK;
+    PGX_CHECK(n <= (1ull << 30), PGX_ERR_CAPACITY, "sort: more than 2^30 elements");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    PGX_TRY(use_device(ctx));
+    const size_t bk = (n * sizeof(int64_t) + 255u) & ~size_t(255);
+    const size_t bv = (n * sizeof(int32_t) + 255u) & ~size_t(255);
+    const size_t bl = (n * 2u * sizeof(int32_t) + 255u) & ~size_t(255);
+    PGX_TRY(ctx->s_crowd.ensure(bk + bv + bl + 256));
+    char *base = ctx->s_crowd.as<char>();
+    long long *dk = reinterpret_cast<long long *>(base);
+    int32_t *dv = reinterpret_cast<int32_t *>(base + bk);
+    int2 *dl = reinterpret_cast<int2 *>(base + bk + bv);
+    int *derr = reinterpret_cast<int *>(base + bk + bv + bl);
+    cudaStream_t s = ctx->stream;
+    PGX_CUDA(cudaMemsetAsync(derr, 0, sizeof(int), s));
+    PGX_CUDA(cudaMemcpyAsync(dk, keys, n * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    PGX_CUDA(cudaMemcpyAsync(dv, values, n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    PGX_TRY(launch_sort_pairs(ctx, dk, dv, n, derr, dl, s));
+    int err = 0;
+    PGX_CUDA(cudaMemcpyAsync(keys, dk, n * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    PGX_CUDA(cudaMemcpyAsync(values, dv, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    PGX_CUDA(cudaMemcpyAsync(&err, derr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PGX_CUDA(cudaStreamSynchronize(s));
+    PGX_CHECK(err == 0, PGX_ERR_CUDA, "device sort: internal error " + std::to_string(err));
     return PGX_OK;
 }
 

@@ -132,6 +132,21 @@ int launch_survival(pgx_context *ctx, const double *d_points, uint64_t n, uint64
 int launch_crowding_single(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, double *d_out,
                            cudaStream_t stream);
 
+// select_best_N_mo / sort_population_mo on device buffers (d_out holds
+// min(N, n) / n indices; d_status nullable: 0 ok, -1 barrier timeout, 1 fewer
+// than two objectives where crowding is needed, 2 internal sort error).
+int launch_select_best(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, uint64_t N, int32_t *d_out,
+                       int32_t *d_status, cudaStream_t stream);
+int launch_sort_population(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, int32_t *d_out,
+                           int32_t *d_status, cudaStream_t stream);
+// After a synchronisation: the error of the last select_best/sort_population
+// pass of shape (n, m) on this context, as the reference would raise it.
+int read_mo_status(pgx_context *ctx, uint64_t n, uint64_t m);
+// std::sort-ordered in-place sort of device (key, value) pairs by one block;
+// d_lists holds n int2, *d_err receives a nonzero code on a broken invariant.
+int launch_sort_pairs(pgx_context *ctx, long long *d_keys, int32_t *d_vals, uint64_t n, int *d_err, int2 *d_lists,
+                      cudaStream_t stream);
+
 // Reads the device status word of the last survival pass of shape (n, m) on
 // this context (after a stream synchronisation): PGX_ERR_TIMEOUT when a grid
 // barrier gave up.

@@ -18,13 +18,17 @@
 //     point q of front k+1 is appended when its last dominator in front k is
 //     processed, so the order is by (max position of q's dominators in front k,
 //     q).
-//  4. crowding_rank / crowding_accumulate: for each front and objective the
-//     sorted position of every point (ties keep the previous objective's
-//     order, as a stable sort in the reference's loop would), then the
-//     reference's neighbour differences over the objective range, in
-//     objective order per point.
+//  4. front_crowding: one block per front sorts the front's members objective
+//     after objective with std::sort's exact order (introsort.cuh; each sort
+//     starts from the previous objective's order, as the reference's loop
+//     does) and adds the reference's neighbour differences over the objective
+//     range, in objective order per point.
+// select_best_N_mo (:344-396) and sort_population_mo (:425-465) reuse 1-4 and
+// the same sort.
+#include "introsort.cuh"
 #include "pgx_internal.cuh"
 
+#include <algorithm>
 #include <climits>
 #include <cmath>
 
@@ -133,10 +137,14 @@ __global__ void __launch_bounds__(256) dominance_kernel(const long long *__restr
 struct peel_state {
     unsigned bar_count;
     unsigned bar_gen;
-    int err;
+    int err;      // a grid barrier gave up
     int n_fronts;
     int counts[2];
+    int status;   // kStatusNeedTwoObjectives: crowding over fewer than two objectives
+    int sort_err; // broken invariant of the device sort (never expected)
 };
+
+constexpr int kStatusNeedTwoObjectives = 1;
 
 // Grid-wide barrier for a cooperative launch; gives up (and flags st->err)
 // after about a second instead of waiting forever.
@@ -362,96 +370,228 @@ __global__ void __launch_bounds__(kPeelThreads) peel_kernel(const uint32_t *__re
     }
 }
 
-// Sorted position, along objective k, of every point of every front of
-// three or more points. The reference sorts one index vector objective after
-// objective (multi_objective.cpp:301-306), so ties along objective k keep the
-// order of objective k-1: the tie-break is the point's position in objective
-// k-1's order (its position in the front for k = 0), which is what a stable
-// sort of that vector yields. Tasks = (front, 256-point chunk), dealt
-// round-robin to blocks; each thread counts the front members before its
-// point against shared-memory tiles of (key, tie-break).
-// Writes sorted[k*n + off + p] = point and inv_pos[k*n + point] = p.
-__global__ void __launch_bounds__(256) crowding_rank_kernel(const long long *__restrict__ keys, uint32_t n, uint32_t k,
-                                                            const int32_t *__restrict__ front_offsets,
-                                                            const int32_t *__restrict__ front_indices,
-                                                            const int32_t *__restrict__ n_fronts,
-                                                            int32_t *__restrict__ sorted, int32_t *__restrict__ inv_pos)
+// ------------------------------------------------------------ crowding and orders
+
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortSmemCap = 4096;                    // (key, value) pairs a block keeps in shared memory
+constexpr int kSortSmemLists = kSortSmemCap / 16 + 2; // ranges per level, shared-memory case
+constexpr size_t kSortSmemBytes =
+    static_cast<size_t>(kSortSmemCap) * (sizeof(dev::key2) + sizeof(int32_t)) + 2u * kSortSmemLists * sizeof(int2);
+
+// Where one block sorts L pairs: its shared memory when they fit, else the
+// caller's slice of the global work arrays (keys, values, 2 * (L / 2) ranges).
+template <typename K>
+struct sort_area {
+    K *k;
+    int32_t *v;
+    int2 *lists;
+    int cap;
+};
+
+template <typename K>
+__device__ sort_area<K> pick_area(unsigned char *smem, int L, K *gk, int32_t *gv, int2 *gl)
 {
-    __shared__ long long tk[kTile];
-    __shared__ int32_t tt[kTile];
-    const int nf = *n_fronts;
-    const uint32_t G = gridDim.x;
-    const long long *kk = keys + static_cast<uint64_t>(k) * n;
-    const int32_t *prev = k > 0 ? inv_pos + static_cast<uint64_t>(k - 1) * n : nullptr;
-    uint64_t base = 0; // tasks dealt so far
-    for (int f = 0; f < nf; ++f) {
-        const int off = front_offsets[f], sz = front_offsets[f + 1] - off;
-        if (sz < 3) continue;
-        const uint32_t tasks = (static_cast<uint32_t>(sz) + 255u) / 256u;
-        // first task of this front owned by this block under round-robin dealing
-        uint32_t t = static_cast<uint32_t>((blockIdx.x + G - static_cast<uint32_t>(base % G)) % G);
-        for (; t < tasks; t += G) {
-            const int pq = static_cast<int>(t * 256u + threadIdx.x);
-            const bool act = pq < sz;
-            const int q = act ? front_indices[off + pq] : 0;
-            const long long kq = act ? kk[q] : 0;
-            const int tq = act ? (prev ? prev[q] : pq) : 0;
-            int p = 0;
-            for (int t0 = 0; t0 < sz; t0 += kTile) {
-                const int lim = min(kTile, sz - t0);
-                __syncthreads();
-                for (int s2 = threadIdx.x; s2 < lim; s2 += blockDim.x) {
-                    const int pt = front_indices[off + t0 + s2];
-                    tk[s2] = kk[pt];
-                    tt[s2] = prev ? prev[pt] : t0 + s2;
-                }
-                __syncthreads();
-                if (act) {
-                    for (int s2 = 0; s2 < lim; ++s2) {
-                        const long long v = tk[s2];
-                        p += (v < kq) | ((v == kq) & (tt[s2] < tq));
-                    }
-                }
-            }
-            if (act) {
-                sorted[static_cast<uint64_t>(k) * n + off + p] = q;
-                inv_pos[static_cast<uint64_t>(k) * n + q] = p;
-            }
+    sort_area<K> a;
+    if (L <= kSortSmemCap) {
+        a.k = reinterpret_cast<K *>(smem);
+        a.v = reinterpret_cast<int32_t *>(smem + kSortSmemCap * sizeof(dev::key2));
+        a.lists = reinterpret_cast<int2 *>(smem + kSortSmemCap * (sizeof(dev::key2) + sizeof(int32_t)));
+        a.cap = kSortSmemLists;
+    } else {
+        a.k = gk;
+        a.v = gv;
+        a.lists = gl;
+        a.cap = L / 2;
+    }
+    return a;
+}
+
+// crowding_distance (multi_objective.cpp:280-315) of one front of L >= 2
+// members (point indices, in front order), by one block, into cd[point]. Per
+// objective: std::sort of the member list by that objective (starting from the
+// previous objective's order), ends := +inf, interior += (f[next] - f[prev]) /
+// (f[last] - f[first]).
+__device__ void front_crowding(const double *__restrict__ pts, uint32_t n, uint32_t m,
+                               const long long *__restrict__ keys, const int32_t *members, int L,
+                               const sort_area<long long> &a, dev::sort_ctl *ctl, int *slots, int *err, double *cd)
+{
+    for (int p = threadIdx.x; p < L; p += blockDim.x) {
+        const int32_t q = members[p];
+        a.v[p] = q;
+        cd[q] = 0.0;
+    }
+    __syncthreads();
+    for (uint32_t k = 0; k < m; ++k) {
+        const long long *kk = keys + static_cast<uint64_t>(k) * n;
+        for (int p = threadIdx.x; p < L; p += blockDim.x) a.k[p] = kk[a.v[p]];
+        __syncthreads();
+        dev::block_std_sort(dev::sort_view<long long>{a.k, a.v}, L, a.lists, a.cap, ctl, slots, err);
+        const int32_t q0 = a.v[0], q1 = a.v[L - 1];
+        const double df = pts[static_cast<uint64_t>(q1) * m + k] - pts[static_cast<uint64_t>(q0) * m + k];
+        for (int p = 1 + static_cast<int>(threadIdx.x); p < L - 1; p += blockDim.x) {
+            const int32_t q = a.v[p];
+            cd[q] += (pts[static_cast<uint64_t>(a.v[p + 1]) * m + k] - pts[static_cast<uint64_t>(a.v[p - 1]) * m + k])
+                     / df;
         }
-        base += tasks;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            cd[q0] = HUGE_VAL;
+            cd[q1] = HUGE_VAL;
+        }
+        __syncthreads();
     }
 }
 
-// crowding_distance per point: ends of each objective get +inf (assignment),
-// interior points add (f[next] - f[prev]) / (f[last] - f[first]), objectives
-// in order (multi_objective.cpp:303-313); fronts of one or two points are
-// +inf (nsga2.cpp:188-193).
-__global__ void crowding_accumulate_kernel(const double *__restrict__ pts, uint32_t n, uint32_t m,
-                                           const int32_t *__restrict__ rank, const int32_t *__restrict__ front_offsets,
-                                           const int32_t *__restrict__ sorted, const int32_t *__restrict__ inv_pos,
-                                           double *__restrict__ out)
+// How fronts of one and two points are treated.
+enum : int {
+    kCrowdNsga2 = 0,         // nsga2.cpp:188-193: +inf for fronts of 1 or 2 points
+    kCrowdSortPopulation = 1 // multi_objective.cpp:441-446: 0 for a single point, else crowding_distance
+};
+
+// Crowding distance of every point within its front: blocks take fronts
+// f = blockIdx.x, blockIdx.x + gridDim.x, ... (n_fronts read on the device).
+__global__ void __launch_bounds__(kSortThreads) front_crowding_kernel(
+    const double *__restrict__ pts, uint32_t n, uint32_t m, const long long *__restrict__ keys,
+    const int32_t *__restrict__ front_offsets, const int32_t *__restrict__ front_indices,
+    const int32_t *__restrict__ n_fronts, int mode, unsigned char *wkey, int32_t *widx, int2 *wlist, double *cd,
+    peel_state *st)
 {
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        const int f = rank[q];
-        const int off = front_offsets[f], end = front_offsets[f + 1];
-        const int sz = end - off;
-        if (sz < 3) {
-            out[q] = HUGE_VAL;
+    extern __shared__ __align__(16) unsigned char sort_smem[];
+    __shared__ dev::sort_ctl ctl;
+    __shared__ int slots[kSortWarps * 64];
+    const int nf = *n_fronts; // -1 after a barrier timeout: nothing to do
+    for (int f = blockIdx.x; f < nf; f += gridDim.x) {
+        const int off = front_offsets[f], L = front_offsets[f + 1] - off;
+        const int32_t *mem = front_indices + off;
+        if (L == 1 || (L == 2 && mode == kCrowdNsga2)) {
+            if (static_cast<int>(threadIdx.x) < L) cd[mem[threadIdx.x]] = mode == kCrowdNsga2 ? HUGE_VAL : 0.0;
             continue;
         }
-        double cd = 0.0;
-        for (uint32_t k = 0; k < m; ++k) {
-            const int32_t *srt = sorted + static_cast<uint64_t>(k) * n + off;
-            const int p = inv_pos[static_cast<uint64_t>(k) * n + q];
-            if (p == 0 || p == sz - 1) {
-                cd = HUGE_VAL;
-            } else {
-                const double df = pts[static_cast<uint64_t>(srt[sz - 1]) * m + k] - pts[static_cast<uint64_t>(srt[0]) * m + k];
-                cd += (pts[static_cast<uint64_t>(srt[p + 1]) * m + k] - pts[static_cast<uint64_t>(srt[p - 1]) * m + k]) / df;
-            }
+        if (m < 2u) {
+            if (threadIdx.x == 0) atomicExch(&st->status, kStatusNeedTwoObjectives);
+            continue;
         }
-        out[q] = cd;
+        const sort_area<long long> a =
+            pick_area<long long>(sort_smem, L, reinterpret_cast<long long *>(wkey) + off, widx + off, wlist + off);
+        front_crowding(pts, n, m, keys, mem, L, a, &ctl, slots, &st->sort_err, cd);
     }
+}
+
+// select_best_N_mo (multi_objective.cpp:344-396) for 2 <= n, 1 <= N < n, by
+// one block after the fronts are known: whole fronts while they fit, then the
+// critical front's members by descending crowding distance (std::sort of the
+// positions 0..L-1 with greater_than_f, ties in std::sort's order).
+__global__ void __launch_bounds__(kSortThreads) select_best_kernel(
+    const double *__restrict__ pts, uint32_t n, uint32_t m, uint32_t N, const long long *__restrict__ keys,
+    const int32_t *__restrict__ front_offsets, const int32_t *__restrict__ front_indices,
+    const int32_t *__restrict__ n_fronts, unsigned char *wkey, int32_t *widx, int2 *wlist, double *wcd, int32_t *out,
+    peel_state *st)
+{
+    extern __shared__ __align__(16) unsigned char sort_smem[];
+    __shared__ dev::sort_ctl ctl;
+    __shared__ int slots[kSortWarps * 64];
+    __shared__ int s_front;
+    const int nf = *n_fronts;
+    if (nf < 1) return; // barrier timeout, reported through st->err
+    if (threadIdx.x == 0) {
+        // first front whose end passes N (front_offsets[nf] = n > N)
+        int lo = 0, hi = nf - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi) / 2;
+            if (static_cast<uint32_t>(front_offsets[mid + 1]) > N)
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        s_front = lo;
+    }
+    __syncthreads();
+    const int c = s_front;
+    const int off = front_offsets[c], L = front_offsets[c + 1] - off;
+    for (int p = threadIdx.x; p < off; p += blockDim.x) out[p] = front_indices[p];
+    if (static_cast<uint32_t>(off) == N) return;
+    if (m < 2u) {
+        if (threadIdx.x == 0) atomicExch(&st->status, kStatusNeedTwoObjectives);
+        return;
+    }
+    const int32_t *mem = front_indices + off;
+    const sort_area<long long> a =
+        pick_area<long long>(sort_smem, L, reinterpret_cast<long long *>(wkey) + off, widx + off, wlist + off);
+    front_crowding(pts, n, m, keys, mem, L, a, &ctl, slots, &st->sort_err, wcd);
+    for (int p = threadIdx.x; p < L; p += blockDim.x) {
+        a.k[p] = ~order_key(wcd[mem[p]]); // descending, NaN first: greater_than_f
+        a.v[p] = p;
+    }
+    __syncthreads();
+    dev::block_std_sort(dev::sort_view<long long>{a.k, a.v}, L, a.lists, a.cap, &ctl, slots, &st->sort_err);
+    const int remaining = static_cast<int>(N) - off;
+    for (int j = threadIdx.x; j < remaining; j += blockDim.x) out[off + j] = mem[a.v[j]];
+}
+
+// sort_population_mo's final std::sort (multi_objective.cpp:455-462) of
+// 0..n-1 by (rank, descending crowding), by one block.
+__global__ void __launch_bounds__(kSortThreads) sort_population_kernel(
+    const int32_t *__restrict__ rank, const double *__restrict__ crowd, uint32_t n, const int32_t *__restrict__ n_fronts,
+    unsigned char *wkey, int32_t *widx, int2 *wlist, int32_t *out, peel_state *st)
+{
+    extern __shared__ __align__(16) unsigned char sort_smem[];
+    __shared__ dev::sort_ctl ctl;
+    __shared__ int slots[kSortWarps * 64];
+    if (*n_fronts < 1 || st->status != 0) return;
+    const int L = static_cast<int>(n);
+    const sort_area<dev::key2> a =
+        pick_area<dev::key2>(sort_smem, L, reinterpret_cast<dev::key2 *>(wkey), widx, wlist);
+    for (int q = threadIdx.x; q < L; q += blockDim.x) {
+        a.k[q] = dev::key2{rank[q], ~order_key(crowd[q])};
+        a.v[q] = q;
+    }
+    __syncthreads();
+    dev::block_std_sort(dev::sort_view<dev::key2>{a.k, a.v}, L, a.lists, a.cap, &ctl, slots, &st->sort_err);
+    for (int j = threadIdx.x; j < L; j += blockDim.x) out[j] = a.v[j];
+}
+
+// (key, value) pairs of a caller's device buffers sorted in place by one
+// block, with std::sort's order of ties.
+__global__ void __launch_bounds__(kSortThreads) sort_pairs_kernel(long long *k, int32_t *v, uint32_t n, int2 *wlist,
+                                                                  int *err)
+{
+    extern __shared__ __align__(16) unsigned char sort_smem[];
+    __shared__ dev::sort_ctl ctl;
+    __shared__ int slots[kSortWarps * 64];
+    const int L = static_cast<int>(n);
+    const sort_area<long long> a = pick_area<long long>(sort_smem, L, k, v, wlist);
+    const bool staged = a.k != k;
+    if (staged) {
+        for (int p = threadIdx.x; p < L; p += blockDim.x) {
+            a.k[p] = k[p];
+            a.v[p] = v[p];
+        }
+    }
+    __syncthreads();
+    dev::block_std_sort(dev::sort_view<long long>{a.k, a.v}, L, a.lists, a.cap, &ctl, slots, err);
+    if (staged) {
+        for (int p = threadIdx.x; p < L; p += blockDim.x) {
+            k[p] = a.k[p];
+            v[p] = a.v[p];
+        }
+    }
+}
+
+// out[i] = i (corner cases of select_best_N_mo / sort_population_mo).
+__global__ void iota_kernel(int32_t *out, uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = static_cast<int32_t>(i);
+}
+
+// Device status word of the MO entry points: 0 ok, -1 a grid barrier gave up,
+// 1 crowding over fewer than two objectives (the reference throws), 2 broken
+// sort invariant.
+__global__ void mo_status_kernel(const peel_state *st, int32_t *status)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0)
+        *status = st->err ? -1 : st->status ? 1 : st->sort_err ? 2 : 0;
 }
 
 // One front holding every point: rank 0, identity order.
@@ -619,7 +759,7 @@ __global__ void init_rem_kernel(uint32_t *rem, uint32_t n, uint32_t W8)
 
 constexpr uint64_t kMaxPoints = 1u << 19; // 524288 points: a 32 GiB bit matrix
 
-size_t align256(size_t b)
+constexpr size_t align256(size_t b)
 {
     return (b + 255u) & ~static_cast<size_t>(255u);
 }
@@ -627,22 +767,24 @@ size_t align256(size_t b)
 // Device scratch of one survival pass (global memory beyond the inputs and
 // outputs). Laid out back to back, each piece 256-byte aligned.
 struct survival_scratch {
-    long long *keys;   // m * n order keys (objective-major)
-    uint32_t *Dt;      // n * W8 dominated-by bit matrix
-    peel_state *st;    // barrier, counters, status
-    uint32_t *rem;     // W8 unassigned-point bit set
-    int32_t *list;     // n members of the front being built
-    int32_t *keyv;     // n their ordering keys
-    int32_t *sorted;   // m * n per-objective sorted front members
-    int32_t *inv_pos;  // m * n position of each point in its sorted front
+    long long *keys;     // m * n order keys (objective-major)
+    uint32_t *Dt;        // n * W8 dominated-by bit matrix
+    peel_state *st;      // barrier, counters, status
+    uint32_t *rem;       // W8 unassigned-point bit set
+    int32_t *list;       // n members of the front being built
+    int32_t *keyv;       // n their ordering keys
+    unsigned char *wkey; // n * 16 B sort keys of fronts too large for shared memory
+    int32_t *widx;       // n sort values
+    int2 *wlist;         // n sort ranges
+    double *wcd;         // n crowding distances (select_best_N_mo, sort_population_mo)
 };
 
-size_t survival_scratch_bytes(uint64_t n, uint64_t m)
+constexpr size_t survival_scratch_bytes(uint64_t n, uint64_t m)
 {
-    const uint64_t mm = m > 0 ? m : 1;
-    const uint64_t W8 = (((n + 31u) / 32u) + 7u) & ~uint64_t(7);
-    return align256(n * mm * sizeof(long long)) + align256(n * W8 * 4u) + align256(sizeof(peel_state))
-           + align256(W8 * 4u) + 2u * align256(n * 4u) + 2u * align256(n * mm * 4u);
+    return align256(n * (m > 0 ? m : 1) * sizeof(long long))
+           + align256(n * ((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u) + align256(sizeof(peel_state))
+           + align256(((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u) + 2u * align256(n * 4u) + align256(n * 16u)
+           + align256(n * 4u) + align256(n * sizeof(int2)) + align256(n * sizeof(double));
 }
 
 survival_scratch carve_survival_scratch(void *base, uint64_t n, uint64_t m)
@@ -663,10 +805,28 @@ survival_scratch carve_survival_scratch(void *base, uint64_t n, uint64_t m)
     p += align256(n * 4u);
     s.keyv = reinterpret_cast<int32_t *>(p);
     p += align256(n * 4u);
-    s.sorted = reinterpret_cast<int32_t *>(p);
-    p += align256(n * mm * 4u);
-    s.inv_pos = reinterpret_cast<int32_t *>(p);
+    s.wkey = reinterpret_cast<unsigned char *>(p);
+    p += align256(n * 16u);
+    s.widx = reinterpret_cast<int32_t *>(p);
+    p += align256(n * 4u);
+    s.wlist = reinterpret_cast<int2 *>(p);
+    p += align256(n * sizeof(int2));
+    s.wcd = reinterpret_cast<double *>(p);
     return s;
+}
+
+int launch_front_crowding(const survival_scratch &sc, const double *d_points, uint32_t n, uint32_t m,
+                          const int32_t *front_offsets, const int32_t *front_indices, const int32_t *n_fronts,
+                          int mode, double *cd, int num_sms, cudaStream_t s)
+{
+    PGX_CUDA(cudaFuncSetAttribute(front_crowding_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(kSortSmemBytes)));
+    const int grid = static_cast<int>(std::min<uint64_t>(n, static_cast<uint64_t>(num_sms) * 2u));
+    front_crowding_kernel<<<grid, kSortThreads, kSortSmemBytes, s>>>(d_points, n, m, sc.keys, front_offsets,
+                                                                     front_indices, n_fronts, mode, sc.wkey, sc.widx,
+                                                                     sc.wlist, cd, sc.st);
+    PGX_CUDA(cudaGetLastError());
+    return PGX_OK;
 }
 
 // The whole survival pass on `stream` over caller-provided scratch: clears
@@ -715,18 +875,8 @@ int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n,
     PGX_CUDA(cudaMemcpyAsync(out.n_fronts, &sc.st->n_fronts, sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
 
     if (out.crowding) {
-        if (m > 0) {
-            for (uint32_t k = 0; k < m; ++k) {
-                crowding_rank_kernel<<<num_sms * 4, 256, 0, s>>>(sc.keys, n, k, out.front_offsets,
-                                                                 out.front_indices, out.n_fronts, sc.sorted,
-                                                                 sc.inv_pos);
-                PGX_CUDA(cudaGetLastError());
-            }
-            *launches += m;
-        }
-        crowding_accumulate_kernel<<<blocks_for(n, 256, num_sms), 256, 0, s>>>(
-            d_points, n, m, out.rank, out.front_offsets, sc.sorted, sc.inv_pos, out.crowding);
-        PGX_CUDA(cudaGetLastError());
+        PGX_TRY(launch_front_crowding(sc, d_points, n, m, out.front_offsets, out.front_indices, out.n_fronts,
+                                      kCrowdNsga2, out.crowding, num_sms, s));
         *launches += 1;
     }
     return PGX_OK;
@@ -758,9 +908,10 @@ int launch_survival(pgx_context *ctx, const double *d_points, uint64_t n, uint64
 int read_survival_status(pgx_context *ctx, uint64_t n, uint64_t m)
 {
     const survival_scratch sc = carve_survival_scratch(ctx->s_state.ptr, n, m);
-    int err = 0;
-    PGX_CUDA(cudaMemcpy(&err, &sc.st->err, sizeof(int), cudaMemcpyDeviceToHost));
-    PGX_CHECK(err == 0, PGX_ERR_TIMEOUT, "fast_non_dominated_sorting: a grid barrier timed out on the device");
+    peel_state st{};
+    PGX_CUDA(cudaMemcpy(&st, sc.st, sizeof(peel_state), cudaMemcpyDeviceToHost));
+    PGX_CHECK(st.err == 0, PGX_ERR_TIMEOUT, "fast_non_dominated_sorting: a grid barrier timed out on the device");
+    PGX_CHECK(st.sort_err == 0, PGX_ERR_CUDA, "device sort: internal error " + std::to_string(st.sort_err));
     return PGX_OK;
 }
 
@@ -775,7 +926,7 @@ int launch_crowding_single(pgx_context *ctx, const double *d_points, uint64_t n6
     PGX_CHECK(n64 <= kMaxPoints && m64 <= 4096u, PGX_ERR_CAPACITY, "crowding_distance: input too large");
     const uint32_t n = static_cast<uint32_t>(n64), m = static_cast<uint32_t>(m64);
     const int sms = ctx->num_sms;
-    // keys, sorted and inv_pos come from the survival scratch layout (no bit matrix use)
+    // keys, status and the sort work arrays come from the survival scratch layout (no bit matrix use)
     PGX_TRY(ctx->s_state.ensure(survival_scratch_bytes(n, m)));
     const survival_scratch sc = carve_survival_scratch(ctx->s_state.ptr, n, m);
     const size_t b_rank = align256(static_cast<size_t>(n) * 4u);
@@ -786,19 +937,53 @@ int launch_crowding_single(pgx_context *ctx, const double *d_points, uint64_t n6
     int32_t *front_offsets = reinterpret_cast<int32_t *>(ctx->s_outs.as<char>() + 2u * b_rank);
     int32_t *n_fronts = reinterpret_cast<int32_t *>(ctx->s_outs.as<char>() + 2u * b_rank + b_off);
     const uint64_t nm = static_cast<uint64_t>(n) * m;
+    PGX_CUDA(cudaMemsetAsync(sc.st, 0, sizeof(peel_state), s));
     single_front_kernel<<<blocks_for(n, 256, sms), 256, 0, s>>>(n, rank, front_offsets, front_indices, n_fronts);
     PGX_CUDA(cudaGetLastError());
     order_keys_kernel<<<blocks_for(nm, 256, sms), 256, 0, s>>>(d_points, n, m, sc.keys);
     PGX_CUDA(cudaGetLastError());
-    for (uint32_t k = 0; k < m; ++k) {
-        crowding_rank_kernel<<<sms * 4, 256, 0, s>>>(sc.keys, n, k, front_offsets, front_indices, n_fronts, sc.sorted,
-                                                     sc.inv_pos);
+    PGX_TRY(launch_front_crowding(sc, d_points, n, m, front_offsets, front_indices, n_fronts, kCrowdSortPopulation,
+                                  d_out, sms, s));
+    ctx->launches += 3;
+    return PGX_OK;
+}
+
+// Output buffers of an fnds pass the MO entry points need but do not return.
+struct fnds_bufs {
+    survival_out o;
+};
+
+int fnds_buffers(pgx_context *ctx, uint32_t n, fnds_bufs *b)
+{
+    const size_t bn = align256(static_cast<size_t>(n) * 4u);
+    const size_t bo = align256((static_cast<size_t>(n) + 1u) * 4u);
+    PGX_TRY(ctx->s_outs.ensure(3u * bn + bo + 256u));
+    char *p = ctx->s_outs.as<char>();
+    b->o.rank = reinterpret_cast<int32_t *>(p);
+    b->o.dom_count = reinterpret_cast<int32_t *>(p + bn);
+    b->o.front_indices = reinterpret_cast<int32_t *>(p + 2u * bn);
+    b->o.front_offsets = reinterpret_cast<int32_t *>(p + 3u * bn);
+    b->o.n_fronts = reinterpret_cast<int32_t *>(p + 3u * bn + bo);
+    b->o.crowding = nullptr;
+    return PGX_OK;
+}
+
+int finish_status(const survival_scratch &sc, int32_t *d_status, cudaStream_t s, uint64_t *launches)
+{
+    if (d_status) {
+        mo_status_kernel<<<1, 32, 0, s>>>(sc.st, d_status);
         PGX_CUDA(cudaGetLastError());
+        ++*launches;
     }
-    crowding_accumulate_kernel<<<blocks_for(n, 256, sms), 256, 0, s>>>(d_points, n, m, rank, front_offsets, sc.sorted,
-                                                                       sc.inv_pos, d_out);
+    return PGX_OK;
+}
+
+int launch_iota(int32_t *d_out, uint64_t n, int num_sms, cudaStream_t s, uint64_t *launches)
+{
+    if (n == 0) return PGX_OK;
+    iota_kernel<<<blocks_for(n, 256, num_sms), 256, 0, s>>>(d_out, static_cast<uint32_t>(n));
     PGX_CUDA(cudaGetLastError());
-    ctx->launches += 3 + m;
+    ++*launches;
     return PGX_OK;
 }
 
@@ -841,6 +1026,85 @@ int extract_dom_list(pgx_context *ctx, uint64_t n64, uint64_t m64, const int64_t
     return PGX_OK;
 }
 
+int launch_select_best(pgx_context *ctx, const double *d_points, uint64_t n64, uint64_t m64, uint64_t N64,
+                       int32_t *d_out, int32_t *d_status, cudaStream_t s)
+{
+    const int sms = ctx->num_sms;
+    if (d_status) PGX_CUDA(cudaMemsetAsync(d_status, 0, sizeof(int32_t), s));
+    if (N64 == 0 || n64 == 0) return PGX_OK;
+    if (n64 == 1 || N64 >= n64) return launch_iota(d_out, n64, sms, s, &ctx->launches);
+    PGX_TRY(check_survival_shape(n64, m64));
+    const uint32_t n = static_cast<uint32_t>(n64), m = static_cast<uint32_t>(m64), N = static_cast<uint32_t>(N64);
+    PGX_TRY(ctx->s_state.ensure(survival_scratch_bytes(n, m)));
+    const survival_scratch sc = carve_survival_scratch(ctx->s_state.ptr, n, m);
+    fnds_bufs fb;
+    PGX_TRY(fnds_buffers(ctx, n, &fb));
+    PGX_TRY(run_survival(sc, d_points, n, m, fb.o, sms, s, &ctx->launches));
+    PGX_CUDA(cudaFuncSetAttribute(select_best_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(kSortSmemBytes)));
+    select_best_kernel<<<1, kSortThreads, kSortSmemBytes, s>>>(d_points, n, m, N, sc.keys, fb.o.front_offsets,
+                                                               fb.o.front_indices, fb.o.n_fronts, sc.wkey, sc.widx,
+                                                               sc.wlist, sc.wcd, d_out, sc.st);
+    PGX_CUDA(cudaGetLastError());
+    ++ctx->launches;
+    return finish_status(sc, d_status, s, &ctx->launches);
+}
+
+int launch_sort_population(pgx_context *ctx, const double *d_points, uint64_t n64, uint64_t m64, int32_t *d_out,
+                           int32_t *d_status, cudaStream_t s)
+{
+    const int sms = ctx->num_sms;
+    if (d_status) PGX_CUDA(cudaMemsetAsync(d_status, 0, sizeof(int32_t), s));
+    if (n64 == 0) return PGX_OK;
+    if (n64 == 1) return launch_iota(d_out, 1, sms, s, &ctx->launches);
+    PGX_TRY(check_survival_shape(n64, m64));
+    const uint32_t n = static_cast<uint32_t>(n64), m = static_cast<uint32_t>(m64);
+    PGX_TRY(ctx->s_state.ensure(survival_scratch_bytes(n, m)));
+    const survival_scratch sc = carve_survival_scratch(ctx->s_state.ptr, n, m);
+    fnds_bufs fb;
+    PGX_TRY(fnds_buffers(ctx, n, &fb));
+    PGX_TRY(run_survival(sc, d_points, n, m, fb.o, sms, s, &ctx->launches));
+    PGX_TRY(launch_front_crowding(sc, d_points, n, m, fb.o.front_offsets, fb.o.front_indices, fb.o.n_fronts,
+                                  kCrowdSortPopulation, sc.wcd, sms, s));
+    PGX_CUDA(cudaFuncSetAttribute(sort_population_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(kSortSmemBytes)));
+    sort_population_kernel<<<1, kSortThreads, kSortSmemBytes, s>>>(fb.o.rank, sc.wcd, n, fb.o.n_fronts, sc.wkey,
+                                                                   sc.widx, sc.wlist, d_out, sc.st);
+    PGX_CUDA(cudaGetLastError());
+    ctx->launches += 2;
+    return finish_status(sc, d_status, s, &ctx->launches);
+}
+
+int launch_sort_pairs(pgx_context *ctx, long long *d_keys, int32_t *d_vals, uint64_t n64, int *d_err, int2 *d_lists,
+                      cudaStream_t s)
+{
+    if (n64 < 2) return PGX_OK;
+    PGX_CHECK(n64 <= (1ull << 30), PGX_ERR_CAPACITY, "sort: more than 2^30 elements");
+    PGX_CUDA(cudaFuncSetAttribute(sort_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(kSortSmemBytes)));
+    sort_pairs_kernel<<<1, kSortThreads, kSortSmemBytes, s>>>(d_keys, d_vals, static_cast<uint32_t>(n64), d_lists,
+                                                              d_err);
+    PGX_CUDA(cudaGetLastError());
+    ++ctx->launches;
+    return PGX_OK;
+}
+
+// After a synchronisation, for the last select_best/sort_population pass of
+// shape (n, m) on this context: the reference's error for crowding over fewer
+// than two objectives, or a timeout / internal error.
+int read_mo_status(pgx_context *ctx, uint64_t n, uint64_t m)
+{
+    const survival_scratch sc = carve_survival_scratch(ctx->s_state.ptr, n, m);
+    peel_state st{};
+    PGX_CUDA(cudaMemcpy(&st, sc.st, sizeof(peel_state), cudaMemcpyDeviceToHost));
+    PGX_CHECK(st.err == 0, PGX_ERR_TIMEOUT, "fast_non_dominated_sorting: a grid barrier timed out on the device");
+    PGX_CHECK(st.status == 0, PGX_ERR_INVALID,
+              "Points in the non dominated front must contain at least two objectives: " + std::to_string(m)
+                  + " detected.");
+    PGX_CHECK(st.sort_err == 0, PGX_ERR_CUDA, "device sort: internal error " + std::to_string(st.sort_err));
+    return PGX_OK;
+}
+
 } // namespace pgx
 
 // ---------------------------------------------------------------------------
@@ -855,7 +1119,7 @@ int extract_dom_list(pgx_context *ctx, uint64_t n64, uint64_t m64, const int64_t
 // (order keys, the dominance bit matrix, peel state, per-objective orders)
 // from one array compiled into the library: g_noalloc_scratch, sized for at
 // most kNoAllocMaxPoints points and kNoAllocMaxObjectives objectives
-// (about 2.6 MB, held by every GPU that loads the library until the process
+// (about 2.5 MB, held by every GPU that loads the library until the process
 // exits). Larger inputs are rejected with PGX_ERR_CAPACITY.
 //
 // Host code cannot use the array's name as a device address (it names a host
@@ -874,21 +1138,8 @@ constexpr uint64_t kNoAllocMaxPoints = 4096;
 constexpr uint64_t kNoAllocMaxObjectives = 8;
 constexpr int kNoAllocMaxDevices = 64;
 
-constexpr size_t noalloc_align(size_t b)
-{
-    return (b + 255u) & ~static_cast<size_t>(255u);
-}
-
-// Bytes of the survival scratch layout for the largest accepted shape.
-constexpr size_t noalloc_bytes(uint64_t n, uint64_t m)
-{
-    return noalloc_align(n * m * 8u) + noalloc_align(n * ((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u)
-           + noalloc_align(sizeof(peel_state)) + noalloc_align(((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u)
-           + 2u * noalloc_align(n * 4u) + 2u * noalloc_align(n * m * 4u);
-}
-
-static __device__ __align__(256) unsigned char g_noalloc_scratch[noalloc_bytes(kNoAllocMaxPoints,
-                                                                               kNoAllocMaxObjectives)];
+static __device__ __align__(256) unsigned char g_noalloc_scratch[survival_scratch_bytes(kNoAllocMaxPoints,
+                                                                                        kNoAllocMaxObjectives)];
 
 struct noalloc_device {
     void *scratch = nullptr; // device address of g_noalloc_scratch on this device

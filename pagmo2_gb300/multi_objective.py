@@ -1,11 +1,16 @@
 """GPU NSGA-II survival with the reference's signatures
-(src/utils/multi_objective.cpp:200-257, :280-315; src/algorithms/nsga2.cpp:183-206).
+(src/utils/multi_objective.cpp:200-257, :280-315, :344-396, :425-465;
+src/algorithms/nsga2.cpp:183-206).
 
 ``fast_non_dominated_sorting(points)`` returns the same 4-tuple as the
 reference's ``fnds_return_type`` (fronts, dom_list, dom_count, rank), with the
 fronts in the reference's order. ``crowding_distance(front)`` returns the
 crowding distances of one front. ``nsga2_survival(points)`` runs the survival
 block of one NSGA-II generation (fronts + per-front crowding) in one call.
+``select_best_N_mo(points, N)`` and ``sort_population_mo(points)`` return the
+reference's index lists. Wherever the reference sorts with std::sort, ties are
+left in the order std::sort (GNU libstdc++) leaves them, so every output is
+bit-exact with the reference.
 """
 from __future__ import annotations
 
@@ -14,6 +19,7 @@ import ctypes as C
 import numpy as np
 
 from . import _native as N
+from . import _native as _nat
 
 
 def _points(points) -> tuple[np.ndarray, int, int]:
@@ -104,3 +110,41 @@ def nsga2_survival(points, ctx: N.Context | None = None):
     N.check(N.lib().pgx_nsga2_survival(ctx.handle, N.ptr(a), n, m, N.ptr(rank), N.ptr(dc), N.ptr(off), N.ptr(idx),
                                        C.addressof(nf), N.ptr(cd)))
     return rank, dc, off[:nf.value + 1].copy(), idx, cd
+
+
+
+def select_best_N_mo(points, N: int, ctx: _nat.Context | None = None) -> list[int]:  # noqa: N802,N803
+    """Indices of the best N points -- whole fronts while they fit, then the
+    critical front by descending crowding distance -- as the reference's
+    select_best_N_mo returns them."""
+    a, n, m = _points(points)
+    if N < 0:
+        raise OverflowError("N must be non-negative")
+    ctx = ctx or _nat.default_context()
+    out = np.empty(max(min(N, n), 1), np.int32)
+    cnt = C.c_uint64()
+    _nat.check(_nat.lib().pgx_select_best_n_mo(ctx.handle, _nat.ptr(a) if a.size else None, n, m, N, _nat.ptr(out),
+                                                C.byref(cnt)))
+    return out[:cnt.value].tolist()
+
+
+def sort_population_mo(points, ctx: _nat.Context | None = None) -> list[int]:
+    """The points ordered by (non-domination rank, descending crowding
+    distance), as the reference's sort_population_mo returns them."""
+    a, n, m = _points(points)
+    ctx = ctx or _nat.default_context()
+    out = np.empty(max(n, 1), np.int32)
+    _nat.check(_nat.lib().pgx_sort_population_mo(ctx.handle, _nat.ptr(a) if a.size else None, n, m, _nat.ptr(out)))
+    return out[:n].tolist()
+
+
+def std_sort_keys(keys, values=None, ctx: _nat.Context | None = None):
+    """(keys, values) sorted by key on the GPU, equal keys left in the order
+    std::sort (GNU libstdc++) leaves them; values default to 0..n-1."""
+    k = np.array(keys, dtype=np.int64).reshape(-1)
+    v = np.arange(k.size, dtype=np.int32) if values is None else np.array(values, dtype=np.int32).reshape(-1)
+    if v.size != k.size:
+        raise ValueError("keys and values differ in length")
+    ctx = ctx or _nat.default_context()
+    _nat.check(_nat.lib().pgx_std_sort_i64(ctx.handle, _nat.ptr(k), _nat.ptr(v), k.size))
+    return k, v

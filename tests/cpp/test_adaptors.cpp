@@ -89,6 +89,12 @@ int main()
     CHECK(throws_with<std::invalid_argument>([] { fast_non_dominated_sorting({{1., 2.}}); },
                                              "At least two points"));
     CHECK(throws_with<std::invalid_argument>([] { crowding_distance({{1.}, {2.}}); }, "at least two objectives"));
+    // select_best_N_mo / sort_population_mo corner cases need no device, as in the reference
+    CHECK(select_best_N_mo({{1., 2.}, {3., 4.}}, 0u).empty());
+    CHECK(select_best_N_mo({}, 10u).empty());
+    CHECK((select_best_N_mo({{1., 2.}}, 10u) == std::vector<pagmo::pop_size_t>{0u}));
+    CHECK((sort_population_mo({{1., 5., 2., 3.}}) == std::vector<pagmo::pop_size_t>{0u}));
+    CHECK(sort_population_mo({}).empty());
 
     std::vector<double> dvs(40);
     for (size_t i = 0; i < dvs.size(); ++i) dvs[i] = -2.0 + 0.1 * static_cast<double>(i);
@@ -99,6 +105,7 @@ int main()
         CHECK(pr.get_fevals() == 0u);
         CHECK(throws_with<std::runtime_error>([&] { pagmo::problem{gpu_rosenbrock{4u}}.fitness({1., 1., 1., 1.}); },
                                               ""));
+        CHECK(throws_with<std::runtime_error>([] { sort_population_mo({{1., 2.}, {2., 1.}}); }, ""));
     } else {
         // with a device: bfe{gpu_bfe} against bfe{thread_bfe}, fevals counted once
         pagmo::problem pr{pagmo::rosenbrock{4u}};
@@ -113,6 +120,27 @@ int main()
         auto w = pagmo::fast_non_dominated_sorting({{0, 7}, {1, 5}, {2, 3}, {4, 2}, {7, 1}, {10, 0}, {2, 6}, {4, 4},
                                                     {10, 2}, {6, 6}, {9, 5}});
         CHECK(r == w);
+        // tie-heavy populations: the index lists equal the reference's, ties included
+        std::vector<pagmo::vector_double> pop;
+        unsigned seed = 7u;
+        for (int i = 0; i < 150; ++i) {
+            pagmo::vector_double f(3);
+            for (auto &v : f) {
+                seed = seed * 1103515245u + 12345u;
+                v = static_cast<double>((seed >> 16) % 4u);
+            }
+            pop.push_back(f);
+        }
+        CHECK(sort_population_mo(pop) == pagmo::sort_population_mo(pop));
+        for (pagmo::pop_size_t N : {1u, 7u, 50u, 75u, 149u, 150u, 300u})
+            CHECK(select_best_N_mo(pop, N) == pagmo::select_best_N_mo(pop, N));
+        const auto cd_gpu = crowding_distance(pop), cd_ref = pagmo::crowding_distance(pop);
+        bool same = cd_gpu.size() == cd_ref.size();
+        for (size_t i = 0; same && i < cd_ref.size(); ++i)
+            same = (std::isnan(cd_gpu[i]) && std::isnan(cd_ref[i])) || cd_gpu[i] == cd_ref[i];
+        CHECK(same);
+        CHECK(throws_with<std::invalid_argument>([] { sort_population_mo({{1.}, {1.}, {2.}}); },
+                                                 "at least two objectives"));
     }
     if (failures) {
         std::fprintf(stderr, "%d check(s) failed\n", failures);
