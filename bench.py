@@ -446,6 +446,20 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops) -> dict:
     ms = timed(surv, reps=10, flush_l2=False)
     out["nsga2_survival_20000x3"] = {"ms": ms, "fronts": int(nf.item()),
                                      "pair_tests_per_s": n * n / (ms * 1e-3)}
+
+    # NSGA-II's selection of the next population from the merged 2 NP points
+    # (nsga2.cpp:300: select_best_N_mo(merged, NP)) and sort_population_mo
+    sel = i32(n)
+    st = i32(1)
+
+    def select():
+        N.check(L.pgx_select_best_n_mo_device(ctx.handle, dp.data_ptr(), n, m, n // 2, sel.data_ptr(),
+                                              st.data_ptr(), sp))
+
+    def sortpop():
+        N.check(L.pgx_sort_population_mo_device(ctx.handle, dp.data_ptr(), n, m, sel.data_ptr(), st.data_ptr(), sp))
+    out["select_best_N_mo_20000x3_N10000"] = {"ms": timed(select, reps=10, flush_l2=False)}
+    out["sort_population_mo_20000x3"] = {"ms": timed(sortpop, reps=10, flush_l2=False)}
     out["archipelago_64_islands"] = run_archipelago(ctx, L, N, W, stream)
     return out
 

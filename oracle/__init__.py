@@ -74,8 +74,8 @@ class _Oracle:
         h.orc_crowding_ex.argtypes = [_vp, _u64, _u64, C.c_int, _vp]
         h.orc_nsga2_crowding_ex.argtypes = [_vp, _u64, _u64, _vp, _vp, _u64, C.c_int, _vp]
         h.orc_sort_last_error.restype = C.c_char_p
-        for name in ("orc_std_sort_keys", "orc_introsort_keys", "orc_introsort_chunked_keys", "orc_heap_sort_keys",
-                     "orc_std_partial_sort_full"):
+        for name in ("orc_std_sort_keys", "orc_introsort_keys", "orc_introsort_chunked_keys",
+                     "orc_introsort_lists_keys", "orc_heap_sort_keys", "orc_std_partial_sort_full"):
             getattr(h, name).argtypes = [_vp, _vp, _u64]
             getattr(h, name).restype = None
         h.orc_quicksort_adversary.argtypes = [_u64, _vp]
@@ -172,12 +172,13 @@ class _Oracle:
     # orderings -----------------------------------------------------------------
     def sort_keys(self, keys, values=None, method="std"):
         """(keys, values) sorted by key: method "std" (std::sort), "intro" (the
-        restated introsort), "chunked" (its 32-wide chunked partition), "heap"
+        restated introsort), "chunked" / "lists" (its two GPU partitions), "heap"
         (restated heapsort) or "std_heap" (std::partial_sort over the whole range)."""
         k = np.array(keys, dtype=np.int64)
         v = np.arange(k.size, dtype=np.int32) if values is None else np.array(values, dtype=np.int32)
         fn = {"std": self.h.orc_std_sort_keys, "intro": self.h.orc_introsort_keys,
-              "chunked": self.h.orc_introsort_chunked_keys, "heap": self.h.orc_heap_sort_keys,
+              "chunked": self.h.orc_introsort_chunked_keys, "lists": self.h.orc_introsort_lists_keys,
+              "heap": self.h.orc_heap_sort_keys,
               "std_heap": self.h.orc_std_partial_sort_full}[method]
         fn(_p(k), _p(v), k.size)
         return k, v

@@ -93,6 +93,7 @@ uint64_t orc_depth_limit_hits(void);
 void orc_std_sort_keys(long long *k, int32_t *v, uint64_t n);
 void orc_introsort_keys(long long *k, int32_t *v, uint64_t n);
 void orc_introsort_chunked_keys(long long *k, int32_t *v, uint64_t n);
+void orc_introsort_lists_keys(long long *k, int32_t *v, uint64_t n);
 void orc_heap_sort_keys(long long *k, int32_t *v, uint64_t n);
 void orc_std_partial_sort_full(long long *k, int32_t *v, uint64_t n);
 /* McIlroy's quicksort adversary against std::sort: n keys. */

@@ -14,9 +14,10 @@
 //       cut = Hoare partition of [first+1, last) around *first;
 //       recurse on [cut, last); last = cut
 //   then one insertion sort over the whole array.
-// orc_introsort_keys restates it; orc_introsort_chunked_keys restates it with
-// the partition computed the way the GPU does (stoppers paired in 32-wide
-// chunks, see below); both are checked against std::sort by the tests.
+// orc_introsort_keys restates it; orc_introsort_chunked_keys and
+// orc_introsort_lists_keys restate it with the partition computed the two ways
+// the GPU does (stoppers paired in 32-wide chunks; complete stopper lists);
+// all three are checked against std::sort by the tests.
 #include "oracle.h"
 
 #include <algorithm>
@@ -145,6 +146,26 @@ long chunked_partition(arr &x, long first, long last)
     }
 }
 
+// The same cut and swaps from the complete stopper lists (the GPU's
+// formulation for long ranges): left stoppers L[0..nl) ascending and right
+// stoppers R[0..nr) descending, all flagged on the original values; K = the
+// number of i with L[i] < R[i] (a prefix), swap those K pairs, cut =
+// min(L[K], R[K-1]), or L[0] when K = 0.
+long lists_partition(arr &x, long first, long last)
+{
+    const key_t pv = x.k[first];
+    std::vector<long> L, R;
+    for (long p = first + 1; p < last; ++p)
+        if (!(x.k[p] < pv)) L.push_back(p);
+    for (long p = last - 1; p > first; --p)
+        if (!(pv < x.k[p])) R.push_back(p);
+    size_t K = 0;
+    while (K < L.size() && K < R.size() && L[K] < R[K]) ++K;
+    for (size_t i = 0; i < K; ++i) x.swap(L[i], R[i]);
+    if (K == 0) return L[0];
+    return K < L.size() ? std::min(L[K], R[K - 1]) : R[K - 1];
+}
+
 // libstdc++ __adjust_heap / __push_heap on x[first .. first+len).
 void adjust_heap(arr &x, long first, long hole, long len, key_t vk, int32_t vv)
 {
@@ -212,7 +233,10 @@ void insertion_sort(arr &x, long first, long last)
     }
 }
 
-template <bool Chunked>
+// Partition formulation of a restated introsort.
+enum class part { hoare, chunked, lists };
+
+template <part P>
 void introsort_loop(arr &x, long first, long last, long depth)
 {
     while (last - first > 16) {
@@ -223,18 +247,20 @@ void introsort_loop(arr &x, long first, long last, long depth)
         }
         --depth;
         median_to_first(x, first, first + 1, first + (last - first) / 2, last - 1);
-        const long cut = Chunked ? chunked_partition(x, first, last) : hoare_partition(x, first, last);
-        introsort_loop<Chunked>(x, cut, last, depth);
+        const long cut = P == part::chunked ? chunked_partition(x, first, last)
+                         : P == part::lists ? lists_partition(x, first, last)
+                                            : hoare_partition(x, first, last);
+        introsort_loop<P>(x, cut, last, depth);
         last = cut;
     }
 }
 
-template <bool Chunked>
+template <part P>
 void introsort(key_t *k, int32_t *v, long n)
 {
     if (n < 2) return;
     arr x{k, v};
-    introsort_loop<Chunked>(x, 0, n, 2 * floor_log2(n));
+    introsort_loop<P>(x, 0, n, 2 * floor_log2(n));
     insertion_sort(x, 0, n);
 }
 
@@ -282,12 +308,17 @@ void orc_std_sort_keys(long long *k, int32_t *v, uint64_t n)
 
 void orc_introsort_keys(long long *k, int32_t *v, uint64_t n)
 {
-    introsort<false>(k, v, static_cast<long>(n));
+    introsort<part::hoare>(k, v, static_cast<long>(n));
 }
 
 void orc_introsort_chunked_keys(long long *k, int32_t *v, uint64_t n)
 {
-    introsort<true>(k, v, static_cast<long>(n));
+    introsort<part::chunked>(k, v, static_cast<long>(n));
+}
+
+void orc_introsort_lists_keys(long long *k, int32_t *v, uint64_t n)
+{
+    introsort<part::lists>(k, v, static_cast<long>(n));
 }
 
 void orc_heap_sort_keys(long long *k, int32_t *v, uint64_t n)

@@ -29,9 +29,16 @@
 //    ballots over 32-position chunks taken alternately from both ends (each
 //    chunk clipped, when it is loaded, to positions no swap has touched, so
 //    its flags are those of the original values) and pairs them in order.
+//  - Ranges longer than kBlockRange are partitioned by the whole block instead:
+//    every left and right stopper of the range is compacted in position order
+//    (block scans over the original values), K = the number of pairs i with
+//    left[i] < right[i] (a prefix of i), the K swaps run in parallel, and the
+//    cut is min(left[K], right[K-1]) (left[0] when K = 0) -- the same pairs
+//    and cut as the sequential loop.
 //  - Ranges of 16 or fewer elements are final: the closing insertion sort of
 //    the whole array moves no element across a partition boundary, so it
-//    equals an insertion sort of each such range, done by one lane.
+//    equals a stable sort of each such range, which a half warp computes by
+//    counting, for each element, the smaller keys and the equal keys before it.
 //  - A range whose depth budget is spent is heapsorted by one lane, with
 //    libstdc++'s make_heap/sort_heap sift order.
 // The oracle restates the same algorithm twice (oracle/sorting.cpp) and the
@@ -79,10 +86,27 @@ struct sort_view {
 
 // Control words of one block's sort (shared memory).
 struct sort_ctl {
-    int take;  // next range of the current level
-    int ncur;  // ranges in the current level
-    int nnext; // ranges queued for the next level
-    int pad;
+    int take;     // next small range of the current level
+    int ncur;     // small ranges in the current level
+    int nnext;    // small ranges queued for the next level
+    int nbig;     // block-partitioned ranges in the current level
+    int nbignext; // block-partitioned ranges queued for the next level
+    int pad[3];
+};
+
+// Ranges longer than this are partitioned by the whole block.
+constexpr int kBlockRange = 512;
+
+// Bookkeeping of one block's sort: level lists of small ranges (2 * small_cap,
+// small_cap >= n / 17 + 1) and of block-partitioned ranges (2 * big_cap,
+// big_cap >= n / kBlockRange + 1), and n + n stopper positions.
+struct sort_work {
+    int2 *small;
+    int small_cap;
+    int2 *big;
+    int big_cap;
+    int *pos_l;
+    int *pos_r;
 };
 
 // Error codes written to the sort's error word (never expected; each marks a
@@ -182,6 +206,114 @@ __device__ void heap_sort(const sort_view<K> &x, int first, int last)
     }
 }
 
+// Stable sort of a leaf x[first .. first+len) (len <= 16) by one half warp:
+// every lane of the half calls it with its half's leaf (len 0: nothing).
+template <typename K>
+__device__ __forceinline__ K shfl16(const K &v, int src);
+template <>
+__device__ __forceinline__ long long shfl16<long long>(const long long &v, int src)
+{
+    return __shfl_sync(kSortFull, v, src, 16);
+}
+template <>
+__device__ __forceinline__ key2 shfl16<key2>(const key2 &v, int src)
+{
+    return key2{__shfl_sync(kSortFull, v.a, src, 16), __shfl_sync(kSortFull, v.b, src, 16)};
+}
+
+template <typename K>
+__device__ void halfwarp_leaf_sort(const sort_view<K> &x, int first, int len)
+{
+    const int sub = static_cast<int>(threadIdx.x & 15u);
+    const bool act = sub < len;
+    K kv{};
+    int32_t vv = 0;
+    if (act) {
+        kv = x.k[first + sub];
+        vv = x.v[first + sub];
+    }
+    int pos = 0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const K kj = shfl16(kv, j);
+        if (act && j < len && (key_less(kj, kv) || (j < sub && !key_less(kv, kj)))) ++pos;
+    }
+    __syncwarp();
+    if (act) {
+        x.k[first + pos] = kv;
+        x.v[first + pos] = vv;
+    }
+    __syncwarp();
+}
+
+// The whole block: median-of-three into `first`, then the Hoare partition of
+// [first+1, last) from the compacted stopper lists; returns the cut (same
+// value in every thread). scan: 64 ints of shared memory.
+template <typename K>
+__device__ int block_partition(const sort_view<K> &x, int first, int last, const sort_work &w, int *scan, int *err)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const int warp = static_cast<int>(threadIdx.x >> 5), nwarps = static_cast<int>(blockDim.x >> 5);
+    const unsigned below = (1u << lane) - 1u;
+    if (threadIdx.x == 0) median_to_first(x, first, first + 1, first + (last - first) / 2, last - 1);
+    __syncthreads();
+    const K pv = x.k[first];
+    int nl = 0, nr = 0; // stoppers so far (uniform)
+    for (int t0 = first + 1; t0 < last; t0 += blockDim.x) {
+        const int p = t0 + static_cast<int>(threadIdx.x);
+        bool fl = false, fr = false;
+        if (p < last) {
+            const K kp = x.k[p];
+            fl = !key_less(kp, pv);
+            fr = !key_less(pv, kp);
+        }
+        const unsigned bl = __ballot_sync(kSortFull, fl), br = __ballot_sync(kSortFull, fr);
+        if (lane == 0) {
+            scan[warp] = __popc(bl);
+            scan[32 + warp] = __popc(br);
+        }
+        __syncthreads();
+        int offl = 0, offr = 0, totl = 0, totr = 0;
+        for (int j = 0; j < nwarps; ++j) {
+            const int a = scan[j], b = scan[32 + j];
+            if (j < warp) {
+                offl += a;
+                offr += b;
+            }
+            totl += a;
+            totr += b;
+        }
+        if (fl) w.pos_l[nl + offl + __popc(bl & below)] = p;
+        if (fr) w.pos_r[nr + offr + __popc(br & below)] = p;
+        nl += totl;
+        nr += totr;
+        __syncthreads();
+    }
+    // pair i = (pos_l[i], pos_r[nr-1-i]); the swappable pairs are a prefix
+    const int mx = min(nl, nr);
+    int kk = 0;
+    for (int i0 = 0; i0 < mx; i0 += blockDim.x) {
+        const int i = i0 + static_cast<int>(threadIdx.x);
+        const bool ok = i < mx && w.pos_l[i] < w.pos_r[nr - 1 - i];
+        const int c = __syncthreads_count(ok);
+        kk += c;
+        if (c < static_cast<int>(blockDim.x)) break;
+    }
+    for (int i = threadIdx.x; i < kk; i += blockDim.x) x.swap(w.pos_l[i], w.pos_r[nr - 1 - i]);
+    int cut;
+    if (nl == 0) {
+        if (threadIdx.x == 0) atomicExch(err, kSortErrNoSentinel);
+        cut = last - 1;
+    } else if (kk == 0) {
+        cut = w.pos_l[0];
+    } else {
+        cut = w.pos_r[nr - kk];
+        if (kk < nl) cut = min(cut, w.pos_l[kk]);
+    }
+    __syncthreads();
+    return cut;
+}
+
 // One warp: median-of-three into `first`, then the Hoare partition of
 // [first+1, last) around it; returns the cut. `slots` is 64 ints of this
 // warp's shared memory. All 32 lanes call it with the same arguments.
@@ -258,68 +390,120 @@ __device__ int warp_partition(const sort_view<K> &x, int first, int last, int *s
     return last - 1;
 }
 
+// Queues a child range for the next level, by size.
+__device__ __forceinline__ void queue_range(int a, int b, int2 *small_next, int2 *big_next, const sort_work &w,
+                                            sort_ctl *ctl, int *err)
+{
+    const int len = b - a;
+    if (len > kBlockRange) {
+        const int slot = atomicAdd(&ctl->nbignext, 1);
+        if (slot < w.big_cap)
+            big_next[slot] = make_int2(a, b);
+        else
+            atomicExch(err, kSortErrListFull);
+    } else if (len > 16) {
+        const int slot = atomicAdd(&ctl->nnext, 1);
+        if (slot < w.small_cap)
+            small_next[slot] = make_int2(a, b);
+        else
+            atomicExch(err, kSortErrListFull);
+    }
+}
+
 // Sorts x[0 .. n) by key with std::sort's order of ties. Every thread of the
-// block calls it (blockDim.x a multiple of 32). lists: 2 * list_cap ranges
-// (list_cap >= n / 17 + 1); slots_all: 64 ints per warp of shared memory; ctl
-// in shared memory. Ends with a __syncthreads.
+// block calls it (blockDim.x a multiple of 32, at most 1024). slots_all: 64
+// ints per warp of shared memory; ctl in shared memory. Ends with a
+// __syncthreads.
 template <typename K>
-__device__ void block_std_sort(const sort_view<K> &x, int n, int2 *lists, int list_cap, sort_ctl *ctl, int *slots_all,
+__device__ void block_std_sort(const sort_view<K> &x, int n, const sort_work &w, sort_ctl *ctl, int *slots_all,
                                int *err)
 {
     const unsigned lane = threadIdx.x & 31u;
-    int *slots = slots_all + (threadIdx.x >> 5) * 64;
+    const int warp = static_cast<int>(threadIdx.x >> 5);
+    int *slots = slots_all + warp * 64;
     if (n <= 16) {
-        if (threadIdx.x == 0 && n > 1) insertion_sort(x, 0, n);
+        if (warp == 0) halfwarp_leaf_sort(x, 0, lane < 16u ? n : 0);
         __syncthreads();
         return;
     }
     int depth = 2 * floor_log2_int(n);
-    int2 *cur = lists, *nxt = lists + list_cap;
+    int2 *small_cur = w.small, *small_next = w.small + w.small_cap;
+    int2 *big_cur = w.big, *big_next = w.big + w.big_cap;
     if (threadIdx.x == 0) {
-        cur[0] = make_int2(0, n);
-        ctl->ncur = 1;
+        ctl->ncur = 0;
+        ctl->nbig = 0;
+        ctl->nnext = 0;
+        ctl->nbignext = 0;
+        queue_range(0, n, small_next, big_next, w, ctl, err);
+        ctl->ncur = ctl->nnext;
+        ctl->nbig = ctl->nbignext;
+    }
+    {
+        int2 *t = small_cur;
+        small_cur = small_next;
+        small_next = t;
+        t = big_cur;
+        big_cur = big_next;
+        big_next = t;
     }
     __syncthreads();
     for (;;) {
-        const int ncur = ctl->ncur;
-        if (ncur == 0) break;
+        const int ncur = min(ctl->ncur, w.small_cap), nbig = min(ctl->nbig, w.big_cap);
+        if (ncur == 0 && nbig == 0) break;
         __syncthreads();
         if (threadIdx.x == 0) {
             ctl->take = 0;
             ctl->nnext = 0;
+            ctl->nbignext = 0;
         }
         __syncthreads();
+        // long ranges: one at a time, by the whole block
+        for (int t = 0; t < nbig; ++t) {
+            const int2 r = big_cur[t];
+            if (depth == 0) {
+                if (threadIdx.x == 0) heap_sort(x, r.x, r.y);
+                __syncthreads();
+                continue;
+            }
+            const int cut = block_partition(x, r.x, r.y, w, slots_all, err);
+            if (threadIdx.x == 0) queue_range(r.x, cut, small_next, big_next, w, ctl, err);
+            if (threadIdx.x == 32 || (blockDim.x == 32 && threadIdx.x == 1))
+                queue_range(cut, r.y, small_next, big_next, w, ctl, err);
+            if (warp == 0) {
+                const int a = lane < 16u ? r.x : cut, len = lane < 16u ? cut - r.x : r.y - cut;
+                halfwarp_leaf_sort(x, a, len <= 16 ? len : 0);
+            }
+            __syncthreads();
+        }
+        // short ranges: one per warp
         for (;;) {
             int t = 0;
             if (lane == 0) t = atomicAdd(&ctl->take, 1);
             t = __shfl_sync(kSortFull, t, 0);
             if (t >= ncur) break;
-            const int2 r = cur[t];
+            const int2 r = small_cur[t];
             if (depth == 0) {
                 if (lane == 0) heap_sort(x, r.x, r.y);
                 __syncwarp();
                 continue;
             }
             const int cut = warp_partition(x, r.x, r.y, slots, err);
-            if (lane < 2u) {
-                const int a = lane == 0 ? r.x : cut, b = lane == 0 ? cut : r.y;
-                if (b - a > 16) {
-                    const int slot = atomicAdd(&ctl->nnext, 1);
-                    if (slot < list_cap)
-                        nxt[slot] = make_int2(a, b);
-                    else
-                        atomicExch(err, kSortErrListFull);
-                } else {
-                    insertion_sort(x, a, b);
-                }
-            }
-            __syncwarp();
+            if (lane == 0) queue_range(r.x, cut, small_next, big_next, w, ctl, err);
+            if (lane == 1) queue_range(cut, r.y, small_next, big_next, w, ctl, err);
+            const int a = lane < 16u ? r.x : cut, len = lane < 16u ? cut - r.x : r.y - cut;
+            halfwarp_leaf_sort(x, a, len <= 16 ? len : 0);
         }
         __syncthreads();
-        if (threadIdx.x == 0) ctl->ncur = min(ctl->nnext, list_cap);
-        int2 *t = cur;
-        cur = nxt;
-        nxt = t;
+        if (threadIdx.x == 0) {
+            ctl->ncur = ctl->nnext;
+            ctl->nbig = ctl->nbignext;
+        }
+        int2 *t = small_cur;
+        small_cur = small_next;
+        small_next = t;
+        t = big_cur;
+        big_cur = big_next;
+        big_next = t;
         --depth;
         __syncthreads();
     }

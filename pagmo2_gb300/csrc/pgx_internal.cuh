@@ -143,9 +143,10 @@ int launch_sort_population(pgx_context *ctx, const double *d_points, uint64_t n,
 // pass of shape (n, m) on this context, as the reference would raise it.
 int read_mo_status(pgx_context *ctx, uint64_t n, uint64_t m);
 // std::sort-ordered in-place sort of device (key, value) pairs by one block;
-// d_lists holds n int2, *d_err receives a nonzero code on a broken invariant.
+// d_lists holds n int2 and d_pos 2 n int32 of scratch, *d_err receives a
+// nonzero code on a broken invariant.
 int launch_sort_pairs(pgx_context *ctx, long long *d_keys, int32_t *d_vals, uint64_t n, int *d_err, int2 *d_lists,
-                      cudaStream_t stream);
+                      int32_t *d_pos, cudaStream_t stream);
 
 // Reads the device status word of the last survival pass of shape (n, m) on
 // this context (after a stream synchronisation): PGX_ERR_TIMEOUT when a grid

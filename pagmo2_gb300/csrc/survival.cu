@@ -374,35 +374,50 @@ __global__ void __launch_bounds__(kPeelThreads) peel_kernel(const uint32_t *__re
 
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortSmemCap = 4096;                    // (key, value) pairs a block keeps in shared memory
-constexpr int kSortSmemLists = kSortSmemCap / 16 + 2; // ranges per level, shared-memory case
-constexpr size_t kSortSmemBytes =
-    static_cast<size_t>(kSortSmemCap) * (sizeof(dev::key2) + sizeof(int32_t)) + 2u * kSortSmemLists * sizeof(int2);
+constexpr int kSortSmemCap = 4096;                                // (key, value) pairs kept in shared memory
+constexpr int kSortSmemSmall = kSortSmemCap / 16 + 2;             // short ranges per level list
+constexpr int kSortSmemBig = kSortSmemCap / dev::kBlockRange + 2; // block-partitioned ranges per level list
+constexpr size_t kSortSmemBytes = static_cast<size_t>(kSortSmemCap) * (sizeof(dev::key2) + 3u * sizeof(int32_t))
+                                  + 2u * (kSortSmemSmall + kSortSmemBig) * sizeof(int2);
 
 // Where one block sorts L pairs: its shared memory when they fit, else the
-// caller's slice of the global work arrays (keys, values, 2 * (L / 2) ranges).
+// caller's slices of the global work arrays (L keys, L values, L ranges, 2 L
+// positions).
 template <typename K>
 struct sort_area {
     K *k;
     int32_t *v;
-    int2 *lists;
-    int cap;
+    dev::sort_work w;
 };
 
 template <typename K>
-__device__ sort_area<K> pick_area(unsigned char *smem, int L, K *gk, int32_t *gv, int2 *gl)
+__device__ sort_area<K> pick_area(unsigned char *smem, int L, K *gk, int32_t *gv, int2 *gl, int32_t *gpos)
 {
     sort_area<K> a;
     if (L <= kSortSmemCap) {
-        a.k = reinterpret_cast<K *>(smem);
-        a.v = reinterpret_cast<int32_t *>(smem + kSortSmemCap * sizeof(dev::key2));
-        a.lists = reinterpret_cast<int2 *>(smem + kSortSmemCap * (sizeof(dev::key2) + sizeof(int32_t)));
-        a.cap = kSortSmemLists;
+        unsigned char *q = smem;
+        a.k = reinterpret_cast<K *>(q);
+        q += kSortSmemCap * sizeof(dev::key2);
+        a.w.small = reinterpret_cast<int2 *>(q);
+        a.w.small_cap = kSortSmemSmall;
+        q += 2u * kSortSmemSmall * sizeof(int2);
+        a.w.big = reinterpret_cast<int2 *>(q);
+        a.w.big_cap = kSortSmemBig;
+        q += 2u * kSortSmemBig * sizeof(int2);
+        a.v = reinterpret_cast<int32_t *>(q);
+        q += kSortSmemCap * sizeof(int32_t);
+        a.w.pos_l = reinterpret_cast<int *>(q);
+        q += kSortSmemCap * sizeof(int32_t);
+        a.w.pos_r = reinterpret_cast<int *>(q);
     } else {
         a.k = gk;
         a.v = gv;
-        a.lists = gl;
-        a.cap = L / 2;
+        a.w.big_cap = L / dev::kBlockRange + 2;
+        a.w.small_cap = (L - 2 * a.w.big_cap) / 2;
+        a.w.small = gl;
+        a.w.big = gl + 2 * a.w.small_cap;
+        a.w.pos_l = gpos;
+        a.w.pos_r = gpos + L;
     }
     return a;
 }
@@ -426,7 +441,7 @@ __device__ void front_crowding(const double *__restrict__ pts, uint32_t n, uint3
         const long long *kk = keys + static_cast<uint64_t>(k) * n;
         for (int p = threadIdx.x; p < L; p += blockDim.x) a.k[p] = kk[a.v[p]];
         __syncthreads();
-        dev::block_std_sort(dev::sort_view<long long>{a.k, a.v}, L, a.lists, a.cap, ctl, slots, err);
+        dev::block_std_sort(dev::sort_view<long long>{a.k, a.v}, L, a.w, ctl, slots, err);
         const int32_t q0 = a.v[0], q1 = a.v[L - 1];
         const double df = pts[static_cast<uint64_t>(q1) * m + k] - pts[static_cast<uint64_t>(q0) * m + k];
         for (int p = 1 + static_cast<int>(threadIdx.x); p < L - 1; p += blockDim.x) {
@@ -454,8 +469,8 @@ enum : int {
 __global__ void __launch_bounds__(kSortThreads) front_crowding_kernel(
     const double *__restrict__ pts, uint32_t n, uint32_t m, const long long *__restrict__ keys,
     const int32_t *__restrict__ front_offsets, const int32_t *__restrict__ front_indices,
-    const int32_t *__restrict__ n_fronts, int mode, unsigned char *wkey, int32_t *widx, int2 *wlist, double *cd,
-    peel_state *st)
+    const int32_t *__restrict__ n_fronts, int mode, unsigned char *wkey, int32_t *widx, int2 *wlist, int32_t *wpos,
+    double *cd, peel_state *st)
 {
     extern __shared__ __align__(16) unsigned char sort_smem[];
     __shared__ dev::sort_ctl ctl;
@@ -473,7 +488,8 @@ __global__ void __launch_bounds__(kSortThreads) front_crowding_kernel(
             continue;
         }
         const sort_area<long long> a =
-            pick_area<long long>(sort_smem, L, reinterpret_cast<long long *>(wkey) + off, widx + off, wlist + off);
+            pick_area<long long>(sort_smem, L, reinterpret_cast<long long *>(wkey) + off, widx + off, wlist + off,
+                                 wpos + 2 * off);
         front_crowding(pts, n, m, keys, mem, L, a, &ctl, slots, &st->sort_err, cd);
     }
 }
@@ -485,7 +501,8 @@ __global__ void __launch_bounds__(kSortThreads) front_crowding_kernel(
 __global__ void __launch_bounds__(kSortThreads) select_best_kernel(
     const double *__restrict__ pts, uint32_t n, uint32_t m, uint32_t N, const long long *__restrict__ keys,
     const int32_t *__restrict__ front_offsets, const int32_t *__restrict__ front_indices,
-    const int32_t *__restrict__ n_fronts, unsigned char *wkey, int32_t *widx, int2 *wlist, double *wcd, int32_t *out,
+    const int32_t *__restrict__ n_fronts, unsigned char *wkey, int32_t *widx, int2 *wlist, int32_t *wpos, double *wcd,
+    int32_t *out,
     peel_state *st)
 {
     extern __shared__ __align__(16) unsigned char sort_smem[];
@@ -517,14 +534,15 @@ __global__ void __launch_bounds__(kSortThreads) select_best_kernel(
     }
     const int32_t *mem = front_indices + off;
     const sort_area<long long> a =
-        pick_area<long long>(sort_smem, L, reinterpret_cast<long long *>(wkey) + off, widx + off, wlist + off);
+        pick_area<long long>(sort_smem, L, reinterpret_cast<long long *>(wkey) + off, widx + off, wlist + off,
+                                 wpos + 2 * off);
     front_crowding(pts, n, m, keys, mem, L, a, &ctl, slots, &st->sort_err, wcd);
     for (int p = threadIdx.x; p < L; p += blockDim.x) {
         a.k[p] = ~order_key(wcd[mem[p]]); // descending, NaN first: greater_than_f
         a.v[p] = p;
     }
     __syncthreads();
-    dev::block_std_sort(dev::sort_view<long long>{a.k, a.v}, L, a.lists, a.cap, &ctl, slots, &st->sort_err);
+    dev::block_std_sort(dev::sort_view<long long>{a.k, a.v}, L, a.w, &ctl, slots, &st->sort_err);
     const int remaining = static_cast<int>(N) - off;
     for (int j = threadIdx.x; j < remaining; j += blockDim.x) out[off + j] = mem[a.v[j]];
 }
@@ -533,7 +551,7 @@ __global__ void __launch_bounds__(kSortThreads) select_best_kernel(
 // 0..n-1 by (rank, descending crowding), by one block.
 __global__ void __launch_bounds__(kSortThreads) sort_population_kernel(
     const int32_t *__restrict__ rank, const double *__restrict__ crowd, uint32_t n, const int32_t *__restrict__ n_fronts,
-    unsigned char *wkey, int32_t *widx, int2 *wlist, int32_t *out, peel_state *st)
+    unsigned char *wkey, int32_t *widx, int2 *wlist, int32_t *wpos, int32_t *out, peel_state *st)
 {
     extern __shared__ __align__(16) unsigned char sort_smem[];
     __shared__ dev::sort_ctl ctl;
@@ -541,26 +559,26 @@ __global__ void __launch_bounds__(kSortThreads) sort_population_kernel(
     if (*n_fronts < 1 || st->status != 0) return;
     const int L = static_cast<int>(n);
     const sort_area<dev::key2> a =
-        pick_area<dev::key2>(sort_smem, L, reinterpret_cast<dev::key2 *>(wkey), widx, wlist);
+        pick_area<dev::key2>(sort_smem, L, reinterpret_cast<dev::key2 *>(wkey), widx, wlist, wpos);
     for (int q = threadIdx.x; q < L; q += blockDim.x) {
         a.k[q] = dev::key2{rank[q], ~order_key(crowd[q])};
         a.v[q] = q;
     }
     __syncthreads();
-    dev::block_std_sort(dev::sort_view<dev::key2>{a.k, a.v}, L, a.lists, a.cap, &ctl, slots, &st->sort_err);
+    dev::block_std_sort(dev::sort_view<dev::key2>{a.k, a.v}, L, a.w, &ctl, slots, &st->sort_err);
     for (int j = threadIdx.x; j < L; j += blockDim.x) out[j] = a.v[j];
 }
 
 // (key, value) pairs of a caller's device buffers sorted in place by one
 // block, with std::sort's order of ties.
 __global__ void __launch_bounds__(kSortThreads) sort_pairs_kernel(long long *k, int32_t *v, uint32_t n, int2 *wlist,
-                                                                  int *err)
+                                                                  int32_t *wpos, int *err)
 {
     extern __shared__ __align__(16) unsigned char sort_smem[];
     __shared__ dev::sort_ctl ctl;
     __shared__ int slots[kSortWarps * 64];
     const int L = static_cast<int>(n);
-    const sort_area<long long> a = pick_area<long long>(sort_smem, L, k, v, wlist);
+    const sort_area<long long> a = pick_area<long long>(sort_smem, L, k, v, wlist, wpos);
     const bool staged = a.k != k;
     if (staged) {
         for (int p = threadIdx.x; p < L; p += blockDim.x) {
@@ -569,7 +587,7 @@ __global__ void __launch_bounds__(kSortThreads) sort_pairs_kernel(long long *k, 
         }
     }
     __syncthreads();
-    dev::block_std_sort(dev::sort_view<long long>{a.k, a.v}, L, a.lists, a.cap, &ctl, slots, err);
+    dev::block_std_sort(dev::sort_view<long long>{a.k, a.v}, L, a.w, &ctl, slots, err);
     if (staged) {
         for (int p = threadIdx.x; p < L; p += blockDim.x) {
             k[p] = a.k[p];
@@ -776,6 +794,7 @@ struct survival_scratch {
     unsigned char *wkey; // n * 16 B sort keys of fronts too large for shared memory
     int32_t *widx;       // n sort values
     int2 *wlist;         // n sort ranges
+    int32_t *wpos;       // 2 n sort stopper positions
     double *wcd;         // n crowding distances (select_best_N_mo, sort_population_mo)
 };
 
@@ -784,7 +803,7 @@ constexpr size_t survival_scratch_bytes(uint64_t n, uint64_t m)
     return align256(n * (m > 0 ? m : 1) * sizeof(long long))
            + align256(n * ((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u) + align256(sizeof(peel_state))
            + align256(((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u) + 2u * align256(n * 4u) + align256(n * 16u)
-           + align256(n * 4u) + align256(n * sizeof(int2)) + align256(n * sizeof(double));
+           + align256(n * 4u) + align256(n * sizeof(int2)) + align256(2u * n * 4u) + align256(n * sizeof(double));
 }
 
 survival_scratch carve_survival_scratch(void *base, uint64_t n, uint64_t m)
@@ -811,6 +830,8 @@ survival_scratch carve_survival_scratch(void *base, uint64_t n, uint64_t m)
     p += align256(n * 4u);
     s.wlist = reinterpret_cast<int2 *>(p);
     p += align256(n * sizeof(int2));
+    s.wpos = reinterpret_cast<int32_t *>(p);
+    p += align256(2u * n * 4u);
     s.wcd = reinterpret_cast<double *>(p);
     return s;
 }
@@ -824,7 +845,7 @@ int launch_front_crowding(const survival_scratch &sc, const double *d_points, ui
     const int grid = static_cast<int>(std::min<uint64_t>(n, static_cast<uint64_t>(num_sms) * 2u));
     front_crowding_kernel<<<grid, kSortThreads, kSortSmemBytes, s>>>(d_points, n, m, sc.keys, front_offsets,
                                                                      front_indices, n_fronts, mode, sc.wkey, sc.widx,
-                                                                     sc.wlist, cd, sc.st);
+                                                                     sc.wlist, sc.wpos, cd, sc.st);
     PGX_CUDA(cudaGetLastError());
     return PGX_OK;
 }
@@ -1044,7 +1065,7 @@ int launch_select_best(pgx_context *ctx, const double *d_points, uint64_t n64, u
                                   static_cast<int>(kSortSmemBytes)));
     select_best_kernel<<<1, kSortThreads, kSortSmemBytes, s>>>(d_points, n, m, N, sc.keys, fb.o.front_offsets,
                                                                fb.o.front_indices, fb.o.n_fronts, sc.wkey, sc.widx,
-                                                               sc.wlist, sc.wcd, d_out, sc.st);
+                                                               sc.wlist, sc.wpos, sc.wcd, d_out, sc.st);
     PGX_CUDA(cudaGetLastError());
     ++ctx->launches;
     return finish_status(sc, d_status, s, &ctx->launches);
@@ -1069,21 +1090,21 @@ int launch_sort_population(pgx_context *ctx, const double *d_points, uint64_t n6
     PGX_CUDA(cudaFuncSetAttribute(sort_population_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(kSortSmemBytes)));
     sort_population_kernel<<<1, kSortThreads, kSortSmemBytes, s>>>(fb.o.rank, sc.wcd, n, fb.o.n_fronts, sc.wkey,
-                                                                   sc.widx, sc.wlist, d_out, sc.st);
+                                                                   sc.widx, sc.wlist, sc.wpos, d_out, sc.st);
     PGX_CUDA(cudaGetLastError());
     ctx->launches += 2;
     return finish_status(sc, d_status, s, &ctx->launches);
 }
 
 int launch_sort_pairs(pgx_context *ctx, long long *d_keys, int32_t *d_vals, uint64_t n64, int *d_err, int2 *d_lists,
-                      cudaStream_t s)
+                      int32_t *d_pos, cudaStream_t s)
 {
     if (n64 < 2) return PGX_OK;
     PGX_CHECK(n64 <= (1ull << 30), PGX_ERR_CAPACITY, "sort: more than 2^30 elements");
     PGX_CUDA(cudaFuncSetAttribute(sort_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(kSortSmemBytes)));
     sort_pairs_kernel<<<1, kSortThreads, kSortSmemBytes, s>>>(d_keys, d_vals, static_cast<uint32_t>(n64), d_lists,
-                                                              d_err);
+                                                              d_pos, d_err);
     PGX_CUDA(cudaGetLastError());
     ++ctx->launches;
     return PGX_OK;

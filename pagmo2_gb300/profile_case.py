@@ -12,6 +12,8 @@ profiler are not benchmark values). Cases:
   rosenbrock_fg / rosenbrock_f  dim 1000
   lj_fg / lj_f                  150 atoms
   survival                      NSGA-II survival of --rows nested-front points x 3
+  select_best                   select_best_N_mo(--rows nested-front points x 3, rows / 2)
+  sort_population               sort_population_mo(--rows nested-front points x 3)
   archipelago                   the fused kernel of a 64-island mixed epoch (--rows unused)
 """
 from __future__ import annotations
@@ -62,6 +64,19 @@ def main() -> None:
         def run():
             N.check(L.pgx_nsga2_survival_device(ctx.handle, dp.data_ptr(), n, 3, rank.data_ptr(), dc.data_ptr(),
                                                 off.data_ptr(), idx.data_ptr(), nf.data_ptr(), cd.data_ptr(), sp))
+    elif a.case in ("select_best", "sort_population"):
+        p = W.nsga2_points(n, 3, layers=30)
+        dp = torch.from_numpy(p).cuda()
+        sel = torch.empty(n, dtype=torch.int32, device="cuda")
+        st = torch.empty(1, dtype=torch.int32, device="cuda")
+
+        def run():
+            if a.case == "select_best":
+                N.check(L.pgx_select_best_n_mo_device(ctx.handle, dp.data_ptr(), n, 3, n // 2, sel.data_ptr(),
+                                                      st.data_ptr(), sp))
+            else:
+                N.check(L.pgx_sort_population_mo_device(ctx.handle, dp.data_ptr(), n, 3, sel.data_ptr(),
+                                                        st.data_ptr(), sp))
     else:
         name, mode = a.case.rsplit("_", 1)
         kind, param, x = {

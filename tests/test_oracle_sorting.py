@@ -2,8 +2,9 @@
 
 pagmo's crowding distance, select_best_N_mo and sort_population_mo sort with
 std::sort, whose order of tied elements is the standard library's (libstdc++
-introsort). The oracle restates that introsort twice -- sequentially and with
-the 32-wide chunked partition the GPU uses -- and both must leave exactly the
+introsort). The oracle restates that introsort three times -- sequentially and
+with the two partition formulations the GPU uses (32-wide chunks; complete
+stopper lists) -- and each must leave exactly the
 permutation std::sort leaves, on random, tie-heavy, patterned and adversarial
 inputs (McIlroy's adversary drives the introsort into its heapsort fallback).
 select_best_N_mo / sort_population_mo are pinned to the reference's known
@@ -30,7 +31,7 @@ def key_cases(orc, rng):
             yield f"adversary with ties {n}", adv // 3
 
 
-@pytest.mark.parametrize("method", ["intro", "chunked"])
+@pytest.mark.parametrize("method", ["intro", "chunked", "lists"])
 def test_restated_introsort_matches_std_sort(orc, method):
     rng = np.random.default_rng(11)
     for label, k in key_cases(orc, rng):
