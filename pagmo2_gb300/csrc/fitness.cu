@@ -7,6 +7,8 @@
 #include "fitness_dev.cuh"
 #include "pgx_internal.cuh"
 
+#include <cstdlib>
+
 namespace pgx
 {
 namespace
@@ -39,6 +41,15 @@ __global__ void __launch_bounds__(256) rosenbrock_v4_kernel(const double *__rest
     const uint64_t stride = static_cast<uint64_t>(gridDim.x) * (blockDim.x / 32u);
     for (uint64_t row = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / 32u; row < n; row += stride)
         rosenbrock_row_v4<GRAD>(x + row * nx, nx, f ? f + row : nullptr, GRAD ? g + row * nx : nullptr);
+}
+
+template <bool GRAD>
+__global__ void __launch_bounds__(256) rosenbrock_v4ff_kernel(const double *__restrict__ x, uint64_t n, uint32_t nx,
+                                                              double *__restrict__ f, double *__restrict__ g)
+{
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * (blockDim.x / 32u);
+    for (uint64_t row = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / 32u; row < n; row += stride)
+        rosenbrock_row_v4_ff<GRAD>(x + row * nx, nx, f ? f + row : nullptr, GRAD ? g + row * nx : nullptr);
 }
 
 template <int MA, bool GRAD>
@@ -167,6 +178,14 @@ int launch_lj_reg(bool grad, const double *x, uint64_t n, uint32_t na, uint32_t 
 
 } // namespace
 
+// PGX_ROSENBROCK_FP64=1 in the environment selects the all-FP64 rosenbrock
+// rows instead of the double-float ones (read at every launch).
+bool rosenbrock_fp64_only()
+{
+    const char *v = std::getenv("PGX_ROSENBROCK_FP64");
+    return v != nullptr && v[0] == '1';
+}
+
 int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64_t n, double *d_f, double *d_g,
                 cudaStream_t stream, int num_sms, uint64_t *launches)
 {
@@ -177,8 +196,12 @@ int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64
     int st = PGX_OK;
     if (kind == PGX_ROSENBROCK && nx >= 128 && nx % 4 == 0 && reinterpret_cast<uintptr_t>(d_x) % 16 == 0
         && (!grad || reinterpret_cast<uintptr_t>(d_g) % 16 == 0)) {
-        st = grad ? launch_simple(rosenbrock_v4_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
-                  : launch_simple(rosenbrock_v4_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
+        if (rosenbrock_fp64_only())
+            st = grad ? launch_simple(rosenbrock_v4_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
+                      : launch_simple(rosenbrock_v4_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
+        else
+            st = grad ? launch_simple(rosenbrock_v4ff_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
+                      : launch_simple(rosenbrock_v4ff_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
     } else if (kind == PGX_RASTRIGIN || kind == PGX_ROSENBROCK) {
         switch (lanes_per_row(nx32)) {
             case 32: st = launch_rows<32>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;

@@ -1,7 +1,8 @@
 // Device routines of the batch fitness/gradient path, shared by the
 // per-problem kernels (fitness.cu) and the fused archipelago kernel
-// (epoch.cu). Every routine evaluates whole rows with a fixed group of lanes
-// and FP64 arithmetic throughout.
+// (epoch.cu). Every routine evaluates whole rows with a fixed group of lanes,
+// in FP64 arithmetic, except rosenbrock_row_v4_ff, which reaches the same
+// accuracy in double-float arithmetic on the FP32 pipe.
 //
 // GB300's FP64 pipe retires two lanes per SM per clock, so these routines are
 // written for the fewest FP64 instructions per element; integer and shuffle
@@ -333,6 +334,275 @@ __device__ __forceinline__ void rosenbrock_row_v4(const double *__restrict__ xr,
     acc_t = group_sum<32>(acc_t, kFull);
     acc_u = group_sum<32>(acc_u, kFull);
     if (lane == 0 && f_out) *f_out = GRAD ? fma(100.0, acc_t, 0.25 * acc_u) : fma(100.0, acc_t, acc_u);
+}
+
+// ------------------------------------------------- rosenbrock on the FP32 pipe
+//
+// GB300 retires 2 FP64 lanes per SM per clock but ~115 FP32 and ~90 integer
+// lanes (and converts between float and double on the FP64 pipe too). This
+// variant evaluates rosenbrock rows in double-float arithmetic: every value is
+// an unevaluated sum hi + lo of two floats (48 significant bits), operated on
+// with error-free transformations -- Knuth's two-sum, Dekker/Møller's
+// fast-two-sum, and the FMA product error e = fma(a, b, -a*b) -- so each
+// result carries a relative error of about 2^-47 of the magnitudes it is formed
+// from. Doubles are split into (hi, lo) and rebuilt from them with integer bit
+// operations (no conversion instructions); the only FP64 instruction left per
+// element adds the two halves of the gradient component. Fitness and gradients
+// therefore stay within ~1e-14 of the first-order error bound of the
+// reference's own FP64 evaluation (the 1e-13 parity tolerance).
+//
+// Range: the split and every intermediate stay finite floats when each
+// element is 0 or 2^-60 <= |x| < 2^20 (|t| < 2^41, so a lane's sum of t^2 over
+// any row of up to 2^31 elements stays below 2^115, and 400 x t < 2^70); the
+// low parts of values below about 2^-100 may lose bits to float underflow,
+// which is far below the error bound because such rows' terms are dominated
+// by (x - 1)^2 ~ 1. A
+// warp processes a chunk of 128 elements on this path only if all of them are
+// in range; otherwise that chunk takes the FP64 path (the same arithmetic as
+// rosenbrock_row_v4), with the running t carried across in both forms.
+
+struct ff {
+    float h, l; // value h + l
+};
+
+__device__ __forceinline__ ff ff_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+__device__ __forceinline__ ff ff_fast_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+// In range for the FP32-pipe path: 0, or biased exponent in [1023-60, 1023+19].
+__device__ __forceinline__ bool ff_in_range(double x)
+{
+    const unsigned hi = static_cast<unsigned>(__double2hiint(x)), lo = static_cast<unsigned>(__double2loint(x));
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    return e - 963u <= 1042u - 963u || ((hi << 1) | lo) == 0u;
+}
+
+// x = h + l: h = x with its mantissa truncated to 24 bits, l = the other 29
+// bits rounded to a float (|x - h - l| <= 2^-48 |x|). x in range.
+__device__ __forceinline__ ff ff_split(double x)
+{
+    const unsigned hi = static_cast<unsigned>(__double2hiint(x)), lo = static_cast<unsigned>(__double2loint(x));
+    const unsigned sign = hi & 0x80000000u, e = (hi >> 20) & 0x7ffu;
+    const bool zero = e == 0u;
+    const float h = __uint_as_float(zero ? sign : sign | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+    const unsigned r = lo & 0x1fffffffu;
+    // r * 2^(e - 1075): the float of r with its exponent lowered by 1075 - e
+    const unsigned rb = __float_as_uint(__uint2float_rn(r)) - ((1075u - e) << 23);
+    const float l = __uint_as_float(r == 0u || zero ? 0u : sign | rb);
+    return {h, l};
+}
+
+// The double of a float, exactly, by bit operations (zero and subnormal
+// floats give a signed zero).
+__device__ __forceinline__ double ff_float_to_double(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned sign = b & 0x80000000u, mag = b & 0x7fffffffu;
+    if (mag < 0x00800000u) return __hiloint2double(static_cast<int>(sign), 0);
+    return __hiloint2double(static_cast<int>(sign | ((mag >> 3) + 0x38000000u)), static_cast<int>(b << 29));
+}
+
+// h + l as one double (one FP64 add).
+__device__ __forceinline__ double ff_to_double(ff v)
+{
+    return ff_float_to_double(v.h) + ff_float_to_double(v.l);
+}
+
+// t = y - x^2 (x^2 = p + pe exactly up to the dropped l(x)^2 term).
+__device__ __forceinline__ ff ff_rosen_t(ff x, ff y)
+{
+    const float p = __fmul_rn(x.h, x.h);
+    float pe = __fmaf_rn(x.h, x.h, -p);
+    pe = __fmaf_rn(__fmul_rn(2.0f, x.h), x.l, pe);
+    const ff s = ff_two_sum(y.h, -p);
+    return ff_fast_two_sum(s.h, __fadd_rn(s.l, __fsub_rn(y.l, pe)));
+}
+
+// acc += v^2 (v = h + l, non-negative terms: no renormalisation needed).
+__device__ __forceinline__ void ff_acc_square(ff &acc, ff v)
+{
+    const float q = __fmul_rn(v.h, v.h);
+    float qe = __fmaf_rn(v.h, v.h, -q);
+    qe = __fmaf_rn(__fmul_rn(2.0f, v.h), v.l, qe);
+    const ff s = ff_two_sum(acc.h, q);
+    acc.h = s.h;
+    acc.l = __fadd_rn(acc.l, __fadd_rn(s.l, qe));
+}
+
+// u = x - 1.
+__device__ __forceinline__ ff ff_minus_one(ff x)
+{
+    const ff s = ff_two_sum(x.h, -1.0f);
+    return ff_fast_two_sum(s.h, __fadd_rn(s.l, x.l));
+}
+
+// g = 200 (tp - 2 x t) + 2 u, as a double.
+__device__ __forceinline__ double ff_rosen_grad(ff x, ff t, ff tp, ff u)
+{
+    const float a = __fmul_rn(x.h, t.h);
+    float ae = __fmaf_rn(x.h, t.h, -a);
+    ae = __fmaf_rn(x.h, t.l, ae);
+    ae = __fmaf_rn(x.l, t.h, ae);
+    const ff w = ff_two_sum(tp.h, __fmul_rn(-2.0f, a));
+    const float wl = __fadd_rn(w.l, __fmaf_rn(-2.0f, ae, tp.l));
+    const float b = __fmul_rn(w.h, 200.0f);
+    float be = __fmaf_rn(w.h, 200.0f, -b);
+    be = __fmaf_rn(wl, 200.0f, be);
+    const ff g = ff_two_sum(b, __fmul_rn(2.0f, u.h));
+    return ff_to_double({g.h, __fadd_rn(g.l, __fmaf_rn(2.0f, u.l, be))});
+}
+
+__device__ __forceinline__ ff ff_group_sum32(ff v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(kFull, v.h, o), ol = __shfl_xor_sync(kFull, v.l, o);
+        const ff s = ff_two_sum(v.h, oh);
+        v = ff_fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(v.l, ol)));
+    }
+    return v;
+}
+
+// One warp per row, each lane owning 4 consecutive elements per 128-element
+// chunk, as rosenbrock_row_v4 (nx % 4 == 0, 16-byte aligned rows).
+template <bool GRAD>
+__device__ __forceinline__ void rosenbrock_row_v4_ff(const double *__restrict__ xr, uint32_t nx, double *f_out,
+                                                     double *__restrict__ gr)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t slots = nx >> 2;
+    const double2 *x2 = reinterpret_cast<const double2 *>(xr);
+    ff acc_t{0.f, 0.f}, acc_u{0.f, 0.f};  // FP32-pipe chunks: sum t^2, sum u^2
+    double dacc_t = 0.0, dacc_u = 0.0;    // FP64 chunks: sum t^2, sum (2u)^2
+    ff carry{0.f, 0.f};                    // t of the previous chunk's last element
+    double carry_d = 0.0;
+    bool carry_is_ff = true;
+    double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
+    if (lane < slots) {
+        a = __ldg(x2 + 2u * lane);
+        b = __ldg(x2 + 2u * lane + 1u);
+    }
+    for (uint32_t base = 0; base < slots; base += 32u) {
+        const uint32_t s = base + lane;
+        const bool act = s < slots;
+        const uint32_t sn = s + 32u;
+        double2 na = make_double2(0.0, 0.0), nb = make_double2(0.0, 0.0);
+        if (sn < slots) {
+            na = __ldg(x2 + 2u * sn);
+            nb = __ldg(x2 + 2u * sn + 1u);
+        }
+        const double x0 = a.x, x1 = a.y, x2v = b.x, x3 = b.y;
+        double xn = __shfl_down_sync(kFull, x0, 1);
+        const double head = __shfl_sync(kFull, na.x, 0);
+        if (lane == 31u) xn = head;
+        const bool last_has_next = s + 1u < slots;
+        const bool in = !act || (ff_in_range(x0) && ff_in_range(x1) && ff_in_range(x2v) && ff_in_range(x3)
+                                 && (!last_has_next || ff_in_range(xn)));
+        if (__all_sync(kFull, in)) {
+            if (!carry_is_ff) {
+                carry = ff_split(carry_d);
+                carry_is_ff = true;
+            }
+            const ff f0 = ff_split(x0), f1 = ff_split(x1), f2 = ff_split(x2v), f3 = ff_split(x3);
+            const ff fn = last_has_next ? ff_split(xn) : ff{0.f, 0.f};
+            const ff t0 = ff_rosen_t(f0, f1), t1 = ff_rosen_t(f1, f2), t2 = ff_rosen_t(f2, f3);
+            const ff t3 = last_has_next ? ff_rosen_t(f3, fn) : ff{0.f, 0.f};
+            ff tp;
+            tp.h = __shfl_up_sync(kFull, t3.h, 1);
+            tp.l = __shfl_up_sync(kFull, t3.l, 1);
+            if (lane == 0) tp = carry;
+            carry.h = __shfl_sync(kFull, t3.h, 31);
+            carry.l = __shfl_sync(kFull, t3.l, 31);
+            if (act) {
+                const ff u0 = ff_minus_one(f0), u1 = ff_minus_one(f1), u2 = ff_minus_one(f2);
+                ff_acc_square(acc_t, t0);
+                ff_acc_square(acc_t, t1);
+                ff_acc_square(acc_t, t2);
+                ff_acc_square(acc_u, u0);
+                ff_acc_square(acc_u, u1);
+                ff_acc_square(acc_u, u2);
+                ff u3{0.f, 0.f};
+                if (last_has_next) {
+                    u3 = ff_minus_one(f3);
+                    ff_acc_square(acc_t, t3);
+                    ff_acc_square(acc_u, u3);
+                }
+                if (GRAD) {
+                    double2 g01, g23;
+                    g01.x = ff_rosen_grad(f0, t0, tp, u0);
+                    g01.y = ff_rosen_grad(f1, t1, t0, u1);
+                    g23.x = ff_rosen_grad(f2, t2, t1, u2);
+                    if (last_has_next) {
+                        g23.y = ff_rosen_grad(f3, t3, t2, u3);
+                    } else {
+                        // g_{n-1} = 200 t_{n-2}
+                        const float bh = __fmul_rn(t2.h, 200.0f);
+                        const float bl = __fmaf_rn(t2.l, 200.0f, __fmaf_rn(t2.h, 200.0f, -bh));
+                        g23.y = ff_to_double({bh, bl});
+                    }
+                    double2 *g2 = reinterpret_cast<double2 *>(gr);
+                    g2[2u * s] = g01;
+                    g2[2u * s + 1u] = g23;
+                }
+            }
+        } else {
+            if (carry_is_ff) {
+                carry_d = ff_to_double(carry);
+                carry_is_ff = false;
+            }
+            const double t0 = fma(-x0, x0, x1);
+            const double t1 = fma(-x1, x1, x2v);
+            const double t2 = fma(-x2v, x2v, x3);
+            const double t3 = last_has_next ? fma(-x3, x3, xn) : 0.0;
+            double tp = __shfl_up_sync(kFull, t3, 1);
+            if (lane == 0) tp = carry_d;
+            carry_d = __shfl_sync(kFull, t3, 31);
+            if (act) {
+                const double c0 = (x0 + x0) - 2.0, c1 = (x1 + x1) - 2.0, c2 = (x2v + x2v) - 2.0;
+                dacc_t = fma(t0, t0, dacc_t);
+                dacc_t = fma(t1, t1, dacc_t);
+                dacc_t = fma(t2, t2, dacc_t);
+                dacc_u = fma(c0, c0, dacc_u);
+                dacc_u = fma(c1, c1, dacc_u);
+                dacc_u = fma(c2, c2, dacc_u);
+                double c3 = 0.0;
+                if (last_has_next) {
+                    c3 = (x3 + x3) - 2.0;
+                    dacc_t = fma(t3, t3, dacc_t);
+                    dacc_u = fma(c3, c3, dacc_u);
+                }
+                if (GRAD) {
+                    double2 g01, g23;
+                    g01.x = fma(200.0, fma(-(x0 + x0), t0, tp), c0);
+                    g01.y = fma(200.0, fma(-(x1 + x1), t1, t0), c1);
+                    g23.x = fma(200.0, fma(-(x2v + x2v), t2, t1), c2);
+                    g23.y = last_has_next ? fma(200.0, fma(-(x3 + x3), t3, t2), c3) : 200.0 * t2;
+                    double2 *g2 = reinterpret_cast<double2 *>(gr);
+                    g2[2u * s] = g01;
+                    g2[2u * s + 1u] = g23;
+                }
+            }
+        }
+        a = na;
+        b = nb;
+    }
+    acc_t = ff_group_sum32(acc_t);
+    acc_u = ff_group_sum32(acc_u);
+    dacc_t = group_sum<32>(dacc_t, kFull);
+    dacc_u = group_sum<32>(dacc_u, kFull);
+    if (lane == 0 && f_out) {
+        const double st = ff_to_double(acc_t) + dacc_t, su = ff_to_double(acc_u) + 0.25 * dacc_u;
+        *f_out = fma(100.0, st, su);
+    }
 }
 
 // ------------------------------------------------------------- lennard_jones

@@ -106,6 +106,9 @@ int lanes_per_row(uint32_t nx);
 // Whether lennard_jones clusters of na atoms use the flattened pair walk.
 bool lj_use_flat(uint32_t na);
 
+// True when PGX_ROSENBROCK_FP64=1: rosenbrock rows in FP64 arithmetic only.
+bool rosenbrock_fp64_only();
+
 // rastrigin/rosenbrock with a forced row variant (lanes 1..32, or 0 for the
 // 4-wide rosenbrock rows); for the autotuner.
 int launch_rows_variant(int kind, uint64_t nx, const double *d_x, uint64_t n, double *d_f, double *d_g, int lanes,

@@ -237,3 +237,57 @@ def test_gpu_bfe_rejects_unknown_problems(ctx):
 
     with pytest.raises(ValueError, match="Cannot use a gpu_bfe on the problem 'other'"):
         B.gpu_bfe()(other(), np.zeros(4))
+
+
+# ------------------------------------------- rosenbrock on the FP32 pipe (double-float)
+
+def mixed_range_rows(rng, n, nx):
+    """Rows where some 128-element chunks hold values outside the double-float
+    range (|x| >= 2^20, 0 < |x| < 2^-60), zeros, signed zeros and the optimum."""
+    x = rng.uniform(-5, 10, (n, nx))
+    x[0] = 1.0                                  # the optimum: f = 0, g = 0 exactly
+    x[1, 5] = 3.0e6                             # above 2^20: that chunk on the FP64 path
+    x[2, min(300, nx - 1)] = 1e-30              # below 2^-60
+    x[3, ::7] = 0.0
+    x[4, ::5] = -0.0
+    x[5, 126] = 2.0 ** 20                       # first value out of range
+    x[5, 127] = 2.0 ** 20 - 1.0                 # largest in range
+    x[6, nx // 2:nx // 2 + 60] = rng.uniform(-1e-12, 1e-12, 60)
+    x[7] = 1.0 + rng.integers(-3, 4, nx) * 2.0 ** -52  # one ulp from the optimum
+    x[8, -1] = 1e8                              # the last chunk alone out of range
+    x[9, 0] = -7e5                              # in range (< 2^20)
+    return x
+
+
+def test_rosenbrock_double_float_ranges(ctx, orc):
+    rng = np.random.default_rng(31)
+    for nx in (128, 1000, 1024, 4096):
+        x = mixed_range_rows(rng, 16, nx)
+        f, g = check_against_oracle(orc, ctx, N.ROSENBROCK, nx, x)
+        assert f[0] == 0.0 and np.all(g[0] == 0.0)
+
+
+def test_rosenbrock_double_float_matches_fp64_rows(ctx, orc, monkeypatch):
+    x = W.rosenbrock_batch(256, 1000, seed=33)
+    f, g = P.rosenbrock(1000, ctx).batch_gradient(x)
+    monkeypatch.setenv("PGX_ROSENBROCK_FP64", "1")
+    f64, g64 = P.rosenbrock(1000, ctx).batch_gradient(x)
+    fl, fs = orc.batch_fitness_ld(N.ROSENBROCK, 1000, x)
+    gl, gs = orc.batch_gradient_ld(N.ROSENBROCK, 1000, x)
+    for a, b in ((f, fl), (f64, fl)):
+        assert rel_err(a, b, fs) <= TOL
+    for a, b in ((g, gl), (g64, gl)):
+        assert rel_err(a, b, gs) <= TOL
+    # the all-FP64 rows are close to rounding level
+    assert rel_err(f64, fl, fs) <= 1e-15 and rel_err(g64, gl, gs) <= 1e-15
+
+
+def test_rosenbrock_double_float_nonfinite(ctx, orc):
+    x = W.rosenbrock_batch(4, 256, seed=34)
+    x[0, 10] = math.nan
+    x[1, 200] = math.inf
+    x[2, 0] = -math.inf
+    f = P.rosenbrock(256, ctx).batch_fitness(x)
+    fr = orc.batch_fitness(N.ROSENBROCK, 256, x)
+    for a, b in zip(f, fr):
+        assert (math.isnan(a) and math.isnan(b)) or a == b or abs(a - b) <= 1e-13 * abs(b), (a, b)
