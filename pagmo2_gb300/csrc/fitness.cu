@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(256) rosenbrock_v4_kernel(const double *__rest
 }
 
 template <bool GRAD>
-__global__ void __launch_bounds__(256) rosenbrock_v4ff_kernel(const double *__restrict__ x, uint64_t n, uint32_t nx,
+__global__ void __launch_bounds__(256, 4) rosenbrock_v4ff_kernel(const double *__restrict__ x, uint64_t n, uint32_t nx,
                                                               double *__restrict__ f, double *__restrict__ g)
 {
     const uint64_t stride = static_cast<uint64_t>(gridDim.x) * (blockDim.x / 32u);

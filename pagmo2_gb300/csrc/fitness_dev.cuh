@@ -378,27 +378,27 @@ __device__ __forceinline__ ff ff_fast_two_sum(float a, float b)
     return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
 
-// In range for the FP32-pipe path: 0, or biased exponent in [1023-60, 1023+19].
-__device__ __forceinline__ bool ff_in_range(double x)
-{
-    const unsigned hi = static_cast<unsigned>(__double2hiint(x)), lo = static_cast<unsigned>(__double2loint(x));
-    const unsigned e = (hi >> 20) & 0x7ffu;
-    return e - 963u <= 1042u - 963u || ((hi << 1) | lo) == 0u;
-}
-
-// x = h + l: h = x with its mantissa truncated to 24 bits, l = the other 29
-// bits rounded to a float (|x - h - l| <= 2^-48 |x|). x in range.
-__device__ __forceinline__ ff ff_split(double x)
+// x = h + l with h = x rounded to a 24-bit mantissa and l the signed rest
+// (29 bits, |l| <= 2^-24 |h|) rounded to a float: |x - h - l| <= 2^-48 |x|.
+// ok = x is 0 or in the range of the FP32-pipe path (biased exponent in
+// [1023-60, 1023+19]); h and l are meaningful only then.
+__device__ __forceinline__ ff ff_split(double x, bool &ok)
 {
     const unsigned hi = static_cast<unsigned>(__double2hiint(x)), lo = static_cast<unsigned>(__double2loint(x));
     const unsigned sign = hi & 0x80000000u, e = (hi >> 20) & 0x7ffu;
-    const bool zero = e == 0u;
-    const float h = __uint_as_float(zero ? sign : sign | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
-    const unsigned r = lo & 0x1fffffffu;
-    // r * 2^(e - 1075): the float of r with its exponent lowered by 1075 - e
-    const unsigned rb = __float_as_uint(__uint2float_rn(r)) - ((1075u - e) << 23);
-    const float l = __uint_as_float(r == 0u || zero ? 0u : sign | rb);
-    return {h, l};
+    const bool zero = ((hi << 1) | lo) == 0u;
+    ok = e - 963u <= 1042u - 963u || zero;
+    // round to nearest at bit 29 of the mantissa: add 2^28 with carry
+    const unsigned lr = lo + 0x10000000u;
+    const unsigned hr = hi + (lr < lo ? 1u : 0u);
+    // float bits: exponent e - 896 (the top exponent bits drop out of hr << 3)
+    const unsigned hb = ((hr << 3) + 0x40000000u) & 0x7fffffffu;
+    const float h = __uint_as_float(zero ? sign : sign | hb | (lr >> 29));
+    // the rest: signed 29-bit integer (lo's low bits minus the rounding) * 2^(e - 1075)
+    const int rr = static_cast<int>(lo << 3) >> 3;
+    const unsigned es = e < 963u ? 963u : e;
+    const float scale = __uint_as_float(sign | ((es - 948u) << 23));
+    return {h, __fmul_rn(__int2float_rn(rr), scale)};
 }
 
 // The double of a float, exactly, by bit operations (zero and subnormal
@@ -505,15 +505,15 @@ __device__ __forceinline__ void rosenbrock_row_v4_ff(const double *__restrict__ 
         const double head = __shfl_sync(kFull, na.x, 0);
         if (lane == 31u) xn = head;
         const bool last_has_next = s + 1u < slots;
-        const bool in = !act || (ff_in_range(x0) && ff_in_range(x1) && ff_in_range(x2v) && ff_in_range(x3)
-                                 && (!last_has_next || ff_in_range(xn)));
-        if (__all_sync(kFull, in)) {
-            if (!carry_is_ff) {
-                carry = ff_split(carry_d);
-                carry_is_ff = true;
-            }
-            const ff f0 = ff_split(x0), f1 = ff_split(x1), f2 = ff_split(x2v), f3 = ff_split(x3);
-            const ff fn = last_has_next ? ff_split(xn) : ff{0.f, 0.f};
+        bool k0, k1, k2, k3, kn;
+        const ff f0 = ff_split(x0, k0), f1 = ff_split(x1, k1), f2 = ff_split(x2v, k2), f3 = ff_split(x3, k3);
+        const ff fn = ff_split(last_has_next ? xn : 0.0, kn);
+        // the t carried in from an FP64 chunk must itself be in range
+        bool kc = true;
+        const ff carry_in = carry_is_ff ? carry : ff_split(carry_d, kc);
+        if (__all_sync(kFull, (!act || (k0 && k1 && k2 && k3 && kn)) && kc)) {
+            carry = carry_in;
+            carry_is_ff = true;
             const ff t0 = ff_rosen_t(f0, f1), t1 = ff_rosen_t(f1, f2), t2 = ff_rosen_t(f2, f3);
             const ff t3 = last_has_next ? ff_rosen_t(f3, fn) : ff{0.f, 0.f};
             ff tp;

@@ -256,6 +256,8 @@ def mixed_range_rows(rng, n, nx):
     x[7] = 1.0 + rng.integers(-3, 4, nx) * 2.0 ** -52  # one ulp from the optimum
     x[8, -1] = 1e8                              # the last chunk alone out of range
     x[9, 0] = -7e5                              # in range (< 2^20)
+    x[10, 127] = 1e60                           # chunk boundary: the carried t (~1e120) is out of range
+    x[11, 127] = -3e7                           # chunk boundary, moderately out of range
     return x
 
 
