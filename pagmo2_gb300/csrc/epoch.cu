@@ -88,7 +88,7 @@ __device__ __forceinline__ void run_tile(const tile_desc &d, double *sm)
                 rosenbrock_row_v4<GRAD>(d.x + static_cast<uint64_t>(r) * d.nx, d.nx, d.f + r,
                                         GRAD ? d.g + static_cast<uint64_t>(r) * d.nx : nullptr);
             break;
-        case kRows4FF: // double-float rows on the FP32 pipe
+        case kRows4FF: // double-float rows on the FP32 pipe (opt-in)
             for (uint32_t r = 0; r < d.rows; ++r)
                 rosenbrock_row_v4_ff<GRAD>(d.x + static_cast<uint64_t>(r) * d.nx, d.nx, d.f + r,
                                            GRAD ? d.g + static_cast<uint64_t>(r) * d.nx : nullptr);
@@ -224,7 +224,7 @@ int tune(pgx_context *ctx, int kind, uint64_t param, uint64_t nx, bool grad, tun
     PGX_CUDA(cudaGetDeviceProperties(&prop, ctx->device));
     std::ostringstream ks;
     ks << kind << ':' << param << ':' << nx << ':' << (grad ? 1 : 0) << ':' << prop.multiProcessorCount << ':'
-       << prop.major << prop.minor << (kind == PGX_ROSENBROCK && !rosenbrock_fp64_only() ? ":ff" : "");
+       << prop.major << prop.minor << (kind == PGX_ROSENBROCK && rosenbrock_double_float() ? ":ff" : "");
     const std::string key = ks.str();
     {
         std::lock_guard<std::mutex> g(g_tune_lock);
@@ -501,7 +501,7 @@ int build_plan(pgx_epoch *ep, const pgx_request *reqs, int n_reqs)
                 d.ma = 1;
                 d.lanes = 32;
             } else if (p.tune.lanes == 0) {
-                d.variant = rosenbrock_fp64_only() ? kRows4 : kRows4FF;
+                d.variant = rosenbrock_double_float() ? kRows4FF : kRows4;
                 d.lanes = 32;
             } else {
                 d.variant = kRows;

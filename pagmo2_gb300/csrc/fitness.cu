@@ -178,11 +178,13 @@ int launch_lj_reg(bool grad, const double *x, uint64_t n, uint32_t na, uint32_t 
 
 } // namespace
 
-// PGX_ROSENBROCK_FP64=1 in the environment selects the all-FP64 rosenbrock
-// rows instead of the double-float ones (read at every launch).
-bool rosenbrock_fp64_only()
+// Rosenbrock rows are evaluated in FP64 arithmetic. PGX_ROSENBROCK_DOUBLE_FLOAT=1
+// in the environment (read at every launch) opts in to the double-float rows
+// (about 2x faster on GB300, error within 2e-14 of the FP64 error bound, not
+// FP64 arithmetic).
+bool rosenbrock_double_float()
 {
-    const char *v = std::getenv("PGX_ROSENBROCK_FP64");
+    const char *v = std::getenv("PGX_ROSENBROCK_DOUBLE_FLOAT");
     return v != nullptr && v[0] == '1';
 }
 
@@ -196,7 +198,7 @@ int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64
     int st = PGX_OK;
     if (kind == PGX_ROSENBROCK && nx >= 128 && nx % 4 == 0 && reinterpret_cast<uintptr_t>(d_x) % 16 == 0
         && (!grad || reinterpret_cast<uintptr_t>(d_g) % 16 == 0)) {
-        if (rosenbrock_fp64_only())
+        if (!rosenbrock_double_float())
             st = grad ? launch_simple(rosenbrock_v4_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
                       : launch_simple(rosenbrock_v4_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
         else
@@ -255,7 +257,7 @@ int launch_rows_variant(int kind, uint64_t nx, const double *d_x, uint64_t n, do
     if (lanes == 0) {
         PGX_CHECK(kind == PGX_ROSENBROCK && nx % 4 == 0 && reinterpret_cast<uintptr_t>(d_x) % 16 == 0,
                   PGX_ERR_INVALID, "4-wide rows need rosenbrock, nx % 4 == 0 and aligned rows");
-        if (rosenbrock_fp64_only())
+        if (!rosenbrock_double_float())
             return grad ? launch_simple(rosenbrock_v4_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
                         : launch_simple(rosenbrock_v4_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
         return grad ? launch_simple(rosenbrock_v4ff_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)

@@ -106,8 +106,9 @@ int lanes_per_row(uint32_t nx);
 // Whether lennard_jones clusters of na atoms use the flattened pair walk.
 bool lj_use_flat(uint32_t na);
 
-// True when PGX_ROSENBROCK_FP64=1: rosenbrock rows in FP64 arithmetic only.
-bool rosenbrock_fp64_only();
+// True when PGX_ROSENBROCK_DOUBLE_FLOAT=1: rosenbrock rows in double-float
+// arithmetic on the FP32 pipe (an opt-in; the default is FP64 arithmetic).
+bool rosenbrock_double_float();
 
 // rastrigin/rosenbrock with a forced row variant (lanes 1..32, or 0 for the
 // 4-wide rosenbrock rows); for the autotuner.

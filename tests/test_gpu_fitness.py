@@ -239,7 +239,7 @@ def test_gpu_bfe_rejects_unknown_problems(ctx):
         B.gpu_bfe()(other(), np.zeros(4))
 
 
-# ------------------------------------------- rosenbrock on the FP32 pipe (double-float)
+# ------------------------------ opt-in: rosenbrock on the FP32 pipe (double-float)
 
 def mixed_range_rows(rng, n, nx):
     """Rows where some 128-element chunks hold values outside the double-float
@@ -261,7 +261,13 @@ def mixed_range_rows(rng, n, nx):
     return x
 
 
-def test_rosenbrock_double_float_ranges(ctx, orc):
+@pytest.fixture
+def double_float(monkeypatch):
+    """Opt in to the double-float rosenbrock rows for one test."""
+    monkeypatch.setenv("PGX_ROSENBROCK_DOUBLE_FLOAT", "1")
+
+
+def test_rosenbrock_double_float_ranges(ctx, orc, double_float):
     rng = np.random.default_rng(31)
     for nx in (128, 1000, 1024, 4096):
         x = mixed_range_rows(rng, 16, nx)
@@ -271,9 +277,9 @@ def test_rosenbrock_double_float_ranges(ctx, orc):
 
 def test_rosenbrock_double_float_matches_fp64_rows(ctx, orc, monkeypatch):
     x = W.rosenbrock_batch(256, 1000, seed=33)
+    f64, g64 = P.rosenbrock(1000, ctx).batch_gradient(x)  # default: FP64 arithmetic
+    monkeypatch.setenv("PGX_ROSENBROCK_DOUBLE_FLOAT", "1")
     f, g = P.rosenbrock(1000, ctx).batch_gradient(x)
-    monkeypatch.setenv("PGX_ROSENBROCK_FP64", "1")
-    f64, g64 = P.rosenbrock(1000, ctx).batch_gradient(x)
     fl, fs = orc.batch_fitness_ld(N.ROSENBROCK, 1000, x)
     gl, gs = orc.batch_gradient_ld(N.ROSENBROCK, 1000, x)
     for a, b in ((f, fl), (f64, fl)):
@@ -284,7 +290,7 @@ def test_rosenbrock_double_float_matches_fp64_rows(ctx, orc, monkeypatch):
     assert rel_err(f64, fl, fs) <= 1e-15 and rel_err(g64, gl, gs) <= 1e-15
 
 
-def test_rosenbrock_double_float_nonfinite(ctx, orc):
+def test_rosenbrock_double_float_nonfinite(ctx, orc, double_float):
     x = W.rosenbrock_batch(4, 256, seed=34)
     x[0, 10] = math.nan
     x[1, 200] = math.inf
