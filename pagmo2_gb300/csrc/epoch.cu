@@ -14,8 +14,11 @@
 #include "pgx_internal.cuh"
 
 #include <dlfcn.h>
+#include <unistd.h>
 
 #include <algorithm>
+#include <condition_variable>
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -299,32 +302,103 @@ struct copy_item {
     size_t bytes;
 };
 
+// Process-wide pool of copy threads, created on first use and kept (its
+// workers are detached and sleep on a condition variable between jobs, so a
+// copy does not pay for thread creation). One job runs at a time; the calling
+// thread works on it too. Pieces are taken from an atomic counter.
+class copy_pool {
+public:
+    static copy_pool &get()
+    {
+        // never destroyed (workers may outlive static destructors); a forked
+        // child, which inherits no worker threads, builds its own
+        static std::mutex lock;
+        static copy_pool *p = nullptr;
+        static pid_t owner = 0;
+        std::lock_guard<std::mutex> g(lock);
+        if (p == nullptr || owner != getpid()) {
+            p = new copy_pool();
+            owner = getpid();
+        }
+        return *p;
+    }
+
+    void run(const std::vector<copy_item> &pieces)
+    {
+        std::lock_guard<std::mutex> job(job_lock_);
+        {
+            std::lock_guard<std::mutex> g(m_);
+            pieces_ = &pieces;
+            next_.store(0);
+            pending_ = workers_;
+            ++generation_;
+        }
+        cv_.notify_all();
+        work(pieces);
+        std::unique_lock<std::mutex> g(m_);
+        done_cv_.wait(g, [this] { return pending_ == 0; });
+        pieces_ = nullptr;
+    }
+
+private:
+    copy_pool()
+    {
+        const unsigned hw = std::thread::hardware_concurrency();
+        workers_ = std::min(15u, hw > 1 ? hw - 1 : 0u);
+        for (unsigned t = 0; t < workers_; ++t) std::thread([this] { loop(); }).detach();
+    }
+
+    void work(const std::vector<copy_item> &pieces)
+    {
+        for (size_t i = next_.fetch_add(1); i < pieces.size(); i = next_.fetch_add(1))
+            std::memcpy(pieces[i].dst, pieces[i].src, pieces[i].bytes);
+    }
+
+    void loop()
+    {
+        uint64_t seen = 0;
+        for (;;) {
+            const std::vector<copy_item> *job;
+            {
+                std::unique_lock<std::mutex> g(m_);
+                cv_.wait(g, [&] { return generation_ != seen; });
+                seen = generation_;
+                job = pieces_;
+            }
+            if (job) work(*job);
+            std::lock_guard<std::mutex> g(m_);
+            if (--pending_ == 0) done_cv_.notify_one();
+        }
+    }
+
+    std::mutex job_lock_, m_;
+    std::condition_variable cv_, done_cv_;
+    const std::vector<copy_item> *pieces_ = nullptr;
+    std::atomic<size_t> next_{0};
+    unsigned workers_ = 0, pending_ = 0;
+    uint64_t generation_ = 0;
+};
+
 void parallel_copy(const std::vector<copy_item> &items)
 {
     size_t total = 0;
     for (const auto &c : items) total += c.bytes;
-    unsigned hw = std::thread::hardware_concurrency();
-    const unsigned nt = total < (size_t(8) << 20) ? 1u : std::min(16u, hw ? hw : 1u);
-    if (nt <= 1) {
+    if (total < (size_t(4) << 20)) {
         for (const auto &c : items)
             if (c.bytes) std::memcpy(c.dst, c.src, c.bytes);
         return;
     }
-    // cut into pieces of at most 2 MiB so the threads stay balanced
+    // pieces of at most 512 KiB, taken dynamically, keep the threads balanced
+    constexpr size_t kPiece = size_t(512) << 10;
     std::vector<copy_item> pieces;
+    pieces.reserve(total / kPiece + items.size());
     for (const auto &c : items) {
-        for (size_t off = 0; off < c.bytes; off += (size_t(2) << 20)) {
-            const size_t b = std::min(c.bytes - off, size_t(2) << 20);
+        for (size_t off = 0; off < c.bytes; off += kPiece) {
+            const size_t b = std::min(c.bytes - off, kPiece);
             pieces.push_back({static_cast<char *>(c.dst) + off, static_cast<const char *>(c.src) + off, b});
         }
     }
-    std::vector<std::thread> pool;
-    for (unsigned t = 0; t < nt; ++t) {
-        pool.emplace_back([&pieces, t, nt]() {
-            for (size_t i = t; i < pieces.size(); i += nt) std::memcpy(pieces[i].dst, pieces[i].src, pieces[i].bytes);
-        });
-    }
-    for (auto &th : pool) th.join();
+    copy_pool::get().run(pieces);
 }
 
 struct req_plan {
