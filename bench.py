@@ -126,6 +126,21 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ helpers
 
+def replicas_value(ms_local: float, rows_per_rank: int, ws: int, dist=None, device: str = "cpu"):
+    """Whole-job throughput of N independent replicas (weak scaling): every
+    rank evaluates its own batch, the step time is the slowest rank's (an
+    all-reduce MAX, the only collective, outside the timed region) and the
+    value is all ranks' rows over it. Returns (ms, rows/s)."""
+    ms = ms_local
+    if dist is not None and ws > 1:
+        import torch
+
+        t = torch.tensor([ms_local], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, ws * rows_per_rank / (ms * 1e-3)
+
+
 def measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -283,11 +298,7 @@ def main():
     ms = e0.elapsed_time(e1) / args.steps
     gpu_launches = ctx.launches - launches0
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * rows_n / (ms * 1e-3)
+    ms, value = replicas_value(ms, rows_n, ws, dist, device="cuda")
 
     # ---- FP64 / HBM roofline of the rosenbrock kernel
     fp = C.c_double()
