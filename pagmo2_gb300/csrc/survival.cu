@@ -72,6 +72,80 @@ __device__ __forceinline__ bool dom_fixed(const long long (&a)[M], const long lo
     return le && lt;
 }
 
+// Symmetric tiles for 1 <= m <= 4: one warp compares a block of 32 points i
+// (its lanes) with a block of 32 points j (staged in shared memory) for
+// I-block <= J-block only. Per objective two compares, a_i < a_j and
+// a_i > a_j, give both directions: i dominates j iff no ">" and some "<",
+// j dominates i iff no "<" and some ">". The i-dominates-j bits of the 32 rows
+// j come from ballots (one word per row, coalesced through shared memory);
+// the j-dominates-i bits of each lane's row i collect in a register word.
+// A diagonal tile writes its rows once. dom_count comes from a popcount pass.
+template <int M>
+__global__ void __launch_bounds__(256) dominance_sym_kernel(const long long *__restrict__ keys, uint32_t n,
+                                                            uint32_t W8, uint32_t *__restrict__ Dt)
+{
+    __shared__ long long jk[M][32];
+    __shared__ uint32_t tile[32][9];
+    const uint32_t bj = blockIdx.y;              // J-block
+    const uint32_t bi0 = blockIdx.x * 8u;        // first I-block of this CTA
+    if (bi0 > bj) return;                        // whole CTA above the diagonal
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t J0 = bj * 32u;
+    for (unsigned t = threadIdx.x; t < static_cast<unsigned>(M) * 32u; t += blockDim.x) {
+        const unsigned k = t >> 5, jj = t & 31u;
+        const uint32_t j = J0 + jj;
+        jk[k][jj] = j < n ? keys[static_cast<uint64_t>(k) * n + j] : 0;
+    }
+    __syncthreads();
+    const uint32_t bi = bi0 + warp;
+    const bool active = bi <= bj;                // warp-uniform
+    const uint32_t i = bi * 32u + lane;
+    const bool iv = active && i < n;
+    long long ik[M];
+#pragma unroll
+    for (int k = 0; k < M; ++k) ik[k] = iv ? keys[static_cast<uint64_t>(k) * n + i] : 0;
+    uint32_t row_i = 0u; // bit jj: j = J0 + jj dominates i
+    if (active) {
+        for (unsigned jj = 0; jj < 32u; ++jj) {
+            bool any_lt = false, any_gt = false;
+#pragma unroll
+            for (int k = 0; k < M; ++k) {
+                const long long b = jk[k][jj];
+                any_lt |= ik[k] < b;
+                any_gt |= ik[k] > b;
+            }
+            const bool valid = iv && J0 + jj < n;
+            const bool i_dom_j = valid && any_lt && !any_gt;
+            const bool j_dom_i = valid && any_gt && !any_lt;
+            const unsigned word = __ballot_sync(kFull, i_dom_j);
+            if (lane == 0) tile[jj][warp] = word;
+            row_i |= static_cast<uint32_t>(j_dom_i) << jj;
+        }
+        // the rows i of an off-diagonal tile: word J-block of row i
+        if (bi != bj && i < n) Dt[static_cast<uint64_t>(i) * W8 + bj] = row_i;
+    }
+    __syncthreads();
+    // the rows j: words bi0 .. bi0+7 of rows J0 .. J0+31 (blocks at or below the diagonal)
+    const unsigned jj = threadIdx.x >> 3, ww = threadIdx.x & 7u;
+    const uint32_t j = J0 + jj;
+    if (j < n && bi0 + ww <= bj) Dt[static_cast<uint64_t>(j) * W8 + bi0 + ww] = tile[jj][ww];
+}
+
+// dom_count[j] = popcount of row j of Dt (one warp per row).
+__global__ void row_popcount_kernel(const uint32_t *__restrict__ Dt, uint32_t n, uint32_t W8,
+                                    int32_t *__restrict__ dom_count)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warps = static_cast<uint64_t>(gridDim.x) * (blockDim.x >> 5);
+    for (uint64_t r = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        int c = 0;
+        for (uint32_t w = lane; w < W8; w += 32u) c += __popc(Dt[r * W8 + w]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+        if (lane == 0) dom_count[r] = c;
+    }
+}
+
 // CTA tile: 32 dominated candidates j (rows of Dt) x 256 dominators i (8 words).
 // Warp w tests i = 32*(w0+w) + lane against each j and ballots the row word.
 // M > 0: objectives in registers; M == 0: runtime m, keys read from global.
@@ -735,14 +809,26 @@ int blocks_for(uint64_t work, int threads, int num_sms)
 int launch_dominance(const long long *keys, uint32_t n, uint32_t m, uint32_t W, uint32_t W8, uint32_t *Dt,
                      int32_t *dom_count, cudaStream_t s)
 {
-    dim3 grid((W8 + 7u) / 8u, (n + 31u) / 32u);
-    switch (m) {
-        case 1: dominance_kernel<1><<<grid, 256, 0, s>>>(keys, n, m, W, W8, Dt, dom_count); break;
-        case 2: dominance_kernel<2><<<grid, 256, 0, s>>>(keys, n, m, W, W8, Dt, dom_count); break;
-        case 3: dominance_kernel<3><<<grid, 256, 0, s>>>(keys, n, m, W, W8, Dt, dom_count); break;
-        case 4: dominance_kernel<4><<<grid, 256, 0, s>>>(keys, n, m, W, W8, Dt, dom_count); break;
-        default: dominance_kernel<0><<<grid, 256, 0, s>>>(keys, n, m, W, W8, Dt, dom_count); break;
+    if (m >= 1u && m <= 4u) {
+        // symmetric tiles cover words 0 .. W-1 of every row; zero the padding words W .. W8-1
+        if (W8 > W)
+            PGX_CUDA(cudaMemset2DAsync(Dt + W, static_cast<size_t>(W8) * 4u, 0, static_cast<size_t>(W8 - W) * 4u, n,
+                                       s));
+        dim3 grid((W + 7u) / 8u, W);
+        switch (m) {
+            case 1: dominance_sym_kernel<1><<<grid, 256, 0, s>>>(keys, n, W8, Dt); break;
+            case 2: dominance_sym_kernel<2><<<grid, 256, 0, s>>>(keys, n, W8, Dt); break;
+            case 3: dominance_sym_kernel<3><<<grid, 256, 0, s>>>(keys, n, W8, Dt); break;
+            default: dominance_sym_kernel<4><<<grid, 256, 0, s>>>(keys, n, W8, Dt); break;
+        }
+        PGX_CUDA(cudaGetLastError());
+        const int blocks = static_cast<int>(std::min<uint64_t>((static_cast<uint64_t>(n) + 7u) / 8u, 65535u));
+        row_popcount_kernel<<<blocks, 256, 0, s>>>(Dt, n, W8, dom_count);
+        PGX_CUDA(cudaGetLastError());
+        return PGX_OK;
     }
+    dim3 grid((W8 + 7u) / 8u, (n + 31u) / 32u);
+    dominance_kernel<0><<<grid, 256, 0, s>>>(keys, n, m, W, W8, Dt, dom_count);
     PGX_CUDA(cudaGetLastError());
     return PGX_OK;
 }
@@ -870,7 +956,7 @@ int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n,
                                                                                                  sc.keys);
         PGX_CUDA(cudaGetLastError());
         PGX_TRY(launch_dominance(sc.keys, n, m, W, W8, sc.Dt, out.dom_count, s));
-        *launches += 2;
+        *launches += m <= 4u ? 3 : 2; // keys, dominance tiles (+ row popcounts)
     } else {
         PGX_CUDA(cudaMemsetAsync(sc.Dt, 0, static_cast<size_t>(n) * W8 * sizeof(uint32_t), s));
     }
