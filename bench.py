@@ -386,7 +386,8 @@ def main():
 
     secondary = {}
     if rank == 0 and not args.no_secondary:
-        secondary = run_secondary(ctx, L, N, W, stream, fp64_peak_tflops)
+        secondary = run_secondary(ctx, L, N, W, stream, fp64_peak_tflops,
+                                  cpu_ok=rank == 0 and ws == 1 and not args.no_cpu)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -396,6 +397,19 @@ def main():
         dt = time_cpu(step)
         cpu = {"value": sample / dt, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": f"{sample} of the {N_ROWS} rows, fitness (thread_bfe) + gradient, median of repeats"}
+        # the per-call path: problem::fitness row by row on one thread
+        import oracle
+
+        ref = oracle.reference()
+        xs = x[:1024]
+        serial = (lambda: ref.fitness_rows(N.ROSENBROCK, DIM, xs)) if ref is not None else \
+            (lambda: oracle.oracle().batch_fitness(N.ROSENBROCK, DIM, xs, 1))
+        serial()
+        t = time.perf_counter()
+        serial()
+        cpu["serial_problem_fitness"] = {"evals_per_s": xs.shape[0] / (time.perf_counter() - t), "threads": 1,
+                                         "kind": "reference" if ref is not None else "port",
+                                         "sample": "1024 rows, fitness only, one problem::fitness call per row"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -415,7 +429,7 @@ def main():
         dist.destroy_process_group()
 
 
-def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops) -> dict:
+def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops, cpu_ok=True) -> dict:
     """The other kernels of the path, device resident, CUDA-event timed."""
     import torch
 
@@ -479,6 +493,35 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops) -> dict:
     ms = timed(surv, reps=10, flush_l2=False)
     out["nsga2_survival_20000x3"] = {"ms": ms, "fronts": int(nf.item()),
                                      "pair_tests_per_s": n * n / (ms * 1e-3)}
+    # end to end through the host-buffer entry point (points up, fronts and crowding down)
+    from pagmo2_gb300 import multi_objective as MO
+
+    MO.nsga2_survival(p, ctx)
+    t = time.perf_counter()
+    for _ in range(5):
+        MO.nsga2_survival(p, ctx)
+    out["nsga2_survival_20000x3"]["e2e_ms"] = (time.perf_counter() - t) / 5 * 1e3
+    # the reference's fast_non_dominated_sorting is single-threaded and O(n^2 m):
+    # timed on a 2000-point sample of the same construction, beside the GPU
+    if cpu_ok:
+        import oracle
+
+        ps = W.nsga2_points(2000, 3, layers=30)
+        ref = oracle.reference()
+        fn = (lambda: ref.fnds(ps)) if ref is not None else (lambda: oracle.oracle().fnds(ps, dom_list=True))
+        fn()
+        t = time.perf_counter()
+        for _ in range(3):
+            fn()
+        cpu_ms = (time.perf_counter() - t) / 3 * 1e3
+        MO.nsga2_survival(ps, ctx)
+        t = time.perf_counter()
+        for _ in range(10):
+            MO.fnds_arrays(ps, ctx)
+        out["fnds_2000x3_vs_cpu"] = {"cpu_ms": cpu_ms, "cpu_kind": "reference" if ref is not None else "port",
+                                     "cpu_threads": 1, "gpu_e2e_ms": (time.perf_counter() - t) / 10 * 1e3,
+                                     "note": "fast_non_dominated_sorting incl. dom_list on the CPU; the GPU call "
+                                             "returns ranks, counts and fronts from host buffers"}
 
     # NSGA-II's selection of the next population from the merged 2 NP points
     # (nsga2.cpp:300: select_best_N_mo(merged, NP)) and sort_population_mo
