@@ -8,9 +8,9 @@ Inputs are seeded synthetic batches resident on the device; --warmup launches
 are followed by --launches timed ones (CUDA events; numbers printed under a
 profiler are not benchmark values). Cases:
 
-  rastrigin_fg / rastrigin_f    dim 50
-  rosenbrock_fg / rosenbrock_f  dim 1000
-  lj_fg / lj_f                  150 atoms
+  rastrigin_fg / rastrigin_f    dim 50 (--dim)
+  rosenbrock_fg / rosenbrock_f  dim 1000 (--dim)
+  lj_fg / lj_f                  150 atoms (--atoms)
   survival                      NSGA-II survival of --rows nested-front points x 3
   select_best                   select_best_N_mo(--rows nested-front points x 3, rows / 2)
   sort_population               sort_population_mo(--rows nested-front points x 3)
@@ -33,6 +33,8 @@ def main() -> None:
     ap.add_argument("--rows", type=int, default=16384)
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--launches", type=int, default=3)
+    ap.add_argument("--atoms", type=int, default=150, help="lennard_jones cluster size (lj_* cases)")
+    ap.add_argument("--dim", type=int, default=0, help="rastrigin/rosenbrock dimension (default 50 / 1000)")
     a = ap.parse_args()
 
     import torch
@@ -80,9 +82,9 @@ def main() -> None:
     else:
         name, mode = a.case.rsplit("_", 1)
         kind, param, x = {
-            "rastrigin": (N.RASTRIGIN, 50, lambda: W.rastrigin_batch(n, 50)),
-            "rosenbrock": (N.ROSENBROCK, 1000, lambda: W.rosenbrock_batch(n, 1000)),
-            "lj": (N.LENNARD_JONES, 150, lambda: W.lj_batch(n, 150)),
+            "rastrigin": (N.RASTRIGIN, a.dim or 50, lambda: W.rastrigin_batch(n, a.dim or 50)),
+            "rosenbrock": (N.ROSENBROCK, a.dim or 1000, lambda: W.rosenbrock_batch(n, a.dim or 1000)),
+            "lj": (N.LENNARD_JONES, a.atoms, lambda: W.lj_batch(n, a.atoms)),
         }[name]
         x = x()
         dx = torch.from_numpy(x).cuda()
