@@ -236,7 +236,9 @@ def run_reference(args):
             "config": {"workload": f"rosenbrock fitness+gradient, {N_ROWS} x {DIM}, FP64", "batch": N_ROWS,
                        "dim": DIM, "parallelism": "host threads"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
-                             "sample": f"first {sample} of the {N_ROWS} rows x {DIM} per step, fitness (bfe{{thread_bfe}}) + problem::gradient on {threads} threads"},
+                             "sample": f"first {sample} of the {N_ROWS} rows x {DIM} per step, fitness (bfe{{thread_bfe}}) + problem::gradient on {threads} threads; "
+                                       + ("reference compiled with a std::thread stand-in for TBB's parallel_for"
+                                          if kind == "reference" else "the oracle's restatement on std::threads")},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -396,7 +398,10 @@ def main():
         step, kind = cpu_reference_step_fn(N.ROSENBROCK, DIM, x[:sample], True, threads)
         dt = time_cpu(step)
         cpu = {"value": sample / dt, "unit": UNIT, "cores": threads, "kind": kind,
-               "sample": f"{sample} of the {N_ROWS} rows, fitness (thread_bfe) + gradient, median of repeats"}
+               "sample": f"{sample} of the {N_ROWS} rows, fitness (bfe{{thread_bfe}}) + problem::gradient, median of "
+                         f"repeats after a warm-up; "
+                         + ("reference compiled with a std::thread stand-in for TBB's parallel_for"
+                            if kind == "reference" else "the oracle's restatement on std::threads")}
         # the per-call path: problem::fitness row by row on one thread
         import oracle
 

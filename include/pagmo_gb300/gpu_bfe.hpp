@@ -15,6 +15,7 @@
 #include <stdexcept>
 #include <string>
 
+#include <pagmo/bfe.hpp>
 #include <pagmo/problem.hpp>
 #include <pagmo/problems/lennard_jones.hpp>
 #include <pagmo/problems/rastrigin.hpp>
@@ -85,5 +86,9 @@ private:
 };
 
 } // namespace pagmo_gb300
+
+// Registration with pagmo's Boost.Serialization machinery (include/pagmo/bfe.hpp:54-62):
+// the key here, the implementation in one translation unit (pagmo_gb300/s11n_implement.hpp).
+PAGMO_S11N_BFE_EXPORT_KEY(pagmo_gb300::gpu_bfe)
 
 #endif

@@ -16,6 +16,7 @@
 #include <utility>
 #include <vector>
 
+#include <pagmo/problem.hpp>
 #include <pagmo/threading.hpp>
 #include <pagmo/types.hpp>
 
@@ -155,5 +156,11 @@ public:
 };
 
 } // namespace pagmo_gb300
+
+// Registration with pagmo's Boost.Serialization machinery (include/pagmo/problem.hpp:67-76):
+// the keys here, the implementations in one translation unit (pagmo_gb300/s11n_implement.hpp).
+PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_rastrigin)
+PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_rosenbrock)
+PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_lennard_jones)
 
 #endif

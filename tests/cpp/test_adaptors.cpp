@@ -22,6 +22,7 @@
 #include <pagmo_gb300/gpu_bfe.hpp>
 #include <pagmo_gb300/gpu_problems.hpp>
 #include <pagmo_gb300/multi_objective.hpp>
+#include <pagmo_gb300/s11n_implement.hpp>
 
 using namespace pagmo_gb300;
 

@@ -154,6 +154,32 @@ def estimate_gradient_h(fun, x, dx=1e-2):
     return g
 
 
+def estimate_gradient(fun, x, dx=1e-8):
+    """Central differences (include/pagmo/utils/gradients_and_hessians.hpp:131-155)."""
+    g = np.empty_like(x)
+    for j in range(x.size):
+        h = max(abs(x[j]), 1.0) * dx
+        y1 = x.copy()
+        y2 = x.copy()
+        y1[j] += h
+        y2[j] -= h
+        g[j] = (fun(y1) - fun(y2)) / (2.0 * h)
+    return g
+
+
+def test_gradients_against_central_differences(ctx, orc):
+    # dx = 1e-8: the rounding error of f(x +- h) is ~eps |f| / h, so this is a loose sanity bound
+    for kind, param, x in ((N.RASTRIGIN, 6, W.uniform_batch(1, 6, 1, 5)[0]),
+                           (N.ROSENBROCK, 6, W.uniform_batch(2, 6, 1, 6)[0]),
+                           (N.LENNARD_JONES, 8, W.lj_lattice_batch(1, 8, seed=7)[0])):
+        udp = P.from_kind(kind, param, ctx)
+        g = udp.gradient(x)
+        fd = estimate_gradient(lambda y: orc.batch_fitness_ld(kind, param, y[None, :])[0][0], x)
+        f0 = abs(orc.batch_fitness_ld(kind, param, x[None, :])[0][0])
+        tol = 1e-5 * max(1.0, np.max(np.abs(g))) + 1e-16 * f0 / 1e-8
+        assert np.max(np.abs(g - fd)) <= tol, (kind, np.max(np.abs(g - fd)), tol)
+
+
 def test_gradients_against_finite_differences(ctx, orc):
     for kind, param, x, dx, tol in ((N.RASTRIGIN, 6, W.uniform_batch(1, 6, 1, 5)[0], 1e-3, 1e-6),
                                     (N.ROSENBROCK, 6, W.uniform_batch(2, 6, 1, 6)[0], 1e-3, 1e-6),
