@@ -1,6 +1,6 @@
 // gpu_bfe: a user-defined batch fitness evaluator (UDBFE) for pagmo::bfe
-// that evaluates pagmo's own rastrigin, rosenbrock and lennard_jones UDPs,
-// and the GPU UDPs of gpu_problems.hpp, on a GB300.
+// that evaluates pagmo's own rastrigin, rosenbrock, lennard_jones, ackley,
+// griewank and schwefel UDPs, and the GPU UDPs of gpu_problems.hpp, on a GB300.
 //
 // A UDBFE is a callable vector_double(const problem &, const vector_double &)
 // (include/pagmo/bfe.hpp:68-108). Like every UDBFE it leaves the fevals
@@ -17,9 +17,12 @@
 
 #include <pagmo/bfe.hpp>
 #include <pagmo/problem.hpp>
+#include <pagmo/problems/ackley.hpp>
+#include <pagmo/problems/griewank.hpp>
 #include <pagmo/problems/lennard_jones.hpp>
 #include <pagmo/problems/rastrigin.hpp>
 #include <pagmo/problems/rosenbrock.hpp>
+#include <pagmo/problems/schwefel.hpp>
 #include <pagmo/threading.hpp>
 #include <pagmo/types.hpp>
 
@@ -39,6 +42,9 @@ public:
         if (const auto *g = p.extract<gpu_rastrigin>()) return g->batch_fitness(dvs);
         if (const auto *g = p.extract<gpu_rosenbrock>()) return g->batch_fitness(dvs);
         if (const auto *g = p.extract<gpu_lennard_jones>()) return g->batch_fitness(dvs);
+        if (const auto *g = p.extract<gpu_ackley>()) return g->batch_fitness(dvs);
+        if (const auto *g = p.extract<gpu_griewank>()) return g->batch_fitness(dvs);
+        if (const auto *g = p.extract<gpu_schwefel>()) return g->batch_fitness(dvs);
         int kind = 0;
         std::uint64_t param = p.get_nx();
         if (p.extract<pagmo::rastrigin>()) {
@@ -48,9 +54,16 @@ public:
         } else if (p.extract<pagmo::lennard_jones>()) {
             kind = PGX_LENNARD_JONES;
             param = (p.get_nx() + 6u) / 3u;
+        } else if (p.extract<pagmo::ackley>()) {
+            kind = PGX_ACKLEY;
+        } else if (p.extract<pagmo::griewank>()) {
+            kind = PGX_GRIEWANK;
+        } else if (p.extract<pagmo::schwefel>()) {
+            kind = PGX_SCHWEFEL;
         } else {
             throw std::invalid_argument("Cannot use a gpu_bfe on the problem '" + p.get_name()
-                                        + "': only rastrigin, rosenbrock and lennard_jones are evaluated on the GPU");
+                                        + "': only rastrigin, rosenbrock, lennard_jones, ackley, griewank and "
+                                          "schwefel are evaluated on the GPU");
         }
         const std::uint64_t n = dvs.size() / p.get_nx(); // pagmo::bfe checked divisibility
         pagmo::vector_double fvs(n);

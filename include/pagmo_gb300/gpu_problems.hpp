@@ -28,12 +28,16 @@ namespace pagmo_gb300
 namespace detail
 {
 
+// Fitness, batch fitness, bounds and serialization of a GPU UDP. Problems
+// whose reference UDP has no gradient (ackley, griewank, schwefel) stop
+// here, so pagmo's has_gradient is false for them and problem::gradient
+// raises not_implemented_error, as for the reference UDPs.
 template <int Kind>
-class gpu_udp
+class gpu_udp_fitness
 {
 public:
-    gpu_udp() = default;
-    explicit gpu_udp(std::uint64_t param, int device = 0) : m_param(param), m_device(device)
+    gpu_udp_fitness() = default;
+    explicit gpu_udp_fitness(std::uint64_t param, int device = 0) : m_param(param), m_device(device)
     {
         check(pgx_problem_nx(Kind, param, &m_nx)); // the reference constructors' checks and messages
     }
@@ -49,24 +53,6 @@ public:
         pagmo::vector_double f(n);
         if (n) check(pgx_batch_fitness(device_context(m_device), Kind, m_param, dvs.data(), n, f.data()));
         return f;
-    }
-
-    pagmo::vector_double gradient(const pagmo::vector_double &x) const
-    {
-        return batch_gradient(x).second;
-    }
-
-    // (fitness, gradient) of a whole batch in one GPU pass: n fitness values
-    // and n * nx gradient entries, row-major.
-    std::pair<pagmo::vector_double, pagmo::vector_double> batch_gradient(const pagmo::vector_double &dvs) const
-    {
-        const std::uint64_t n = rows(dvs);
-        std::pair<pagmo::vector_double, pagmo::vector_double> out{pagmo::vector_double(n),
-                                                                  pagmo::vector_double(n * m_nx)};
-        if (n)
-            check(pgx_batch_gradient(device_context(m_device), Kind, m_param, dvs.data(), n, out.first.data(),
-                                     out.second.data()));
-        return out;
     }
 
     std::pair<pagmo::vector_double, pagmo::vector_double> get_bounds() const
@@ -112,6 +98,33 @@ protected:
     int m_device = 0;
 };
 
+// A GPU UDP with the gradient hook (rastrigin, rosenbrock, lennard_jones).
+template <int Kind>
+class gpu_udp : public gpu_udp_fitness<Kind>
+{
+public:
+    gpu_udp() = default;
+    explicit gpu_udp(std::uint64_t param, int device = 0) : gpu_udp_fitness<Kind>(param, device) {}
+
+    pagmo::vector_double gradient(const pagmo::vector_double &x) const
+    {
+        return batch_gradient(x).second;
+    }
+
+    // (fitness, gradient) of a whole batch in one GPU pass: n fitness values
+    // and n * nx gradient entries, row-major.
+    std::pair<pagmo::vector_double, pagmo::vector_double> batch_gradient(const pagmo::vector_double &dvs) const
+    {
+        const std::uint64_t n = this->rows(dvs);
+        std::pair<pagmo::vector_double, pagmo::vector_double> out{pagmo::vector_double(n),
+                                                                  pagmo::vector_double(n * this->m_nx)};
+        if (n)
+            check(pgx_batch_gradient(device_context(this->m_device), Kind, this->m_param, dvs.data(), n,
+                                     out.first.data(), out.second.data()));
+        return out;
+    }
+};
+
 } // namespace detail
 
 // rastrigin{dim}: f = 10 n + sum (x_i^2 - 10 cos(2 pi x_i)) on [-5.12, 5.12]^n.
@@ -155,6 +168,54 @@ public:
     }
 };
 
+// ackley{dim}: -20 exp(-0.2 sqrt(sum x^2 / n)) - exp(sum cos(2 pi x) / n) + 20 + e on [-15, 30]^n
+// (src/problems/ackley.cpp). Fitness only, as the reference.
+class gpu_ackley : public detail::gpu_udp_fitness<PGX_ACKLEY>
+{
+public:
+    explicit gpu_ackley(unsigned dim = 1u, int device = 0) : gpu_udp_fitness(dim, device) {}
+    std::string get_name() const
+    {
+        return "Ackley Function";
+    }
+    pagmo::vector_double best_known() const
+    {
+        return pagmo::vector_double(m_nx, 0.);
+    }
+};
+
+// griewank{dim}: sum x^2 / 4000 - prod cos(x_i / sqrt(i + 1)) + 1 on [-600, 600]^n
+// (src/problems/griewank.cpp). Fitness only, as the reference.
+class gpu_griewank : public detail::gpu_udp_fitness<PGX_GRIEWANK>
+{
+public:
+    explicit gpu_griewank(unsigned dim = 1u, int device = 0) : gpu_udp_fitness(dim, device) {}
+    std::string get_name() const
+    {
+        return "Griewank Function";
+    }
+    pagmo::vector_double best_known() const
+    {
+        return pagmo::vector_double(m_nx, 0.);
+    }
+};
+
+// schwefel{dim}: 418.9828872724338 n - sum x sin(sqrt|x|) on [-500, 500]^n
+// (src/problems/schwefel.cpp). Fitness only, as the reference.
+class gpu_schwefel : public detail::gpu_udp_fitness<PGX_SCHWEFEL>
+{
+public:
+    explicit gpu_schwefel(unsigned dim = 1u, int device = 0) : gpu_udp_fitness(dim, device) {}
+    std::string get_name() const
+    {
+        return "Schwefel Function";
+    }
+    pagmo::vector_double best_known() const
+    {
+        return pagmo::vector_double(m_nx, 420.9687);
+    }
+};
+
 } // namespace pagmo_gb300
 
 // Registration with pagmo's Boost.Serialization machinery (include/pagmo/problem.hpp:67-76):
@@ -162,5 +223,8 @@ public:
 PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_rastrigin)
 PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_rosenbrock)
 PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_lennard_jones)
+PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_ackley)
+PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_griewank)
+PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_schwefel)
 
 #endif

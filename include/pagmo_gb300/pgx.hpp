@@ -11,18 +11,22 @@
 #include <stdexcept>
 #include <string>
 
+#include <pagmo/exceptions.hpp>
+
 #include "../pgx.h"
 
 namespace pagmo_gb300
 {
 
 // PGX_ERR_INVALID -> std::invalid_argument (pagmo_throw(std::invalid_argument, ...)),
-// PGX_ERR_CAPACITY -> std::overflow_error, anything else -> std::runtime_error.
+// PGX_ERR_NOTIMPL -> pagmo::not_implemented_error, PGX_ERR_CAPACITY ->
+// std::overflow_error, anything else -> std::runtime_error.
 inline void check(int status)
 {
     if (status == PGX_OK) return;
     const std::string msg = pgx_last_error();
     if (status == PGX_ERR_INVALID) throw std::invalid_argument(msg);
+    if (status == PGX_ERR_NOTIMPL) throw pagmo::not_implemented_error(msg);
     if (status == PGX_ERR_CAPACITY) throw std::overflow_error(msg);
     throw std::runtime_error(msg.empty() ? "pgx error " + std::to_string(status) : msg);
 }

@@ -13,5 +13,8 @@ PAGMO_S11N_BFE_IMPLEMENT(pagmo_gb300::gpu_bfe)
 PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_rastrigin)
 PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_rosenbrock)
 PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_lennard_jones)
+PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_ackley)
+PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_griewank)
+PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_schwefel)
 
 #endif

@@ -16,7 +16,10 @@
  *    Gradients are dense, n_dvs rows of nx doubles: for nf = 1 this is the
  *    layout of problem::gradient (src/problem.cpp:456-467, dense sparsity).
  *  - Problems: PGX_RASTRIGIN (param = dim >= 1), PGX_ROSENBROCK (param =
- *    dim >= 2), PGX_LENNARD_JONES (param = atoms >= 3, nx = 3*atoms - 6).
+ *    dim >= 2), PGX_LENNARD_JONES (param = atoms >= 3, nx = 3*atoms - 6);
+ *    PGX_ACKLEY, PGX_GRIEWANK, PGX_SCHWEFEL (param = dim >= 1) have no
+ *    gradient in the reference, so gradient requests for them return
+ *    PGX_ERR_NOTIMPL, and archipelago epochs take the first three kinds only.
  *  - Every function returns PGX_OK (0) or an error status; the message of the
  *    calling thread's last error is pgx_last_error(). PGX_ERR_INVALID maps to
  *    pagmo's std::invalid_argument. There is no CPU fallback: without a usable
@@ -52,11 +55,15 @@ extern "C" {
 #define PGX_ERR_TIMEOUT 3  /* a bounded device-side wait gave up */
 #define PGX_ERR_CAPACITY 4 /* a size exceeds a fixed capacity */
 #define PGX_ERR_NODEVICE 5 /* no CUDA device could be opened */
+#define PGX_ERR_NOTIMPL 6  /* not provided by the UDP (pagmo: not_implemented_error) */
 
 /* problem kinds (the reference UDPs) */
 #define PGX_RASTRIGIN 1     /* src/problems/rastrigin.cpp */
 #define PGX_ROSENBROCK 2    /* src/problems/rosenbrock.cpp */
 #define PGX_LENNARD_JONES 3 /* src/problems/lennard_jones.cpp */
+#define PGX_ACKLEY 4        /* src/problems/ackley.cpp (fitness only) */
+#define PGX_GRIEWANK 5      /* src/problems/griewank.cpp (fitness only) */
+#define PGX_SCHWEFEL 6      /* src/problems/schwefel.cpp (fitness only) */
 
 typedef struct pgx_context pgx_context;
 typedef struct pgx_epoch pgx_epoch;

@@ -116,6 +116,11 @@ bool check_kind(int kind, uint64_t param, uint64_t nx)
         case 3:
             if (param < 3u || nx != 3u * param - 6u) break;
             return true;
+        case 4:
+        case 5:
+        case 6:
+            if (param < 1u || nx != param) break;
+            return true;
         default:
             break;
     }
@@ -132,6 +137,12 @@ std::vector<double> row_fitness(int kind, uint64_t param, const std::vector<doub
             return {orc_rastrigin_fitness(x.data(), x.size())};
         case 2:
             return {orc_rosenbrock_fitness(x.data(), x.size())};
+        case 4:
+            return {orc_ackley_fitness(x.data(), x.size())};
+        case 5:
+            return {orc_griewank_fitness(x.data(), x.size())};
+        case 6:
+            return {orc_schwefel_fitness(x.data(), x.size())};
         default:
             return {orc_lj_fitness(x.data(), param)};
     }
@@ -342,6 +353,96 @@ void orc_lj_gradient_ld(const double *x, uint64_t atoms, double *g, double *gsca
     }
 }
 
+// ------------------------------------------- ackley, griewank, schwefel
+
+// src/problems/ackley.cpp:62-77, in the reference's operation order.
+double orc_ackley_fitness(const double *x, uint64_t n)
+{
+    const double omega = 2. * k_pi;
+    double s1 = 0., s2 = 0.;
+    const double nepero = std::exp(1.0);
+    for (uint64_t i = 0; i < n; ++i) {
+        s1 += x[i] * x[i];
+        s2 += std::cos(omega * x[i]);
+    }
+    return -20 * std::exp(-0.2 * std::sqrt(1.0 / static_cast<double>(n) * s1))
+           - std::exp(1.0 / static_cast<double>(n) * s2) + 20 + nepero;
+}
+
+// src/problems/griewank.cpp:62-76.
+double orc_griewank_fitness(const double *x, uint64_t n)
+{
+    const double fr = 4000.;
+    double retval = 0., p = 1.;
+    for (uint64_t i = 0; i < n; ++i) retval += x[i] * x[i];
+    for (uint64_t i = 0; i < n; ++i) p *= std::cos(x[i] / std::sqrt(static_cast<double>(i) + 1.0));
+    return retval / fr - p + 1.;
+}
+
+// src/problems/schwefel.cpp:62-70.
+double orc_schwefel_fitness(const double *x, uint64_t n)
+{
+    double f = 0.;
+    for (uint64_t i = 0; i < n; ++i) f += x[i] * std::sin(std::sqrt(std::abs(x[i])));
+    return 418.9828872724338 * static_cast<double>(n) - f;
+}
+
+// Long-double versions. scale = first-order error bound of the reference's
+// FP64 evaluation: the magnitudes of the combined terms plus the effect of
+// its rounded arguments (omega*x in ackley, x/sqrt(i+1) in griewank,
+// sqrt|x| in schwefel), each per unit roundoff.
+double orc_ackley_fitness_ld(const double *x, uint64_t n, double *scale)
+{
+    const ld om = static_cast<ld>(k_omega);
+    ld s1 = 0, s2 = 0, arg = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const ld xi = x[i];
+        s1 += xi * xi;
+        s2 += cosl(om * xi);
+        arg += fabsl(om * xi);
+    }
+    const ld nn = static_cast<ld>(n), r = sqrtl(s1 / nn);
+    const ld a = 20.0L * expl(-0.2L * r), b = expl(s2 / nn), e = expl(1.0L);
+    if (scale) *scale = static_cast<double>(a * (1.0L + 0.2L * r) + b * (1.0L + arg / nn) + 20.0L + e);
+    return static_cast<double>(-a - b + 20.0L + e);
+}
+
+double orc_griewank_fitness_ld(const double *x, uint64_t n, double *scale)
+{
+    std::vector<ld> c(n), sn(n), arg(n), pre(n + 1), suf(n + 1);
+    ld sum = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const ld xi = x[i];
+        sum += xi * xi;
+        arg[i] = xi / sqrtl(static_cast<ld>(i) + 1.0L);
+        c[i] = cosl(arg[i]);
+        sn[i] = sinl(arg[i]);
+    }
+    pre[0] = 1;
+    for (uint64_t i = 0; i < n; ++i) pre[i + 1] = pre[i] * c[i];
+    suf[n] = 1;
+    for (uint64_t i = n; i-- > 0;) suf[i] = suf[i + 1] * c[i];
+    ld sens = 0;
+    for (uint64_t i = 0; i < n; ++i) sens += fabsl(pre[i] * suf[i + 1] * sn[i] * arg[i]);
+    const ld p = pre[n];
+    if (scale) *scale = static_cast<double>(sum / 4000.0L + 1.0L + fabsl(p) * static_cast<ld>(2u * n) + 2.0L * sens);
+    return static_cast<double>(sum / 4000.0L - p + 1.0L);
+}
+
+double orc_schwefel_fitness_ld(const double *x, uint64_t n, double *scale)
+{
+    ld f = 0, s = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const ld xi = x[i], q = sqrtl(fabsl(xi));
+        const ld t = xi * sinl(q);
+        f += t;
+        s += fabsl(t) + fabsl(xi * cosl(q)) * q;
+    }
+    const ld c = 418.9828872724338L * static_cast<ld>(n);
+    if (scale) *scale = static_cast<double>(c + s);
+    return static_cast<double>(c - f);
+}
+
 // ---------------------------------------------------------------- batch runners
 
 int orc_batch_fitness(int kind, uint64_t param, const double *dvs, uint64_t n, uint64_t nx, double *f, int nthreads)
@@ -363,6 +464,10 @@ int orc_batch_fitness(int kind, uint64_t param, const double *dvs, uint64_t n, u
 int orc_batch_gradient(int kind, uint64_t param, const double *dvs, uint64_t n, uint64_t nx, double *g, int nthreads)
 {
     if (!check_kind(kind, param, nx)) return 1;
+    if (kind >= 4) {
+        g_err = "The gradient has been requested but it is not implemented in the UDP";
+        return 1;
+    }
     parallel_rows(n, nthreads, [&](uint64_t b, uint64_t e) {
         std::vector<double> tmp(nx), out(nx);
         for (; b != e; ++b) {
@@ -391,6 +496,12 @@ int orc_batch_fitness_ld(int kind, uint64_t param, const double *dvs, uint64_t n
                 f[b] = orc_rastrigin_fitness_ld(x, nx, sc);
             else if (kind == 2)
                 f[b] = orc_rosenbrock_fitness_ld(x, nx, sc);
+            else if (kind == 4)
+                f[b] = orc_ackley_fitness_ld(x, nx, sc);
+            else if (kind == 5)
+                f[b] = orc_griewank_fitness_ld(x, nx, sc);
+            else if (kind == 6)
+                f[b] = orc_schwefel_fitness_ld(x, nx, sc);
             else
                 f[b] = orc_lj_fitness_ld(x, param, sc);
         }
@@ -402,6 +513,10 @@ int orc_batch_gradient_ld(int kind, uint64_t param, const double *dvs, uint64_t 
                           double *gscale, int nthreads)
 {
     if (!check_kind(kind, param, nx)) return 1;
+    if (kind >= 4) {
+        g_err = "The gradient has been requested but it is not implemented in the UDP";
+        return 1;
+    }
     parallel_rows(n, nthreads, [&](uint64_t b, uint64_t e) {
         for (; b != e; ++b) {
             const double *x = dvs + b * nx;

@@ -20,7 +20,8 @@
  *    used to state relative errors that survive cancellation.
  *
  * Problem kinds: 1 = rastrigin (param = dim), 2 = rosenbrock (param = dim),
- * 3 = lennard_jones (param = atoms, dim = 3*atoms-6).
+ * 3 = lennard_jones (param = atoms, dim = 3*atoms-6), 4 = ackley, 5 = griewank,
+ * 6 = schwefel (param = dim; fitness only, as in the reference).
  * Status codes: 0 ok, 1 invalid argument (message via orc_last_error()).
  */
 #ifndef PGX_ORACLE_H
@@ -39,6 +40,9 @@ void orc_rastrigin_gradient(const double *x, uint64_t n, double *g);
 double orc_rosenbrock_fitness(const double *x, uint64_t n);
 void orc_rosenbrock_gradient(const double *x, uint64_t n, double *g);
 double orc_lj_fitness(const double *x, uint64_t atoms);
+double orc_ackley_fitness(const double *x, uint64_t n);
+double orc_griewank_fitness(const double *x, uint64_t n);
+double orc_schwefel_fitness(const double *x, uint64_t n);
 
 /* ---- long-double oracle with condition scales ---- */
 double orc_rastrigin_fitness_ld(const double *x, uint64_t n, double *scale);
@@ -47,6 +51,9 @@ double orc_rosenbrock_fitness_ld(const double *x, uint64_t n, double *scale);
 void orc_rosenbrock_gradient_ld(const double *x, uint64_t n, double *g, double *gscale);
 double orc_lj_fitness_ld(const double *x, uint64_t atoms, double *scale);
 void orc_lj_gradient_ld(const double *x, uint64_t atoms, double *g, double *gscale);
+double orc_ackley_fitness_ld(const double *x, uint64_t n, double *scale);
+double orc_griewank_fitness_ld(const double *x, uint64_t n, double *scale);
+double orc_schwefel_fitness_ld(const double *x, uint64_t n, double *scale);
 
 /* ---- batch runners over row-major dvs (n rows of nx) ---- */
 /* Mirror of bfe{thread_bfe{}}: static partition over nthreads std::threads,

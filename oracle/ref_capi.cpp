@@ -16,9 +16,12 @@
 #include <pagmo/batch_evaluators/thread_bfe.hpp>
 #include <pagmo/bfe.hpp>
 #include <pagmo/problem.hpp>
+#include <pagmo/problems/ackley.hpp>
+#include <pagmo/problems/griewank.hpp>
 #include <pagmo/problems/lennard_jones.hpp>
 #include <pagmo/problems/rastrigin.hpp>
 #include <pagmo/problems/rosenbrock.hpp>
+#include <pagmo/problems/schwefel.hpp>
 #include <pagmo/utils/multi_objective.hpp>
 
 namespace
@@ -34,6 +37,12 @@ pagmo::problem make_problem(int kind, std::uint64_t param)
             return pagmo::problem{pagmo::rosenbrock{static_cast<pagmo::vector_double::size_type>(param)}};
         case 3:
             return pagmo::problem{pagmo::lennard_jones{static_cast<unsigned>(param)}};
+        case 4:
+            return pagmo::problem{pagmo::ackley{static_cast<unsigned>(param)}};
+        case 5:
+            return pagmo::problem{pagmo::griewank{static_cast<unsigned>(param)}};
+        case 6:
+            return pagmo::problem{pagmo::schwefel{static_cast<unsigned>(param)}};
         default:
             throw std::invalid_argument("unknown problem kind " + std::to_string(kind));
     }

@@ -5,7 +5,9 @@ include/pgx.h). This package is its Python host side, mirroring pagmo's
 plugin interface for the batch-fitness path:
 
   problems:         rastrigin, rosenbrock, lennard_jones (GPU UDPs with
-                    batch_fitness, gradient and batch_gradient)
+                    batch_fitness, gradient and batch_gradient); ackley,
+                    griewank, schwefel (batch_fitness; no gradient, as in
+                    the reference)
   batch_evaluators: gpu_bfe (the UDBFE) and a bfe/problem pair reproducing
                     pagmo's input/output checks and fevals accounting
   multi_objective:  fast_non_dominated_sorting, crowding_distance,
@@ -16,4 +18,4 @@ from ._native import Context, default_context  # noqa: F401
 from .batch_evaluators import bfe, gpu_bfe, problem  # noqa: F401
 from .multi_objective import (crowding_distance, fast_non_dominated_sorting, nsga2_survival,  # noqa: F401
                               select_best_N_mo, sort_population_mo)
-from .problems import lennard_jones, rastrigin, rosenbrock  # noqa: F401
+from .problems import ackley, griewank, lennard_jones, rastrigin, rosenbrock, schwefel  # noqa: F401

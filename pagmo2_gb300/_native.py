@@ -16,8 +16,8 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpgx.so"
 
-OK, ERR_INVALID, ERR_CUDA, ERR_TIMEOUT, ERR_CAPACITY, ERR_NODEVICE = 0, 1, 2, 3, 4, 5
-RASTRIGIN, ROSENBROCK, LENNARD_JONES = 1, 2, 3
+OK, ERR_INVALID, ERR_CUDA, ERR_TIMEOUT, ERR_CAPACITY, ERR_NODEVICE, ERR_NOTIMPL = 0, 1, 2, 3, 4, 5, 6
+RASTRIGIN, ROSENBROCK, LENNARD_JONES, ACKLEY, GRIEWANK, SCHWEFEL = 1, 2, 3, 4, 5, 6
 
 # Exported symbols and their signatures (kept in step with include/pgx.h).
 _vp, _u64, _i32, _d = C.c_void_p, C.c_uint64, C.c_int32, C.c_double
@@ -97,6 +97,8 @@ def check(status: int) -> None:
         raise OverflowError(msg)
     if status == ERR_TIMEOUT:
         raise TimeoutError(msg)
+    if status == ERR_NOTIMPL:
+        raise NotImplementedError(msg)
     raise RuntimeError(msg or f"pgx status {status}")
 
 

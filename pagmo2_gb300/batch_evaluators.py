@@ -31,8 +31,8 @@ class gpu_bfe:
         udp = getattr(prob, "udp", prob)
         if not isinstance(udp, P._gpu_udp):
             name = udp.get_name() if hasattr(udp, "get_name") else type(udp).__name__
-            raise ValueError(f"Cannot use a gpu_bfe on the problem '{name}': only the GPU rastrigin, rosenbrock "
-                             "and lennard_jones problems are supported")
+            raise ValueError(f"Cannot use a gpu_bfe on the problem '{name}': only the GPU rastrigin, rosenbrock, "
+                             "lennard_jones, ackley, griewank and schwefel problems are supported")
         return udp.batch_fitness(dvs)
 
 

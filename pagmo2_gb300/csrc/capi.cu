@@ -98,10 +98,33 @@ int problem_nx(int kind, uint64_t param, uint64_t *nx)
                       "Overflow caused by the number of atoms requested: " + std::to_string(param));
             *nx = 3u * param - 6u;
             return PGX_OK;
+        case PGX_ACKLEY:
+            PGX_CHECK(param >= 1u, PGX_ERR_INVALID,
+                      "Ackley Function must have minimum 1 dimension, " + std::to_string(param) + " requested");
+            *nx = param;
+            return PGX_OK;
+        case PGX_GRIEWANK:
+            PGX_CHECK(param >= 1u, PGX_ERR_INVALID,
+                      "Griewank Function must have minimum 1 dimension, " + std::to_string(param) + " requested");
+            *nx = param;
+            return PGX_OK;
+        case PGX_SCHWEFEL:
+            PGX_CHECK(param >= 1u, PGX_ERR_INVALID,
+                      "Schwefel Function must have minimum 1 dimension, " + std::to_string(param) + " requested");
+            *nx = param;
+            return PGX_OK;
         default:
             set_error("unknown problem kind " + std::to_string(kind));
             return PGX_ERR_INVALID;
     }
+}
+
+// problem::gradient of a UDP without gradient (src/problem.cpp:453-467).
+int check_has_gradient(int kind)
+{
+    PGX_CHECK(kind == PGX_RASTRIGIN || kind == PGX_ROSENBROCK || kind == PGX_LENNARD_JONES, PGX_ERR_NOTIMPL,
+              "The gradient has been requested but it is not implemented in the UDP");
+    return PGX_OK;
 }
 
 namespace
@@ -115,6 +138,7 @@ int host_eval(pgx_context *ctx, int kind, uint64_t param, const double *dvs, uin
 {
     uint64_t nx = 0;
     PGX_TRY(problem_nx(kind, param, &nx));
+    if (grads) PGX_TRY(check_has_gradient(kind));
     PGX_CHECK(dvs != nullptr || n == 0, PGX_ERR_INVALID, "null decision vector buffer");
     PGX_CHECK(fvs != nullptr || grads != nullptr, PGX_ERR_INVALID, "no output buffer");
     if (n == 0) return PGX_OK;
@@ -331,6 +355,15 @@ int pgx_problem_bounds(int kind, uint64_t param, double *lb, double *ub)
         } else if (kind == PGX_ROSENBROCK) {
             lb[i] = -5.;
             ub[i] = 10.;
+        } else if (kind == PGX_ACKLEY) { // ackley.cpp:85-90
+            lb[i] = -15.;
+            ub[i] = 30.;
+        } else if (kind == PGX_GRIEWANK) { // griewank.cpp:84-89
+            lb[i] = -600.;
+            ub[i] = 600.;
+        } else if (kind == PGX_SCHWEFEL) { // schwefel.cpp:78-83
+            lb[i] = -500.;
+            ub[i] = 500.;
         } else {
             const bool z = i != 0u && i % 3u == 0u;
             lb[i] = z ? 0.0 : -3.0;
@@ -363,6 +396,7 @@ int pgx_batch_eval_device(pgx_context *ctx, int kind, uint64_t param, const doub
     PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
     uint64_t nx = 0;
     PGX_TRY(problem_nx(kind, param, &nx));
+    if (d_grads) PGX_TRY(check_has_gradient(kind));
     PGX_CHECK(d_fvs != nullptr || d_grads != nullptr, PGX_ERR_INVALID, "no output buffer");
     if (n_dvs == 0) return PGX_OK;
     PGX_CHECK(d_dvs != nullptr, PGX_ERR_INVALID, "null decision vector buffer");

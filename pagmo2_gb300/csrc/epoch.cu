@@ -487,6 +487,8 @@ int build_plan(pgx_epoch *ep, const pgx_request *reqs, int n_reqs)
         p.param = r.param;
         p.n = r.n_dvs;
         PGX_TRY(problem_nx(r.kind, r.param, &p.nx));
+        PGX_CHECK(r.kind == PGX_RASTRIGIN || r.kind == PGX_ROSENBROCK || r.kind == PGX_LENNARD_JONES, PGX_ERR_INVALID,
+                  "archipelago epochs evaluate rastrigin, rosenbrock and lennard_jones requests only");
         PGX_CHECK(p.nx < (1ull << 31), PGX_ERR_CAPACITY, "decision vector dimension exceeds 2^31-1");
         p.grad = r.grads != nullptr;
         p.off_x = ep->total_x;

@@ -34,6 +34,24 @@ __global__ void __launch_bounds__(256) rosenbrock_kernel(const double *__restric
         rosenbrock_row<G, GRAD>(x + row * nx, nx, f ? f + row : nullptr, GRAD ? g + row * nx : nullptr);
 }
 
+// Fitness-only rows of ackley, griewank and schwefel.
+template <int G, int KIND>
+__global__ void __launch_bounds__(256) row_f_kernel(const double *__restrict__ x, uint64_t n, uint32_t nx,
+                                                    double *__restrict__ f, double *__restrict__ g)
+{
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * (blockDim.x / G);
+    for (uint64_t row = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / G; row < n; row += stride) {
+        double *fo = f ? f + row : nullptr;
+        if constexpr (KIND == PGX_ACKLEY)
+            ackley_row<G>(x + row * nx, nx, fo);
+        else if constexpr (KIND == PGX_GRIEWANK)
+            griewank_row<G>(x + row * nx, nx, fo);
+        else
+            schwefel_row<G>(x + row * nx, nx, fo);
+    }
+    (void)g;
+}
+
 template <bool GRAD>
 __global__ void __launch_bounds__(256) rosenbrock_v4_kernel(const double *__restrict__ x, uint64_t n, uint32_t nx,
                                                             double *__restrict__ f, double *__restrict__ g)
@@ -117,11 +135,20 @@ int launch_rows(int kind, bool grad, const double *x, uint64_t n, uint32_t nx, d
                 int num_sms)
 {
     constexpr int pb = 256 / G;
-    if (kind == PGX_RASTRIGIN)
-        return grad ? launch_simple(rastrigin_kernel<G, true>, pb, x, n, nx, f, g, s, num_sms)
-                    : launch_simple(rastrigin_kernel<G, false>, pb, x, n, nx, f, g, s, num_sms);
-    return grad ? launch_simple(rosenbrock_kernel<G, true>, pb, x, n, nx, f, g, s, num_sms)
-                : launch_simple(rosenbrock_kernel<G, false>, pb, x, n, nx, f, g, s, num_sms);
+    switch (kind) {
+        case PGX_RASTRIGIN:
+            return grad ? launch_simple(rastrigin_kernel<G, true>, pb, x, n, nx, f, g, s, num_sms)
+                        : launch_simple(rastrigin_kernel<G, false>, pb, x, n, nx, f, g, s, num_sms);
+        case PGX_ROSENBROCK:
+            return grad ? launch_simple(rosenbrock_kernel<G, true>, pb, x, n, nx, f, g, s, num_sms)
+                        : launch_simple(rosenbrock_kernel<G, false>, pb, x, n, nx, f, g, s, num_sms);
+        case PGX_ACKLEY:
+            return launch_simple(row_f_kernel<G, PGX_ACKLEY>, pb, x, n, nx, f, nullptr, s, num_sms);
+        case PGX_GRIEWANK:
+            return launch_simple(row_f_kernel<G, PGX_GRIEWANK>, pb, x, n, nx, f, nullptr, s, num_sms);
+        default:
+            return launch_simple(row_f_kernel<G, PGX_SCHWEFEL>, pb, x, n, nx, f, nullptr, s, num_sms);
+    }
 }
 
 } // namespace
@@ -204,7 +231,10 @@ int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64
         else
             st = grad ? launch_simple(rosenbrock_v4ff_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
                       : launch_simple(rosenbrock_v4ff_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
-    } else if (kind == PGX_RASTRIGIN || kind == PGX_ROSENBROCK) {
+    } else if (kind == PGX_RASTRIGIN || kind == PGX_ROSENBROCK || kind == PGX_ACKLEY || kind == PGX_GRIEWANK
+               || kind == PGX_SCHWEFEL) {
+        PGX_CHECK(!grad || kind <= PGX_ROSENBROCK, PGX_ERR_NOTIMPL,
+                  "The gradient has been requested but it is not implemented in the UDP");
         switch (lanes_per_row(nx32)) {
             case 32: st = launch_rows<32>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;
             case 16: st = launch_rows<16>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;

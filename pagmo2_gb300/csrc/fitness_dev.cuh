@@ -336,6 +336,79 @@ __device__ __forceinline__ void rosenbrock_row_v4(const double *__restrict__ xr,
     if (lane == 0 && f_out) *f_out = GRAD ? fma(100.0, acc_t, 0.25 * acc_u) : fma(100.0, acc_t, acc_u);
 }
 
+// ------------------------------------------------ ackley, griewank, schwefel
+//
+// Fitness only: the reference gives these UDPs no gradient. One group of G
+// lanes per row, lanes strided over coordinates, sums (and griewank's product)
+// reduced with shuffles; the closing expressions keep the reference's order.
+
+// e as std::exp(1.0) rounds it.
+constexpr double kNepero = 2.71828182845904523536;
+
+template <int G>
+__device__ __forceinline__ double group_prod(double v, unsigned mask)
+{
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v *= __shfl_xor_sync(mask, v, o, G);
+    return v;
+}
+
+// f = -20 exp(-0.2 sqrt(s1/n)) - exp(s2/n) + 20 + e, s1 = sum x^2,
+// s2 = sum cos(2 pi x) (src/problems/ackley.cpp:62-77).
+template <int G>
+__device__ __forceinline__ void ackley_row(const double *__restrict__ xr, uint32_t nx, double *f_out)
+{
+    const unsigned sub = threadIdx.x & (G - 1);
+    const unsigned mask = group_mask<G>();
+    double s1 = 0.0, s2 = 0.0;
+    for (uint32_t i = sub; i < nx; i += G) {
+        const double xi = __ldg(xr + i);
+        int c_neg = 0;
+        const double c = fast_trig_arg(xi) ? cos_2pi(xi, c_neg) : cospi(xi + xi);
+        s1 = fma(xi, xi, s1);
+        s2 = fma(c, unit_sign(c_neg), s2);
+    }
+    s1 = group_sum<G>(s1, mask);
+    s2 = group_sum<G>(s2, mask);
+    if (sub == 0 && f_out) {
+        const double inv_n = 1.0 / static_cast<double>(nx);
+        *f_out = -20.0 * exp(-0.2 * sqrt(inv_n * s1)) - exp(inv_n * s2) + 20.0 + kNepero;
+    }
+}
+
+// f = sum x^2 / 4000 - prod cos(x_i / sqrt(i + 1)) + 1 (src/problems/griewank.cpp:62-76);
+// the division and square root are correctly rounded as in the reference.
+template <int G>
+__device__ __forceinline__ void griewank_row(const double *__restrict__ xr, uint32_t nx, double *f_out)
+{
+    const unsigned sub = threadIdx.x & (G - 1);
+    const unsigned mask = group_mask<G>();
+    double s = 0.0, p = 1.0;
+    for (uint32_t i = sub; i < nx; i += G) {
+        const double xi = __ldg(xr + i);
+        s = fma(xi, xi, s);
+        p *= cos(xi / sqrt(static_cast<double>(i) + 1.0));
+    }
+    s = group_sum<G>(s, mask);
+    p = group_prod<G>(p, mask);
+    if (sub == 0 && f_out) *f_out = s / 4000.0 - p + 1.0;
+}
+
+// f = 418.9828872724338 n - sum x sin(sqrt|x|) (src/problems/schwefel.cpp:62-70).
+template <int G>
+__device__ __forceinline__ void schwefel_row(const double *__restrict__ xr, uint32_t nx, double *f_out)
+{
+    const unsigned sub = threadIdx.x & (G - 1);
+    const unsigned mask = group_mask<G>();
+    double s = 0.0;
+    for (uint32_t i = sub; i < nx; i += G) {
+        const double xi = __ldg(xr + i);
+        s = fma(xi, sin(sqrt(fabs(xi))), s);
+    }
+    s = group_sum<G>(s, mask);
+    if (sub == 0 && f_out) *f_out = 418.9828872724338 * static_cast<double>(nx) - s;
+}
+
 // ------------------------------------------------- rosenbrock on the FP32 pipe
 //
 // GB300 retires 2 FP64 lanes per SM per clock but ~115 FP32 and ~90 integer

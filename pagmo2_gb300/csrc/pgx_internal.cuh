@@ -110,6 +110,9 @@ bool lj_use_flat(uint32_t na);
 // arithmetic on the FP32 pipe (an opt-in; the default is FP64 arithmetic).
 bool rosenbrock_double_float();
 
+// PGX_ERR_NOTIMPL unless the problem kind provides a gradient.
+int check_has_gradient(int kind);
+
 // rastrigin/rosenbrock with a forced row variant (lanes 1..32, or 0 for the
 // 4-wide rosenbrock rows); for the autotuner.
 int launch_rows_variant(int kind, uint64_t nx, const double *d_x, uint64_t n, double *d_f, double *d_g, int lanes,

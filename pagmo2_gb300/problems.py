@@ -1,5 +1,6 @@
-"""GPU-backed user-defined problems mirroring pagmo's rastrigin, rosenbrock and
-lennard_jones UDPs (src/problems/{rastrigin,rosenbrock,lennard_jones}.cpp).
+"""GPU-backed user-defined problems mirroring pagmo's rastrigin, rosenbrock,
+lennard_jones, ackley, griewank and schwefel UDPs
+(src/problems/{rastrigin,rosenbrock,lennard_jones,ackley,griewank,schwefel}.cpp).
 
 They expose the UDP interface pagmo's ``problem`` wraps (``fitness``,
 ``get_bounds``, ``get_name``, ``get_thread_safety``) plus the optional hooks the
@@ -130,5 +131,63 @@ class lennard_jones(_gpu_udp):
         return f"Lennard Jones Cluster ({self.param} atoms)"
 
 
+class _fitness_only_udp(_gpu_udp):
+    """The reference gives these UDPs no gradient: gradient requests raise
+    NotImplementedError, as pagmo's problem::gradient raises
+    not_implemented_error (src/problem.cpp:453-467)."""
+
+    def has_gradient(self) -> bool:
+        return False
+
+    def batch_gradient(self, dvs, with_fitness: bool = True):
+        raise NotImplementedError("The gradient has been requested but it is not implemented in the UDP")
+
+    def gradient(self, x):
+        raise NotImplementedError("The gradient has been requested but it is not implemented in the UDP")
+
+
+class ackley(_fitness_only_udp):
+    """ackley{dim}: f = -20 exp(-0.2 sqrt(sum x^2 / n)) - exp(sum cos(2 pi x) / n) + 20 + e on [-15, 30]^n."""
+    kind = N.ACKLEY
+
+    def __init__(self, dim: int = 1, context=None):
+        super().__init__(dim, context)
+
+    def get_name(self) -> str:
+        return "Ackley Function"
+
+    def best_known(self):
+        return np.zeros(self._nx)
+
+
+class griewank(_fitness_only_udp):
+    """griewank{dim}: f = sum x^2 / 4000 - prod cos(x_i / sqrt(i + 1)) + 1 on [-600, 600]^n."""
+    kind = N.GRIEWANK
+
+    def __init__(self, dim: int = 1, context=None):
+        super().__init__(dim, context)
+
+    def get_name(self) -> str:
+        return "Griewank Function"
+
+    def best_known(self):
+        return np.zeros(self._nx)
+
+
+class schwefel(_fitness_only_udp):
+    """schwefel{dim}: f = 418.9828872724338 n - sum x sin(sqrt|x|) on [-500, 500]^n."""
+    kind = N.SCHWEFEL
+
+    def __init__(self, dim: int = 1, context=None):
+        super().__init__(dim, context)
+
+    def get_name(self) -> str:
+        return "Schwefel Function"
+
+    def best_known(self):
+        return np.full(self._nx, 420.9687)
+
+
 def from_kind(kind: int, param: int, context=None) -> _gpu_udp:
-    return {N.RASTRIGIN: rastrigin, N.ROSENBROCK: rosenbrock, N.LENNARD_JONES: lennard_jones}[kind](param, context)
+    return {N.RASTRIGIN: rastrigin, N.ROSENBROCK: rosenbrock, N.LENNARD_JONES: lennard_jones, N.ACKLEY: ackley,
+            N.GRIEWANK: griewank, N.SCHWEFEL: schwefel}[kind](param, context)

@@ -34,6 +34,9 @@ def bounds(kind: int, param: int) -> tuple[np.ndarray, np.ndarray]:
         return np.full(param, -5.12), np.full(param, 5.12)
     if kind == N.ROSENBROCK:
         return np.full(param, -5.0), np.full(param, 10.0)
+    if kind in (N.ACKLEY, N.GRIEWANK, N.SCHWEFEL):
+        lo, hi = {N.ACKLEY: (-15.0, 30.0), N.GRIEWANK: (-600.0, 600.0), N.SCHWEFEL: (-500.0, 500.0)}[kind]
+        return np.full(param, lo), np.full(param, hi)
     nx = 3 * param - 6
     lb = np.full(nx, -3.0)
     ub = np.full(nx, 3.0)

@@ -14,9 +14,13 @@
 #include <pagmo/batch_evaluators/thread_bfe.hpp>
 #include <pagmo/bfe.hpp>
 #include <pagmo/problem.hpp>
+#include <pagmo/exceptions.hpp>
+#include <pagmo/problems/ackley.hpp>
+#include <pagmo/problems/griewank.hpp>
 #include <pagmo/problems/null_problem.hpp>
 #include <pagmo/problems/rastrigin.hpp>
 #include <pagmo/problems/rosenbrock.hpp>
+#include <pagmo/problems/schwefel.hpp>
 #include <pagmo/utils/multi_objective.hpp>
 
 #include <pagmo_gb300/gpu_bfe.hpp>
@@ -55,6 +59,11 @@ static_assert(pagmo::is_udp<gpu_lennard_jones>::value, "gpu_lennard_jones must b
 static_assert(pagmo::has_batch_fitness<gpu_rosenbrock>::value, "batch_fitness hook");
 static_assert(pagmo::has_gradient<gpu_rosenbrock>::value, "gradient hook");
 static_assert(pagmo::has_gradient<gpu_lennard_jones>::value, "gradient hook");
+static_assert(pagmo::is_udp<gpu_ackley>::value && pagmo::is_udp<gpu_griewank>::value && pagmo::is_udp<gpu_schwefel>::value,
+              "fitness-only GPU UDPs");
+static_assert(!pagmo::has_gradient<gpu_ackley>::value && !pagmo::has_gradient<gpu_schwefel>::value,
+              "no gradient where the reference has none");
+static_assert(pagmo::has_batch_fitness<gpu_griewank>::value, "batch_fitness hook");
 
 int main()
 {
@@ -74,6 +83,16 @@ int main()
     CHECK(throws_with<std::invalid_argument>([] { gpu_rastrigin{0u}; }, "must have minimum 1 dimension"));
     CHECK(throws_with<std::invalid_argument>([] { gpu_rosenbrock{1u}; }, "must have minimum 2 dimensions"));
     CHECK(throws_with<std::invalid_argument>([] { gpu_lennard_jones{2u}; }, "greater than 2"));
+    CHECK(throws_with<std::invalid_argument>([] { gpu_ackley{0u}; }, "Ackley Function must have minimum 1"));
+    CHECK(throws_with<std::invalid_argument>([] { gpu_griewank{0u}; }, "Griewank Function must have minimum 1"));
+    CHECK(throws_with<std::invalid_argument>([] { gpu_schwefel{0u}; }, "Schwefel Function must have minimum 1"));
+    CHECK(pagmo::problem{gpu_ackley{3u}}.get_bounds() == pagmo::problem{pagmo::ackley{3u}}.get_bounds());
+    CHECK(pagmo::problem{gpu_griewank{3u}}.get_bounds() == pagmo::problem{pagmo::griewank{3u}}.get_bounds());
+    CHECK(pagmo::problem{gpu_schwefel{3u}}.get_bounds() == pagmo::problem{pagmo::schwefel{3u}}.get_bounds());
+    CHECK(pagmo::problem{gpu_schwefel{3u}}.get_name() == pagmo::problem{pagmo::schwefel{3u}}.get_name());
+    // no gradient: pagmo's own not_implemented_error, before any device work
+    CHECK(throws_with<pagmo::not_implemented_error>([] { pagmo::problem{gpu_ackley{3u}}.gradient({1., 2., 3.}); },
+                                                    "gradient"));
 
     // the UDBFE wrapped by pagmo::bfe
     pagmo::bfe b{gpu_bfe{}};
@@ -142,6 +161,15 @@ int main()
         CHECK(same);
         CHECK(throws_with<std::invalid_argument>([] { sort_population_mo({{1.}, {1.}, {2.}}); },
                                                  "at least two objectives"));
+        // ackley, griewank, schwefel through bfe{gpu_bfe} against bfe{thread_bfe}
+        std::vector<double> d3(30);
+        for (size_t i = 0; i < d3.size(); ++i) d3[i] = -14.0 + 1.7 * static_cast<double>(i);
+        for (auto prob : {pagmo::problem{pagmo::ackley{3u}}, pagmo::problem{pagmo::griewank{3u}},
+                          pagmo::problem{pagmo::schwefel{3u}}}) {
+            const auto fg = b(prob, d3);
+            const auto fr = pagmo::bfe{pagmo::thread_bfe{}}(prob, d3);
+            for (size_t i = 0; i < fr.size(); ++i) CHECK(std::abs(fg[i] - fr[i]) <= 1e-12 * (1.0 + std::abs(fr[i])));
+        }
     }
     if (failures) {
         std::fprintf(stderr, "%d check(s) failed\n", failures);

@@ -9,10 +9,12 @@ where that exists):
 
 Outputs (numpy .npz, small):
   fitness.npz  per case: the decision vectors, bfe{thread_bfe{}} fitness, and
-               problem::gradient rows (rastrigin, rosenbrock)
+               problem::gradient rows (rastrigin, rosenbrock); ackley,
+               griewank and schwefel (fitness only)
   mo.npz       per case: the objective vectors, fast_non_dominated_sorting
-               (rank, dom_count, fronts, dom_list) and crowding_distance of
-               every front of three or more points
+               (rank, dom_count, fronts, dom_list), crowding_distance of
+               every front of three or more points, sort_population_mo and
+               select_best_N_mo for a few N
 """
 from __future__ import annotations
 
@@ -27,7 +29,7 @@ sys.path.insert(0, str(HERE.parents[1]))
 import oracle  # noqa: E402
 from pagmo2_gb300 import workloads as W  # noqa: E402
 
-RAS, ROS, LJ = 1, 2, 3
+RAS, ROS, LJ, ACK, GRI, SCH = 1, 2, 3, 4, 5, 6
 
 
 def fitness_cases():
@@ -45,6 +47,13 @@ def fitness_cases():
     cases.append(("rastrigin_near_opt", RAS, 64, 1e-3 * np.random.RandomState(105).standard_normal((8, 64))))
     # integer points: exact values in the reference
     cases.append(("rastrigin_ints", RAS, 7, np.random.RandomState(106).randint(-5, 6, (8, 7)).astype(float)))
+    # fitness-only problems (no reference gradient)
+    for kind, name in ((ACK, "ackley"), (GRI, "griewank"), (SCH, "schwefel")):
+        for dim, n, seed in ((1, 16, 501), (3, 16, 502), (50, 32, 503), (173, 8, 504), (1000, 4, 505)):
+            cases.append((f"{name}_{dim}", kind, dim, W.uniform_batch(kind, dim, n, seed + 10 * kind)))
+        cases.append((f"{name}_near_opt", kind, 64,
+                      W.bounds(kind, 64)[0] * 0 + (420.9687 if kind == SCH else 0.0)
+                      + 1e-3 * np.random.RandomState(506 + kind).standard_normal((8, 64))))
     return cases
 
 
@@ -87,7 +96,7 @@ def main():
         fit[f"{name}/kind"] = np.array([kind, param])
         fit[f"{name}/x"] = x
         fit[f"{name}/f"] = f
-        if kind != LJ:
+        if kind in (RAS, ROS):
             fit[f"{name}/g"] = ref.gradient_rows(kind, param, x)
     np.savez_compressed(HERE / "fitness.npz", **fit)
 
@@ -106,6 +115,11 @@ def main():
             elif members.size in (1, 2):
                 cd[members] = np.inf
         mo[f"{name}/crowding"] = cd
+        # select_best_N_mo and sort_population_mo of the same points (ties in std::sort's order)
+        n = p.shape[0]
+        mo[f"{name}/sort_population"] = ref.sort_population_mo(p)
+        for nb in sorted({1, n // 3, n // 2, n - 1}):
+            mo[f"{name}/select_best_{nb}"] = ref.select_best_n_mo(p, nb)
     np.savez_compressed(HERE / "mo.npz", **mo)
     print("wrote", HERE / "fitness.npz", HERE / "mo.npz")
 

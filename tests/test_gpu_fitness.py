@@ -52,6 +52,11 @@ def test_golden_fitness_and_gradient(ctx, orc):
     for name in names:
         kind, param = (int(v) for v in gold[f"{name}/kind"])
         x = gold[f"{name}/x"]
+        if kind >= N.ACKLEY:  # fitness only, as in the reference
+            f, _ = eval_gpu(ctx, kind, param, x, grad=False)
+            fl, fs = orc.batch_fitness_ld(kind, param, x)
+            assert rel_err(f, gold[f"{name}/f"], fs) <= TOL, (name, rel_err(f, gold[f"{name}/f"], fs))
+            continue
         f, g = eval_gpu(ctx, kind, param, x)
         fl, fs = orc.batch_fitness_ld(kind, param, x)
         assert rel_err(f, gold[f"{name}/f"], fs) <= TOL, (name, rel_err(f, gold[f"{name}/f"], fs))
@@ -325,3 +330,56 @@ def test_rosenbrock_double_float_nonfinite(ctx, orc, double_float):
     fr = orc.batch_fitness(N.ROSENBROCK, 256, x)
     for a, b in zip(f, fr):
         assert (math.isnan(a) and math.isnan(b)) or a == b or abs(a - b) <= 1e-13 * abs(b), (a, b)
+
+
+# ------------------------------------------------- ackley, griewank, schwefel (fitness only)
+
+FITNESS_ONLY = [(N.ACKLEY, "ackley"), (N.GRIEWANK, "griewank"), (N.SCHWEFEL, "schwefel")]
+
+
+@pytest.mark.parametrize("kind,name", FITNESS_ONLY)
+@pytest.mark.parametrize("dim", [1, 2, 3, 7, 31, 32, 33, 50, 255, 1000, 4096])
+def test_fitness_only_problems_dims(ctx, orc, kind, name, dim):
+    check_against_oracle(orc, ctx, kind, dim, W.uniform_batch(kind, dim, 37, seed=dim + 10 * kind), grad=False)
+
+
+def test_fitness_only_known_answers(ctx):
+    # tests/ackley.cpp:53-57, tests/griewank.cpp:52-56, tests/schwefel.cpp:52-56
+    x1, x3 = [1.12], [-23.45, 12.34, 111.12]
+    for cls, k1, k3 in ((P.ackley, 4.659037611351948, 21.941495638130885),
+                        (P.griewank, 0.5646311537232878, 4.241511427781268),
+                        (P.schwefel, 418.0067810680098, 1338.0260195323838)):
+        assert math.isclose(cls(1, ctx).fitness(x1)[0], k1, rel_tol=1e-13)
+        assert math.isclose(cls(3, ctx).fitness(x3)[0], k3, rel_tol=1e-13)
+
+
+def test_fitness_only_problems_have_no_gradient(ctx):
+    for cls in (P.ackley, P.griewank, P.schwefel):
+        udp = cls(4, ctx)
+        with pytest.raises(NotImplementedError):
+            udp.gradient([0.1, 0.2, 0.3, 0.4])
+        # the C ABI refuses too
+        x = np.zeros(4)
+        g = np.empty(4)
+        st = N.lib().pgx_batch_gradient(ctx.handle, udp.kind, 4, N.ptr(x), 1, None, N.ptr(g))
+        assert st == N.ERR_NOTIMPL
+
+
+def test_fitness_only_problems_bounds_and_errors(ctx, orc):
+    for kind, name in FITNESS_ONLY:
+        lb, ub = N.problem_bounds(kind, 5)
+        wl, wu = W.bounds(kind, 5)
+        assert np.array_equal(lb, wl) and np.array_equal(ub, wu)
+        with pytest.raises(ValueError, match="minimum 1 dimension"):
+            P.from_kind(kind, 0, ctx)
+
+
+def test_fitness_only_nonfinite_and_gpu_bfe(ctx, orc):
+    for kind, name in FITNESS_ONLY:
+        x = W.uniform_batch(kind, 9, 4, seed=kind)
+        x[0, 2] = math.nan
+        x[1, 1] = math.inf
+        f = B.gpu_bfe()(B.problem(P.from_kind(kind, 9, ctx)), x.ravel())
+        fr = orc.batch_fitness(kind, 9, x)
+        for a, b in zip(f, fr):
+            assert (math.isnan(a) and math.isnan(b)) or a == b or abs(a - b) <= 1e-12 * (1 + abs(b)), (name, a, b)

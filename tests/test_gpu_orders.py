@@ -169,3 +169,17 @@ def test_nan_and_infinite_objectives(ctx, orc):
     rank, dc, off, idx, cd = MO.nsga2_survival(p, ctx)
     want = orc.fnds(p, dom_list=False)
     assert np.array_equal(cd, orc.nsga2_crowding(p, want["front_offsets"], want["front_indices"]), equal_nan=True)
+
+
+def test_select_and_sort_population_golden(ctx):
+    """The reference's own index lists (tests/golden/gen_golden.py), ties and NaN cases included."""
+    from pathlib import Path
+
+    gold = np.load(Path(__file__).resolve().parent / "golden" / "mo.npz")
+    for name in sorted({k.split("/")[0] for k in gold.files}):
+        p = gold[f"{name}/points"]
+        assert MO.sort_population_mo(p, ctx) == gold[f"{name}/sort_population"].tolist(), name
+        for key in gold.files:
+            if key.startswith(f"{name}/select_best_"):
+                nb = int(key.rsplit("_", 1)[1])
+                assert MO.select_best_N_mo(p, nb, ctx) == gold[key].tolist(), key

@@ -180,3 +180,27 @@ def test_oracle_vs_reference_fresh(orc, ref):
     a, b = orc.fnds(p), ref.fnds(p)
     for key in a:
         assert np.array_equal(a[key], b[key]), key
+
+
+def test_select_and_sort_population_golden(orc, mo):
+    for name in cases(mo):
+        p = mo[f"{name}/points"]
+        assert np.array_equal(orc.sort_population_mo(p), mo[f"{name}/sort_population"]), name
+        for key in mo.files:
+            if key.startswith(f"{name}/select_best_"):
+                nb = int(key.rsplit("_", 1)[1])
+                assert np.array_equal(orc.select_best_n_mo(p, nb), mo[key]), key
+
+
+def test_ackley_griewank_schwefel_known_answers(orc):
+    # tests/ackley.cpp:53-57, tests/griewank.cpp:52-56, tests/schwefel.cpp:52-56
+    x1, x3 = np.array([[1.12]]), np.array([[-23.45, 12.34, 111.12]])
+    for kind, k1, k3 in ((4, 4.659037611351948, 21.941495638130885), (5, 0.5646311537232878, 4.241511427781268),
+                         (6, 418.0067810680098, 1338.0260195323838)):
+        assert math.isclose(orc.batch_fitness(kind, 1, x1)[0], k1, rel_tol=1e-15)
+        assert math.isclose(orc.batch_fitness(kind, 3, x3)[0], k3, rel_tol=1e-15)
+        f1, _ = orc.batch_fitness_ld(kind, 1, x1)
+        f3, _ = orc.batch_fitness_ld(kind, 3, x3)
+        assert math.isclose(f1[0], k1, rel_tol=1e-14) and math.isclose(f3[0], k3, rel_tol=1e-14)
+        with pytest.raises(ValueError, match="gradient"):
+            orc.batch_gradient(kind, 3, x3)
