@@ -38,7 +38,7 @@ namespace
 
 using namespace dev;
 
-enum : uint8_t { kRows = 0, kRows4 = 1, kLJReg = 2, kLJFlat = 3, kRows4FF = 4 };
+enum : uint8_t { kRows = 0, kRows4 = 1, kLJReg = 2, kLJFlat = 3 };
 
 // One warp's unit of work: `rows` consecutive rows of one request.
 struct tile_desc {
@@ -91,11 +91,6 @@ __device__ __forceinline__ void run_tile(const tile_desc &d, double *sm)
                 rosenbrock_row_v4<GRAD>(d.x + static_cast<uint64_t>(r) * d.nx, d.nx, d.f + r,
                                         GRAD ? d.g + static_cast<uint64_t>(r) * d.nx : nullptr);
             break;
-        case kRows4FF: // double-float rows on the FP32 pipe (opt-in)
-            for (uint32_t r = 0; r < d.rows; ++r)
-                rosenbrock_row_v4_ff<GRAD>(d.x + static_cast<uint64_t>(r) * d.nx, d.nx, d.f + r,
-                                           GRAD ? d.g + static_cast<uint64_t>(r) * d.nx : nullptr);
-            break;
         case kLJReg: // at most 32 atoms: one atom per lane
             for (uint32_t r = 0; r < d.rows; ++r)
                 lj_cluster_reg<1, GRAD>(d.x + static_cast<uint64_t>(r) * d.nx, d.param, d.nx, sm, d.f + r,
@@ -110,7 +105,7 @@ __device__ __forceinline__ void run_tile(const tile_desc &d, double *sm)
 }
 
 // Persistent: every warp takes the next tile from the counter until none is left.
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 4)
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
     epoch_kernel(const tile_desc *__restrict__ tiles, uint32_t n_tiles, unsigned *next, uint32_t sm_per_warp)
 {
     extern __shared__ double smem[];
@@ -227,7 +222,7 @@ int tune(pgx_context *ctx, int kind, uint64_t param, uint64_t nx, bool grad, tun
     PGX_CUDA(cudaGetDeviceProperties(&prop, ctx->device));
     std::ostringstream ks;
     ks << kind << ':' << param << ':' << nx << ':' << (grad ? 1 : 0) << ':' << prop.multiProcessorCount << ':'
-       << prop.major << prop.minor << (kind == PGX_ROSENBROCK && rosenbrock_double_float() ? ":ff" : "");
+       << prop.major << prop.minor;
     const std::string key = ks.str();
     {
         std::lock_guard<std::mutex> g(g_tune_lock);
@@ -577,7 +572,7 @@ int build_plan(pgx_epoch *ep, const pgx_request *reqs, int n_reqs)
                 d.ma = 1;
                 d.lanes = 32;
             } else if (p.tune.lanes == 0) {
-                d.variant = rosenbrock_double_float() ? kRows4FF : kRows4;
+                d.variant = kRows4; // FP64 rows (the double-float opt-in is not offered in epochs)
                 d.lanes = 32;
             } else {
                 d.variant = kRows;

@@ -287,11 +287,8 @@ int launch_rows_variant(int kind, uint64_t nx, const double *d_x, uint64_t n, do
     if (lanes == 0) {
         PGX_CHECK(kind == PGX_ROSENBROCK && nx % 4 == 0 && reinterpret_cast<uintptr_t>(d_x) % 16 == 0,
                   PGX_ERR_INVALID, "4-wide rows need rosenbrock, nx % 4 == 0 and aligned rows");
-        if (!rosenbrock_double_float())
-            return grad ? launch_simple(rosenbrock_v4_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
-                        : launch_simple(rosenbrock_v4_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
-        return grad ? launch_simple(rosenbrock_v4ff_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
-                    : launch_simple(rosenbrock_v4ff_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
+        return grad ? launch_simple(rosenbrock_v4_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
+                    : launch_simple(rosenbrock_v4_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
     }
     switch (lanes) {
         case 32: return launch_rows<32>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);
