@@ -14,8 +14,9 @@ step = one batch. Prints one JSON line:
          probe; MEASURED_PEAKS.json has no FP64 figure) plus its HBM fraction
   cpu_baseline  the reference's CPU path (compiled reference where present,
          else the oracle's restatement of thread_bfe + gradient) on the host
-  secondary  the other kernels of the path (rastrigin, lennard_jones, NSGA-II
-         survival) measured the same way
+  secondary  the other kernels of the path (rastrigin, lennard_jones, ackley,
+         griewank, schwefel, NSGA-II survival, select_best_N_mo,
+         sort_population_mo, the fused archipelago epoch) measured the same way
 
 --impl reference times the reference's CPU implementation of the same step
 with every host thread. Multi-GPU (torchrun): every rank evaluates its own
@@ -477,6 +478,8 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops, cpu_ok=True) -> dict:
     fitness_case("rastrigin_f_4096x50", N.RASTRIGIN, 50, W.rastrigin_batch(), False)
     fitness_case("rastrigin_fg_1048576x50", N.RASTRIGIN, 50, W.rastrigin_batch(1 << 20, 50), True)
     fitness_case("rosenbrock_f_65536x1000", N.ROSENBROCK, 1000, W.rosenbrock_batch(), False)
+    for kind, name in ((N.ACKLEY, "ackley"), (N.GRIEWANK, "griewank"), (N.SCHWEFEL, "schwefel")):
+        fitness_case(f"{name}_f_1048576x50", kind, 50, W.uniform_batch(kind, 50, 1 << 20, seed=40 + kind), False)
     lj = W.lj_batch()
     fitness_case("lj_fg_16384x150", N.LENNARD_JONES, 150, lj, True)
     fitness_case("lj_f_16384x150", N.LENNARD_JONES, 150, lj, False)

@@ -34,18 +34,30 @@ __global__ void __launch_bounds__(256) rosenbrock_kernel(const double *__restric
         rosenbrock_row<G, GRAD>(x + row * nx, nx, f ? f + row : nullptr, GRAD ? g + row * nx : nullptr);
 }
 
+// Griewank's per-column square roots kept in shared memory (8 KiB).
+constexpr uint32_t kGriewankRoots = 1024;
+
 // Fitness-only rows of ackley, griewank and schwefel.
 template <int G, int KIND>
 __global__ void __launch_bounds__(256) row_f_kernel(const double *__restrict__ x, uint64_t n, uint32_t nx,
                                                     double *__restrict__ f, double *__restrict__ g)
 {
     const uint64_t stride = static_cast<uint64_t>(gridDim.x) * (blockDim.x / G);
+    [[maybe_unused]] uint32_t n_root = 0;
+    [[maybe_unused]] const double *root = nullptr;
+    if constexpr (KIND == PGX_GRIEWANK) {
+        __shared__ double roots[kGriewankRoots];
+        n_root = nx < kGriewankRoots ? nx : kGriewankRoots;
+        for (uint32_t i = threadIdx.x; i < n_root; i += blockDim.x) roots[i] = sqrt(static_cast<double>(i) + 1.0);
+        __syncthreads();
+        root = roots;
+    }
     for (uint64_t row = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / G; row < n; row += stride) {
         double *fo = f ? f + row : nullptr;
         if constexpr (KIND == PGX_ACKLEY)
             ackley_row<G>(x + row * nx, nx, fo);
         else if constexpr (KIND == PGX_GRIEWANK)
-            griewank_row<G>(x + row * nx, nx, fo);
+            griewank_row<G>(x + row * nx, nx, fo, root, n_root);
         else
             schwefel_row<G>(x + row * nx, nx, fo);
     }

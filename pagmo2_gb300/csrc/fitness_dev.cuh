@@ -378,8 +378,11 @@ __device__ __forceinline__ void ackley_row(const double *__restrict__ xr, uint32
 
 // f = sum x^2 / 4000 - prod cos(x_i / sqrt(i + 1)) + 1 (src/problems/griewank.cpp:62-76);
 // the division and square root are correctly rounded as in the reference.
+// sqrt(i + 1) depends on the column only: `root` holds it (the same correctly
+// rounded value) for the first `n_root` columns, computed once per block.
 template <int G>
-__device__ __forceinline__ void griewank_row(const double *__restrict__ xr, uint32_t nx, double *f_out)
+__device__ __forceinline__ void griewank_row(const double *__restrict__ xr, uint32_t nx, double *f_out,
+                                             const double *root = nullptr, uint32_t n_root = 0)
 {
     const unsigned sub = threadIdx.x & (G - 1);
     const unsigned mask = group_mask<G>();
@@ -387,7 +390,8 @@ __device__ __forceinline__ void griewank_row(const double *__restrict__ xr, uint
     for (uint32_t i = sub; i < nx; i += G) {
         const double xi = __ldg(xr + i);
         s = fma(xi, xi, s);
-        p *= cos(xi / sqrt(static_cast<double>(i) + 1.0));
+        const double r = i < n_root ? root[i] : sqrt(static_cast<double>(i) + 1.0);
+        p *= cos(xi / r);
     }
     s = group_sum<G>(s, mask);
     p = group_prod<G>(p, mask);

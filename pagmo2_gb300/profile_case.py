@@ -11,6 +11,7 @@ profiler are not benchmark values). Cases:
   rastrigin_fg / rastrigin_f    dim 50 (--dim)
   rosenbrock_fg / rosenbrock_f  dim 1000 (--dim)
   lj_fg / lj_f                  150 atoms (--atoms)
+  ackley_f / griewank_f / schwefel_f   dim 50 (--dim), fitness only
   survival                      NSGA-II survival of --rows nested-front points x 3
   select_best                   select_best_N_mo(--rows nested-front points x 3, rows / 2)
   sort_population               sort_population_mo(--rows nested-front points x 3)
@@ -85,6 +86,9 @@ def main() -> None:
             "rastrigin": (N.RASTRIGIN, a.dim or 50, lambda: W.rastrigin_batch(n, a.dim or 50)),
             "rosenbrock": (N.ROSENBROCK, a.dim or 1000, lambda: W.rosenbrock_batch(n, a.dim or 1000)),
             "lj": (N.LENNARD_JONES, a.atoms, lambda: W.lj_batch(n, a.atoms)),
+            "ackley": (N.ACKLEY, a.dim or 50, lambda: W.uniform_batch(N.ACKLEY, a.dim or 50, n, 44)),
+            "griewank": (N.GRIEWANK, a.dim or 50, lambda: W.uniform_batch(N.GRIEWANK, a.dim or 50, n, 45)),
+            "schwefel": (N.SCHWEFEL, a.dim or 50, lambda: W.uniform_batch(N.SCHWEFEL, a.dim or 50, n, 46)),
         }[name]
         x = x()
         dx = torch.from_numpy(x).cuda()
