@@ -480,6 +480,25 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops, cpu_ok=True) -> dict:
     fitness_case("rosenbrock_f_65536x1000", N.ROSENBROCK, 1000, W.rosenbrock_batch(), False)
     for kind, name in ((N.ACKLEY, "ackley"), (N.GRIEWANK, "griewank"), (N.SCHWEFEL, "schwefel")):
         fitness_case(f"{name}_f_1048576x50", kind, 50, W.uniform_batch(kind, 50, 1 << 20, seed=40 + kind), False)
+    # ZDT / DTLZ: n x nobj objective rows
+    import ctypes as C
+
+    def mo_case(name, kind, pid, param, n, fdim=0):
+        spec = N.mo_problem(kind, pid, param, fdim, 100)
+        nx, nobj, _ = N.mo_problem_dims(spec)
+        dx = torch.from_numpy(W.mo_uniform_batch(kind, pid, param, n, seed=50 + pid, fdim=fdim)).cuda()
+        df = torch.empty((n, nobj), dtype=torch.float64, device="cuda")
+
+        def fn():
+            N.check(L.pgx_mo_batch_fitness_device(ctx.handle, C.byref(spec), dx.data_ptr(), n, df.data_ptr(), sp))
+        ms = timed(fn)
+        bytes_ = n * (nx + nobj) * 8
+        out[name] = {"evals_per_s": n / (ms * 1e-3), "ms": ms, "hbm_gbs": bytes_ / (ms * 1e-3) / 1e9}
+
+    for pid in (1, 4, 6):
+        mo_case(f"zdt{pid}_f_1048576x30", N.ZDT, pid, 30, 1 << 20)
+    for pid in (1, 2, 4, 6, 7):
+        mo_case(f"dtlz{pid}_f_1048576x12_m3", N.DTLZ, pid, 12, 1 << 20, fdim=3)
     lj = W.lj_batch()
     fitness_case("lj_fg_16384x150", N.LENNARD_JONES, 150, lj, True)
     fitness_case("lj_f_16384x150", N.LENNARD_JONES, 150, lj, False)
@@ -543,6 +562,35 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops, cpu_ok=True) -> dict:
     def sortpop():
         N.check(L.pgx_sort_population_mo_device(ctx.handle, dp.data_ptr(), n, m, sel.data_ptr(), st.data_ptr(), sp))
     out["select_best_N_mo_20000x3_N10000"] = {"ms": timed(select, reps=10, flush_l2=False)}
+
+    # One NSGA-II generation's evaluate-and-select on ZDT1 (30 variables): the
+    # merged 2 NP = 20000 offspring and parents evaluated (nsga2.cpp:253,
+    # bfe) and the next NP = 10000 selected (nsga2.cpp:300, select_best_N_mo),
+    # device resident, beside the reference doing the same on the CPU.
+    zspec = N.mo_problem(N.ZDT, 1, 30)
+    zx = W.mo_uniform_batch(N.ZDT, 1, 30, n, seed=61)
+    dzx = torch.from_numpy(zx).cuda()
+    dzf = torch.empty((n, 2), dtype=torch.float64, device="cuda")
+
+    def generation():
+        N.check(L.pgx_mo_batch_fitness_device(ctx.handle, C.byref(zspec), dzx.data_ptr(), n, dzf.data_ptr(), sp))
+        N.check(L.pgx_select_best_n_mo_device(ctx.handle, dzf.data_ptr(), n, 2, n // 2, sel.data_ptr(),
+                                              st.data_ptr(), sp))
+    gen = {"ms": timed(generation, reps=10, flush_l2=False)}
+    if cpu_ok:
+        import oracle
+
+        ref = oracle.reference()
+        t = time.perf_counter()
+        if ref is not None:
+            ref.select_best_n_mo(ref.mo_thread_bfe((N.ZDT, 1, 30), zx), n // 2)
+        else:
+            orc = oracle.oracle()
+            orc.select_best_n_mo(orc.mo_fitness((N.ZDT, 1, 30), zx), n // 2)
+        gen["cpu_ms"] = (time.perf_counter() - t) * 1e3
+        gen["cpu_kind"] = "reference" if ref is not None else "port"
+        gen["note"] = "CPU: fitness on every host thread, select_best_N_mo single-threaded, as in the reference"
+    out["nsga2_generation_zdt1_20000x30"] = gen
     out["sort_population_mo_20000x3"] = {"ms": timed(sortpop, reps=10, flush_l2=False)}
     out["archipelago_64_islands"] = run_archipelago(ctx, L, N, W, stream)
     return out

@@ -1,6 +1,7 @@
 // gpu_bfe: a user-defined batch fitness evaluator (UDBFE) for pagmo::bfe
 // that evaluates pagmo's own rastrigin, rosenbrock, lennard_jones, ackley,
-// griewank and schwefel UDPs, and the GPU UDPs of gpu_problems.hpp, on a GB300.
+// griewank, schwefel, zdt and dtlz UDPs (DTLZ4 excepted), and the GPU UDPs of
+// gpu_problems.hpp, on a GB300.
 //
 // A UDBFE is a callable vector_double(const problem &, const vector_double &)
 // (include/pagmo/bfe.hpp:68-108). Like every UDBFE it leaves the fevals
@@ -18,11 +19,13 @@
 #include <pagmo/bfe.hpp>
 #include <pagmo/problem.hpp>
 #include <pagmo/problems/ackley.hpp>
+#include <pagmo/problems/dtlz.hpp>
 #include <pagmo/problems/griewank.hpp>
 #include <pagmo/problems/lennard_jones.hpp>
 #include <pagmo/problems/rastrigin.hpp>
 #include <pagmo/problems/rosenbrock.hpp>
 #include <pagmo/problems/schwefel.hpp>
+#include <pagmo/problems/zdt.hpp>
 #include <pagmo/threading.hpp>
 #include <pagmo/types.hpp>
 
@@ -45,6 +48,9 @@ public:
         if (const auto *g = p.extract<gpu_ackley>()) return g->batch_fitness(dvs);
         if (const auto *g = p.extract<gpu_griewank>()) return g->batch_fitness(dvs);
         if (const auto *g = p.extract<gpu_schwefel>()) return g->batch_fitness(dvs);
+        if (const auto *g = p.extract<gpu_zdt>()) return g->batch_fitness(dvs);
+        if (const auto *g = p.extract<gpu_dtlz>()) return g->batch_fitness(dvs);
+        if (p.extract<pagmo::zdt>() || p.extract<pagmo::dtlz>()) return mo_fitness(p, dvs);
         int kind = 0;
         std::uint64_t param = p.get_nx();
         if (p.extract<pagmo::rastrigin>()) {
@@ -62,8 +68,8 @@ public:
             kind = PGX_SCHWEFEL;
         } else {
             throw std::invalid_argument("Cannot use a gpu_bfe on the problem '" + p.get_name()
-                                        + "': only rastrigin, rosenbrock, lennard_jones, ackley, griewank and "
-                                          "schwefel are evaluated on the GPU");
+                                        + "': only rastrigin, rosenbrock, lennard_jones, ackley, griewank, "
+                                          "schwefel, zdt and dtlz are evaluated on the GPU");
         }
         const std::uint64_t n = dvs.size() / p.get_nx(); // pagmo::bfe checked divisibility
         pagmo::vector_double fvs(n);
@@ -74,6 +80,32 @@ public:
     std::string get_name() const
     {
         return "GB300 batch fitness evaluator";
+    }
+    // pagmo's zdt and dtlz: the problem id comes from get_name() ("ZDT3",
+    // zdt.cpp:164-167; "DTLZ2", dtlz.cpp:169-172), the parameters from the
+    // dimensions. DTLZ4's alpha is not readable through pagmo's public
+    // interface, so pagmo::dtlz{4, ...} is refused (gpu_dtlz carries it).
+    pagmo::vector_double mo_fitness(const pagmo::problem &p, const pagmo::vector_double &dvs) const
+    {
+        pgx_mo_problem mp{};
+        const std::string name = p.get_name();
+        const bool is_zdt = p.extract<pagmo::zdt>() != nullptr;
+        mp.kind = is_zdt ? PGX_ZDT : PGX_DTLZ;
+        mp.prob_id = static_cast<std::uint32_t>(std::stoul(name.substr(is_zdt ? 3u : 4u)));
+        if (is_zdt) {
+            mp.param = mp.prob_id == 5u ? (p.get_nx() - 30u) / 5u + 1u : p.get_nx();
+        } else {
+            if (mp.prob_id == 4u)
+                throw std::invalid_argument("Cannot use a gpu_bfe on pagmo's DTLZ4: its alpha is not exposed by "
+                                            "the problem; use pagmo_gb300::gpu_dtlz{4, dim, fdim, alpha}");
+            mp.param = p.get_nx();
+            mp.fdim = p.get_nobj();
+            mp.alpha = 100u;
+        }
+        const std::uint64_t n = dvs.size() / p.get_nx(); // pagmo::bfe checked divisibility
+        pagmo::vector_double fvs(n * p.get_nobj());
+        if (n) check(pgx_mo_batch_fitness(device_context(m_device), &mp, dvs.data(), n, fvs.data()));
+        return fvs;
     }
 
     std::string get_extra_info() const

@@ -1,7 +1,7 @@
-// GPU-backed user-defined problems for pagmo: the rastrigin, rosenbrock and
-// lennard_jones UDPs (src/problems/{rastrigin,rosenbrock,lennard_jones}.cpp)
-// with the same dimensions, bounds, names and constructor errors, whose
-// evaluations run on a GB300 through libpgx.
+// GPU-backed user-defined problems for pagmo: the rastrigin, rosenbrock,
+// lennard_jones, ackley, griewank, schwefel, zdt and dtlz UDPs
+// (src/problems/*.cpp) with the same dimensions, bounds, names and
+// constructor errors, whose evaluations run on a GB300 through libpgx.
 //
 // Besides fitness/get_bounds (the UDP minimum, include/pagmo/problem.hpp:436-448)
 // they provide batch_fitness, which member_bfe and default_bfe pick
@@ -16,6 +16,7 @@
 #include <utility>
 #include <vector>
 
+#include <pagmo/population.hpp>
 #include <pagmo/problem.hpp>
 #include <pagmo/threading.hpp>
 #include <pagmo/types.hpp>
@@ -216,6 +217,160 @@ public:
     }
 };
 
+namespace detail
+{
+
+// ZDT / DTLZ on the GPU: fitness vectors of nobj objectives, batch_fitness in
+// pagmo's fvs layout (n rows of nobj), p_distance of a vector or the mean over
+// a population (src/problems/zdt.cpp:179-224, src/problems/dtlz.cpp:131-163).
+class gpu_mo_udp
+{
+public:
+    gpu_mo_udp() = default;
+    gpu_mo_udp(int kind, unsigned prob_id, std::uint64_t param, std::uint64_t fdim, unsigned alpha, int device)
+        : m_device(device)
+    {
+        m_p.kind = kind;
+        m_p.prob_id = prob_id;
+        m_p.param = param;
+        m_p.fdim = fdim;
+        m_p.alpha = alpha;
+        check(pgx_mo_problem_dims(&m_p, &m_nx, &m_nobj, &m_nix)); // the reference constructors' checks
+    }
+    pagmo::vector_double fitness(const pagmo::vector_double &x) const
+    {
+        return batch_fitness(x);
+    }
+    pagmo::vector_double batch_fitness(const pagmo::vector_double &dvs) const
+    {
+        const std::uint64_t n = rows(dvs);
+        pagmo::vector_double f(n * m_nobj);
+        if (n) check(pgx_mo_batch_fitness(device_context(m_device), &m_p, dvs.data(), n, f.data()));
+        return f;
+    }
+    pagmo::vector_double::size_type get_nobj() const
+    {
+        return m_nobj;
+    }
+    std::pair<pagmo::vector_double, pagmo::vector_double> get_bounds() const
+    {
+        std::pair<pagmo::vector_double, pagmo::vector_double> b{pagmo::vector_double(m_nx),
+                                                                pagmo::vector_double(m_nx)};
+        check(pgx_mo_problem_bounds(&m_p, b.first.data(), b.second.data()));
+        return b;
+    }
+    pagmo::thread_safety get_thread_safety() const
+    {
+        return pagmo::thread_safety::constant;
+    }
+    // p_distance of every row of a batch.
+    pagmo::vector_double batch_p_distance(const pagmo::vector_double &dvs) const
+    {
+        const std::uint64_t n = rows(dvs);
+        pagmo::vector_double out(n);
+        if (n) check(pgx_mo_p_distance(device_context(m_device), &m_p, dvs.data(), n, out.data()));
+        return out;
+    }
+    // Mean p_distance over the population, summed in row order as the reference does.
+    double p_distance(const pagmo::population &pop) const
+    {
+        pagmo::vector_double flat;
+        flat.reserve(pop.size() * m_nx);
+        for (const auto &x : pop.get_x()) flat.insert(flat.end(), x.begin(), x.end());
+        const auto d = batch_p_distance(flat);
+        double c = 0.0;
+        for (double v : d) c += v;
+        return c / static_cast<double>(pop.size());
+    }
+    template <typename Archive>
+    void serialize(Archive &ar, unsigned)
+    {
+        ar &m_p.kind;
+        ar &m_p.prob_id;
+        ar &m_p.param;
+        ar &m_p.fdim;
+        ar &m_p.alpha;
+        ar &m_nx;
+        ar &m_nobj;
+        ar &m_nix;
+        ar &m_device;
+    }
+
+protected:
+    std::uint64_t rows(const pagmo::vector_double &dvs) const
+    {
+        if (m_nx == 0 || dvs.size() % m_nx)
+            throw std::invalid_argument("Invalid argument for a batch fitness evaluation: the length of the vector "
+                                        "representing the decision vectors, "
+                                        + std::to_string(dvs.size())
+                                        + ", is not an exact multiple of the dimension of the problem, "
+                                        + std::to_string(m_nx));
+        return dvs.size() / m_nx;
+    }
+    pgx_mo_problem m_p{};
+    std::uint64_t m_nx = 0, m_nobj = 0, m_nix = 0;
+    int m_device = 0;
+};
+
+} // namespace detail
+
+// zdt{prob_id, param}: the six two-objective ZDT problems (src/problems/zdt.cpp);
+// param is the dimension, except for ZDT5, whose 30 + 5 (param - 1) bits it counts.
+class gpu_zdt : public detail::gpu_mo_udp
+{
+public:
+    explicit gpu_zdt(unsigned prob_id = 1u, unsigned param = 30u, int device = 0)
+        : gpu_mo_udp(PGX_ZDT, prob_id, param, 0u, 0u, device)
+    {
+    }
+    std::string get_name() const
+    {
+        return "ZDT" + std::to_string(m_p.prob_id);
+    }
+    pagmo::vector_double::size_type get_nix() const
+    {
+        return m_nix;
+    }
+    using gpu_mo_udp::p_distance;
+    // zdt.cpp:204-224 does not check the size of x: the metric of a vector of
+    // another length is that of the same ZDT problem at that length.
+    double p_distance(const pagmo::vector_double &x) const
+    {
+        if (x.size() == m_nx) return batch_p_distance(x)[0];
+        if (m_p.prob_id == 5u) {
+            if (x.size() < 30u) throw std::invalid_argument("a ZDT5 decision vector has at least 30 entries");
+            const gpu_zdt other(5u, static_cast<unsigned>((x.size() - 30u) / 5u + 1u), m_device);
+            return other.batch_p_distance(pagmo::vector_double(x.begin(), x.begin() + other.m_nx))[0];
+        }
+        return gpu_zdt(m_p.prob_id, static_cast<unsigned>(x.size()), m_device).batch_p_distance(x)[0];
+    }
+};
+
+// dtlz{prob_id, dim, fdim, alpha}: the seven scalable DTLZ problems on [0, 1]^dim
+// (src/problems/dtlz.cpp).
+class gpu_dtlz : public detail::gpu_mo_udp
+{
+public:
+    explicit gpu_dtlz(unsigned prob_id = 1u, pagmo::vector_double::size_type dim = 5u,
+                      pagmo::vector_double::size_type fdim = 3u, unsigned alpha = 100u, int device = 0)
+        : gpu_mo_udp(PGX_DTLZ, prob_id, dim, fdim, alpha, device)
+    {
+    }
+    std::string get_name() const
+    {
+        return "DTLZ" + std::to_string(m_p.prob_id);
+    }
+    using gpu_mo_udp::p_distance;
+    double p_distance(const pagmo::vector_double &x) const
+    {
+        // dtlz.cpp:156-163
+        if (x.size() != m_nx)
+            throw std::invalid_argument("The size of the decision vector should be " + std::to_string(m_nx)
+                                        + " while " + std::to_string(x.size()) + " was detected");
+        return batch_p_distance(x)[0];
+    }
+};
+
 } // namespace pagmo_gb300
 
 // Registration with pagmo's Boost.Serialization machinery (include/pagmo/problem.hpp:67-76):
@@ -226,5 +381,7 @@ PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_lennard_jones)
 PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_ackley)
 PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_griewank)
 PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_schwefel)
+PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_zdt)
+PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_dtlz)
 
 #endif

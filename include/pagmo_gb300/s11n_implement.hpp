@@ -16,5 +16,7 @@ PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_lennard_jones)
 PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_ackley)
 PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_griewank)
 PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_schwefel)
+PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_zdt)
+PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_dtlz)
 
 #endif

@@ -11,8 +11,10 @@
  *
  * Conventions
  *  - Decision vectors are row-major: n_dvs rows of nx doubles, exactly the
- *    layout pagmo::bfe receives (src/problem.cpp:383-392). Fitness vectors are
- *    n_dvs doubles (all three problems are single-objective, nf = 1).
+ *    layout pagmo::bfe receives (src/problem.cpp:383-392). Fitness vectors of
+ *    the single-objective kinds are n_dvs doubles (nf = 1); those of the
+ *    multi-objective ZDT and DTLZ problems (pgx_mo_*) are n_dvs rows of nobj
+ *    doubles, again pagmo's fvs layout.
  *    Gradients are dense, n_dvs rows of nx doubles: for nf = 1 this is the
  *    layout of problem::gradient (src/problem.cpp:456-467, dense sparsity).
  *  - Problems: PGX_RASTRIGIN (param = dim >= 1), PGX_ROSENBROCK (param =
@@ -64,6 +66,8 @@ extern "C" {
 #define PGX_ACKLEY 4        /* src/problems/ackley.cpp (fitness only) */
 #define PGX_GRIEWANK 5      /* src/problems/griewank.cpp (fitness only) */
 #define PGX_SCHWEFEL 6      /* src/problems/schwefel.cpp (fitness only) */
+#define PGX_ZDT 7           /* src/problems/zdt.cpp (multi-objective, pgx_mo_*) */
+#define PGX_DTLZ 8          /* src/problems/dtlz.cpp (multi-objective, pgx_mo_*) */
 
 typedef struct pgx_context pgx_context;
 typedef struct pgx_epoch pgx_epoch;
@@ -120,6 +124,46 @@ PGX_API int pgx_batch_gradient(pgx_context *ctx, int kind, uint64_t param, const
    d_fvs may be NULL when d_grads is not. Asynchronous on `stream`. */
 PGX_API int pgx_batch_eval_device(pgx_context *ctx, int kind, uint64_t param, const double *d_dvs, uint64_t n_dvs,
                           double *d_fvs, double *d_grads, void *stream);
+
+/* ------------------------------------- multi-objective test problems (ZDT, DTLZ) */
+
+/* A ZDT or DTLZ problem as its reference constructor takes it:
+   zdt(prob_id, param) (src/problems/zdt.cpp:55-66; param is the dimension,
+   except for ZDT5 whose 30 + 5 (param - 1) bits it counts) and
+   dtlz(prob_id, dim, fdim, alpha) (src/problems/dtlz.cpp:53-74; pagmo's
+   defaults are dim 5, fdim 3, alpha 100). */
+typedef struct pgx_mo_problem {
+    int kind;         /* PGX_ZDT or PGX_DTLZ */
+    uint32_t prob_id; /* ZDT 1-6, DTLZ 1-7 */
+    uint64_t param;   /* ZDT: param; DTLZ: dim */
+    uint64_t fdim;    /* DTLZ: number of objectives (>= 2, < dim); ignored for ZDT */
+    uint32_t alpha;   /* DTLZ4's exponent; ignored otherwise */
+} pgx_mo_problem;
+
+/* get_nx / get_nobj / get_nix of the problem (zdt.cpp:108-158, zdt.hpp:154-157,
+   dtlz.cpp:116-119, dtlz.hpp:116-119); validates it with the constructors'
+   messages (PGX_ERR_INVALID). Any output pointer may be NULL. */
+PGX_API int pgx_mo_problem_dims(const pgx_mo_problem *p, uint64_t *nx, uint64_t *nobj, uint64_t *nix);
+
+/* Box bounds, nx doubles each (zdt.cpp:108-133, dtlz.cpp:116-119). */
+PGX_API int pgx_mo_problem_bounds(const pgx_mo_problem *p, double *lb, double *ub);
+
+/* Batch fitness, host buffers: dvs n_dvs*nx, fvs n_dvs*nobj (row i holds
+   fitness(dv_i), zdt.cpp:76-100, dtlz.cpp:84-107). Replaces the fitness loop
+   of bfe{thread_bfe{}} / member_bfe for these problems; touches no fevals. */
+PGX_API int pgx_mo_batch_fitness(pgx_context *ctx, const pgx_mo_problem *p, const double *dvs, uint64_t n_dvs,
+                                 double *fvs);
+
+/* Device-resident variant, asynchronous on `stream`: d_fvs n_dvs*nobj, for
+   example the points of a following pgx_nsga2_survival_device call. */
+PGX_API int pgx_mo_batch_fitness_device(pgx_context *ctx, const pgx_mo_problem *p, const double *d_dvs,
+                                        uint64_t n_dvs, double *d_fvs, void *stream);
+
+/* p_distance(dv) of every row (zdt.cpp:204-224, dtlz.cpp:156-163): out
+   n_dvs doubles. p_distance(population) is their mean, summed in row order
+   (zdt.cpp:179-187, dtlz.cpp:131-139). */
+PGX_API int pgx_mo_p_distance(pgx_context *ctx, const pgx_mo_problem *p, const double *dvs, uint64_t n_dvs,
+                              double *out);
 
 /* --------------------------------------------------- NSGA-II survival (MO) */
 

@@ -50,6 +50,12 @@ def _pts2d(pts):
     return p
 
 
+def _mo_spec(spec):
+    """(family, prob_id, param, fdim, alpha) with defaults for the missing tail."""
+    t = tuple(spec) + (0, 0, 0, 0, 0)[len(spec):]
+    return int(t[0]), int(t[1]), int(t[2]), int(t[3]), int(t[4])
+
+
 class _Oracle:
     def __init__(self, path: Path):
         self.h = C.CDLL(str(path))
@@ -84,6 +90,14 @@ class _Oracle:
         h.orc_quicksort_adversary.restype = None
         h.orc_select_best_n_mo.argtypes = [_vp, _u64, _u64, _u64, _vp, _vp]
         h.orc_sort_population_mo.argtypes = [_vp, _u64, _u64, _vp]
+        h.orc_mo_last_error.restype = C.c_char_p
+        h.orc_zdt_p_distance.restype = C.c_double
+        h.orc_zdt_p_distance.argtypes = [C.c_uint, _vp, _u64]
+        h.orc_mo_dims.argtypes = [C.c_int, C.c_uint, _u64, _u64, _vp, _vp]
+        h.orc_mo_batch_fitness.argtypes = [C.c_int, C.c_uint, _u64, _u64, C.c_uint, _vp, _u64, _u64, _vp, C.c_int]
+        h.orc_mo_batch_fitness_ld.argtypes = [C.c_int, C.c_uint, _u64, _u64, C.c_uint, _vp, _u64, _u64, _vp, _vp,
+                                              C.c_int]
+        h.orc_mo_batch_p_distance.argtypes = [C.c_int, C.c_uint, _u64, _u64, _vp, _u64, _u64, _vp, _vp, C.c_int]
 
     def _chk(self, st):
         if st != 0:
@@ -207,6 +221,49 @@ class _Oracle:
         self._chk_sort(self.h.orc_sort_population_mo(_p(p), n, m, _p(out)))
         return out[:n].astype(np.int64)
 
+    # ZDT / DTLZ ------------------------------------------------------------------
+    # spec = (family, prob_id, param, fdim, alpha): family 7 = zdt{prob_id, param},
+    # family 8 = dtlz{prob_id, dim=param, fdim, alpha} (the GPU library's kinds).
+    def _chk_mo(self, st):
+        if st != 0:
+            raise ValueError(self.h.orc_mo_last_error().decode())
+
+    def mo_dims(self, spec):
+        fam, pid, param, fdim, _ = _mo_spec(spec)
+        nx, nobj = C.c_uint64(), C.c_uint64()
+        self._chk_mo(self.h.orc_mo_dims(fam, pid, param, fdim, C.byref(nx), C.byref(nobj)))
+        return nx.value, nobj.value
+
+    def mo_fitness(self, spec, dvs, threads=0):
+        """Mirror of the reference's fitness over the rows: n x nobj."""
+        fam, pid, param, fdim, alpha = _mo_spec(spec)
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        n, nx = x.shape
+        f = np.empty((n, self.mo_dims(spec)[1]))
+        self._chk_mo(self.h.orc_mo_batch_fitness(fam, pid, param, fdim, alpha, _p(x), n, nx, _p(f), threads))
+        return f
+
+    def mo_fitness_ld(self, spec, dvs, threads=0):
+        """(values, error scales), long double, n x nobj each."""
+        fam, pid, param, fdim, alpha = _mo_spec(spec)
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        n, nx = x.shape
+        nobj = self.mo_dims(spec)[1]
+        f, sc = np.empty((n, nobj)), np.empty((n, nobj))
+        self._chk_mo(self.h.orc_mo_batch_fitness_ld(fam, pid, param, fdim, alpha, _p(x), n, nx, _p(f), _p(sc),
+                                                    threads))
+        return f, sc
+
+    def mo_p_distance(self, spec, dvs, ld=False, threads=0):
+        """p_distance of every row (mirror), or (values, scales) in long double."""
+        fam, pid, param, fdim, _ = _mo_spec(spec)
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        n, nx = x.shape
+        out = np.empty(n)
+        sc = np.empty(n) if ld else None
+        self._chk_mo(self.h.orc_mo_batch_p_distance(fam, pid, param, fdim, _p(x), n, nx, _p(out), _p(sc), threads))
+        return (out, sc) if ld else out
+
 
 class _Reference:
     """The reference's own compiled sources (only where they were built)."""
@@ -227,6 +284,11 @@ class _Reference:
         h.ref_pareto_dominance.argtypes = [_vp, _vp, _u64, _vp]
         h.ref_select_best_n_mo.argtypes = [_vp, _u64, _u64, _u64, _vp, _vp]
         h.ref_sort_population_mo.argtypes = [_vp, _u64, _u64, _vp]
+        mo = [C.c_int, C.c_uint, _u64, _u64, C.c_uint]
+        h.ref_mo_dims.argtypes = mo + [_vp, _vp, _vp]
+        h.ref_mo_bounds.argtypes = mo + [_vp, _vp]
+        h.ref_mo_thread_bfe.argtypes = mo + [_vp, _u64, _u64, _vp]
+        h.ref_mo_p_distance.argtypes = mo + [_vp, _u64, _u64, _vp]
 
     def _chk(self, st):
         if st == 1:
@@ -325,6 +387,33 @@ class _Reference:
         r = C.c_int()
         self._chk(self.h.ref_pareto_dominance(_p(a), _p(b), a.size, C.byref(r)))
         return bool(r.value)
+
+    # ZDT / DTLZ (spec as in the oracle) ---------------------------------------------
+    def mo_dims(self, spec):
+        """(nx, nobj, nix) of the constructed reference problem."""
+        nx, nobj, nix = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self._chk(self.h.ref_mo_dims(*_mo_spec(spec), C.byref(nx), C.byref(nobj), C.byref(nix)))
+        return nx.value, nobj.value, nix.value
+
+    def mo_bounds(self, spec):
+        nx = self.mo_dims(spec)[0]
+        lb, ub = np.empty(nx), np.empty(nx)
+        self._chk(self.h.ref_mo_bounds(*_mo_spec(spec), _p(lb), _p(ub)))
+        return lb, ub
+
+    def mo_thread_bfe(self, spec, dvs):
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        n, nx = x.shape
+        f = np.empty((n, self.mo_dims(spec)[1]))
+        self._chk(self.h.ref_mo_thread_bfe(*_mo_spec(spec), _p(x), n, nx, _p(f)))
+        return f
+
+    def mo_p_distance(self, spec, dvs):
+        x = np.ascontiguousarray(dvs, dtype=np.float64)
+        n, nx = x.shape
+        out = np.empty(n)
+        self._chk(self.h.ref_mo_p_distance(*_mo_spec(spec), _p(x), n, nx, _p(out)))
+        return out
 
 
 _oracle = None

@@ -6,6 +6,7 @@
 // multiply-adds (the reference is compiled the same way by oracle/Makefile,
 // and x86-64 builds of pagmo never contract without -mfma).
 #include "oracle.h"
+#include "rows.hpp"
 
 #include <algorithm>
 #include <cfloat>
@@ -20,6 +21,9 @@
 
 namespace
 {
+using orc_detail::parallel_rows;
+using orc_detail::resolve_threads;
+
 thread_local std::string g_err;
 
 // The reference's pi (include/pagmo/detail/constants.hpp:37-40) and its
@@ -73,35 +77,6 @@ inline bool dominates(const double *a, const double *b, uint64_t m)
         if (lt_f(a[i], b[i])) strict = true;
     }
     return strict;
-}
-
-int resolve_threads(int nthreads)
-{
-    if (nthreads > 0) return nthreads;
-    unsigned h = std::thread::hardware_concurrency();
-    return h ? static_cast<int>(h) : 1;
-}
-
-// Static partition of [0, n) over nthreads std::threads (the stand-in for the
-// TBB parallel_for of src/batch_evaluators/thread_bfe.cpp:125-137).
-template <typename F>
-void parallel_rows(uint64_t n, int nthreads, F &&body)
-{
-    uint64_t nt = static_cast<uint64_t>(resolve_threads(nthreads));
-    if (nt > n) nt = n;
-    if (nt <= 1u) {
-        if (n) body(uint64_t(0), n);
-        return;
-    }
-    std::vector<std::thread> pool;
-    const uint64_t chunk = n / nt, rem = n % nt;
-    uint64_t b = 0;
-    for (uint64_t t = 0; t < nt; ++t) {
-        const uint64_t e = b + chunk + (t < rem ? 1u : 0u);
-        pool.emplace_back([&body, b, e]() { body(b, e); });
-        b = e;
-    }
-    for (auto &th : pool) th.join();
 }
 
 bool check_kind(int kind, uint64_t param, uint64_t nx)

@@ -110,6 +110,20 @@ void orc_quicksort_adversary(uint64_t n, long long *out);
 int orc_select_best_n_mo(const double *pts, uint64_t n, uint64_t m, uint64_t N, uint64_t *out, uint64_t *n_out);
 int orc_sort_population_mo(const double *pts, uint64_t n, uint64_t m, uint64_t *out);
 
+/* ---- ZDT (family 7) and DTLZ (family 8) multi-objective problems (mo_problems.cpp) ---- */
+const char *orc_mo_last_error(void);
+int orc_mo_dims(int family, unsigned prob_id, uint64_t param, uint64_t fdim, uint64_t *nx, uint64_t *nobj);
+void orc_zdt_fitness(unsigned prob_id, const double *x, uint64_t n, double *f);
+double orc_zdt_p_distance(unsigned prob_id, const double *x, uint64_t n);
+void orc_dtlz_fitness(unsigned prob_id, uint64_t fdim, unsigned alpha, const double *x, uint64_t n, double *f);
+double orc_dtlz_p_distance(unsigned prob_id, uint64_t fdim, const double *x, uint64_t n);
+int orc_mo_batch_fitness(int family, unsigned prob_id, uint64_t param, uint64_t fdim, unsigned alpha,
+                         const double *dvs, uint64_t n, uint64_t nx, double *f, int nthreads);
+int orc_mo_batch_fitness_ld(int family, unsigned prob_id, uint64_t param, uint64_t fdim, unsigned alpha,
+                            const double *dvs, uint64_t n, uint64_t nx, double *f, double *scale, int nthreads);
+int orc_mo_batch_p_distance(int family, unsigned prob_id, uint64_t param, uint64_t fdim, const double *dvs,
+                            uint64_t n, uint64_t nx, double *out, double *scale, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,11 +17,13 @@
 #include <pagmo/bfe.hpp>
 #include <pagmo/problem.hpp>
 #include <pagmo/problems/ackley.hpp>
+#include <pagmo/problems/dtlz.hpp>
 #include <pagmo/problems/griewank.hpp>
 #include <pagmo/problems/lennard_jones.hpp>
 #include <pagmo/problems/rastrigin.hpp>
 #include <pagmo/problems/rosenbrock.hpp>
 #include <pagmo/problems/schwefel.hpp>
+#include <pagmo/problems/zdt.hpp>
 #include <pagmo/utils/multi_objective.hpp>
 
 namespace
@@ -46,6 +48,16 @@ pagmo::problem make_problem(int kind, std::uint64_t param)
         default:
             throw std::invalid_argument("unknown problem kind " + std::to_string(kind));
     }
+}
+
+// family 7: pagmo::zdt{prob_id, param}; family 8: pagmo::dtlz{prob_id, dim, fdim, alpha}.
+pagmo::problem make_mo_problem(int family, unsigned prob_id, std::uint64_t param, std::uint64_t fdim, unsigned alpha)
+{
+    if (family == 7) return pagmo::problem{pagmo::zdt{prob_id, static_cast<unsigned>(param)}};
+    if (family == 8)
+        return pagmo::problem{pagmo::dtlz{prob_id, static_cast<pagmo::vector_double::size_type>(param),
+                                          static_cast<pagmo::vector_double::size_type>(fdim), alpha}};
+    throw std::invalid_argument("unknown multi-objective family " + std::to_string(family));
 }
 
 template <typename F>
@@ -184,6 +196,66 @@ int ref_bounds(int kind, std::uint64_t param, double *lb, double *ub)
         auto b = p.get_bounds();
         std::memcpy(lb, b.first.data(), b.first.size() * sizeof(double));
         std::memcpy(ub, b.second.data(), b.second.size() * sizeof(double));
+    });
+}
+
+// ZDT / DTLZ: dimensions (nx, nobj, nix) and bounds of the constructed problem;
+// construction errors come back as status 1 with the reference's message.
+int ref_mo_dims(int family, unsigned prob_id, std::uint64_t param, std::uint64_t fdim, unsigned alpha,
+                std::uint64_t *nx, std::uint64_t *nobj, std::uint64_t *nix)
+{
+    return guard([&] {
+        auto p = make_mo_problem(family, prob_id, param, fdim, alpha);
+        *nx = p.get_nx();
+        *nobj = p.get_nobj();
+        *nix = p.get_nix();
+    });
+}
+
+int ref_mo_bounds(int family, unsigned prob_id, std::uint64_t param, std::uint64_t fdim, unsigned alpha, double *lb,
+                  double *ub)
+{
+    return guard([&] {
+        auto p = make_mo_problem(family, prob_id, param, fdim, alpha);
+        auto b = p.get_bounds();
+        std::memcpy(lb, b.first.data(), b.first.size() * sizeof(double));
+        std::memcpy(ub, b.second.data(), b.second.size() * sizeof(double));
+    });
+}
+
+// bfe{thread_bfe{}} over n rows of a ZDT / DTLZ problem: fvs is n x nobj.
+int ref_mo_thread_bfe(int family, unsigned prob_id, std::uint64_t param, std::uint64_t fdim, unsigned alpha,
+                      const double *dvs, std::uint64_t n_dvs, std::uint64_t nx, double *fvs)
+{
+    return guard([&] {
+        auto p = make_mo_problem(family, prob_id, param, fdim, alpha);
+        pagmo::bfe b{pagmo::thread_bfe{}};
+        pagmo::vector_double in(dvs, dvs + n_dvs * nx);
+        auto out = b(p, in);
+        std::memcpy(fvs, out.data(), out.size() * sizeof(double));
+    });
+}
+
+// p_distance(x) of every row (zdt.cpp:204-224, dtlz.cpp:156-163).
+int ref_mo_p_distance(int family, unsigned prob_id, std::uint64_t param, std::uint64_t fdim, unsigned alpha,
+                      const double *dvs, std::uint64_t n_dvs, std::uint64_t nx, double *out)
+{
+    return guard([&] {
+        pagmo::vector_double x(nx);
+        if (family == 7) {
+            pagmo::zdt udp{prob_id, static_cast<unsigned>(param)};
+            for (std::uint64_t i = 0; i < n_dvs; ++i) {
+                std::memcpy(x.data(), dvs + i * nx, nx * sizeof(double));
+                out[i] = udp.p_distance(x);
+            }
+        } else {
+            pagmo::dtlz udp{prob_id, static_cast<pagmo::vector_double::size_type>(param),
+                            static_cast<pagmo::vector_double::size_type>(fdim), alpha};
+            for (std::uint64_t i = 0; i < n_dvs; ++i) {
+                std::memcpy(x.data(), dvs + i * nx, nx * sizeof(double));
+                out[i] = udp.p_distance(x);
+            }
+        }
     });
 }
 

@@ -7,7 +7,8 @@ plugin interface for the batch-fitness path:
   problems:         rastrigin, rosenbrock, lennard_jones (GPU UDPs with
                     batch_fitness, gradient and batch_gradient); ackley,
                     griewank, schwefel (batch_fitness; no gradient, as in
-                    the reference)
+                    the reference); zdt, dtlz (multi-objective batch_fitness
+                    and p_distance)
   batch_evaluators: gpu_bfe (the UDBFE) and a bfe/problem pair reproducing
                     pagmo's input/output checks and fevals accounting
   multi_objective:  fast_non_dominated_sorting, crowding_distance,
@@ -18,4 +19,4 @@ from ._native import Context, default_context  # noqa: F401
 from .batch_evaluators import bfe, gpu_bfe, problem  # noqa: F401
 from .multi_objective import (crowding_distance, fast_non_dominated_sorting, nsga2_survival,  # noqa: F401
                               select_best_N_mo, sort_population_mo)
-from .problems import ackley, griewank, lennard_jones, rastrigin, rosenbrock, schwefel  # noqa: F401
+from .problems import ackley, dtlz, griewank, lennard_jones, rastrigin, rosenbrock, schwefel, zdt  # noqa: F401

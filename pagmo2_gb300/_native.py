@@ -18,6 +18,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpgx.so"
 
 OK, ERR_INVALID, ERR_CUDA, ERR_TIMEOUT, ERR_CAPACITY, ERR_NODEVICE, ERR_NOTIMPL = 0, 1, 2, 3, 4, 5, 6
 RASTRIGIN, ROSENBROCK, LENNARD_JONES, ACKLEY, GRIEWANK, SCHWEFEL = 1, 2, 3, 4, 5, 6
+ZDT, DTLZ = 7, 8
 
 # Exported symbols and their signatures (kept in step with include/pgx.h).
 _vp, _u64, _i32, _d = C.c_void_p, C.c_uint64, C.c_int32, C.c_double
@@ -52,6 +53,11 @@ SIGNATURES = {
     "pgx_epoch_info": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(_u64)]),
     "pgx_epoch_destroy": (None, [_vp]),
     "pgx_requests_run_plain": (C.c_int, [_vp, _vp, C.c_int]),
+    "pgx_mo_problem_dims": (C.c_int, [_vp, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_u64)]),
+    "pgx_mo_problem_bounds": (C.c_int, [_vp, _vp, _vp]),
+    "pgx_mo_batch_fitness": (C.c_int, [_vp, _vp, _vp, _u64, _vp]),
+    "pgx_mo_batch_fitness_device": (C.c_int, [_vp, _vp, _vp, _u64, _vp, _vp]),
+    "pgx_mo_p_distance": (C.c_int, [_vp, _vp, _vp, _u64, _vp]),
 }
 
 
@@ -59,6 +65,13 @@ class pgx_request(C.Structure):
     """struct pgx_request of include/pgx.h."""
     _fields_ = [("kind", C.c_int), ("param", C.c_uint64), ("n_dvs", C.c_uint64), ("dvs", C.c_void_p),
                 ("fvs", C.c_void_p), ("grads", C.c_void_p)]
+
+
+class pgx_mo_problem(C.Structure):
+    """struct pgx_mo_problem of include/pgx.h: zdt(prob_id, param) or dtlz(prob_id, dim=param, fdim, alpha)."""
+    _fields_ = [("kind", C.c_int), ("prob_id", C.c_uint32), ("param", C.c_uint64), ("fdim", C.c_uint64),
+                ("alpha", C.c_uint32)]
+
 
 _lib = None
 _lib_lock = threading.Lock()
@@ -164,4 +177,24 @@ def problem_bounds(kind: int, param: int) -> tuple[np.ndarray, np.ndarray]:
     lb = np.empty(nx)
     ub = np.empty(nx)
     check(lib().pgx_problem_bounds(kind, param, ptr(lb), ptr(ub)))
+    return lb, ub
+
+
+def mo_problem(kind: int, prob_id: int, param: int, fdim: int = 0, alpha: int = 0) -> pgx_mo_problem:
+    if min(prob_id, param, fdim, alpha) < 0:
+        raise OverflowError("can't convert negative value to unsigned int")
+    return pgx_mo_problem(kind, prob_id, param, fdim, alpha)
+
+
+def mo_problem_dims(p: pgx_mo_problem) -> tuple[int, int, int]:
+    """(nx, nobj, nix) of a ZDT / DTLZ problem; ValueError with the reference's message if it is invalid."""
+    nx, nobj, nix = C.c_uint64(), C.c_uint64(), C.c_uint64()
+    check(lib().pgx_mo_problem_dims(C.byref(p), C.byref(nx), C.byref(nobj), C.byref(nix)))
+    return int(nx.value), int(nobj.value), int(nix.value)
+
+
+def mo_problem_bounds(p: pgx_mo_problem) -> tuple[np.ndarray, np.ndarray]:
+    nx = mo_problem_dims(p)[0]
+    lb, ub = np.empty(nx), np.empty(nx)
+    check(lib().pgx_mo_problem_bounds(C.byref(p), ptr(lb), ptr(ub)))
     return lb, ub

@@ -29,10 +29,10 @@ class gpu_bfe:
 
     def __call__(self, prob, dvs) -> np.ndarray:
         udp = getattr(prob, "udp", prob)
-        if not isinstance(udp, P._gpu_udp):
+        if not isinstance(udp, (P._gpu_udp, P._gpu_mo_udp)):
             name = udp.get_name() if hasattr(udp, "get_name") else type(udp).__name__
             raise ValueError(f"Cannot use a gpu_bfe on the problem '{name}': only the GPU rastrigin, rosenbrock, "
-                             "lennard_jones, ackley, griewank and schwefel problems are supported")
+                             "lennard_jones, ackley, griewank, schwefel, zdt and dtlz problems are supported")
         return udp.batch_fitness(dvs)
 
 

@@ -127,27 +127,23 @@ int check_has_gradient(int kind)
     return PGX_OK;
 }
 
-namespace
-{
-
 // Host-buffer batch evaluation: the rows are cut into chunks; chunk c's
 // upload (h2d stream), evaluation (compute stream) and download (d2h stream)
 // are chained by events, so uploads, kernels and downloads of consecutive
-// chunks overlap.
-int host_eval(pgx_context *ctx, int kind, uint64_t param, const double *dvs, uint64_t n, double *fvs, double *grads)
+// chunks overlap. Each row has nx inputs, out_w outputs in fvs and, when
+// grads is set, nx gradient entries.
+int host_rows(pgx_context *ctx, uint64_t nx, uint64_t out_w, const double *dvs, uint64_t n, double *fvs, double *grads,
+              const row_launcher &launch)
 {
-    uint64_t nx = 0;
-    PGX_TRY(problem_nx(kind, param, &nx));
-    if (grads) PGX_TRY(check_has_gradient(kind));
     PGX_CHECK(dvs != nullptr || n == 0, PGX_ERR_INVALID, "null decision vector buffer");
     PGX_CHECK(fvs != nullptr || grads != nullptr, PGX_ERR_INVALID, "no output buffer");
     if (n == 0) return PGX_OK;
-    PGX_CHECK(n <= (uint64_t(1) << 40) / nx, PGX_ERR_CAPACITY, "batch too large");
+    PGX_CHECK(n <= (uint64_t(1) << 40) / (nx > out_w ? nx : out_w), PGX_ERR_CAPACITY, "batch too large");
     std::lock_guard<std::mutex> g(ctx->lock);
     PGX_TRY(use_device(ctx));
-    const size_t row_in = nx * sizeof(double);
+    const size_t row_in = nx * sizeof(double), row_out = out_w * sizeof(double);
     PGX_TRY(ctx->d_in.ensure(n * row_in));
-    PGX_TRY(ctx->d_out.ensure(n * sizeof(double)));
+    PGX_TRY(ctx->d_out.ensure(n * row_out));
     if (grads) PGX_TRY(ctx->d_grad.ensure(n * row_in));
     double *din = ctx->d_in.as<double>();
     double *dout = ctx->d_out.as<double>();
@@ -166,19 +162,34 @@ int host_eval(pgx_context *ctx, int kind, uint64_t param, const double *dvs, uin
         PGX_CUDA(cudaEventRecord(up, ctx->h2d));
         PGX_CUDA(cudaStreamWaitEvent(ctx->stream, up, 0));
         uint64_t l = 0;
-        PGX_TRY(launch_eval(kind, param, nx, din + r0 * nx, nr, dout + r0, dgrad ? dgrad + r0 * nx : nullptr,
-                            ctx->stream, ctx->num_sms, &l));
+        PGX_TRY(launch(din + r0 * nx, nr, dout + r0 * out_w, dgrad ? dgrad + r0 * nx : nullptr, ctx->stream, &l));
         ctx->launches += l;
         PGX_CUDA(cudaEventRecord(done, ctx->stream));
         PGX_CUDA(cudaStreamWaitEvent(ctx->d2h, done, 0));
         if (fvs)
-            PGX_CUDA(cudaMemcpyAsync(fvs + r0, dout + r0, nr * sizeof(double), cudaMemcpyDeviceToHost, ctx->d2h));
+            PGX_CUDA(cudaMemcpyAsync(fvs + r0 * out_w, dout + r0 * out_w, nr * row_out, cudaMemcpyDeviceToHost,
+                                     ctx->d2h));
         if (grads)
             PGX_CUDA(cudaMemcpyAsync(grads + r0 * nx, dgrad + r0 * nx, nr * row_in, cudaMemcpyDeviceToHost, ctx->d2h));
     }
     PGX_CUDA(cudaStreamSynchronize(ctx->d2h));
     PGX_CUDA(cudaStreamSynchronize(ctx->stream));
     return PGX_OK;
+}
+
+namespace
+{
+
+int host_eval(pgx_context *ctx, int kind, uint64_t param, const double *dvs, uint64_t n, double *fvs, double *grads)
+{
+    uint64_t nx = 0;
+    PGX_TRY(problem_nx(kind, param, &nx));
+    if (grads) PGX_TRY(check_has_gradient(kind));
+    const int num_sms = ctx->num_sms;
+    return host_rows(ctx, nx, 1, dvs, n, fvs, grads,
+                     [&](const double *din, uint64_t nr, double *dout, double *dgrad, cudaStream_t s, uint64_t *l) {
+                         return launch_eval(kind, param, nx, din, nr, dout, dgrad, s, num_sms, l);
+                     });
 }
 
 struct dev_survival {

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -93,6 +94,17 @@ namespace pgx
 
 // Scope guard: makes ctx->device current for the calling thread.
 int use_device(pgx_context *ctx);
+
+// ------------------------------------------------------- host row pipeline
+// Launches the evaluation of nr rows already on the device (inputs din, nx per
+// row; outputs dout and, when set, dgrad) on stream s, adding its kernel
+// launches to *launches.
+using row_launcher = std::function<int(const double *din, uint64_t nr, double *dout, double *dgrad, cudaStream_t s,
+                                       uint64_t *launches)>;
+// Host-buffer batch evaluation through the context's chunked upload /
+// evaluate / download pipeline; out_w outputs per row in fvs.
+int host_rows(pgx_context *ctx, uint64_t nx, uint64_t out_w, const double *dvs, uint64_t n, double *fvs, double *grads,
+              const row_launcher &launch);
 
 // ------------------------------------------------------------ problem facts
 

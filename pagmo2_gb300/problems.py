@@ -1,6 +1,6 @@
 """GPU-backed user-defined problems mirroring pagmo's rastrigin, rosenbrock,
-lennard_jones, ackley, griewank and schwefel UDPs
-(src/problems/{rastrigin,rosenbrock,lennard_jones,ackley,griewank,schwefel}.cpp).
+lennard_jones, ackley, griewank, schwefel, zdt and dtlz UDPs
+(src/problems/{rastrigin,rosenbrock,lennard_jones,ackley,griewank,schwefel,zdt,dtlz}.cpp).
 
 They expose the UDP interface pagmo's ``problem`` wraps (``fitness``,
 ``get_bounds``, ``get_name``, ``get_thread_safety``) plus the optional hooks the
@@ -12,6 +12,8 @@ the GPU through libpgx; the per-row ``fitness``/``gradient`` are one-row
 batches (correct, but only the batch calls are fast).
 """
 from __future__ import annotations
+
+import ctypes as C
 
 import numpy as np
 
@@ -186,6 +188,122 @@ class schwefel(_fitness_only_udp):
 
     def best_known(self):
         return np.full(self._nx, 420.9687)
+
+
+class _gpu_mo_udp:
+    """ZDT / DTLZ on the GPU: fitness vectors of nobj objectives, batch fitness
+    in pagmo's fvs layout (n rows of nobj, flattened), p_distance per vector
+    or averaged over a population (src/problems/zdt.cpp, src/problems/dtlz.cpp)."""
+    thread_safety = "constant"
+
+    def __init__(self, spec: N.pgx_mo_problem, context: N.Context | None = None):
+        self._spec = spec
+        self._nx, self._nobj, self._nix = N.mo_problem_dims(spec)  # the reference constructors' checks
+        self._ctx = context
+
+    @property
+    def ctx(self) -> N.Context:
+        return self._ctx if self._ctx is not None else N.default_context()
+
+    def get_nx(self) -> int:
+        return self._nx
+
+    def get_nobj(self) -> int:
+        return self._nobj
+
+    def get_nf(self) -> int:
+        return self._nobj
+
+    def get_nix(self) -> int:
+        return self._nix
+
+    def get_bounds(self):
+        return N.mo_problem_bounds(self._spec)
+
+    def get_thread_safety(self) -> str:
+        return self.thread_safety
+
+    def has_gradient(self) -> bool:
+        return False
+
+    def batch_fitness(self, dvs) -> np.ndarray:
+        x = _as_rows(dvs, self._nx)
+        n = x.size // self._nx
+        f = np.empty(n * self._nobj)
+        if n:
+            N.check(N.lib().pgx_mo_batch_fitness(self.ctx.handle, C.byref(self._spec), N.ptr(x), n, N.ptr(f)))
+        return f
+
+    def batch_p_distance(self, dvs) -> np.ndarray:
+        """p_distance of every decision vector of a batch."""
+        x = _as_rows(dvs, self._nx)
+        n = x.size // self._nx
+        out = np.empty(n)
+        if n:
+            N.check(N.lib().pgx_mo_p_distance(self.ctx.handle, C.byref(self._spec), N.ptr(x), n, N.ptr(out)))
+        return out
+
+    def fitness(self, x) -> np.ndarray:
+        x = np.asarray(x, dtype=np.float64)
+        if x.size != self._nx:
+            raise ValueError(f"A decision vector is incompatible with a problem of type '{self.get_name()}': "
+                             f"the number of dimensions of the problem is {self._nx}, while the decision vector "
+                             f"has a size of {x.size} (the two values should be equal)")
+        return self.batch_fitness(x)
+
+    def p_distance(self, x) -> float:
+        """p_distance(x) of one decision vector, or the mean over a population
+        (anything with get_x()), summed in row order as the reference does."""
+        if hasattr(x, "get_x"):
+            pts = np.asarray(x.get_x(), dtype=np.float64).reshape(-1, self._nx)
+            if pts.shape[0] == 0:
+                return float("nan")
+            vals = self.batch_p_distance(pts)
+            return float(np.cumsum(vals)[-1] / vals.size)
+        return self._p_distance_vector(np.asarray(x, dtype=np.float64).reshape(-1))
+
+    def _p_distance_vector(self, v: np.ndarray) -> float:
+        # dtlz.cpp:156-163 checks the size
+        if v.size != self._nx:
+            raise ValueError(f"The size of the decision vector should be {self._nx} while {v.size} was detected")
+        return float(self.batch_p_distance(v)[0])
+
+
+class zdt(_gpu_mo_udp):
+    """zdt{prob_id, param}: the six two-objective ZDT problems (param is the
+    dimension, except for ZDT5 whose 30 + 5 (param - 1) bits it counts)."""
+
+    def __init__(self, prob_id: int = 1, param: int = 30, context=None):
+        self.prob_id, self.param = int(prob_id), int(param)
+        super().__init__(N.mo_problem(N.ZDT, self.prob_id, self.param), context)
+
+    def get_name(self) -> str:
+        return f"ZDT{self.prob_id}"
+
+    def _p_distance_vector(self, v: np.ndarray) -> float:
+        # zdt.cpp:204-224 does not check the size: the metric of a vector of
+        # another length is that of the same ZDT problem at that length
+        if v.size == self._nx:
+            return float(self.batch_p_distance(v)[0])
+        if self.prob_id == 5:
+            if v.size < 30:
+                raise ValueError(f"a ZDT5 decision vector has at least 30 entries, {v.size} given")
+            other = zdt(5, (v.size - 30) // 5 + 1, self._ctx)
+            return float(other.batch_p_distance(v[:other.get_nx()])[0])
+        if v.size < 2:
+            raise ValueError(f"a ZDT decision vector has at least 2 entries, {v.size} given")
+        return float(zdt(self.prob_id, v.size, self._ctx).batch_p_distance(v)[0])
+
+
+class dtlz(_gpu_mo_udp):
+    """dtlz{prob_id, dim, fdim, alpha}: the seven scalable DTLZ problems on [0, 1]^dim."""
+
+    def __init__(self, prob_id: int = 1, dim: int = 5, fdim: int = 3, alpha: int = 100, context=None):
+        self.prob_id, self.dim, self.fdim, self.alpha = int(prob_id), int(dim), int(fdim), int(alpha)
+        super().__init__(N.mo_problem(N.DTLZ, self.prob_id, self.dim, self.fdim, self.alpha), context)
+
+    def get_name(self) -> str:
+        return f"DTLZ{self.prob_id}"
 
 
 def from_kind(kind: int, param: int, context=None) -> _gpu_udp:

@@ -12,6 +12,8 @@ profiler are not benchmark values). Cases:
   rosenbrock_fg / rosenbrock_f  dim 1000 (--dim)
   lj_fg / lj_f                  150 atoms (--atoms)
   ackley_f / griewank_f / schwefel_f   dim 50 (--dim), fitness only
+  zdt<k>_f                      ZDT k, param 30 (--dim), objectives n x 2
+  dtlz<k>_f                     DTLZ k, dim 12 (--dim), 3 objectives (--fdim)
   survival                      NSGA-II survival of --rows nested-front points x 3
   select_best                   select_best_N_mo(--rows nested-front points x 3, rows / 2)
   sort_population               sort_population_mo(--rows nested-front points x 3)
@@ -36,6 +38,7 @@ def main() -> None:
     ap.add_argument("--launches", type=int, default=3)
     ap.add_argument("--atoms", type=int, default=150, help="lennard_jones cluster size (lj_* cases)")
     ap.add_argument("--dim", type=int, default=0, help="rastrigin/rosenbrock dimension (default 50 / 1000)")
+    ap.add_argument("--fdim", type=int, default=3, help="DTLZ objectives (dtlz* cases)")
     a = ap.parse_args()
 
     import torch
@@ -80,6 +83,20 @@ def main() -> None:
             else:
                 N.check(L.pgx_sort_population_mo_device(ctx.handle, dp.data_ptr(), n, 3, sel.data_ptr(),
                                                         st.data_ptr(), sp))
+    elif a.case.startswith(("zdt", "dtlz")):
+        import ctypes as C
+
+        fam = N.ZDT if a.case.startswith("zdt") else N.DTLZ
+        pid = int(a.case.split("_")[0][3 if fam == N.ZDT else 4:])
+        param = a.dim or (30 if fam == N.ZDT else 12)
+        spec = N.mo_problem(fam, pid, param, a.fdim if fam == N.DTLZ else 0, 100)
+        nx, nobj, _ = N.mo_problem_dims(spec)
+        x = W.mo_uniform_batch(fam, pid, param, n, seed=47, fdim=a.fdim)
+        dx = torch.from_numpy(x).cuda()
+        df = torch.empty((n, nobj), dtype=torch.float64, device="cuda")
+
+        def run():
+            N.check(L.pgx_mo_batch_fitness_device(ctx.handle, C.byref(spec), dx.data_ptr(), n, df.data_ptr(), sp))
     else:
         name, mode = a.case.rsplit("_", 1)
         kind, param, x = {

@@ -59,6 +59,25 @@ def uniform_batch(kind: int, param: int, n: int, seed: int) -> np.ndarray:
     return lb + (ub - lb) * u
 
 
+def mo_bounds(kind: int, prob_id: int, param: int, fdim: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    """Box bounds of zdt{prob_id, param} / dtlz{prob_id, param, fdim} (host-side,
+    src/problems/zdt.cpp:108-133, src/problems/dtlz.cpp:116-119)."""
+    if kind == N.ZDT:
+        nx = 30 + 5 * (param - 1) if prob_id == 5 else param
+        lb, ub = np.zeros(nx), np.ones(nx)
+        if prob_id == 4:
+            lb[1:], ub[1:] = -5.0, 5.0
+        return lb, ub
+    return np.zeros(param), np.ones(param)
+
+
+def mo_uniform_batch(kind: int, prob_id: int, param: int, n: int, seed: int, fdim: int = 0) -> np.ndarray:
+    """n ZDT / DTLZ decision vectors, uniform within the bounds."""
+    lb, ub = mo_bounds(kind, prob_id, param, fdim)
+    rs = np.random.RandomState(seed)
+    return lb + (ub - lb) * rs.random_sample((n, lb.size))
+
+
 def rastrigin_batch(n: int = 4096, dim: int = 50, seed: int = 1) -> np.ndarray:
     return uniform_batch(N.RASTRIGIN, dim, n, seed)
 

@@ -16,11 +16,13 @@
 #include <pagmo/problem.hpp>
 #include <pagmo/exceptions.hpp>
 #include <pagmo/problems/ackley.hpp>
+#include <pagmo/problems/dtlz.hpp>
 #include <pagmo/problems/griewank.hpp>
 #include <pagmo/problems/null_problem.hpp>
 #include <pagmo/problems/rastrigin.hpp>
 #include <pagmo/problems/rosenbrock.hpp>
 #include <pagmo/problems/schwefel.hpp>
+#include <pagmo/problems/zdt.hpp>
 #include <pagmo/utils/multi_objective.hpp>
 
 #include <pagmo_gb300/gpu_bfe.hpp>
@@ -59,6 +61,12 @@ static_assert(pagmo::is_udp<gpu_lennard_jones>::value, "gpu_lennard_jones must b
 static_assert(pagmo::has_batch_fitness<gpu_rosenbrock>::value, "batch_fitness hook");
 static_assert(pagmo::has_gradient<gpu_rosenbrock>::value, "gradient hook");
 static_assert(pagmo::has_gradient<gpu_lennard_jones>::value, "gradient hook");
+static_assert(pagmo::is_udp<gpu_zdt>::value && pagmo::is_udp<gpu_dtlz>::value, "gpu_zdt / gpu_dtlz must be UDPs");
+static_assert(pagmo::has_batch_fitness<gpu_zdt>::value && pagmo::has_batch_fitness<gpu_dtlz>::value,
+              "batch_fitness hook of the multi-objective UDPs");
+static_assert(!pagmo::has_gradient<gpu_zdt>::value && !pagmo::has_gradient<gpu_dtlz>::value,
+              "zdt and dtlz have no gradient in the reference");
+static_assert(pagmo::has_get_nobj<gpu_dtlz>::value && pagmo::has_integer_part<gpu_zdt>::value, "nobj / nix hooks");
 static_assert(pagmo::is_udp<gpu_ackley>::value && pagmo::is_udp<gpu_griewank>::value && pagmo::is_udp<gpu_schwefel>::value,
               "fitness-only GPU UDPs");
 static_assert(!pagmo::has_gradient<gpu_ackley>::value && !pagmo::has_gradient<gpu_schwefel>::value,
@@ -94,8 +102,30 @@ int main()
     CHECK(throws_with<pagmo::not_implemented_error>([] { pagmo::problem{gpu_ackley{3u}}.gradient({1., 2., 3.}); },
                                                     "gradient"));
 
+    // ZDT / DTLZ: constructor errors, dimensions, bounds and names as the reference's
+    CHECK(throws_with<std::invalid_argument>([] { gpu_zdt{7u, 23u}; }, "prob_id=7 was detected"));
+    CHECK(throws_with<std::invalid_argument>([] { gpu_zdt{2u, 1u}; }, "minimum value of 2"));
+    CHECK(throws_with<std::invalid_argument>([] { gpu_dtlz{9u, 7u, 3u, 100u}; }, "prob_id=9 was detected"));
+    CHECK(throws_with<std::invalid_argument>([] { gpu_dtlz{1u, 7u, 1u, 100u}; }, "minimum of 2 objectives"));
+    CHECK(throws_with<std::invalid_argument>([] { gpu_dtlz{1u, 3u, 3u, 100u}; }, "has to be larger"));
+    for (unsigned id = 1u; id <= 6u; ++id) {
+        const unsigned param = id == 4u ? 10u : 11u;
+        pagmo::problem a{gpu_zdt{id, param}}, r{pagmo::zdt{id, param}};
+        CHECK(a.get_nx() == r.get_nx() && a.get_nobj() == r.get_nobj() && a.get_nix() == r.get_nix());
+        CHECK(a.get_bounds() == r.get_bounds() && a.get_name() == r.get_name());
+    }
+    for (unsigned id = 1u; id <= 7u; ++id) {
+        pagmo::problem a{gpu_dtlz{id, 12u, 4u}}, r{pagmo::dtlz{id, 12u, 4u}};
+        CHECK(a.get_nx() == r.get_nx() && a.get_nobj() == r.get_nobj() && a.get_nix() == r.get_nix());
+        CHECK(a.get_bounds() == r.get_bounds() && a.get_name() == r.get_name());
+    }
+    CHECK(throws_with<std::invalid_argument>([] { gpu_dtlz{2u, 4u}.p_distance(pagmo::vector_double(3, 0.5)); },
+                                             "The size of the decision vector should be 4 while 3 was detected"));
+
     // the UDBFE wrapped by pagmo::bfe
     pagmo::bfe b{gpu_bfe{}};
+    CHECK(throws_with<std::invalid_argument>([&b] { b(pagmo::problem{pagmo::dtlz{4u}}, pagmo::vector_double(10, 0.5)); },
+                                             "alpha is not exposed"));
     CHECK(b.get_name() == "GB300 batch fitness evaluator");
     CHECK(b.get_thread_safety() == pagmo::thread_safety::basic);
     CHECK(b.is<gpu_bfe>());
@@ -126,6 +156,9 @@ int main()
         CHECK(throws_with<std::runtime_error>([&] { pagmo::problem{gpu_rosenbrock{4u}}.fitness({1., 1., 1., 1.}); },
                                               ""));
         CHECK(throws_with<std::runtime_error>([] { sort_population_mo({{1., 2.}, {2., 1.}}); }, ""));
+        pagmo::problem pz{pagmo::zdt{1u, 4u}};
+        CHECK(throws_with<std::runtime_error>([&] { b(pz, dvs); }, ""));
+        CHECK(pz.get_fevals() == 0u);
     } else {
         // with a device: bfe{gpu_bfe} against bfe{thread_bfe}, fevals counted once
         pagmo::problem pr{pagmo::rosenbrock{4u}};
@@ -168,6 +201,17 @@ int main()
                           pagmo::problem{pagmo::schwefel{3u}}}) {
             const auto fg = b(prob, d3);
             const auto fr = pagmo::bfe{pagmo::thread_bfe{}}(prob, d3);
+            for (size_t i = 0; i < fr.size(); ++i) CHECK(std::abs(fg[i] - fr[i]) <= 1e-12 * (1.0 + std::abs(fr[i])));
+        }
+        // pagmo's zdt and dtlz through bfe{gpu_bfe}, and the GPU UDPs, against bfe{thread_bfe}
+        std::vector<double> u(60);
+        for (size_t i = 0; i < u.size(); ++i) u[i] = 0.0125 + 0.0163 * static_cast<double>(i % 61);
+        for (auto prob : {pagmo::problem{pagmo::zdt{1u, 6u}}, pagmo::problem{pagmo::zdt{3u, 6u}},
+                          pagmo::problem{pagmo::dtlz{2u, 6u, 3u}}, pagmo::problem{pagmo::dtlz{7u, 6u, 3u}},
+                          pagmo::problem{gpu_zdt{2u, 6u}}, pagmo::problem{gpu_dtlz{4u, 6u, 3u, 100u}}}) {
+            const auto fg = b(prob, u);
+            const auto fr = pagmo::bfe{pagmo::thread_bfe{}}(prob, u);
+            CHECK(fg.size() == fr.size());
             for (size_t i = 0; i < fr.size(); ++i) CHECK(std::abs(fg[i] - fr[i]) <= 1e-12 * (1.0 + std::abs(fr[i])));
         }
     }

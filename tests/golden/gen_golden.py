@@ -11,6 +11,9 @@ Outputs (numpy .npz, small):
   fitness.npz  per case: the decision vectors, bfe{thread_bfe{}} fitness, and
                problem::gradient rows (rastrigin, rosenbrock); ackley,
                griewank and schwefel (fitness only)
+  mo_problems.npz  per ZDT / DTLZ case: the problem (kind, prob_id, param,
+               fdim, alpha), the decision vectors, bfe{thread_bfe{}} fitness
+               (n x nobj) and p_distance of every row
   mo.npz       per case: the objective vectors, fast_non_dominated_sorting
                (rank, dom_count, fronts, dom_list), crowding_distance of
                every front of three or more points, sort_population_mo and
@@ -57,6 +60,31 @@ def fitness_cases():
     return cases
 
 
+ZDT, DTLZ = 7, 8
+
+
+def mo_problem_cases():
+    """(name, (kind, prob_id, param, fdim, alpha), dvs) for ZDT and DTLZ."""
+    cases = []
+    for pid, params in ((1, (2, 30, 173)), (2, (2, 30)), (3, (2, 30)), (4, (2, 10)), (5, (2, 11, 30)),
+                        (6, (2, 10, 64))):
+        for param in params:
+            x = W.mo_uniform_batch(ZDT, pid, param, 16, 600 + 10 * pid + param)
+            x[0, :] = W.mo_bounds(ZDT, pid, param)[0]  # lower corner
+            x[1, :] = W.mo_bounds(ZDT, pid, param)[1]  # upper corner
+            cases.append((f"zdt{pid}_{param}", (ZDT, pid, param, 0, 0), x))
+    for pid in range(1, 8):
+        for dim, fdim, alpha in ((5, 3, 100), (12, 3, 100), (10, 2, 100), (30, 10, 100), (50, 40, 3)):
+            if pid != 4 and alpha != 100:
+                alpha = 100
+            x = W.mo_uniform_batch(DTLZ, pid, dim, 16, 700 + 10 * pid + dim)
+            x[0, :] = 0.0
+            x[1, :] = 1.0
+            x[2, :] = 0.5
+            cases.append((f"dtlz{pid}_{dim}_{fdim}_{alpha}", (DTLZ, pid, dim, fdim, alpha), x))
+    return cases
+
+
 def mo_cases():
     cases = []
     # tests/multi_objective.cpp fnds examples
@@ -100,6 +128,15 @@ def main():
             fit[f"{name}/g"] = ref.gradient_rows(kind, param, x)
     np.savez_compressed(HERE / "fitness.npz", **fit)
 
+    mop = {}
+    for name, spec, x in mo_problem_cases():
+        x = np.ascontiguousarray(x)
+        mop[f"{name}/spec"] = np.array(spec, dtype=np.int64)
+        mop[f"{name}/x"] = x
+        mop[f"{name}/f"] = ref.mo_thread_bfe(spec, x)
+        mop[f"{name}/p_distance"] = ref.mo_p_distance(spec, x)
+    np.savez_compressed(HERE / "mo_problems.npz", **mop)
+
     mo = {}
     for name, p in mo_cases():
         r = ref.fnds(p)
@@ -121,7 +158,7 @@ def main():
         for nb in sorted({1, n // 3, n // 2, n - 1}):
             mo[f"{name}/select_best_{nb}"] = ref.select_best_n_mo(p, nb)
     np.savez_compressed(HERE / "mo.npz", **mo)
-    print("wrote", HERE / "fitness.npz", HERE / "mo.npz")
+    print("wrote", HERE / "fitness.npz", HERE / "mo_problems.npz", HERE / "mo.npz")
 
 
 if __name__ == "__main__":
