@@ -303,9 +303,14 @@ void dtlz_fitness(unsigned id, uint64_t m, unsigned alpha, const double *x, uint
 
 // ------------------------------------------------ long double with error scales
 
-// A value and its first-order error scale (in units of the unit roundoff):
-// the magnitude of every rounding that produced it, carried through the
-// operations by their absolute partial derivatives.
+// A value and its error scale (in units of the unit roundoff u = 2^-53): the
+// magnitude of every rounding that produced it, carried through the
+// operations by their absolute partial derivatives. Products and sin/cos also
+// carry the second-order term (u m_a m_b, u m_a^2 / 2): where two factors are
+// both near zero (DTLZ's cos(pi/2 x) at x = 1, which the reference evaluates
+// to 6e-17 and an exact reduction to 0) the first-order bound alone vanishes.
+constexpr ld kU = 1.0L / 9007199254740992.0L; // 2^-53
+
 struct em {
     ld v, m;
 };
@@ -330,7 +335,7 @@ em operator-(em a, em b)
 em operator*(em a, em b)
 {
     const ld v = a.v * b.v;
-    return {v, a.m * fabsl(b.v) + fabsl(a.v) * b.m + fabsl(v)};
+    return {v, a.m * fabsl(b.v) + fabsl(a.v) * b.m + kU * a.m * b.m + fabsl(v)};
 }
 em operator/(em a, em b)
 {
@@ -351,11 +356,15 @@ em e_sqrt(em a)
 }
 em e_sin(em a)
 {
-    return call(sinl(a.v), cosl(a.v), a);
+    em r = call(sinl(a.v), cosl(a.v), a);
+    r.m += 0.5L * kU * a.m * a.m;
+    return r;
 }
 em e_cos(em a)
 {
-    return call(cosl(a.v), sinl(a.v), a);
+    em r = call(cosl(a.v), sinl(a.v), a);
+    r.m += 0.5L * kU * a.m * a.m;
+    return r;
 }
 em e_exp(em a)
 {
