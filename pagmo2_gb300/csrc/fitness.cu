@@ -11,6 +11,23 @@
 
 namespace pgx
 {
+
+// Threads per block for n rows of `lanes` lanes: 256, or fewer for batches
+// that would not give every SM a block (4096 rows of 4 lanes fill only 64
+// blocks of 256): the blocks shrink (to 64 threads at least) until the grid
+// covers the SMs. The lanes per row, and so every row's result, stay the same.
+int row_block_threads(uint64_t n, int lanes, int num_sms)
+{
+    const uint64_t total = n * static_cast<uint64_t>(lanes);
+    const uint64_t sms = static_cast<uint64_t>(num_sms > 0 ? num_sms : 1);
+    if (total >= 256u * sms) return 256;
+    uint64_t t = (total + sms - 1u) / sms;
+    t = (t + 31u) & ~uint64_t(31);
+    if (t < 64u) t = 64u;
+    if (t < static_cast<uint64_t>(lanes)) t = static_cast<uint64_t>(lanes);
+    return static_cast<int>(t > 256u ? 256u : t);
+}
+
 namespace
 {
 
@@ -131,12 +148,12 @@ int grid_for(K kernel, int threads, size_t smem, uint64_t work_items, int per_bl
 }
 
 template <typename K>
-int launch_simple(K kernel, int per_block, const double *x, uint64_t n, uint32_t nx, double *f, double *g,
+int launch_simple(K kernel, int lanes, const double *x, uint64_t n, uint32_t nx, double *f, double *g,
                   cudaStream_t s, int num_sms)
 {
-    constexpr int threads = 256;
+    const int threads = row_block_threads(n, lanes, num_sms);
     int grid = 1;
-    PGX_TRY(grid_for(kernel, threads, 0, n, per_block, num_sms, &grid));
+    PGX_TRY(grid_for(kernel, threads, 0, n, threads / lanes, num_sms, &grid));
     kernel<<<grid, threads, 0, s>>>(x, n, nx, f, g);
     PGX_CUDA(cudaGetLastError());
     return PGX_OK;
@@ -146,7 +163,7 @@ template <int G>
 int launch_rows(int kind, bool grad, const double *x, uint64_t n, uint32_t nx, double *f, double *g, cudaStream_t s,
                 int num_sms)
 {
-    constexpr int pb = 256 / G;
+    constexpr int pb = G; // lanes per row
     switch (kind) {
         case PGX_RASTRIGIN:
             return grad ? launch_simple(rastrigin_kernel<G, true>, pb, x, n, nx, f, g, s, num_sms)
@@ -238,11 +255,11 @@ int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64
     if (kind == PGX_ROSENBROCK && nx >= 128 && nx % 4 == 0 && reinterpret_cast<uintptr_t>(d_x) % 16 == 0
         && (!grad || reinterpret_cast<uintptr_t>(d_g) % 16 == 0)) {
         if (!rosenbrock_double_float())
-            st = grad ? launch_simple(rosenbrock_v4_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
-                      : launch_simple(rosenbrock_v4_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
+            st = grad ? launch_simple(rosenbrock_v4_kernel<true>, 32, d_x, n, nx32, d_f, d_g, stream, num_sms)
+                      : launch_simple(rosenbrock_v4_kernel<false>, 32, d_x, n, nx32, d_f, d_g, stream, num_sms);
         else
-            st = grad ? launch_simple(rosenbrock_v4ff_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
-                      : launch_simple(rosenbrock_v4ff_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
+            st = grad ? launch_simple(rosenbrock_v4ff_kernel<true>, 32, d_x, n, nx32, d_f, d_g, stream, num_sms)
+                      : launch_simple(rosenbrock_v4ff_kernel<false>, 32, d_x, n, nx32, d_f, d_g, stream, num_sms);
     } else if (kind == PGX_RASTRIGIN || kind == PGX_ROSENBROCK || kind == PGX_ACKLEY || kind == PGX_GRIEWANK
                || kind == PGX_SCHWEFEL) {
         PGX_CHECK(!grad || kind <= PGX_ROSENBROCK, PGX_ERR_NOTIMPL,
@@ -299,8 +316,8 @@ int launch_rows_variant(int kind, uint64_t nx, const double *d_x, uint64_t n, do
     if (lanes == 0) {
         PGX_CHECK(kind == PGX_ROSENBROCK && nx % 4 == 0 && reinterpret_cast<uintptr_t>(d_x) % 16 == 0,
                   PGX_ERR_INVALID, "4-wide rows need rosenbrock, nx % 4 == 0 and aligned rows");
-        return grad ? launch_simple(rosenbrock_v4_kernel<true>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms)
-                    : launch_simple(rosenbrock_v4_kernel<false>, 8, d_x, n, nx32, d_f, d_g, stream, num_sms);
+        return grad ? launch_simple(rosenbrock_v4_kernel<true>, 32, d_x, n, nx32, d_f, d_g, stream, num_sms)
+                    : launch_simple(rosenbrock_v4_kernel<false>, 32, d_x, n, nx32, d_f, d_g, stream, num_sms);
     }
     switch (lanes) {
         case 32: return launch_rows<32>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);

@@ -278,7 +278,7 @@ struct mo_shape {
 template <typename K, typename... A>
 int launch_grid(K kernel, int lanes, uint64_t n, int num_sms, cudaStream_t s, A... args)
 {
-    constexpr int threads = 256;
+    const int threads = row_block_threads(n, lanes, num_sms);
     int occ = 0;
     PGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, 0));
     if (occ < 1) occ = 1;
@@ -332,7 +332,8 @@ int launch_dtlz(const mo_shape &p, const double *x, uint64_t n, bool pd, double 
 }
 
 // Lanes per row: 2, 8 or 32, after the widest group that keeps the row's main
-// loop at least 94 % busy.
+// loop at least 94 % busy (a function of the problem only, so that a row's
+// result does not depend on the batch it comes in).
 int mo_lanes(const mo_shape &p)
 {
     uint32_t work;

@@ -114,6 +114,9 @@ int problem_nx(int kind, uint64_t param, uint64_t *nx);
 
 // Lanes per row (1..32) used by the strided rastrigin/rosenbrock row kernels.
 int lanes_per_row(uint32_t nx);
+// Threads per block of the row kernels for n rows of `lanes` lanes: 256, or
+// fewer so that small batches still give every SM a block.
+int row_block_threads(uint64_t n, int lanes, int num_sms);
 
 // Whether lennard_jones clusters of na atoms use the flattened pair walk.
 bool lj_use_flat(uint32_t na);
