@@ -557,8 +557,10 @@ int pgx_std_sort_i64(pgx_context *ctx, int64_t *keys, int32_t *values, uint64_t 
     const size_t bk = (n * sizeof(int64_t) + 255u) & ~size_t(255);
     const size_t bv = (n * sizeof(int32_t) + 255u) & ~size_t(255);
     const size_t bl = (n * 2u * sizeof(int32_t) + 255u) & ~size_t(255);
-    PGX_TRY(ctx->s_crowd.ensure(bk + bv + 2u * bl + 256));
+    const size_t bs = (sort_pairs_state_bytes() + 255u) & ~size_t(255);
+    PGX_TRY(ctx->s_crowd.ensure(bk + bv + 2u * bl + 256 + bs));
     char *base = ctx->s_crowd.as<char>();
+    void *dstate = base + bk + bv + 2u * bl + 256;
     long long *dk = reinterpret_cast<long long *>(base);
     int32_t *dv = reinterpret_cast<int32_t *>(base + bk);
     int2 *dl = reinterpret_cast<int2 *>(base + bk + bv);
@@ -568,7 +570,7 @@ int pgx_std_sort_i64(pgx_context *ctx, int64_t *keys, int32_t *values, uint64_t 
     PGX_CUDA(cudaMemsetAsync(derr, 0, sizeof(int), s));
     PGX_CUDA(cudaMemcpyAsync(dk, keys, n * sizeof(int64_t), cudaMemcpyHostToDevice, s));
     PGX_CUDA(cudaMemcpyAsync(dv, values, n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-    PGX_TRY(launch_sort_pairs(ctx, dk, dv, n, derr, dl, dpos, s));
+    PGX_TRY(launch_sort_pairs(ctx, dk, dv, n, derr, dl, dpos, dstate, s));
     int err = 0;
     PGX_CUDA(cudaMemcpyAsync(keys, dk, n * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     PGX_CUDA(cudaMemcpyAsync(values, dv, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));

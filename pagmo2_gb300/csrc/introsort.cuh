@@ -412,11 +412,12 @@ __device__ __forceinline__ void queue_range(int a, int b, int2 *small_next, int2
 
 // Sorts x[0 .. n) by key with std::sort's order of ties. Every thread of the
 // block calls it (blockDim.x a multiple of 32, at most 1024). slots_all: 64
-// ints per warp of shared memory; ctl in shared memory. Ends with a
-// __syncthreads.
+// ints per warp of shared memory; ctl in shared memory. depth0 >= 0 continues
+// an introsort whose depth budget at this range is depth0 (a subrange of a
+// larger sort); -1 starts one (2 floor(log2 n)). Ends with a __syncthreads.
 template <typename K>
 __device__ void block_std_sort(const sort_view<K> &x, int n, const sort_work &w, sort_ctl *ctl, int *slots_all,
-                               int *err)
+                               int *err, int depth0 = -1)
 {
     const unsigned lane = threadIdx.x & 31u;
     const int warp = static_cast<int>(threadIdx.x >> 5);
@@ -426,7 +427,7 @@ __device__ void block_std_sort(const sort_view<K> &x, int n, const sort_work &w,
         __syncthreads();
         return;
     }
-    int depth = 2 * floor_log2_int(n);
+    int depth = depth0 >= 0 ? depth0 : 2 * floor_log2_int(n);
     int2 *small_cur = w.small, *small_next = w.small + w.small_cap;
     int2 *big_cur = w.big, *big_next = w.big + w.big_cap;
     if (threadIdx.x == 0) {

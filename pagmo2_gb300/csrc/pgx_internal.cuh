@@ -167,8 +167,11 @@ int read_mo_status(pgx_context *ctx, uint64_t n, uint64_t m);
 // std::sort-ordered in-place sort of device (key, value) pairs by one block;
 // d_lists holds n int2 and d_pos 2 n int32 of scratch, *d_err receives a
 // nonzero code on a broken invariant.
+// d_state: sort_pairs_state_bytes() of device scratch (grid barrier state of
+// the grid-wide sort used beyond 4096 pairs).
 int launch_sort_pairs(pgx_context *ctx, long long *d_keys, int32_t *d_vals, uint64_t n, int *d_err, int2 *d_lists,
-                      int32_t *d_pos, cudaStream_t stream);
+                      int32_t *d_pos, void *d_state, cudaStream_t stream);
+size_t sort_pairs_state_bytes();
 
 // Reads the device status word of the last survival pass of shape (n, m) on
 // this context (after a stream synchronisation): PGX_ERR_TIMEOUT when a grid

@@ -11,7 +11,8 @@
 //  2. dominance_kernel: the "dominated-by" bit matrix Dt, row j holding bit i
 //     when point i dominates point j, built 32x256 pairs per CTA with
 //     __ballot_sync; dom_count[j] = popcount of row j.
-//  3. peel_kernel: a cooperative persistent kernel peels fronts. Front k+1 is
+//  3. peel2_kernel (peel_kernel beyond 131072 points): a cooperative
+//     persistent kernel peels fronts. Front k+1 is
 //     every unassigned point whose row has no unassigned dominator. The
 //     reference's order inside a front (first front ascending; later fronts in
 //     the order its dom_list traversal appends them) is rebuilt exactly: a
@@ -216,6 +217,7 @@ struct peel_state {
     int counts[2];
     int status;   // kStatusNeedTwoObjectives: crowding over fewer than two objectives
     int sort_err; // broken invariant of the device sort (never expected)
+    int gs[72];   // grid sort: [0] shared-memory ranges, [1 + level] block-partitioned ranges per level
 };
 
 constexpr int kStatusNeedTwoObjectives = 1;
@@ -444,6 +446,411 @@ __global__ void __launch_bounds__(kPeelThreads) peel_kernel(const uint32_t *__re
     }
 }
 
+// Front peeling with witnesses and one grid barrier per front (n <= 131072
+// points, the unassigned set staged in every block's shared memory).
+//
+// Front 0 is every point with no dominator: its members, in ascending index
+// order (the reference's first front), come from the dom_count == 0 bit set
+// and its prefix popcounts, which every block computes for itself.
+// For k >= 1, Phase A finds the members of front k. Each unassigned point j
+// keeps a witness wit[j], an unassigned dominator found earlier: while the
+// witness stays unassigned, j is settled by one shared-memory bit test. When
+// the witness is peeled, j's row of Dt is scanned again from the witness's
+// word (the words before it held no unassigned dominator then, and the
+// unassigned set only shrinks); no unassigned dominator left makes j a member
+// of front k. A block first tests the witnesses of the points of its own rem
+// words, queueing the points that need a scan, then its warps scan the queue.
+// A member's ordering key is the highest position, in front k-1, of one of
+// its dominators (the reference appends q when its last dominator in front
+// k-1 is processed): for k = 1 the highest-index dominator among front 0's
+// bits (positions there follow indices); for k >= 2 a reverse scan of front
+// k-1 by position.
+// After the barrier, every block loads the L members of front k and counts
+// their positions (by key, then index) itself, clears them from its rem copy
+// and keeps them by position for the next front's keys; block b writes
+// front_indices and rank for the positions p with p % gridDim.x == b. No
+// second barrier is needed: nothing of front k is read from global memory
+// before the next barrier. A front larger than kTile takes the grid-wide
+// counting of peel_kernel and a second barrier instead.
+constexpr int kQueue = 4096; // witness rescans queued per block and front
+
+struct peel2_args {
+    const uint32_t *Dt;
+    const int32_t *dom_count;
+    uint32_t n, W, W8;
+    int32_t *wit;       // n witnesses (-1: none yet)
+    int32_t *list;      // 2 n: members of fronts k (parity k & 1)
+    int32_t *keyv;      // 2 n: their ordering keys
+    int32_t *cnt;       // n + 2 per-front member counters, zeroed
+    int32_t *rank, *front_offsets, *front_indices;
+    peel_state *st;
+};
+
+// In-place exclusive prefix sum of h[0, R) by the whole block (R <= 4
+// entries per thread here); wtot holds 32 ints of scratch.
+__device__ void block_exclusive_scan(int32_t *h, int R, int *wtot)
+{
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int per = (R + static_cast<int>(blockDim.x) - 1) / static_cast<int>(blockDim.x);
+    const int b0 = min(R, static_cast<int>(threadIdx.x) * per), b1 = min(R, b0 + per);
+    int local = 0;
+    for (int i = b0; i < b1; ++i) local += h[i];
+    int incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, incl, o);
+        if (static_cast<int>(lane) >= o) incl += t;
+    }
+    if (lane == 31u) wtot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        int t = lane < nwarp ? wtot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(kFull, t, o);
+            if (static_cast<int>(lane) >= o) t += u;
+        }
+        if (lane < nwarp) wtot[lane] = t;
+    }
+    __syncthreads();
+    int run = incl - local + (warp > 0 ? wtot[warp - 1] : 0);
+    for (int i = b0; i < b1; ++i) {
+        const int c = h[i];
+        h[i] = run;
+        run += c;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ bool bit_of(const uint32_t *s, int32_t q)
+{
+    return (s[q >> 5] >> (q & 31)) & 1u;
+}
+
+__global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
+{
+    extern __shared__ uint32_t dyn[];
+    const uint32_t W = a.W, n = a.n;
+    uint32_t *s_rem = dyn;                                          // W
+    uint32_t *s_Z = s_rem + W;                                      // W: front 0
+    int32_t *s_Zp = reinterpret_cast<int32_t *>(s_Z + W);           // W: exclusive prefix popcounts of s_Z
+    int32_t *s_prev = s_Zp + W;                                     // 2 kTile: front k-1 by position
+    int32_t *s_key = s_prev + 2 * kTile;                            // kTile
+    int32_t *s_idx = s_key + kTile;                                 // kTile
+    int32_t *s_queue = s_idx + kTile;                               // kQueue
+    __shared__ int32_t s_list[kLocalMembers], s_lkey[kLocalMembers];
+    __shared__ int s_cnt, s_base, s_qn, s_wtot[32];
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const unsigned nwarp_b = blockDim.x >> 5;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    // this block's rem words in Phase A
+    const uint32_t wpb = (W + gridDim.x - 1u) / gridDim.x;
+    const uint32_t w_lo = min(W, blockIdx.x * wpb), w_hi = min(W, w_lo + wpb);
+
+    // ---- front 0 from dom_count (every block for itself)
+    for (uint32_t w = warp; w < W; w += nwarp_b) {
+        const uint32_t q = w * 32u + lane;
+        const bool valid = q < n;
+        const bool zero = valid && __ldg(a.dom_count + q) == 0;
+        const uint32_t z = __ballot_sync(kFull, zero), v = __ballot_sync(kFull, valid);
+        if (lane == 0) {
+            s_Z[w] = z;
+            s_rem[w] = v & ~z;
+        }
+    }
+    __syncthreads();
+    {
+        // exclusive prefix popcounts of s_Z: each thread a run of consecutive words
+        const uint32_t per = (W + blockDim.x - 1u) / blockDim.x;
+        const uint32_t b0 = min(W, threadIdx.x * per), b1 = min(W, b0 + per);
+        int local = 0;
+        for (uint32_t w = b0; w < b1; ++w) local += __popc(s_Z[w]);
+        int incl = local;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, incl, o);
+            if (static_cast<int>(lane) >= o) incl += t;
+        }
+        if (lane == 31u) s_wtot[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            int t = lane < nwarp_b ? s_wtot[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(kFull, t, o);
+                if (static_cast<int>(lane) >= o) t += u;
+            }
+            if (lane < nwarp_b) s_wtot[lane] = t; // inclusive warp totals
+        }
+        __syncthreads();
+        int run = incl - local + (warp > 0 ? s_wtot[warp - 1] : 0);
+        for (uint32_t w = b0; w < b1; ++w) {
+            s_Zp[w] = run;
+            run += __popc(s_Z[w]);
+        }
+    }
+    __syncthreads();
+    const int L0 = s_wtot[nwarp_b - 1];
+    // front 0's global writes, spread over the blocks by word
+    for (uint32_t w = blockIdx.x * nwarp_b + warp; w < W; w += gridDim.x * nwarp_b) {
+        const uint32_t z = s_Z[w];
+        if ((z >> lane) & 1u) {
+            const uint32_t q = w * 32u + lane;
+            const int p = s_Zp[w] + __popc(z & ((1u << lane) - 1u));
+            a.front_indices[p] = static_cast<int32_t>(q);
+            a.rank[q] = 0;
+        }
+    }
+    if (tid == 0) a.front_offsets[1] = L0;
+    int off = L0, off_prev = 0, size_prev = L0;
+    bool prev_global = false; // front k-1 by position only in global memory (a large front)
+    int k = 1;
+    for (; off < static_cast<int>(n); ++k) {
+        if (threadIdx.x == 0) {
+            s_cnt = 0;
+            s_qn = 0;
+        }
+        if (prev_global && size_prev <= 2 * kTile) {
+            for (int t = threadIdx.x; t < size_prev; t += blockDim.x) s_prev[t] = __ldcg(a.front_indices + off_prev + t);
+        }
+        const bool prev_in_smem = k >= 2 && size_prev <= 2 * kTile;
+        __syncthreads();
+        // ---- Phase A, stage 1: witness tests over this block's words
+        for (uint32_t w = w_lo + warp; w < w_hi; w += nwarp_b) {
+            const uint32_t bits = s_rem[w];
+            if (!bits) continue;
+            const int32_t j = static_cast<int32_t>(w * 32u + lane);
+            const bool cand = (bits >> lane) & 1u;
+            bool need = false;
+            if (cand) {
+                const int32_t wj = __ldcg(a.wit + j);
+                need = !(wj >= 0 && bit_of(s_rem, wj));
+            }
+            const uint32_t b = __ballot_sync(kFull, need);
+            if (b) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(&s_qn, __popc(b));
+                base = __shfl_sync(kFull, base, 0);
+                if (need) s_queue[base + __popc(b & ((1u << lane) - 1u))] = j;
+            }
+        }
+        __syncthreads();
+        // ---- stage 2: scans of the queued rows
+        const int qn = s_qn;
+        for (int t = static_cast<int>(warp); t < qn; t += static_cast<int>(nwarp_b)) {
+            const int32_t j = s_queue[t];
+            const uint32_t *row = a.Dt + static_cast<uint64_t>(j) * a.W8;
+            const int32_t wj = __ldcg(a.wit + j);
+            const uint32_t ws = wj >= 0 ? static_cast<uint32_t>(wj) >> 5 : 0u;
+            int32_t found = -1;
+            for (uint32_t base = ws; base < W && found < 0; base += 256u) {
+                uint32_t x[8];
+#pragma unroll
+                for (uint32_t u = 0; u < 8u; ++u) {
+                    const uint32_t ww = base + u * 32u + lane;
+                    x[u] = ww < W ? (__ldg(row + ww) & s_rem[ww]) : 0u;
+                }
+#pragma unroll
+                for (uint32_t u = 0; u < 8u; ++u) {
+                    const uint32_t bb = __ballot_sync(kFull, x[u] != 0u);
+                    if (found < 0 && bb) {
+                        const int l0 = __ffs(bb) - 1;
+                        const uint32_t xv = __shfl_sync(kFull, x[u], l0);
+                        found = static_cast<int32_t>((base + u * 32u + static_cast<uint32_t>(l0)) * 32u) + __ffs(xv) - 1;
+                    }
+                }
+            }
+            if (found >= 0) {
+                if (lane == 0) a.wit[j] = found;
+                continue;
+            }
+            // a member of front k: its key
+            int key = -1;
+            if (k == 1) {
+                // the highest-index dominator among front 0 (positions follow indices there)
+                for (int top = static_cast<int>(W) - 1; top >= 0 && key < 0; top -= 256) {
+                    uint32_t x[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int ww = top - u * 32 - static_cast<int>(lane);
+                        x[u] = ww >= 0 ? (__ldg(row + ww) & s_Z[ww]) : 0u;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const uint32_t bb = __ballot_sync(kFull, x[u] != 0u);
+                        if (key < 0 && bb) {
+                            const int l0 = __ffs(bb) - 1; // lowest lane = highest word of this group
+                            const uint32_t xv = __shfl_sync(kFull, x[u], l0);
+                            const int ww = top - u * 32 - l0;
+                            const int hb = 31 - __clz(xv);
+                            key = s_Zp[ww] + __popc(s_Z[ww] & ((hb == 0) ? 0u : (0xffffffffu >> (32 - hb))));
+                        }
+                    }
+                }
+            } else {
+                for (int top = size_prev - 1; top >= 0 && key < 0; top -= 128) {
+                    unsigned bal[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int p = top - 32 * u - static_cast<int>(lane);
+                        bool h = false;
+                        if (p >= 0) {
+                            const uint32_t d = static_cast<uint32_t>(prev_in_smem ? s_prev[p]
+                                                                                  : __ldcg(a.front_indices + off_prev + p));
+                            h = (__ldg(row + (d >> 5)) >> (d & 31u)) & 1u;
+                        }
+                        bal[u] = __ballot_sync(kFull, h);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        if (key < 0 && bal[u]) key = top - 32 * u - (__ffs(bal[u]) - 1);
+                    }
+                }
+            }
+            if (lane == 0) {
+                const int ls = atomicAdd(&s_cnt, 1);
+                if (ls < kLocalMembers) {
+                    s_list[ls] = j;
+                    s_lkey[ls] = key;
+                } else {
+                    const int s = atomicAdd(a.cnt + k, 1);
+                    a.list[(k & 1) * n + s] = j;
+                    a.keyv[(k & 1) * n + s] = key;
+                }
+            }
+        }
+        __syncthreads();
+        const int local = min(s_cnt, kLocalMembers);
+        if (threadIdx.x == 0) s_base = local ? atomicAdd(a.cnt + k, local) : 0;
+        __syncthreads();
+        for (int t = threadIdx.x; t < local; t += blockDim.x) {
+            a.list[(k & 1) * n + s_base + t] = s_list[t];
+            a.keyv[(k & 1) * n + s_base + t] = s_lkey[t];
+        }
+        if (!grid_sync(a.st)) {
+            if (threadIdx.x == 0) atomicExch(&a.st->n_fronts, -1);
+            return;
+        }
+        const int L = *reinterpret_cast<volatile int *>(a.cnt + k);
+        if (L == 0) break; // cannot happen while points remain (a dominance cycle would need one); guards the loop
+        const int32_t *lst = a.list + (k & 1) * n;
+        const int32_t *kv = a.keyv + (k & 1) * n;
+        // keys are positions in front k-1: [0, size_prev)
+        const int R = size_prev;
+        if (L <= kTile && R <= kQueue) {
+            // ---- Phase C in every block: a counting sort by key, ties by index
+            int32_t *h = s_queue;              // R bucket counters, then bucket starts / ends
+            int32_t *s_blist = s_prev + kTile; // members in bucket order
+            for (int t = threadIdx.x; t < R; t += blockDim.x) h[t] = 0;
+            for (int t = threadIdx.x; t < L; t += blockDim.x) {
+                int kq = __ldcg(kv + t);
+                if (kq < 0 || kq >= R) { // a member without a dominator in front k-1: never expected
+                    atomicExch(&a.st->sort_err, 1);
+                    kq = kq < 0 ? 0 : R - 1;
+                }
+                s_key[t] = kq;
+                s_idx[t] = __ldcg(lst + t);
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < L; t += blockDim.x) atomicAdd(h + s_key[t], 1);
+            __syncthreads();
+            block_exclusive_scan(h, R, s_wtot);
+            constexpr int kPer = kTile / kPeelThreads;
+            int b0[kPer], pos[kPer];
+#pragma unroll
+            for (int i = 0; i < kPer; ++i) {
+                const int t = threadIdx.x + i * kPeelThreads;
+                b0[i] = t < L ? h[s_key[t]] : 0;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < kPer; ++i) {
+                const int t = threadIdx.x + i * kPeelThreads;
+                if (t < L) s_blist[atomicAdd(h + s_key[t], 1)] = t;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < kPer; ++i) {
+                const int t = threadIdx.x + i * kPeelThreads;
+                pos[i] = 0;
+                if (t < L) {
+                    const int e = h[s_key[t]], q = s_idx[t];
+                    int p = b0[i];
+                    for (int u = b0[i]; u < e; ++u) p += s_idx[s_blist[u]] < q;
+                    pos[i] = p;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < kPer; ++i) {
+                const int t = threadIdx.x + i * kPeelThreads;
+                if (t < L) {
+                    const int q = s_idx[t], p = pos[i];
+                    s_prev[p] = q; // front k by position, for the keys of front k+1
+                    atomicAnd(s_rem + (q >> 5), ~(1u << (q & 31)));
+                    if (p % static_cast<int>(gridDim.x) == static_cast<int>(blockIdx.x)) {
+                        a.front_indices[off + p] = q;
+                        a.rank[q] = k;
+                    }
+                }
+            }
+            prev_global = false;
+        } else {
+            // ---- a large front: block b ranks members [m_lo, m_hi), one warp per
+            // member, lanes splitting the comparisons against shared-memory tiles;
+            // then a barrier (the next keys read front k from global memory)
+            for (int t = threadIdx.x; t < L; t += blockDim.x) {
+                const int q = __ldcg(lst + t);
+                atomicAnd(s_rem + (q >> 5), ~(1u << (q & 31)));
+            }
+            const int mpb = (L + static_cast<int>(gridDim.x) - 1) / static_cast<int>(gridDim.x);
+            const int m_lo = min(L, static_cast<int>(blockIdx.x) * mpb), m_hi = min(L, m_lo + mpb);
+            int32_t *cntm = s_queue; // mpb <= kQueue (checked on the host)
+            for (int t = threadIdx.x; t < m_hi - m_lo; t += blockDim.x) cntm[t] = 0;
+            for (int t0 = 0; t0 < L; t0 += kTile) {
+                const int lim = min(kTile, L - t0);
+                __syncthreads();
+                for (int t = threadIdx.x; t < lim; t += blockDim.x) {
+                    s_key[t] = __ldcg(kv + t0 + t);
+                    s_idx[t] = __ldcg(lst + t0 + t);
+                }
+                __syncthreads();
+                for (int sidx = m_lo + static_cast<int>(warp); sidx < m_hi; sidx += static_cast<int>(nwarp_b)) {
+                    const int q = __ldcg(lst + sidx), kq = __ldcg(kv + sidx);
+                    int p = 0;
+                    for (int t = static_cast<int>(lane); t < lim; t += 32) {
+                        const int kt = s_key[t], qt = s_idx[t];
+                        p += (kt < kq) | ((kt == kq) & (qt < q));
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(kFull, p, o);
+                    if (lane == 0) cntm[sidx - m_lo] += p;
+                }
+            }
+            __syncthreads();
+            for (int sidx = m_lo + static_cast<int>(threadIdx.x); sidx < m_hi; sidx += static_cast<int>(blockDim.x)) {
+                const int q = __ldcg(lst + sidx), p = cntm[sidx - m_lo];
+                a.front_indices[off + p] = q;
+                a.rank[q] = k;
+            }
+            prev_global = true;
+            if (!grid_sync(a.st)) {
+                if (threadIdx.x == 0) atomicExch(&a.st->n_fronts, -1);
+                return;
+            }
+        }
+        if (tid == 0) a.front_offsets[k + 1] = off + L;
+        off_prev = off;
+        size_prev = L;
+        off += L;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        a.st->n_fronts = *reinterpret_cast<volatile int *>(&a.st->err) ? -1 : k;
+        a.front_offsets[0] = 0;
+    }
+}
+
 // ------------------------------------------------------------ crowding and orders
 
 constexpr int kSortThreads = 256;
@@ -561,11 +968,247 @@ __global__ void __launch_bounds__(kSortThreads) front_crowding_kernel(
             if (threadIdx.x == 0) atomicExch(&st->status, kStatusNeedTwoObjectives);
             continue;
         }
+        if (L > kSortSmemCap) continue; // big_crowding_kernel
         const sort_area<long long> a =
             pick_area<long long>(sort_smem, L, reinterpret_cast<long long *>(wkey) + off, widx + off, wlist + off,
                                  wpos + 2 * off);
         front_crowding(pts, n, m, keys, mem, L, a, &ctl, slots, &st->sort_err, cd);
     }
+}
+
+// ---------------------------------------------------------- grid-wide sorts
+//
+// Sorts longer than kSortSmemCap run on every block of a cooperative launch
+// (one block of kGridSortThreads per SM), still with std::sort's exact
+// permutation: the introsort's levels are processed in order, each range
+// longer than kSortSmemCap partitioned by one block (block_partition: the
+// same median-of-three and Hoare pairs as the sequential loop), the levels
+// separated by grid barriers; ranges of 17..kSortSmemCap elements are then
+// sorted by one block each in shared memory, continuing the introsort with
+// the depth budget they were created with, and ranges of 16 or fewer are
+// sorted as leaves when they appear. Ranges of one level are disjoint, so the
+// blocks that take them do not change the result.
+constexpr int kGridSortThreads = 1024;
+constexpr int kGridSortWarps = kGridSortThreads / 32;
+
+struct grid_sort_mem {
+    int2 *lists;  // L int2 of scratch: two level lists, the shared-memory ranges and their depths
+    int32_t *pos; // 2 L stopper positions
+};
+
+// Queues child [a, b) (depth budget d) of a partition by the grid.
+__device__ __forceinline__ void grid_queue(int a, int b, int d, int2 *next, int big_cap, int2 *bot, int2 *bot_d,
+                                           int bot_cap, int *nnext, int *nbot, int *err)
+{
+    const int len = b - a;
+    if (len > kSortSmemCap) {
+        const int slot = atomicAdd(nnext, 1);
+        if (slot < big_cap)
+            next[slot] = make_int2(a, b);
+        else
+            atomicExch(err, dev::kSortErrListFull);
+    } else if (len > 16) {
+        const int slot = atomicAdd(nbot, 1);
+        if (slot < bot_cap) {
+            bot[slot] = make_int2(a, b);
+            bot_d[slot] = make_int2(d, 0);
+        } else {
+            atomicExch(err, dev::kSortErrListFull);
+        }
+    }
+}
+
+// Every block of the cooperative launch calls it with the same arguments
+// (L > kSortSmemCap). Returns false when a grid barrier gave up.
+template <typename K>
+__device__ bool grid_std_sort(const dev::sort_view<K> &x, int L, const grid_sort_mem &g, peel_state *st,
+                              unsigned char *sort_smem, dev::sort_ctl *ctl, int *slots, int *err)
+{
+    const int big_cap = L / (kSortSmemCap + 1) + 2, bot_cap = L / 17 + 2;
+    int2 *big[2] = {g.lists, g.lists + big_cap};
+    int2 *bot = g.lists + 2 * big_cap, *bot_d = bot + bot_cap;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int i = 0; i < 72; ++i) st->gs[i] = 0;
+        st->gs[1] = 1;
+        big[0][0] = make_int2(0, L);
+    }
+    if (!grid_sync(st)) return false;
+    const unsigned lane = threadIdx.x & 31u;
+    const int warp = static_cast<int>(threadIdx.x >> 5);
+    int depth = 2 * dev::floor_log2_int(L);
+    for (int level = 0; level < 70; ++level, --depth) {
+        const int nbig = min(*reinterpret_cast<volatile int *>(&st->gs[1 + level]), big_cap);
+        if (nbig == 0) break;
+        int2 *cur = big[level & 1], *next = big[(level + 1) & 1];
+        for (int t = blockIdx.x; t < nbig; t += gridDim.x) {
+            const int2 r = cur[t];
+            if (depth == 0) {
+                if (threadIdx.x == 0) dev::heap_sort(x, r.x, r.y);
+                __syncthreads();
+                continue;
+            }
+            dev::sort_work w{};
+            w.pos_l = g.pos + r.x;
+            w.pos_r = g.pos + L + r.x;
+            const int cut = dev::block_partition(x, r.x, r.y, w, slots, err);
+            if (threadIdx.x == 0)
+                grid_queue(r.x, cut, depth - 1, next, big_cap, bot, bot_d, bot_cap, &st->gs[2 + level], &st->gs[0], err);
+            if (threadIdx.x == 32)
+                grid_queue(cut, r.y, depth - 1, next, big_cap, bot, bot_d, bot_cap, &st->gs[2 + level], &st->gs[0], err);
+            if (warp == 0) {
+                const int a = lane < 16u ? r.x : cut, len = lane < 16u ? cut - r.x : r.y - cut;
+                dev::halfwarp_leaf_sort(x, a, len <= 16 ? len : 0);
+            }
+            __syncthreads();
+        }
+        if (!grid_sync(st)) return false;
+    }
+    // the shared-memory ranges, one block each
+    const int nbot = min(*reinterpret_cast<volatile int *>(&st->gs[0]), bot_cap);
+    for (int t = blockIdx.x; t < nbot; t += gridDim.x) {
+        const int2 r = bot[t];
+        const int d = bot_d[t].x, len = r.y - r.x;
+        const sort_area<K> a = pick_area<K>(sort_smem, len, nullptr, nullptr, nullptr, nullptr);
+        for (int i = threadIdx.x; i < len; i += blockDim.x) {
+            a.k[i] = x.k[r.x + i];
+            a.v[i] = x.v[r.x + i];
+        }
+        __syncthreads();
+        dev::block_std_sort(dev::sort_view<K>{a.k, a.v}, len, a.w, ctl, slots, err, d);
+        for (int i = threadIdx.x; i < len; i += blockDim.x) {
+            x.k[r.x + i] = a.k[i];
+            x.v[r.x + i] = a.v[i];
+        }
+        __syncthreads();
+    }
+    return grid_sync(st);
+}
+
+// Crowding distance of one front longer than kSortSmemCap by every block of a
+// cooperative launch: the same per-objective sorts as front_crowding, each
+// starting from the previous objective's order, and the same neighbour
+// differences. kb, v: L keys and values of scratch. Returns false when a grid
+// barrier gave up.
+__device__ bool grid_front_crowding(const double *__restrict__ pts, uint32_t n, uint32_t m,
+                                    const long long *__restrict__ keys, const int32_t *mem, int L, long long *kb,
+                                    int32_t *v, const grid_sort_mem &g, peel_state *st, unsigned char *sort_smem,
+                                    dev::sort_ctl *ctl, int *slots, double *cd)
+{
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x, gn = gridDim.x * blockDim.x;
+    for (uint32_t p = gt; p < static_cast<uint32_t>(L); p += gn) {
+        const int32_t q = mem[p];
+        v[p] = q;
+        cd[q] = 0.0;
+    }
+    if (!grid_sync(st)) return false;
+    for (uint32_t k = 0; k < m; ++k) {
+        const long long *kk = keys + static_cast<uint64_t>(k) * n;
+        for (uint32_t p = gt; p < static_cast<uint32_t>(L); p += gn) kb[p] = kk[v[p]];
+        if (!grid_sync(st)) return false;
+        if (!grid_std_sort(dev::sort_view<long long>{kb, v}, L, g, st, sort_smem, ctl, slots, &st->sort_err))
+            return false;
+        const int32_t q0 = v[0], q1 = v[L - 1];
+        const double df = pts[static_cast<uint64_t>(q1) * m + k] - pts[static_cast<uint64_t>(q0) * m + k];
+        for (uint32_t p = 1u + gt; p < static_cast<uint32_t>(L - 1); p += gn) {
+            const int32_t q = v[p];
+            cd[q] += (pts[static_cast<uint64_t>(v[p + 1]) * m + k] - pts[static_cast<uint64_t>(v[p - 1]) * m + k])
+                     / df;
+        }
+        if (!grid_sync(st)) return false;
+        if (gt == 0) {
+            cd[q0] = HUGE_VAL;
+            cd[q1] = HUGE_VAL;
+        }
+        if (!grid_sync(st)) return false;
+    }
+    return true;
+}
+
+// The fronts longer than kSortSmemCap (front_crowding_kernel skips them), one
+// after the other.
+__global__ void __launch_bounds__(kGridSortThreads) big_crowding_kernel(
+    const double *__restrict__ pts, uint32_t n, uint32_t m, const long long *__restrict__ keys,
+    const int32_t *__restrict__ front_offsets, const int32_t *__restrict__ front_indices,
+    const int32_t *__restrict__ n_fronts, unsigned char *wkey, int32_t *widx, int2 *wlist, int32_t *wpos, double *cd,
+    peel_state *st)
+{
+    extern __shared__ __align__(16) unsigned char sort_smem[];
+    __shared__ dev::sort_ctl ctl;
+    __shared__ int slots[kGridSortWarps * 64];
+    const int nf = *n_fronts;
+    if (m < 2u) return; // front_crowding_kernel reports it
+    for (int f = 0; f < nf; ++f) {
+        const int off = front_offsets[f], L = front_offsets[f + 1] - off;
+        if (L <= kSortSmemCap) continue;
+        const grid_sort_mem g{wlist + off, wpos + 2 * off};
+        if (!grid_front_crowding(pts, n, m, keys, front_indices + off, L, reinterpret_cast<long long *>(wkey) + off,
+                                 widx + off, g, st, sort_smem, &ctl, slots, cd))
+            return;
+    }
+}
+
+// The critical front of select_best_N_mo when it is longer than kSortSmemCap
+// (select_best_kernel copies the whole fronts before it and leaves the rest):
+// the critical front's crowding and its descending sort, by the whole grid.
+__global__ void __launch_bounds__(kGridSortThreads) select_best_big_kernel(
+    const double *__restrict__ pts, uint32_t n, uint32_t m, uint32_t N, const long long *__restrict__ keys,
+    const int32_t *__restrict__ front_offsets, const int32_t *__restrict__ front_indices,
+    const int32_t *__restrict__ n_fronts, unsigned char *wkey, int32_t *widx, int2 *wlist, int32_t *wpos, double *wcd,
+    int32_t *out, peel_state *st)
+{
+    extern __shared__ __align__(16) unsigned char sort_smem[];
+    __shared__ dev::sort_ctl ctl;
+    __shared__ int slots[kGridSortWarps * 64];
+    const int nf = *n_fronts;
+    if (nf < 1 || m < 2u) return;
+    int lo = 0, hi = nf - 1; // first front whose end passes N
+    while (lo < hi) {
+        const int mid = (lo + hi) / 2;
+        if (static_cast<uint32_t>(front_offsets[mid + 1]) > N)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    const int off = front_offsets[lo], L = front_offsets[lo + 1] - off;
+    if (L <= kSortSmemCap || static_cast<uint32_t>(off) == N) return;
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x, gn = gridDim.x * blockDim.x;
+    const int32_t *mem = front_indices + off; // the whole fronts before it: copied by select_best_kernel
+    long long *kb = reinterpret_cast<long long *>(wkey) + off;
+    int32_t *v = widx + off;
+    const grid_sort_mem g{wlist + off, wpos + 2 * off};
+    if (!grid_front_crowding(pts, n, m, keys, mem, L, kb, v, g, st, sort_smem, &ctl, slots, wcd)) return;
+    for (uint32_t p = gt; p < static_cast<uint32_t>(L); p += gn) {
+        kb[p] = ~order_key(wcd[mem[p]]); // descending, NaN first: greater_than_f
+        v[p] = static_cast<int32_t>(p);
+    }
+    if (!grid_sync(st)) return;
+    if (!grid_std_sort(dev::sort_view<long long>{kb, v}, L, g, st, sort_smem, &ctl, slots, &st->sort_err)) return;
+    const uint32_t remaining = N - static_cast<uint32_t>(off);
+    for (uint32_t j = gt; j < remaining; j += gn) out[off + j] = mem[v[j]];
+}
+
+// sort_population_mo's final sort of 0..n-1 by (rank, descending crowding)
+// for n > kSortSmemCap, by the whole grid.
+__global__ void __launch_bounds__(kGridSortThreads) sort_population_big_kernel(
+    const int32_t *__restrict__ rank, const double *__restrict__ crowd, uint32_t n, const int32_t *__restrict__ n_fronts,
+    unsigned char *wkey, int32_t *widx, int2 *wlist, int32_t *wpos, int32_t *out, peel_state *st)
+{
+    extern __shared__ __align__(16) unsigned char sort_smem[];
+    __shared__ dev::sort_ctl ctl;
+    __shared__ int slots[kGridSortWarps * 64];
+    if (*n_fronts < 1 || *reinterpret_cast<volatile int *>(&st->status) != 0) return;
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x, gn = gridDim.x * blockDim.x;
+    dev::key2 *kb = reinterpret_cast<dev::key2 *>(wkey);
+    for (uint32_t q = gt; q < n; q += gn) {
+        kb[q] = dev::key2{rank[q], ~order_key(crowd[q])};
+        widx[q] = static_cast<int32_t>(q);
+    }
+    if (!grid_sync(st)) return;
+    const grid_sort_mem g{wlist, wpos};
+    if (!grid_std_sort(dev::sort_view<dev::key2>{kb, widx}, static_cast<int>(n), g, st, sort_smem, &ctl, slots,
+                       &st->sort_err))
+        return;
+    for (uint32_t j = gt; j < n; j += gn) out[j] = widx[j];
 }
 
 // select_best_N_mo (multi_objective.cpp:344-396) for 2 <= n, 1 <= N < n, by
@@ -606,6 +1249,7 @@ __global__ void __launch_bounds__(kSortThreads) select_best_kernel(
         if (threadIdx.x == 0) atomicExch(&st->status, kStatusNeedTwoObjectives);
         return;
     }
+    if (L > kSortSmemCap) return; // select_best_big_kernel
     const int32_t *mem = front_indices + off;
     const sort_area<long long> a =
         pick_area<long long>(sort_smem, L, reinterpret_cast<long long *>(wkey) + off, widx + off, wlist + off,
@@ -667,6 +1311,20 @@ __global__ void __launch_bounds__(kSortThreads) sort_pairs_kernel(long long *k, 
             k[p] = a.k[p];
             v[p] = a.v[p];
         }
+    }
+}
+
+// The same for n > kSortSmemCap, by the whole grid (cooperative launch).
+__global__ void __launch_bounds__(kGridSortThreads) sort_pairs_grid_kernel(long long *k, int32_t *v, uint32_t n,
+                                                                          int2 *wlist, int32_t *wpos, peel_state *st,
+                                                                          int *err)
+{
+    extern __shared__ __align__(16) unsigned char sort_smem[];
+    __shared__ dev::sort_ctl ctl;
+    __shared__ int slots[kGridSortWarps * 64];
+    const grid_sort_mem g{wlist, wpos};
+    if (!grid_std_sort(dev::sort_view<long long>{k, v}, static_cast<int>(n), g, st, sort_smem, &ctl, slots, err)) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(err, 100); // a grid barrier gave up
     }
 }
 
@@ -875,8 +1533,10 @@ struct survival_scratch {
     uint32_t *Dt;        // n * W8 dominated-by bit matrix
     peel_state *st;      // barrier, counters, status
     uint32_t *rem;       // W8 unassigned-point bit set
-    int32_t *list;       // n members of the front being built
-    int32_t *keyv;       // n their ordering keys
+    int32_t *list;       // 2 n members of the front being built (two parities)
+    int32_t *keyv;       // 2 n their ordering keys
+    int32_t *wit;        // n peeling witnesses
+    int32_t *cnt;        // n + 2 per-front member counters
     unsigned char *wkey; // n * 16 B sort keys of fronts too large for shared memory
     int32_t *widx;       // n sort values
     int2 *wlist;         // n sort ranges
@@ -888,7 +1548,8 @@ constexpr size_t survival_scratch_bytes(uint64_t n, uint64_t m)
 {
     return align256(n * (m > 0 ? m : 1) * sizeof(long long))
            + align256(n * ((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u) + align256(sizeof(peel_state))
-           + align256(((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u) + 2u * align256(n * 4u) + align256(n * 16u)
+           + align256(((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u) + 2u * align256(2u * n * 4u)
+           + align256(n * 4u) + align256((n + 2u) * 4u) + align256(n * 16u)
            + align256(n * 4u) + align256(n * sizeof(int2)) + align256(2u * n * 4u) + align256(n * sizeof(double));
 }
 
@@ -907,9 +1568,13 @@ survival_scratch carve_survival_scratch(void *base, uint64_t n, uint64_t m)
     s.rem = reinterpret_cast<uint32_t *>(p);
     p += align256(W8 * 4u);
     s.list = reinterpret_cast<int32_t *>(p);
-    p += align256(n * 4u);
+    p += align256(2u * n * 4u);
     s.keyv = reinterpret_cast<int32_t *>(p);
+    p += align256(2u * n * 4u);
+    s.wit = reinterpret_cast<int32_t *>(p);
     p += align256(n * 4u);
+    s.cnt = reinterpret_cast<int32_t *>(p);
+    p += align256((n + 2u) * 4u);
     s.wkey = reinterpret_cast<unsigned char *>(p);
     p += align256(n * 16u);
     s.widx = reinterpret_cast<int32_t *>(p);
@@ -920,6 +1585,27 @@ survival_scratch carve_survival_scratch(void *base, uint64_t n, uint64_t m)
     p += align256(2u * n * 4u);
     s.wcd = reinterpret_cast<double *>(p);
     return s;
+}
+
+// Kernels launch_front_crowding issues for n points of m objectives.
+constexpr int crowding_launches(uint32_t n, uint32_t m)
+{
+    return n > static_cast<uint32_t>(kSortSmemCap) && m >= 2u ? 2 : 1;
+}
+
+// Cooperative launch of a grid-sort kernel: one block of kGridSortThreads per
+// SM (the grid barriers need every block resident).
+template <typename... A>
+int launch_cooperative_sort_kernel(const void *kernel, int num_sms, cudaStream_t s, A... args)
+{
+    PGX_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(kSortSmemBytes)));
+    int occ = 0;
+    PGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kGridSortThreads, kSortSmemBytes));
+    PGX_CHECK(occ >= 1, PGX_ERR_CUDA, "grid sort kernel cannot be resident");
+    void *argv[] = {static_cast<void *>(&args)...};
+    PGX_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(num_sms), dim3(kGridSortThreads), argv, kSortSmemBytes, s));
+    return PGX_OK;
 }
 
 int launch_front_crowding(const survival_scratch &sc, const double *d_points, uint32_t n, uint32_t m,
@@ -933,6 +1619,12 @@ int launch_front_crowding(const survival_scratch &sc, const double *d_points, ui
                                                                      front_indices, n_fronts, mode, sc.wkey, sc.widx,
                                                                      sc.wlist, sc.wpos, cd, sc.st);
     PGX_CUDA(cudaGetLastError());
+    if (n > static_cast<uint32_t>(kSortSmemCap) && m >= 2u) {
+        // fronts longer than the shared-memory sorts: every SM on each of them
+        PGX_TRY(launch_cooperative_sort_kernel(reinterpret_cast<const void *>(big_crowding_kernel), num_sms, s,
+                                               d_points, n, m, sc.keys, front_offsets, front_indices, n_fronts,
+                                               sc.wkey, sc.widx, sc.wlist, sc.wpos, cd, sc.st));
+    }
     return PGX_OK;
 }
 
@@ -962,6 +1654,24 @@ int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n,
     }
 
     // cooperative peel: every block resident at once (the grid barrier needs it)
+    const uint32_t wpb = (W + static_cast<uint32_t>(num_sms) - 1u) / static_cast<uint32_t>(num_sms);
+    if (W <= static_cast<uint32_t>(kRemWords) && 32u * wpb <= static_cast<uint32_t>(kQueue)
+        && n <= static_cast<uint64_t>(kQueue) * static_cast<uint32_t>(num_sms)) {
+        const size_t smem2 = (3u * static_cast<size_t>(W) + 4u * kTile + kQueue) * sizeof(int32_t);
+        PGX_CUDA(cudaFuncSetAttribute(peel2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem2)));
+        int occ2 = 0;
+        PGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, peel2_kernel, kPeelThreads, smem2));
+        PGX_CHECK(occ2 >= 1, PGX_ERR_CUDA, "peel kernel cannot be resident");
+        PGX_CUDA(cudaMemsetAsync(sc.wit, 0xff, static_cast<size_t>(n) * sizeof(int32_t), s));
+        PGX_CUDA(cudaMemsetAsync(sc.cnt, 0, (static_cast<size_t>(n) + 2u) * sizeof(int32_t), s));
+        peel2_args pa{sc.Dt, out.dom_count, n, W, W8, sc.wit, sc.list, sc.keyv, sc.cnt,
+                      out.rank, out.front_offsets, out.front_indices, sc.st};
+        void *args2[] = {&pa};
+        PGX_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(peel2_kernel), dim3(num_sms),
+                                             dim3(kPeelThreads), args2, smem2, s));
+        *launches += 1;
+    } else {
     const size_t smem = 2u * kTile * sizeof(int32_t);
     int occ = 0;
     PGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, peel_kernel, kPeelThreads, smem));
@@ -979,12 +1689,13 @@ int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n,
                                              smem, s));
         *launches += 1;
     }
+    }
     PGX_CUDA(cudaMemcpyAsync(out.n_fronts, &sc.st->n_fronts, sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
 
     if (out.crowding) {
         PGX_TRY(launch_front_crowding(sc, d_points, n, m, out.front_offsets, out.front_indices, out.n_fronts,
                                       kCrowdNsga2, out.crowding, num_sms, s));
-        *launches += 1;
+        *launches += crowding_launches(n, m);
     }
     return PGX_OK;
 }
@@ -1051,7 +1762,7 @@ int launch_crowding_single(pgx_context *ctx, const double *d_points, uint64_t n6
     PGX_CUDA(cudaGetLastError());
     PGX_TRY(launch_front_crowding(sc, d_points, n, m, front_offsets, front_indices, n_fronts, kCrowdSortPopulation,
                                   d_out, sms, s));
-    ctx->launches += 3;
+    ctx->launches += 2 + crowding_launches(n, m);
     return PGX_OK;
 }
 
@@ -1154,6 +1865,14 @@ int launch_select_best(pgx_context *ctx, const double *d_points, uint64_t n64, u
                                                                sc.wlist, sc.wpos, sc.wcd, d_out, sc.st);
     PGX_CUDA(cudaGetLastError());
     ++ctx->launches;
+    if (n > static_cast<uint32_t>(kSortSmemCap) && m >= 2u) {
+        // a critical front longer than the shared-memory sorts: every SM on it
+        PGX_TRY(launch_cooperative_sort_kernel(reinterpret_cast<const void *>(select_best_big_kernel), sms, s,
+                                               d_points, n, m, N, sc.keys, fb.o.front_offsets, fb.o.front_indices,
+                                               fb.o.n_fronts, sc.wkey, sc.widx, sc.wlist, sc.wpos, sc.wcd, d_out,
+                                               sc.st));
+        ++ctx->launches;
+    }
     return finish_status(sc, d_status, s, &ctx->launches);
 }
 
@@ -1173,20 +1892,41 @@ int launch_sort_population(pgx_context *ctx, const double *d_points, uint64_t n6
     PGX_TRY(run_survival(sc, d_points, n, m, fb.o, sms, s, &ctx->launches));
     PGX_TRY(launch_front_crowding(sc, d_points, n, m, fb.o.front_offsets, fb.o.front_indices, fb.o.n_fronts,
                                   kCrowdSortPopulation, sc.wcd, sms, s));
-    PGX_CUDA(cudaFuncSetAttribute(sort_population_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(kSortSmemBytes)));
-    sort_population_kernel<<<1, kSortThreads, kSortSmemBytes, s>>>(fb.o.rank, sc.wcd, n, fb.o.n_fronts, sc.wkey,
-                                                                   sc.widx, sc.wlist, sc.wpos, d_out, sc.st);
-    PGX_CUDA(cudaGetLastError());
-    ctx->launches += 2;
+    if (n > static_cast<uint32_t>(kSortSmemCap)) {
+        PGX_TRY(launch_cooperative_sort_kernel(reinterpret_cast<const void *>(sort_population_big_kernel), sms, s,
+                                               static_cast<const int32_t *>(fb.o.rank),
+                                               static_cast<const double *>(sc.wcd), n,
+                                               static_cast<const int32_t *>(fb.o.n_fronts), sc.wkey, sc.widx,
+                                               sc.wlist, sc.wpos, d_out, sc.st));
+    } else {
+        PGX_CUDA(cudaFuncSetAttribute(sort_population_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(kSortSmemBytes)));
+        sort_population_kernel<<<1, kSortThreads, kSortSmemBytes, s>>>(fb.o.rank, sc.wcd, n, fb.o.n_fronts, sc.wkey,
+                                                                       sc.widx, sc.wlist, sc.wpos, d_out, sc.st);
+        PGX_CUDA(cudaGetLastError());
+    }
+    ctx->launches += 1 + crowding_launches(n, m);
     return finish_status(sc, d_status, s, &ctx->launches);
 }
 
+size_t sort_pairs_state_bytes()
+{
+    return sizeof(peel_state);
+}
+
 int launch_sort_pairs(pgx_context *ctx, long long *d_keys, int32_t *d_vals, uint64_t n64, int *d_err, int2 *d_lists,
-                      int32_t *d_pos, cudaStream_t s)
+                      int32_t *d_pos, void *d_state, cudaStream_t s)
 {
     if (n64 < 2) return PGX_OK;
     PGX_CHECK(n64 <= (1ull << 30), PGX_ERR_CAPACITY, "sort: more than 2^30 elements");
+    if (n64 > static_cast<uint64_t>(kSortSmemCap)) {
+        PGX_CUDA(cudaMemsetAsync(d_state, 0, sizeof(peel_state), s));
+        PGX_TRY(launch_cooperative_sort_kernel(reinterpret_cast<const void *>(sort_pairs_grid_kernel), ctx->num_sms,
+                                               s, d_keys, d_vals, static_cast<uint32_t>(n64), d_lists, d_pos,
+                                               static_cast<peel_state *>(d_state), d_err));
+        ++ctx->launches;
+        return PGX_OK;
+    }
     PGX_CUDA(cudaFuncSetAttribute(sort_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(kSortSmemBytes)));
     sort_pairs_kernel<<<1, kSortThreads, kSortSmemBytes, s>>>(d_keys, d_vals, static_cast<uint32_t>(n64), d_lists,

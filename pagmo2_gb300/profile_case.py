@@ -39,6 +39,7 @@ def main() -> None:
     ap.add_argument("--atoms", type=int, default=150, help="lennard_jones cluster size (lj_* cases)")
     ap.add_argument("--dim", type=int, default=0, help="rastrigin/rosenbrock dimension (default 50 / 1000)")
     ap.add_argument("--fdim", type=int, default=3, help="DTLZ objectives (dtlz* cases)")
+    ap.add_argument("--layers", type=int, default=30, help="nested fronts of the survival/select_best/sort cases")
     a = ap.parse_args()
 
     import torch
@@ -61,7 +62,7 @@ def main() -> None:
         def run():
             ep.launch_device(sp)
     elif a.case == "survival":
-        p = W.nsga2_points(n, 3, layers=30)
+        p = W.nsga2_points(n, 3, layers=a.layers)
         dp = torch.from_numpy(p).cuda()
         i32 = lambda k: torch.empty(k, dtype=torch.int32, device="cuda")  # noqa: E731
         rank, dc, off, idx, nf = i32(n), i32(n), i32(n + 1), i32(n), i32(1)
@@ -71,7 +72,7 @@ def main() -> None:
             N.check(L.pgx_nsga2_survival_device(ctx.handle, dp.data_ptr(), n, 3, rank.data_ptr(), dc.data_ptr(),
                                                 off.data_ptr(), idx.data_ptr(), nf.data_ptr(), cd.data_ptr(), sp))
     elif a.case in ("select_best", "sort_population"):
-        p = W.nsga2_points(n, 3, layers=30)
+        p = W.nsga2_points(n, 3, layers=a.layers)
         dp = torch.from_numpy(p).cuda()
         sel = torch.empty(n, dtype=torch.int32, device="cuda")
         st = torch.empty(1, dtype=torch.int32, device="cuda")
