@@ -641,22 +641,36 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
             const int32_t j = s_queue[t];
             const uint32_t *row = a.Dt + static_cast<uint64_t>(j) * a.W8;
             const int32_t wj = __ldcg(a.wit + j);
-            const uint32_t ws = wj >= 0 ? static_cast<uint32_t>(wj) >> 5 : 0u;
+            // 512 words per round, four per 16-byte load (rows start on 32-byte
+            // boundaries; words from W on are masked)
+            const uint32_t ws = (wj >= 0 ? static_cast<uint32_t>(wj) >> 5 : 0u) & ~3u;
             int32_t found = -1;
-            for (uint32_t base = ws; base < W && found < 0; base += 256u) {
-                uint32_t x[8];
+            for (uint32_t base = ws; base < W && found < 0; base += 512u) {
+                uint4 x[4];
 #pragma unroll
-                for (uint32_t u = 0; u < 8u; ++u) {
-                    const uint32_t ww = base + u * 32u + lane;
-                    x[u] = ww < W ? (__ldg(row + ww) & s_rem[ww]) : 0u;
+                for (uint32_t u = 0; u < 4u; ++u) {
+                    const uint32_t wi = base + 4u * (u * 32u + lane);
+                    x[u] = make_uint4(0u, 0u, 0u, 0u);
+                    if (wi < W) {
+                        const uint4 d = __ldg(reinterpret_cast<const uint4 *>(row + wi));
+                        const uint4 r = *reinterpret_cast<const uint4 *>(s_rem + wi);
+                        x[u].x = d.x & r.x;
+                        x[u].y = wi + 1u < W ? d.y & r.y : 0u;
+                        x[u].z = wi + 2u < W ? d.z & r.z : 0u;
+                        x[u].w = wi + 3u < W ? d.w & r.w : 0u;
+                    }
                 }
 #pragma unroll
-                for (uint32_t u = 0; u < 8u; ++u) {
-                    const uint32_t bb = __ballot_sync(kFull, x[u] != 0u);
+                for (uint32_t u = 0; u < 4u; ++u) {
+                    const uint32_t bb = __ballot_sync(kFull, (x[u].x | x[u].y | x[u].z | x[u].w) != 0u);
                     if (found < 0 && bb) {
                         const int l0 = __ffs(bb) - 1;
-                        const uint32_t xv = __shfl_sync(kFull, x[u], l0);
-                        found = static_cast<int32_t>((base + u * 32u + static_cast<uint32_t>(l0)) * 32u) + __ffs(xv) - 1;
+                        const uint32_t c0 = __shfl_sync(kFull, x[u].x, l0), c1 = __shfl_sync(kFull, x[u].y, l0);
+                        const uint32_t c2 = __shfl_sync(kFull, x[u].z, l0), c3 = __shfl_sync(kFull, x[u].w, l0);
+                        const uint32_t c = c0 ? 0u : (c1 ? 1u : (c2 ? 2u : 3u));
+                        const uint32_t xv = c0 ? c0 : (c1 ? c1 : (c2 ? c2 : c3));
+                        const uint32_t word = base + 4u * (u * 32u + static_cast<uint32_t>(l0)) + c;
+                        found = static_cast<int32_t>(word * 32u) + __ffs(xv) - 1;
                     }
                 }
             }
