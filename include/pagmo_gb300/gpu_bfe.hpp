@@ -1,7 +1,7 @@
 // gpu_bfe: a user-defined batch fitness evaluator (UDBFE) for pagmo::bfe
 // that evaluates pagmo's own rastrigin, rosenbrock, lennard_jones, ackley,
-// griewank, schwefel, zdt and dtlz UDPs (DTLZ4 excepted), and the GPU UDPs of
-// gpu_problems.hpp, on a GB300.
+// griewank, schwefel, zdt and dtlz UDPs (DTLZ4 excepted), the GPU UDPs of
+// gpu_problems.hpp, and any of these inside pagmo's translate, on a GB300.
 //
 // A UDBFE is a callable vector_double(const problem &, const vector_double &)
 // (include/pagmo/bfe.hpp:68-108). Like every UDBFE it leaves the fevals
@@ -25,6 +25,7 @@
 #include <pagmo/problems/rastrigin.hpp>
 #include <pagmo/problems/rosenbrock.hpp>
 #include <pagmo/problems/schwefel.hpp>
+#include <pagmo/problems/translate.hpp>
 #include <pagmo/problems/zdt.hpp>
 #include <pagmo/threading.hpp>
 #include <pagmo/types.hpp>
@@ -51,6 +52,15 @@ public:
         if (const auto *g = p.extract<gpu_zdt>()) return g->batch_fitness(dvs);
         if (const auto *g = p.extract<gpu_dtlz>()) return g->batch_fitness(dvs);
         if (p.extract<pagmo::zdt>() || p.extract<pagmo::dtlz>()) return mo_fitness(p, dvs);
+        if (const auto *t = p.extract<pagmo::translate>()) {
+            // translate::batch_fitness (src/problems/translate.cpp:118-146): the
+            // decision vectors shifted back, then the inner problem's evaluation
+            const auto &tr = t->get_translation();
+            const auto nx = tr.size();
+            pagmo::vector_double back(dvs.size());
+            for (std::size_t i = 0; i < dvs.size(); ++i) back[i] = dvs[i] - tr[i % nx];
+            return (*this)(t->get_inner_problem(), back);
+        }
         int kind = 0;
         std::uint64_t param = p.get_nx();
         if (p.extract<pagmo::rastrigin>()) {

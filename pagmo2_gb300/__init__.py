@@ -19,4 +19,5 @@ from ._native import Context, default_context  # noqa: F401
 from .batch_evaluators import bfe, gpu_bfe, problem  # noqa: F401
 from .multi_objective import (crowding_distance, fast_non_dominated_sorting, nsga2_survival,  # noqa: F401
                               select_best_N_mo, sort_population_mo)
-from .problems import ackley, dtlz, griewank, lennard_jones, rastrigin, rosenbrock, schwefel, zdt  # noqa: F401
+from .problems import (ackley, dtlz, griewank, lennard_jones, rastrigin, rosenbrock, schwefel,  # noqa: F401
+                       translate, zdt)

@@ -29,6 +29,8 @@ class gpu_bfe:
 
     def __call__(self, prob, dvs) -> np.ndarray:
         udp = getattr(prob, "udp", prob)
+        if isinstance(udp, P.translate):
+            return udp.batch_fitness(dvs)
         if not isinstance(udp, (P._gpu_udp, P._gpu_mo_udp)):
             name = udp.get_name() if hasattr(udp, "get_name") else type(udp).__name__
             raise ValueError(f"Cannot use a gpu_bfe on the problem '{name}': only the GPU rastrigin, rosenbrock, "

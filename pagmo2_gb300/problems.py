@@ -306,6 +306,58 @@ class dtlz(_gpu_mo_udp):
         return f"DTLZ{self.prob_id}"
 
 
+class translate:
+    """translate{udp, translation} (src/problems/translate.cpp): f(x) = inner(x - translation), bounds shifted by
+    the translation; batch_fitness shifts the whole batch back and forwards it to the inner problem's batch_fitness
+    (translate.cpp:118-146), so a GPU UDP inside stays a one-pass GPU evaluation."""
+
+    def __init__(self, udp, translation):
+        self.inner = udp
+        self.translation = np.ascontiguousarray(np.asarray(translation, dtype=np.float64).reshape(-1))
+        if self.translation.size != udp.get_nx():
+            raise ValueError(f"Length of shift vector is: {self.translation.size} while the problem dimension is: "
+                             f"{udp.get_nx()}")
+        self.thread_safety = getattr(udp, "thread_safety", "basic")
+
+    def get_nx(self) -> int:
+        return self.inner.get_nx()
+
+    def get_nobj(self) -> int:
+        return self.inner.get_nobj()
+
+    def get_nf(self) -> int:
+        return self.inner.get_nf()
+
+    def get_bounds(self):
+        lb, ub = self.inner.get_bounds()
+        return lb + self.translation, ub + self.translation
+
+    def get_name(self) -> str:
+        return self.inner.get_name() + " [translated]"
+
+    def get_thread_safety(self) -> str:
+        return self.thread_safety
+
+    def has_gradient(self) -> bool:
+        return self.inner.has_gradient() if hasattr(self.inner, "has_gradient") else hasattr(self.inner, "gradient")
+
+    def _back(self, dvs) -> np.ndarray:
+        x = _as_rows(dvs, self.get_nx()).reshape(-1, self.get_nx())
+        return (x - self.translation).reshape(-1)
+
+    def batch_fitness(self, dvs) -> np.ndarray:
+        return self.inner.batch_fitness(self._back(dvs))
+
+    def fitness(self, x) -> np.ndarray:
+        return self.inner.fitness(np.asarray(x, dtype=np.float64) - self.translation)
+
+    def gradient(self, x) -> np.ndarray:
+        return self.inner.gradient(np.asarray(x, dtype=np.float64) - self.translation)
+
+    def batch_gradient(self, dvs, with_fitness: bool = True):
+        return self.inner.batch_gradient(self._back(dvs), with_fitness)
+
+
 def from_kind(kind: int, param: int, context=None) -> _gpu_udp:
     return {N.RASTRIGIN: rastrigin, N.ROSENBROCK: rosenbrock, N.LENNARD_JONES: lennard_jones, N.ACKLEY: ackley,
             N.GRIEWANK: griewank, N.SCHWEFEL: schwefel}[kind](param, context)

@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include <pagmo/batch_evaluators/member_bfe.hpp>
 #include <pagmo/batch_evaluators/thread_bfe.hpp>
 #include <pagmo/bfe.hpp>
 #include <pagmo/problem.hpp>
@@ -22,6 +23,7 @@
 #include <pagmo/problems/rastrigin.hpp>
 #include <pagmo/problems/rosenbrock.hpp>
 #include <pagmo/problems/schwefel.hpp>
+#include <pagmo/problems/translate.hpp>
 #include <pagmo/problems/zdt.hpp>
 #include <pagmo/utils/multi_objective.hpp>
 
@@ -61,6 +63,7 @@ static_assert(pagmo::is_udp<gpu_lennard_jones>::value, "gpu_lennard_jones must b
 static_assert(pagmo::has_batch_fitness<gpu_rosenbrock>::value, "batch_fitness hook");
 static_assert(pagmo::has_gradient<gpu_rosenbrock>::value, "gradient hook");
 static_assert(pagmo::has_gradient<gpu_lennard_jones>::value, "gradient hook");
+static_assert(pagmo::has_batch_fitness<pagmo::translate>::value, "translate forwards batch_fitness");
 static_assert(pagmo::is_udp<gpu_zdt>::value && pagmo::is_udp<gpu_dtlz>::value, "gpu_zdt / gpu_dtlz must be UDPs");
 static_assert(pagmo::has_batch_fitness<gpu_zdt>::value && pagmo::has_batch_fitness<gpu_dtlz>::value,
               "batch_fitness hook of the multi-objective UDPs");
@@ -159,6 +162,10 @@ int main()
         pagmo::problem pz{pagmo::zdt{1u, 4u}};
         CHECK(throws_with<std::runtime_error>([&] { b(pz, dvs); }, ""));
         CHECK(pz.get_fevals() == 0u);
+        // translate{rosenbrock}: gpu_bfe reaches the inner problem (and the device)
+        pagmo::problem pt{pagmo::translate{pagmo::rosenbrock{4u}, {0.1, 0.2, 0.3, 0.4}}};
+        CHECK(throws_with<std::runtime_error>([&] { b(pt, dvs); }, ""));
+        CHECK(!throws_with<std::invalid_argument>([&] { b(pt, dvs); }, "Cannot use a gpu_bfe"));
     } else {
         // with a device: bfe{gpu_bfe} against bfe{thread_bfe}, fevals counted once
         pagmo::problem pr{pagmo::rosenbrock{4u}};
@@ -202,6 +209,20 @@ int main()
             const auto fg = b(prob, d3);
             const auto fr = pagmo::bfe{pagmo::thread_bfe{}}(prob, d3);
             for (size_t i = 0; i < fr.size(); ++i) CHECK(std::abs(fg[i] - fr[i]) <= 1e-12 * (1.0 + std::abs(fr[i])));
+        }
+        // translate: around pagmo's rosenbrock through gpu_bfe, around a GPU UDP through its batch_fitness
+        {
+            const pagmo::vector_double shift{0.5, -0.25, 1.5, 2.0};
+            pagmo::problem pt{pagmo::translate{pagmo::rosenbrock{4u}, shift}};
+            pagmo::problem pg2{pagmo::translate{gpu_rosenbrock{4u}, shift}};
+            CHECK(pg2.has_batch_fitness());
+            const auto fr = pagmo::bfe{pagmo::thread_bfe{}}(pt, dvs);
+            const auto f1 = b(pt, dvs);
+            const auto f2 = pagmo::bfe{pagmo::member_bfe{}}(pg2, dvs);
+            for (size_t i = 0; i < fr.size(); ++i) {
+                CHECK(std::abs(f1[i] - fr[i]) <= 1e-13 * std::abs(fr[i]));
+                CHECK(std::abs(f2[i] - fr[i]) <= 1e-13 * std::abs(fr[i]));
+            }
         }
         // pagmo's zdt and dtlz through bfe{gpu_bfe}, and the GPU UDPs, against bfe{thread_bfe}
         std::vector<double> u(60);

@@ -383,3 +383,20 @@ def test_fitness_only_nonfinite_and_gpu_bfe(ctx, orc):
         fr = orc.batch_fitness(kind, 9, x)
         for a, b in zip(f, fr):
             assert (math.isnan(a) and math.isnan(b)) or a == b or abs(a - b) <= 1e-12 * (1 + abs(b)), (name, a, b)
+
+
+def test_translate_forwards_the_batch(ctx, orc):
+    """translate{udp, t} (src/problems/translate.cpp:118-146): the batch shifted back and evaluated by the inner
+    GPU UDP in one pass, through batch_fitness and through gpu_bfe."""
+    rng = np.random.RandomState(8)
+    for udp, kind, param in ((P.rosenbrock(50, ctx), N.ROSENBROCK, 50), (P.zdt(1, 30, ctx), None, None)):
+        t = rng.uniform(-1, 1, udp.get_nx())
+        tr = P.translate(udp, t)
+        lb, ub = tr.get_bounds()
+        assert np.array_equal(lb, udp.get_bounds()[0] + t)
+        x = rng.uniform(0, 1, (300, udp.get_nx())) * (ub - lb) + lb
+        f = tr.batch_fitness(x)
+        assert np.array_equal(f, udp.batch_fitness(x - t))
+        assert np.array_equal(B.gpu_bfe()(tr, x.ravel()), f)
+    with pytest.raises(ValueError, match="Length of shift vector is: 3 while the problem dimension is: 50"):
+        P.translate(P.rosenbrock(50, ctx), [1.0, 2.0, 3.0])
