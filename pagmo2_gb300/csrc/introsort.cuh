@@ -273,16 +273,21 @@ __device__ int block_partition(const sort_view<K> &x, int first, int last, const
             scan[32 + warp] = __popc(br);
         }
         __syncthreads();
-        int offl = 0, offr = 0, totl = 0, totr = 0;
-        for (int j = 0; j < nwarps; ++j) {
-            const int a = scan[j], b = scan[32 + j];
-            if (j < warp) {
-                offl += a;
-                offr += b;
+        // exclusive prefix of the warps' counts: each warp scans the (up to 32)
+        // counts with shuffles
+        int cl = static_cast<int>(lane) < nwarps ? scan[lane] : 0;
+        int cr = static_cast<int>(lane) < nwarps ? scan[32 + lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int tl = __shfl_up_sync(kSortFull, cl, o), tr = __shfl_up_sync(kSortFull, cr, o);
+            if (static_cast<int>(lane) >= o) {
+                cl += tl;
+                cr += tr;
             }
-            totl += a;
-            totr += b;
         }
+        const int totl = __shfl_sync(kSortFull, cl, 31), totr = __shfl_sync(kSortFull, cr, 31);
+        const int offl = warp > 0 ? __shfl_sync(kSortFull, cl, warp - 1) : 0;
+        const int offr = warp > 0 ? __shfl_sync(kSortFull, cr, warp - 1) : 0;
         if (fl) w.pos_l[nl + offl + __popc(bl & below)] = p;
         if (fr) w.pos_r[nr + offr + __popc(br & below)] = p;
         nl += totl;
@@ -381,18 +386,40 @@ __device__ int warp_partition(const sort_view<K> &x, int first, int last, int *s
             lastR = __shfl_sync(kSortFull, rp, v - 1);
         }
         if (v < mm) return min(__shfl_sync(kSortFull, lp, v), lastR);
-        for (int j = 0; j < mm; ++j) {
-            lmask &= lmask - 1u;
-            rmask &= rmask - 1u;
-        }
+        // drop the mm paired (lowest) stoppers of each mask
+        lmask &= ~__ballot_sync(kSortFull, ((lmask >> lane) & 1u) && __popc(lmask & below) < mm);
+        rmask &= ~__ballot_sync(kSortFull, ((rmask >> lane) & 1u) && __popc(rmask & below) < mm);
     }
     if (lane == 0) atomicExch(err, kSortErrGuard);
     return last - 1;
 }
 
-// Queues a child range for the next level, by size.
-__device__ __forceinline__ void queue_range(int a, int b, int2 *small_next, int2 *big_next, const sort_work &w,
-                                            sort_ctl *ctl, int *err)
+// Ranges of 17..kBlockRange elements wait in a ring of int4 (first, last,
+// depth budget, publication ticket + 1) shared by the block's warps: any
+// warp takes the next ticket, waits until that slot is published (or until no
+// range is outstanding), partitions the range and publishes its children. The
+// ranges outstanding at any time are disjoint and longer than 16, so at most
+// n / 17 of them exist and a ring of n / 17 + 1 slots never overwrites a slot
+// before its range is done. ctl->take: next ticket to take; ctl->nnext: next
+// ticket to publish; ctl->ncur: ranges outstanding.
+constexpr unsigned long long kRingSpinLimit = 1ull << 22;
+
+__device__ __forceinline__ void ring_push(int4 *ring, int cap, sort_ctl *ctl, int a, int b, int d)
+{
+    const int t = atomicAdd(&ctl->nnext, 1);
+    int4 *slot = ring + (t % cap);
+    slot->x = a;
+    slot->y = b;
+    slot->z = d;
+    __threadfence_block();
+    atomicExch(&slot->w, t + 1);
+}
+
+// A child [a, b) of a partition with depth budget d: to the next level's
+// block-partition list, to the ring, or (16 or fewer) left for the caller's
+// leaf sort. Returns 1 when it went to the ring.
+__device__ __forceinline__ int place_child(int a, int b, int d, int2 *big_next, const sort_work &w, int4 *ring,
+                                           int cap, sort_ctl *ctl, int *err)
 {
     const int len = b - a;
     if (len > kBlockRange) {
@@ -401,13 +428,14 @@ __device__ __forceinline__ void queue_range(int a, int b, int2 *small_next, int2
             big_next[slot] = make_int2(a, b);
         else
             atomicExch(err, kSortErrListFull);
-    } else if (len > 16) {
-        const int slot = atomicAdd(&ctl->nnext, 1);
-        if (slot < w.small_cap)
-            small_next[slot] = make_int2(a, b);
-        else
-            atomicExch(err, kSortErrListFull);
+        return 0;
     }
+    if (len > 16) {
+        atomicAdd(&ctl->ncur, 1);
+        ring_push(ring, cap, ctl, a, b, d);
+        return 1;
+    }
+    return 0;
 }
 
 // Sorts x[0 .. n) by key with std::sort's order of ties. Every thread of the
@@ -415,6 +443,13 @@ __device__ __forceinline__ void queue_range(int a, int b, int2 *small_next, int2
 // ints per warp of shared memory; ctl in shared memory. depth0 >= 0 continues
 // an introsort whose depth budget at this range is depth0 (a subrange of a
 // larger sort); -1 starts one (2 floor(log2 n)). Ends with a __syncthreads.
+//
+// Ranges longer than kBlockRange are partitioned level by level by the whole
+// block; the shorter ones they produce go to the ring, which the warps then
+// drain, each taking ranges as they come (no barrier between levels: a warp
+// goes on with other ranges while deeper parts of the recursion proceed).
+// Ranges are disjoint and each carries the depth budget the sequential
+// recursion would give it, so the order of the work does not change the result.
 template <typename K>
 __device__ void block_std_sort(const sort_view<K> &x, int n, const sort_work &w, sort_ctl *ctl, int *slots_all,
                                int *err, int depth0 = -1)
@@ -428,37 +463,31 @@ __device__ void block_std_sort(const sort_view<K> &x, int n, const sort_work &w,
         return;
     }
     int depth = depth0 >= 0 ? depth0 : 2 * floor_log2_int(n);
-    int2 *small_cur = w.small, *small_next = w.small + w.small_cap;
+    int4 *ring = reinterpret_cast<int4 *>(w.small); // 2 small_cap int2 = small_cap int4
+    const int cap = w.small_cap;
     int2 *big_cur = w.big, *big_next = w.big + w.big_cap;
+    for (int i = threadIdx.x; i < cap; i += blockDim.x) ring[i].w = 0;
+    __syncthreads();
     if (threadIdx.x == 0) {
+        ctl->take = 0;
+        ctl->nnext = 0;
         ctl->ncur = 0;
         ctl->nbig = 0;
-        ctl->nnext = 0;
         ctl->nbignext = 0;
-        queue_range(0, n, small_next, big_next, w, ctl, err);
-        ctl->ncur = ctl->nnext;
-        ctl->nbig = ctl->nbignext;
-    }
-    {
-        int2 *t = small_cur;
-        small_cur = small_next;
-        small_next = t;
-        t = big_cur;
-        big_cur = big_next;
-        big_next = t;
+        if (n > kBlockRange) {
+            big_cur[0] = make_int2(0, n);
+            ctl->nbig = 1;
+        } else {
+            atomicAdd(&ctl->ncur, 1);
+            ring_push(ring, cap, ctl, 0, n, depth);
+        }
     }
     __syncthreads();
+    // ---- ranges longer than kBlockRange, one level at a time, by the whole block
     for (;;) {
-        const int ncur = min(ctl->ncur, w.small_cap), nbig = min(ctl->nbig, w.big_cap);
-        if (ncur == 0 && nbig == 0) break;
+        const int nbig = min(ctl->nbig, w.big_cap);
+        if (nbig == 0) break;
         __syncthreads();
-        if (threadIdx.x == 0) {
-            ctl->take = 0;
-            ctl->nnext = 0;
-            ctl->nbignext = 0;
-        }
-        __syncthreads();
-        // long ranges: one at a time, by the whole block
         for (int t = 0; t < nbig; ++t) {
             const int2 r = big_cur[t];
             if (depth == 0) {
@@ -467,46 +496,66 @@ __device__ void block_std_sort(const sort_view<K> &x, int n, const sort_work &w,
                 continue;
             }
             const int cut = block_partition(x, r.x, r.y, w, slots_all, err);
-            if (threadIdx.x == 0) queue_range(r.x, cut, small_next, big_next, w, ctl, err);
+            if (threadIdx.x == 0) place_child(r.x, cut, depth - 1, big_next, w, ring, cap, ctl, err);
             if (threadIdx.x == 32 || (blockDim.x == 32 && threadIdx.x == 1))
-                queue_range(cut, r.y, small_next, big_next, w, ctl, err);
+                place_child(cut, r.y, depth - 1, big_next, w, ring, cap, ctl, err);
             if (warp == 0) {
                 const int a = lane < 16u ? r.x : cut, len = lane < 16u ? cut - r.x : r.y - cut;
                 halfwarp_leaf_sort(x, a, len <= 16 ? len : 0);
             }
             __syncthreads();
         }
-        // short ranges: one per warp
-        for (;;) {
-            int t = 0;
-            if (lane == 0) t = atomicAdd(&ctl->take, 1);
-            t = __shfl_sync(kSortFull, t, 0);
-            if (t >= ncur) break;
-            const int2 r = small_cur[t];
-            if (depth == 0) {
-                if (lane == 0) heap_sort(x, r.x, r.y);
-                __syncwarp();
-                continue;
-            }
-            const int cut = warp_partition(x, r.x, r.y, slots, err);
-            if (lane == 0) queue_range(r.x, cut, small_next, big_next, w, ctl, err);
-            if (lane == 1) queue_range(cut, r.y, small_next, big_next, w, ctl, err);
-            const int a = lane < 16u ? r.x : cut, len = lane < 16u ? cut - r.x : r.y - cut;
-            halfwarp_leaf_sort(x, a, len <= 16 ? len : 0);
-        }
-        __syncthreads();
         if (threadIdx.x == 0) {
-            ctl->ncur = ctl->nnext;
             ctl->nbig = ctl->nbignext;
+            ctl->nbignext = 0;
         }
-        int2 *t = small_cur;
-        small_cur = small_next;
-        small_next = t;
-        t = big_cur;
+        int2 *t = big_cur;
         big_cur = big_next;
         big_next = t;
         --depth;
         __syncthreads();
+    }
+    // ---- the ring: every warp takes ranges until none is outstanding
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&ctl->take, 1);
+        t = __shfl_sync(kSortFull, t, 0);
+        volatile int4 *slot = ring + (t % cap);
+        bool got = false;
+        for (unsigned long long spins = 0;; ++spins) {
+            int seq = 0, pend = 0;
+            if (lane == 0) {
+                seq = slot->w;
+                pend = *reinterpret_cast<volatile int *>(&ctl->ncur);
+            }
+            seq = __shfl_sync(kSortFull, seq, 0);
+            pend = __shfl_sync(kSortFull, pend, 0);
+            if (seq == t + 1) {
+                got = true;
+                break;
+            }
+            if (pend == 0) break;
+            if (spins > kRingSpinLimit) {
+                if (lane == 0) atomicExch(err, kSortErrGuard);
+                break;
+            }
+            __nanosleep(32);
+        }
+        if (!got) break;
+        __threadfence_block();
+        const int a = slot->x, b = slot->y, d = slot->z;
+        if (d == 0) {
+            if (lane == 0) heap_sort(x, a, b);
+            __syncwarp();
+        } else {
+            const int cut = warp_partition(x, a, b, slots, err);
+            if (lane == 0) place_child(a, cut, d - 1, big_next, w, ring, cap, ctl, err);
+            if (lane == 1) place_child(cut, b, d - 1, big_next, w, ring, cap, ctl, err);
+            const int la = lane < 16u ? a : cut, len = lane < 16u ? cut - a : b - cut;
+            halfwarp_leaf_sort(x, la, len <= 16 ? len : 0);
+        }
+        __syncwarp();
+        if (lane == 0) atomicSub(&ctl->ncur, 1);
     }
     __syncthreads();
 }

@@ -867,7 +867,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
 
 // ------------------------------------------------------------ crowding and orders
 
-constexpr int kSortThreads = 256;
+constexpr int kSortThreads = 1024;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortSmemCap = 4096;                                // (key, value) pairs kept in shared memory
 constexpr int kSortSmemSmall = kSortSmemCap / 16 + 2;             // short ranges per level list
@@ -907,10 +907,12 @@ __device__ sort_area<K> pick_area(unsigned char *smem, int L, K *gk, int32_t *gv
     } else {
         a.k = gk;
         a.v = gv;
+        // the small-range list doubles as a ring of int4: start it on a 16-byte boundary
+        int2 *g0 = gl + ((reinterpret_cast<uintptr_t>(gl) & 15u) ? 1 : 0);
         a.w.big_cap = L / dev::kBlockRange + 2;
-        a.w.small_cap = (L - 2 * a.w.big_cap) / 2;
-        a.w.small = gl;
-        a.w.big = gl + 2 * a.w.small_cap;
+        a.w.small_cap = (L - 1 - 2 * a.w.big_cap) / 2;
+        a.w.small = g0;
+        a.w.big = g0 + 2 * a.w.small_cap;
         a.w.pos_l = gpos;
         a.w.pos_r = gpos + L;
     }
