@@ -125,6 +125,14 @@ PGX_API int pgx_batch_gradient(pgx_context *ctx, int kind, uint64_t param, const
 PGX_API int pgx_batch_eval_device(pgx_context *ctx, int kind, uint64_t param, const double *d_dvs, uint64_t n_dvs,
                           double *d_fvs, double *d_grads, void *stream);
 
+/* Self-test of the bounded device waits (no counterpart in the reference):
+   runs a two-block cooperative kernel in which one block never reaches the
+   grid barrier, so the other's wait gives up after spin_limit polls (about
+   spin_limit x 100 ns; 1 .. 2^24) and flags the timeout. *timed_out receives
+   1 when the wait gave up and returned, as the survival kernels' barriers do
+   (their callers then report PGX_ERR_TIMEOUT); the context stays usable. */
+PGX_API int pgx_selftest_barrier_timeout(pgx_context *ctx, uint64_t spin_limit, int32_t *timed_out);
+
 /* ------------------------------------- multi-objective test problems (ZDT, DTLZ) */
 
 /* A ZDT or DTLZ problem as its reference constructor takes it:

@@ -580,6 +580,16 @@ int pgx_std_sort_i64(pgx_context *ctx, int64_t *keys, int32_t *values, uint64_t 
     return PGX_OK;
 }
 
+int pgx_selftest_barrier_timeout(pgx_context *ctx, uint64_t spin_limit, int32_t *timed_out)
+{
+    PGX_CHECK(ctx != nullptr && timed_out != nullptr, PGX_ERR_INVALID, "null argument");
+    PGX_CHECK(spin_limit >= 1u && spin_limit <= (uint64_t(1) << 24), PGX_ERR_INVALID,
+              "spin limit out of range [1, 2^24]");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    PGX_TRY(use_device(ctx));
+    return run_barrier_timeout_test(ctx, spin_limit, timed_out);
+}
+
 int pgx_fnds_dom_list(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, int64_t *dl_offsets,
                       int32_t *dl_indices, uint64_t capacity, uint64_t *dl_total)
 {

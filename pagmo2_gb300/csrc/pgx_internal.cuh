@@ -172,6 +172,8 @@ int read_mo_status(pgx_context *ctx, uint64_t n, uint64_t m);
 int launch_sort_pairs(pgx_context *ctx, long long *d_keys, int32_t *d_vals, uint64_t n, int *d_err, int2 *d_lists,
                       int32_t *d_pos, void *d_state, cudaStream_t stream);
 size_t sort_pairs_state_bytes();
+// Self-test of the bounded grid barriers (one block never arrives).
+int run_barrier_timeout_test(pgx_context *ctx, uint64_t spin_limit, int32_t *timed_out);
 
 // Reads the device status word of the last survival pass of shape (n, m) on
 // this context (after a stream synchronisation): PGX_ERR_TIMEOUT when a grid

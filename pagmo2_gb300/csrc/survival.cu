@@ -223,8 +223,8 @@ struct peel_state {
 constexpr int kStatusNeedTwoObjectives = 1;
 
 // Grid-wide barrier for a cooperative launch; gives up (and flags st->err)
-// after about a second instead of waiting forever.
-__device__ bool grid_sync(peel_state *st)
+// after about a second (spin_limit polls) instead of waiting forever.
+__device__ bool grid_sync(peel_state *st, unsigned long long spin_limit = kSpinLimit)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -241,7 +241,7 @@ __device__ bool grid_sync(peel_state *st)
             volatile int *verr = &st->err;
             while (*vgen == g0) {
                 if (*verr) break; // another block gave up: do not wait for it
-                if (++spins > kSpinLimit) {
+                if (++spins > spin_limit) {
                     atomicExch(&st->err, 1);
                     break;
                 }
@@ -1344,6 +1344,15 @@ __global__ void __launch_bounds__(kGridSortThreads) sort_pairs_grid_kernel(long 
     }
 }
 
+// Self-test of the bounded grid barrier: block 1 never arrives, so block 0's
+// wait runs out after spin_limit polls and flags st->err, and the kernel
+// returns. Launched cooperatively with two blocks (both resident).
+__global__ void barrier_timeout_test_kernel(peel_state *st, unsigned long long spin_limit)
+{
+    if (blockIdx.x != 0) return;
+    grid_sync(st, spin_limit);
+}
+
 // out[i] = i (corner cases of select_best_N_mo / sort_population_mo).
 __global__ void iota_kernel(int32_t *out, uint32_t n)
 {
@@ -1923,6 +1932,26 @@ int launch_sort_population(pgx_context *ctx, const double *d_points, uint64_t n6
     }
     ctx->launches += 1 + crowding_launches(n, m);
     return finish_status(sc, d_status, s, &ctx->launches);
+}
+
+// Runs barrier_timeout_test_kernel on scratch state of its own; *timed_out
+// receives the barrier's error flag (1 expected).
+int run_barrier_timeout_test(pgx_context *ctx, uint64_t spin_limit, int32_t *timed_out)
+{
+    PGX_TRY(ctx->s_crowd.ensure(align256(sizeof(peel_state))));
+    peel_state *st = ctx->s_crowd.as<peel_state>();
+    cudaStream_t s = ctx->stream;
+    PGX_CUDA(cudaMemsetAsync(st, 0, sizeof(peel_state), s));
+    unsigned long long limit = spin_limit;
+    void *args[] = {&st, &limit};
+    PGX_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(barrier_timeout_test_kernel), dim3(2),
+                                         dim3(32), args, 0, s));
+    ++ctx->launches;
+    peel_state h{};
+    PGX_CUDA(cudaMemcpyAsync(&h, st, sizeof(peel_state), cudaMemcpyDeviceToHost, s));
+    PGX_CUDA(cudaStreamSynchronize(s));
+    *timed_out = h.err;
+    return PGX_OK;
 }
 
 size_t sort_pairs_state_bytes()

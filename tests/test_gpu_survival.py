@@ -11,6 +11,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+from pagmo2_gb300 import _native as N
 from pagmo2_gb300 import multi_objective as MO
 from pagmo2_gb300 import workloads as W
 
@@ -115,3 +116,21 @@ def test_single_objective_front_of_three_raises_in_survival(ctx):
         MO.nsga2_survival(np.array([[1.0], [1.0], [1.0]]), ctx)
     rank, dc, off, idx, cd = MO.nsga2_survival(np.array([[1.0], [2.0], [3.0]]), ctx)
     assert rank.tolist() == [0, 1, 2] and cd.tolist() == [math.inf] * 3
+
+
+def test_grid_barrier_wait_is_bounded(ctx, orc):
+    """Failure detection without a fault: a cooperative kernel whose second block never arrives at the grid
+    barrier; the first block's wait gives up after a bounded number of polls, the kernel returns, the host reads
+    the flag, and the same context then runs a full survival pass."""
+    import ctypes as C
+    import time
+
+    flag = C.c_int32(-1)
+    t = time.perf_counter()
+    N.check(N.lib().pgx_selftest_barrier_timeout(ctx.handle, 1 << 14, C.byref(flag)))
+    assert flag.value == 1
+    assert time.perf_counter() - t < 30.0
+    p = W.nsga2_points(1000, 3, layers=8)
+    rank, dc, off, idx, cd = MO.nsga2_survival(p, ctx)
+    want = orc.fnds(p, dom_list=False)
+    assert np.array_equal(off, want["front_offsets"]) and np.array_equal(idx, want["front_indices"])
