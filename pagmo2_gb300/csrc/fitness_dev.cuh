@@ -141,8 +141,11 @@ __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uin
     const unsigned sub = threadIdx.x & (G - 1);
     const unsigned mask = group_mask<G>();
     double sx = 0.0, sc = 0.0;
+    // the next element's load is issued before this one's arithmetic
+    double xn = sub < nx ? __ldg(xr + sub) : 0.0;
     for (uint32_t i = sub; i < nx; i += G) {
-        const double xi = __ldg(xr + i);
+        const double xi = xn;
+        if (i + G < nx) xn = __ldg(xr + i + G);
         double s = 0.0, c;
         int s_neg = 0, c_neg = 0;
         if (fast_trig_arg(xi)) {
@@ -361,8 +364,10 @@ __device__ __forceinline__ void ackley_row(const double *__restrict__ xr, uint32
     const unsigned sub = threadIdx.x & (G - 1);
     const unsigned mask = group_mask<G>();
     double s1 = 0.0, s2 = 0.0;
+    double xn = sub < nx ? __ldg(xr + sub) : 0.0;
     for (uint32_t i = sub; i < nx; i += G) {
-        const double xi = __ldg(xr + i);
+        const double xi = xn;
+        if (i + G < nx) xn = __ldg(xr + i + G);
         int c_neg = 0;
         const double c = fast_trig_arg(xi) ? cos_2pi(xi, c_neg) : cospi(xi + xi);
         s1 = fma(xi, xi, s1);
@@ -387,8 +392,10 @@ __device__ __forceinline__ void griewank_row(const double *__restrict__ xr, uint
     const unsigned sub = threadIdx.x & (G - 1);
     const unsigned mask = group_mask<G>();
     double s = 0.0, p = 1.0;
+    double xn = sub < nx ? __ldg(xr + sub) : 0.0;
     for (uint32_t i = sub; i < nx; i += G) {
-        const double xi = __ldg(xr + i);
+        const double xi = xn;
+        if (i + G < nx) xn = __ldg(xr + i + G);
         s = fma(xi, xi, s);
         const double r = i < n_root ? root[i] : sqrt(static_cast<double>(i) + 1.0);
         p *= cos(xi / r);
@@ -405,8 +412,10 @@ __device__ __forceinline__ void schwefel_row(const double *__restrict__ xr, uint
     const unsigned sub = threadIdx.x & (G - 1);
     const unsigned mask = group_mask<G>();
     double s = 0.0;
+    double xn = sub < nx ? __ldg(xr + sub) : 0.0;
     for (uint32_t i = sub; i < nx; i += G) {
-        const double xi = __ldg(xr + i);
+        const double xi = xn;
+        if (i + G < nx) xn = __ldg(xr + i + G);
         s = fma(xi, sin(sqrt(fabs(xi))), s);
     }
     s = group_sum<G>(s, mask);
