@@ -592,6 +592,34 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops, cpu_ok=True) -> dict:
         gen["cpu_kind"] = "reference" if ref is not None else "port"
         gen["note"] = "CPU: fitness on every host thread, select_best_N_mo single-threaded, as in the reference"
     out["nsga2_generation_zdt1_20000x30"] = gen
+
+    # hypervolume (3 objectives) of the survival workload's points and of its first front
+    r = p.max(axis=0) + 0.5
+    dr = np.ascontiguousarray(r)
+    dhv = torch.empty(1, dtype=torch.float64, device="cuda")
+    for name, pts in (("hypervolume_20000x3", p),):
+        dpts = torch.from_numpy(np.ascontiguousarray(pts)).cuda()
+
+        def hvol():
+            N.check(L.pgx_hypervolume_device(ctx.handle, dpts.data_ptr(), pts.shape[0], 3, N.ptr(dr),
+                                             dhv.data_ptr(), sp))
+        rec = {"ms": timed(hvol, reps=10, flush_l2=False), "value": float(dhv.item())}
+        if cpu_ok:
+            import oracle
+
+            ref = oracle.reference()
+            if ref is not None:
+                t = time.perf_counter()
+                rec["cpu_value"] = ref.hypervolume(pts, r)
+                rec["cpu_ms"] = (time.perf_counter() - t) * 1e3
+                rec["cpu_kind"] = "reference (hv3d sweep, single-threaded)"
+            else:
+                # the port is a long-double O(n^2 log n) restatement: a 2000-point sample
+                t = time.perf_counter()
+                oracle.oracle().hypervolume(pts[:2000], r)
+                rec["cpu_ms_2000_points"] = (time.perf_counter() - t) * 1e3
+                rec["cpu_kind"] = "port (long double slabs, O(n^2 log n)), first 2000 points"
+        out[name] = rec
     out["sort_population_mo_20000x3"] = {"ms": timed(sortpop, reps=10, flush_l2=False)}
     out["archipelago_64_islands"] = run_archipelago(ctx, L, N, W, stream)
     return out

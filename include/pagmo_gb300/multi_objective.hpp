@@ -156,6 +156,29 @@ inline nsga2_survival_result nsga2_survival(const std::vector<pagmo::vector_doub
     return r;
 }
 
+// hypervolume(points).compute(ref) for 2 or 3 objectives
+// (src/utils/hypervolume.cpp:203-228, hv2d / hv3d) on the GPU, with the
+// reference's checks and messages; 4 or more objectives throw
+// pagmo::not_implemented_error.
+inline double hypervolume_compute(const std::vector<pagmo::vector_double> &points, const pagmo::vector_double &ref,
+                                  int device = 0)
+{
+    if (points.empty()) throw std::invalid_argument("Point set cannot be empty.");
+    const auto m = points[0].size();
+    if (m <= 1u) throw std::invalid_argument("Points of dimension > 1 required.");
+    std::vector<double> flat;
+    flat.reserve(points.size() * m);
+    for (const auto &p : points) {
+        if (p.size() != m) throw std::invalid_argument("All point set dimensions must be equal.");
+        flat.insert(flat.end(), p.begin(), p.end());
+    }
+    if (ref.size() != m)
+        throw std::invalid_argument("Point set dimensions and reference point dimension must be equal.");
+    double out = 0.0;
+    check(pgx_hypervolume(device_context(device), flat.data(), points.size(), m, ref.data(), &out));
+    return out;
+}
+
 } // namespace pagmo_gb300
 
 #endif

@@ -173,6 +173,27 @@ PGX_API int pgx_mo_batch_fitness_device(pgx_context *ctx, const pgx_mo_problem *
 PGX_API int pgx_mo_p_distance(pgx_context *ctx, const pgx_mo_problem *p, const double *dvs, uint64_t n_dvs,
                               double *out);
 
+/* ------------------------------------------------------------- hypervolume */
+
+/* hypervolume(points).compute(ref) for 2 or 3 objectives
+   (src/utils/hypervolume.cpp:203-228 with hv2d / hv3d,
+   src/utils/hv_algos/hv_hv2d.cpp:48-68, hv_hv3d.cpp:75-116): the measure of
+   the region the n points (row-major, m = 2 or 3) dominate, bounded by ref.
+   The reference's checks and messages (hypervolume.cpp:406-449,
+   hv_algorithm.cpp:226-258: empty set, NaN, a point outside or equal to the
+   reference point) give PGX_ERR_INVALID; 4 or more objectives (pagmo's hvwfg)
+   give PGX_ERR_NOTIMPL. FP64; the value differs from the reference's sweep
+   by summation order only (non-negative slabs, no cancellation). */
+PGX_API int pgx_hypervolume(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, const double *ref,
+                            double *out);
+
+/* Device-resident variant: d_points on the device, ref on the host (m
+   doubles), the volume written to *d_out, asynchronous on `stream`. The
+   input checks that need the points (NaN, points beyond ref) are the
+   caller's. */
+PGX_API int pgx_hypervolume_device(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m,
+                                   const double *ref, double *d_out, void *stream);
+
 /* --------------------------------------------------- NSGA-II survival (MO) */
 
 /* fast_non_dominated_sorting (src/utils/multi_objective.cpp:200-257) over n

@@ -93,6 +93,7 @@ class _Oracle:
         h.orc_mo_last_error.restype = C.c_char_p
         h.orc_zdt_p_distance.restype = C.c_double
         h.orc_zdt_p_distance.argtypes = [C.c_uint, _vp, _u64]
+        h.orc_hypervolume_ld.argtypes = [_vp, _u64, _u64, _vp, _vp]
         h.orc_mo_dims.argtypes = [C.c_int, C.c_uint, _u64, _u64, _vp, _vp]
         h.orc_mo_batch_fitness.argtypes = [C.c_int, C.c_uint, _u64, _u64, C.c_uint, _vp, _u64, _u64, _vp, C.c_int]
         h.orc_mo_batch_fitness_ld.argtypes = [C.c_int, C.c_uint, _u64, _u64, C.c_uint, _vp, _u64, _u64, _vp, _vp,
@@ -221,6 +222,16 @@ class _Oracle:
         self._chk_sort(self.h.orc_sort_population_mo(_p(p), n, m, _p(out)))
         return out[:n].astype(np.int64)
 
+    # hypervolume -------------------------------------------------------------------
+    def hypervolume(self, pts, ref):
+        """Long-double hypervolume of 2 or 3 objectives."""
+        p = _pts2d(pts)
+        r = np.ascontiguousarray(ref, dtype=np.float64)
+        out = C.c_double()
+        if self.h.orc_hypervolume_ld(_p(p), p.shape[0], p.shape[1], _p(r), C.byref(out)) != 0:
+            raise ValueError("hypervolume oracle: 2 or 3 objectives and at least one point")
+        return out.value
+
     # ZDT / DTLZ ------------------------------------------------------------------
     # spec = (family, prob_id, param, fdim, alpha): family 7 = zdt{prob_id, param},
     # family 8 = dtlz{prob_id, dim=param, fdim, alpha} (the GPU library's kinds).
@@ -285,6 +296,7 @@ class _Reference:
         h.ref_select_best_n_mo.argtypes = [_vp, _u64, _u64, _u64, _vp, _vp]
         h.ref_sort_population_mo.argtypes = [_vp, _u64, _u64, _vp]
         mo = [C.c_int, C.c_uint, _u64, _u64, C.c_uint]
+        h.ref_hypervolume.argtypes = [_vp, _u64, _u64, _vp, _vp]
         h.ref_mo_dims.argtypes = mo + [_vp, _vp, _vp]
         h.ref_mo_bounds.argtypes = mo + [_vp, _vp]
         h.ref_mo_thread_bfe.argtypes = mo + [_vp, _u64, _u64, _vp]
@@ -387,6 +399,14 @@ class _Reference:
         r = C.c_int()
         self._chk(self.h.ref_pareto_dominance(_p(a), _p(b), a.size, C.byref(r)))
         return bool(r.value)
+
+    def hypervolume(self, pts, ref):
+        """hypervolume(points, true).compute(ref) of the reference."""
+        p = _pts2d(pts)
+        r = np.ascontiguousarray(ref, dtype=np.float64)
+        out = C.c_double()
+        self._chk(self.h.ref_hypervolume(_p(p), p.shape[0], p.shape[1], _p(r), C.byref(out)))
+        return out.value
 
     # ZDT / DTLZ (spec as in the oracle) ---------------------------------------------
     def mo_dims(self, spec):

@@ -124,6 +124,9 @@ int orc_mo_batch_fitness_ld(int family, unsigned prob_id, uint64_t param, uint64
 int orc_mo_batch_p_distance(int family, unsigned prob_id, uint64_t param, uint64_t fdim, const double *dvs,
                             uint64_t n, uint64_t nx, double *out, double *scale, int nthreads);
 
+/* ---- hypervolume of 2 or 3 objectives, long double (hypervolume.cpp) ---- */
+int orc_hypervolume_ld(const double *pts, uint64_t n, uint64_t m, const double *ref, double *out);
+
 #ifdef __cplusplus
 }
 #endif

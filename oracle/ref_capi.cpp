@@ -24,6 +24,7 @@
 #include <pagmo/problems/rosenbrock.hpp>
 #include <pagmo/problems/schwefel.hpp>
 #include <pagmo/problems/zdt.hpp>
+#include <pagmo/utils/hypervolume.hpp>
 #include <pagmo/utils/multi_objective.hpp>
 
 namespace
@@ -196,6 +197,16 @@ int ref_bounds(int kind, std::uint64_t param, double *lb, double *ub)
         auto b = p.get_bounds();
         std::memcpy(lb, b.first.data(), b.first.size() * sizeof(double));
         std::memcpy(ub, b.second.data(), b.second.size() * sizeof(double));
+    });
+}
+
+// hypervolume(points, true).compute(ref) (src/utils/hypervolume.cpp:203-228):
+// errors come back as status 1 with the reference's message.
+int ref_hypervolume(const double *pts, std::uint64_t n, std::uint64_t m, const double *r, double *out)
+{
+    return guard([&] {
+        pagmo::hypervolume hv(rows(pts, n, m), true);
+        *out = hv.compute(pagmo::vector_double(r, r + m));
     });
 }
 

@@ -12,12 +12,13 @@ plugin interface for the batch-fitness path:
   batch_evaluators: gpu_bfe (the UDBFE) and a bfe/problem pair reproducing
                     pagmo's input/output checks and fevals accounting
   multi_objective:  fast_non_dominated_sorting, crowding_distance,
-                    nsga2_survival, select_best_N_mo, sort_population_mo
+                    nsga2_survival, select_best_N_mo, sort_population_mo,
+                    hypervolume (2 or 3 objectives)
   workloads:        seeded synthetic inputs
 """
 from ._native import Context, default_context  # noqa: F401
 from .batch_evaluators import bfe, gpu_bfe, problem  # noqa: F401
-from .multi_objective import (crowding_distance, fast_non_dominated_sorting, nsga2_survival,  # noqa: F401
-                              select_best_N_mo, sort_population_mo)
+from .multi_objective import (crowding_distance, fast_non_dominated_sorting, hypervolume,  # noqa: F401
+                              nsga2_survival, select_best_N_mo, sort_population_mo)
 from .problems import (ackley, dtlz, griewank, lennard_jones, rastrigin, rosenbrock, schwefel,  # noqa: F401
                        translate, zdt)

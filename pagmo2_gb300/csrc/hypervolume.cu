@@ -1,0 +1,288 @@
+// Hypervolume of 2 or 3 objectives on the GPU (pagmo's hypervolume::compute,
+// src/utils/hypervolume.cpp:203-228, which picks hv2d for two objectives and
+// hv3d for three: src/utils/hv_algos/hv_hv2d.cpp:48-68, hv_hv3d.cpp:75-116).
+//
+// The dominated region is summed as non-negative slabs (no cancellation):
+//  - 2D: with the points sorted by y, the staircase width W(t) = max over the
+//    first t+1 points of (r_x - x), and HV = sum_t (y_{t+1} - y_t) W(t) with
+//    y_n = r_y (hv2d's own sweep, summed as a tree).
+//  - 3D: with the points sorted by z, level i holds the 2D area A_i of the
+//    points up to level i, and HV = sum_i (z_{i+1} - z_i) A_i with z_n = r_z.
+//    Every level is an independent warp: over the points in y order, the
+//    running maximum of (r_x - x) among the points whose z rank is at most i
+//    times the y steps. O(n^2) work, all levels in parallel.
+// Order: both sorts are counting ranks over the NaN-aware int64 order keys
+// (ties by index); a tie does not change any slab (its step is zero). The
+// widths r_x - x are non-negative on valid input, so their running maximum
+// is taken on the IEEE bit patterns with integer operations.
+#include "pgx_internal.cuh"
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <sstream>
+#include <string>
+#include <vector>
+
+namespace pgx
+{
+namespace
+{
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ long long hv_key(double v)
+{
+    if (isnan(v)) return LLONG_MAX;
+    if (v == 0.0) return 0;
+    const long long b = __double_as_longlong(v);
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+
+// keys of coordinates 1 (y) and, for 3D, 2 (z): kyz[c * n + t]
+__global__ void hv_keys_kernel(const double *__restrict__ pts, uint32_t n, uint32_t m, long long *__restrict__ kyz)
+{
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        kyz[t] = hv_key(pts[static_cast<uint64_t>(t) * m + 1]);
+        if (m == 3u) kyz[static_cast<uint64_t>(n) + t] = hv_key(pts[static_cast<uint64_t>(t) * m + 2]);
+    }
+}
+
+// rank[c * n + t]: position of point t when sorted by coordinate c + 1 (ties
+// by index); blockIdx.y = c, keys staged through shared memory
+__global__ void hv_rank_kernel(const long long *__restrict__ kyz, uint32_t n, int32_t *__restrict__ rank)
+{
+    __shared__ long long tile[1024];
+    const uint32_t c = blockIdx.y;
+    const long long *k = kyz + static_cast<uint64_t>(c) * n;
+    for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < n; b0 += gridDim.x * blockDim.x) {
+        const uint32_t t = b0 + threadIdx.x;
+        const bool act = t < n;
+        const long long kt = act ? k[t] : 0;
+        int r = 0;
+        for (uint32_t j0 = 0; j0 < n; j0 += 1024u) {
+            const uint32_t lim = n - j0 < 1024u ? n - j0 : 1024u;
+            __syncthreads();
+            for (uint32_t j = threadIdx.x; j < lim; j += blockDim.x) tile[j] = k[j0 + j];
+            __syncthreads();
+            if (act) {
+                for (uint32_t j = 0; j < lim; ++j) {
+                    const long long kj = tile[j];
+                    r += (kj < kt) | ((kj == kt) & (j0 + j < t));
+                }
+            }
+        }
+        if (act) rank[static_cast<uint64_t>(c) * n + t] = r;
+    }
+}
+
+// points into y order: ys, the widths r_x - x (as bits), and for 3D the z
+// rank of each y position and the z values in z order
+__global__ void hv_scatter_kernel(const double *__restrict__ pts, uint32_t n, uint32_t m, double rx,
+                                  const int32_t *__restrict__ rank, double *__restrict__ ys,
+                                  long long *__restrict__ wbits, int32_t *__restrict__ zr, double *__restrict__ zs)
+{
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const double *p = pts + static_cast<uint64_t>(t) * m;
+        const int32_t ry = rank[t];
+        ys[ry] = p[1];
+        wbits[ry] = __double_as_longlong(rx - p[0]);
+        if (m == 3u) {
+            const int32_t rz = rank[static_cast<uint64_t>(n) + t];
+            zr[ry] = rz;
+            zs[rz] = p[2];
+        }
+    }
+}
+
+__device__ __forceinline__ long long warp_incl_max(long long v)
+{
+    const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long u = __shfl_up_sync(kFull, v, o);
+        if (static_cast<int>(lane) >= o && u > v) v = u;
+    }
+    return v;
+}
+
+// One warp per level i (3D) or a single level with every point (2D, zr null):
+// A = sum_t (y_{t+1} - y_t) * max_{t' <= t, zr[t'] <= i} w[t']; term[i] =
+// (z_{i+1} - z_i) * A (3D) or A (2D).
+__global__ void hv_levels_kernel(const double *__restrict__ ys, const long long *__restrict__ wbits,
+                                 const int32_t *__restrict__ zr, const double *__restrict__ zs, uint32_t n, double ry,
+                                 double rz, uint32_t levels, double *__restrict__ term)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < levels; i += nw) {
+        double dz = 1.0;
+        if (zr) {
+            dz = (i + 1u < n ? zs[i + 1u] : rz) - zs[i];
+            if (dz == 0.0) { // a level of no thickness adds nothing
+                if (lane == 0) term[i] = 0.0;
+                continue;
+            }
+        }
+        long long carry = 0; // bits of +0.0: no point yet
+        double a = 0.0;
+        for (uint32_t t0 = 0; t0 < n; t0 += 32u) {
+            const uint32_t t = t0 + lane;
+            long long v = 0;
+            double dy = 0.0;
+            if (t < n) {
+                if (!zr || static_cast<uint32_t>(zr[t]) <= i) v = wbits[t];
+                dy = (t + 1u < n ? ys[t + 1u] : ry) - ys[t];
+            }
+            v = warp_incl_max(v);
+            if (carry > v) v = carry;
+            carry = __shfl_sync(kFull, v, 31);
+            a = fma(dy, __longlong_as_double(v), a);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
+        if (lane == 0) term[i] = zr ? dz * a : a;
+    }
+}
+
+// out = sum of term[0 .. L) in a fixed tree (one block)
+__global__ void hv_sum_kernel(const double *__restrict__ term, uint32_t L, double *__restrict__ out)
+{
+    __shared__ double part[1024];
+    double s = 0.0;
+    for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) s += term[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (unsigned h = blockDim.x / 2u; h > 0; h >>= 1) {
+        if (threadIdx.x < h) part[threadIdx.x] += part[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = part[0];
+}
+
+// hypervolume::verify_after_construct and verify_before_compute with
+// hv_algorithm::assert_minimisation (src/utils/hypervolume.cpp:406-449,
+// src/utils/hv_algos/hv_algorithm.cpp:226-258), on host data.
+int hv_check(const double *pts, uint64_t n, uint64_t m, const double *r)
+{
+    PGX_CHECK(n > 0u, PGX_ERR_INVALID, "Point set cannot be empty.");
+    PGX_CHECK(m > 1u, PGX_ERR_INVALID, "Points of dimension > 1 required.");
+    for (uint64_t i = 0; i < n * m; ++i)
+        PGX_CHECK(!std::isnan(pts[i]), PGX_ERR_INVALID,
+                  "A nan value has been encountered in the hypervolume points. Cannot construct the hypervolume object");
+    PGX_CHECK(m == 2u || m == 3u, PGX_ERR_NOTIMPL,
+              "hypervolume on the GPU: 2 or 3 objectives (pagmo's hv2d and hv3d); " + std::to_string(m) + " given");
+    for (uint64_t i = 0; i < n; ++i) {
+        bool outside = false, all_equal = true;
+        for (uint64_t k = 0; k < m; ++k) {
+            outside |= r[k] < pts[i * m + k];
+            all_equal &= r[k] == pts[i * m + k];
+        }
+        if (outside || all_equal) {
+            std::string sp("("), sr("(");
+            for (uint64_t k = 0; k < m; ++k) {
+                sp += std::to_string(pts[i * m + k]);
+                sr += std::to_string(r[k]);
+                sp += k + 1 < m ? ", " : ")";
+                sr += k + 1 < m ? ", " : ")";
+            }
+            std::ostringstream ss;
+            ss << "Reference point is invalid: another point seems to be outside the reference point boundary, or "
+                  "be equal to it:"
+               << std::endl
+               << " P[" << i << "]\t= " << sp << std::endl
+               << " R\t= " << sr << std::endl;
+            set_error(ss.str());
+            return PGX_ERR_INVALID;
+        }
+    }
+    return PGX_OK;
+}
+
+size_t align256(size_t b)
+{
+    return (b + 255u) & ~size_t(255);
+}
+
+// All kernels on stream s over device points; *d_out receives the volume.
+int launch_hypervolume(pgx_context *ctx, const double *d_pts, uint32_t n, uint32_t m, const double *r,
+                       double *d_out, cudaStream_t s)
+{
+    const uint32_t nc = m - 1u;
+    const size_t b_keys = align256(static_cast<size_t>(n) * nc * 8u), b_rank = align256(static_cast<size_t>(n) * nc * 4u);
+    const size_t b_d = align256(static_cast<size_t>(n) * 8u), b_i = align256(static_cast<size_t>(n) * 4u);
+    PGX_TRY(ctx->s_crowd.ensure(b_keys + b_rank + 4u * b_d + b_i + 256u));
+    char *base = ctx->s_crowd.as<char>();
+    long long *kyz = reinterpret_cast<long long *>(base);
+    int32_t *rank = reinterpret_cast<int32_t *>(base + b_keys);
+    double *ys = reinterpret_cast<double *>(base + b_keys + b_rank);
+    long long *wbits = reinterpret_cast<long long *>(base + b_keys + b_rank + b_d);
+    double *zs = reinterpret_cast<double *>(base + b_keys + b_rank + 2u * b_d);
+    double *term = reinterpret_cast<double *>(base + b_keys + b_rank + 3u * b_d);
+    int32_t *zr = reinterpret_cast<int32_t *>(base + b_keys + b_rank + 4u * b_d);
+    const int sms = ctx->num_sms;
+    const int g1 = static_cast<int>(std::min<uint64_t>((n + 255u) / 256u, static_cast<uint64_t>(sms) * 8u));
+    hv_keys_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, kyz);
+    PGX_CUDA(cudaGetLastError());
+    const int g2 = static_cast<int>(std::min<uint64_t>((n + 255u) / 256u, static_cast<uint64_t>(sms) * 4u));
+    hv_rank_kernel<<<dim3(g2, nc), 256, 0, s>>>(kyz, n, rank);
+    PGX_CUDA(cudaGetLastError());
+    hv_scatter_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, r[0], rank, ys, wbits, m == 3u ? zr : nullptr,
+                                         m == 3u ? zs : nullptr);
+    PGX_CUDA(cudaGetLastError());
+    const uint32_t levels = m == 3u ? n : 1u;
+    const int g3 = static_cast<int>(std::min<uint64_t>((static_cast<uint64_t>(levels) * 32u + 255u) / 256u,
+                                                       static_cast<uint64_t>(sms) * 8u));
+    hv_levels_kernel<<<g3, 256, 0, s>>>(ys, wbits, m == 3u ? zr : nullptr, m == 3u ? zs : nullptr, n, r[1],
+                                        m == 3u ? r[2] : 0.0, levels, term);
+    PGX_CUDA(cudaGetLastError());
+    hv_sum_kernel<<<1, 1024, 0, s>>>(term, levels, d_out);
+    PGX_CUDA(cudaGetLastError());
+    ctx->launches += 5;
+    return PGX_OK;
+}
+
+} // namespace
+} // namespace pgx
+
+using namespace pgx;
+
+extern "C" {
+
+int pgx_hypervolume(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, const double *ref, double *out)
+{
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    PGX_CHECK(out != nullptr && (points != nullptr || n == 0) && ref != nullptr, PGX_ERR_INVALID, "null buffer");
+    PGX_TRY(hv_check(points, n, m, ref));
+    PGX_CHECK(n < (1u << 24), PGX_ERR_CAPACITY, "hypervolume: more than 2^24 points");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    PGX_TRY(use_device(ctx));
+    const size_t bp = align256(static_cast<size_t>(n) * m * 8u);
+    PGX_TRY(ctx->s_points.ensure(bp + 256u));
+    double *dp = ctx->s_points.as<double>();
+    double *dout = reinterpret_cast<double *>(ctx->s_points.as<char>() + bp);
+    cudaStream_t s = ctx->stream;
+    PGX_CUDA(cudaMemcpyAsync(dp, points, static_cast<size_t>(n) * m * 8u, cudaMemcpyHostToDevice, s));
+    PGX_TRY(launch_hypervolume(ctx, dp, static_cast<uint32_t>(n), static_cast<uint32_t>(m), ref, dout, s));
+    PGX_CUDA(cudaMemcpyAsync(out, dout, sizeof(double), cudaMemcpyDeviceToHost, s));
+    PGX_CUDA(cudaStreamSynchronize(s));
+    return PGX_OK;
+}
+
+int pgx_hypervolume_device(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m, const double *ref,
+                           double *d_out, void *stream)
+{
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    PGX_CHECK(d_points != nullptr && d_out != nullptr && ref != nullptr, PGX_ERR_INVALID, "null buffer");
+    PGX_CHECK(n > 0u, PGX_ERR_INVALID, "Point set cannot be empty.");
+    PGX_CHECK(m > 1u, PGX_ERR_INVALID, "Points of dimension > 1 required.");
+    PGX_CHECK(m == 2u || m == 3u, PGX_ERR_NOTIMPL,
+              "hypervolume on the GPU: 2 or 3 objectives (pagmo's hv2d and hv3d); " + std::to_string(m) + " given");
+    PGX_CHECK(n < (1u << 24), PGX_ERR_CAPACITY, "hypervolume: more than 2^24 points");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    PGX_TRY(use_device(ctx));
+    return launch_hypervolume(ctx, d_points, static_cast<uint32_t>(n), static_cast<uint32_t>(m), ref, d_out,
+                              static_cast<cudaStream_t>(stream));
+}
+
+} // extern "C"

@@ -148,3 +148,44 @@ def std_sort_keys(keys, values=None, ctx: _nat.Context | None = None):
     ctx = ctx or _nat.default_context()
     _nat.check(_nat.lib().pgx_std_sort_i64(ctx.handle, _nat.ptr(k), _nat.ptr(v), k.size))
     return k, v
+
+
+class hypervolume:
+    """pagmo's hypervolume indicator (src/utils/hypervolume.cpp) for 2 or 3 objectives: compute(ref) is the
+    measure of the region the points dominate, bounded by the reference point, on the GPU (hv2d / hv3d's
+    result; 4 or more objectives, pagmo's hvwfg, raise NotImplementedError). Construction checks the points as
+    the reference does (hypervolume.cpp:406-432)."""
+
+    def __init__(self, points, verify: bool = True, context: N.Context | None = None):
+        rows = points.get_f() if hasattr(points, "get_f") else points
+        if len(rows) == 0:
+            raise ValueError("Point set cannot be empty.")
+        if isinstance(rows, np.ndarray) and rows.ndim == 2:
+            a = np.ascontiguousarray(rows, dtype=np.float64)
+        else:
+            vs = [np.asarray(r, dtype=np.float64).reshape(-1) for r in rows]
+            if vs[0].size <= 1:
+                raise ValueError("Points of dimension > 1 required.")
+            if any(v.size != vs[0].size for v in vs):
+                raise ValueError("All point set dimensions must be equal.")
+            a = np.ascontiguousarray(np.stack(vs))
+        if a.shape[1] <= 1:
+            raise ValueError("Points of dimension > 1 required.")
+        if verify and np.isnan(a).any():
+            raise ValueError("A nan value has been encountered in the hypervolume points. Cannot construct the "
+                             "hypervolume object")
+        self._points = a
+        self._ctx = context
+
+    def get_points(self) -> np.ndarray:
+        return self._points.copy()
+
+    def compute(self, ref) -> float:
+        r = np.ascontiguousarray(np.asarray(ref, dtype=np.float64).reshape(-1))
+        n, m = self._points.shape
+        if r.size != m:
+            raise ValueError("Point set dimensions and reference point dimension must be equal.")
+        ctx = self._ctx if self._ctx is not None else N.default_context()
+        out = C.c_double()
+        N.check(N.lib().pgx_hypervolume(ctx.handle, N.ptr(self._points), n, m, N.ptr(r), C.byref(out)))
+        return out.value

@@ -14,6 +14,7 @@ Outputs (numpy .npz, small):
   mo_problems.npz  per ZDT / DTLZ case: the problem (kind, prob_id, param,
                fdim, alpha), the decision vectors, bfe{thread_bfe{}} fitness
                (n x nobj) and p_distance of every row
+  hv.npz       per case: points, reference point and hypervolume(points).compute(ref)
   mo.npz       per case: the objective vectors, fast_non_dominated_sorting
                (rank, dom_count, fronts, dom_list), crowding_distance of
                every front of three or more points, sort_population_mo and
@@ -85,6 +86,22 @@ def mo_problem_cases():
     return cases
 
 
+def hv_cases():
+    """(name, points, reference point) for hypervolume of 2 and 3 objectives."""
+    rs = np.random.RandomState(900)
+    cases = []
+    for n, m in ((1, 2), (3, 2), (128, 2), (1000, 2), (2, 3), (128, 3), (700, 3), (3000, 3)):
+        cases.append((f"uniform_{n}x{m}", rs.random_sample((n, m)), np.full(m, 1.1)))
+    for n, m in ((200, 2), (400, 3)):
+        pts = np.floor(rs.random_sample((n, m)) * 8) / 8  # ties and duplicates
+        pts[:5, 0] = 1.0  # on the border of the reference point in one coordinate
+        cases.append((f"grid_{n}x{m}", pts, np.full(m, 1.0)))
+    w = -np.log(rs.random_sample((600, 3)))
+    w /= w.sum(axis=1, keepdims=True)
+    cases.append(("simplex_layers_1800x3", np.concatenate([w, 1.5 * w, 2.0 * w]), np.full(3, 2.5)))
+    return cases
+
+
 def mo_cases():
     cases = []
     # tests/multi_objective.cpp fnds examples
@@ -137,6 +154,13 @@ def main():
         mop[f"{name}/p_distance"] = ref.mo_p_distance(spec, x)
     np.savez_compressed(HERE / "mo_problems.npz", **mop)
 
+    hv = {}
+    for name, pts, r in hv_cases():
+        hv[f"{name}/points"] = pts
+        hv[f"{name}/ref"] = r
+        hv[f"{name}/hv"] = np.array([ref.hypervolume(pts, r)])
+    np.savez_compressed(HERE / "hv.npz", **hv)
+
     mo = {}
     for name, p in mo_cases():
         r = ref.fnds(p)
@@ -158,7 +182,7 @@ def main():
         for nb in sorted({1, n // 3, n // 2, n - 1}):
             mo[f"{name}/select_best_{nb}"] = ref.select_best_n_mo(p, nb)
     np.savez_compressed(HERE / "mo.npz", **mo)
-    print("wrote", HERE / "fitness.npz", HERE / "mo_problems.npz", HERE / "mo.npz")
+    print("wrote", HERE / "fitness.npz", HERE / "mo_problems.npz", HERE / "hv.npz", HERE / "mo.npz")
 
 
 if __name__ == "__main__":
