@@ -133,6 +133,17 @@ PGX_API int pgx_batch_eval_device(pgx_context *ctx, int kind, uint64_t param, co
    (their callers then report PGX_ERR_TIMEOUT); the context stays usable. */
 PGX_API int pgx_selftest_barrier_timeout(pgx_context *ctx, uint64_t spin_limit, int32_t *timed_out);
 
+/* Self-test of the reciprocal and its cube in the Lennard-Jones pair loops
+   (no counterpart in the reference, whose pair sum divides and cubes in FP64:
+   src/problems/lennard_jones.cpp:83): inv[i] = the device's 1/d[i] and, when
+   inv_cube is not null, inv_cube[i] = its 1/d[i]^3, as those loops compute
+   them, for host arrays of n values. For 2^-100 <= d < 2^101 (integer fixed
+   point): 1/d within one half unit of the last place of the exact value plus
+   2^-10 units, 1/d^3 plus 2^-5 units; for the other positive normal d with a
+   normal reciprocal (an FP64 Newton step, then two FP64 multiplies): 1/d
+   within one unit. Other d are not covered (the pair loops flag d = 0 apart). */
+PGX_API int pgx_selftest_lj_reciprocal(pgx_context *ctx, const double *d, uint64_t n, double *inv, double *inv_cube);
+
 /* ------------------------------------- multi-objective test problems (ZDT, DTLZ) */
 
 /* A ZDT or DTLZ problem as its reference constructor takes it:

@@ -59,6 +59,7 @@ SIGNATURES = {
     "pgx_mo_batch_fitness_device": (C.c_int, [_vp, _vp, _vp, _u64, _vp, _vp]),
     "pgx_mo_p_distance": (C.c_int, [_vp, _vp, _vp, _u64, _vp]),
     "pgx_selftest_barrier_timeout": (C.c_int, [_vp, _u64, C.POINTER(C.c_int32)]),
+    "pgx_selftest_lj_reciprocal": (C.c_int, [_vp, _vp, _u64, _vp, _vp]),
     "pgx_hypervolume": (C.c_int, [_vp, _vp, _u64, _u64, _vp, C.POINTER(C.c_double)]),
     "pgx_hypervolume_device": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp]),
 }

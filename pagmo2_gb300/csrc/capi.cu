@@ -590,6 +590,14 @@ int pgx_selftest_barrier_timeout(pgx_context *ctx, uint64_t spin_limit, int32_t 
     return run_barrier_timeout_test(ctx, spin_limit, timed_out);
 }
 
+int pgx_selftest_lj_reciprocal(pgx_context *ctx, const double *d, uint64_t n, double *inv, double *inv_cube)
+{
+    PGX_CHECK(ctx != nullptr && (n == 0 || (d != nullptr && inv != nullptr)), PGX_ERR_INVALID, "null argument");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    PGX_TRY(use_device(ctx));
+    return run_lj_reciprocal(ctx, d, n, inv, inv_cube);
+}
+
 int pgx_fnds_dom_list(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, int64_t *dl_offsets,
                       int32_t *dl_indices, uint64_t capacity, uint64_t *dl_total)
 {

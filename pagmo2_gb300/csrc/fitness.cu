@@ -329,4 +329,40 @@ int launch_rows_variant(int kind, uint64_t nx, const double *d_x, uint64_t n, do
     }
 }
 
+namespace
+{
+__global__ void lj_reciprocal_kernel(const double *__restrict__ d, uint64_t n, double *__restrict__ inv,
+                                     double *__restrict__ cube)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        double r, s;
+        dev::lj_rcp_cube(d[i], r, s);
+        inv[i] = r;
+        cube[i] = s;
+    }
+}
+} // namespace
+
+// The Lennard-Jones pair loops' 1/d and 1/d^3 on host values (self-test).
+int run_lj_reciprocal(pgx_context *ctx, const double *d, uint64_t n, double *inv, double *cube)
+{
+    if (n == 0) return PGX_OK;
+    const size_t b = (n * sizeof(double) + 255u) & ~size_t(255);
+    PGX_TRY(ctx->s_points.ensure(3u * b));
+    double *dd = ctx->s_points.as<double>();
+    double *dinv = reinterpret_cast<double *>(ctx->s_points.as<char>() + b);
+    double *dcube = reinterpret_cast<double *>(ctx->s_points.as<char>() + 2u * b);
+    cudaStream_t s = ctx->stream;
+    PGX_CUDA(cudaMemcpyAsync(dd, d, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    const int grid = static_cast<int>(std::min<uint64_t>((n + 255u) / 256u, static_cast<uint64_t>(ctx->num_sms) * 8u));
+    lj_reciprocal_kernel<<<grid, 256, 0, s>>>(dd, n, dinv, dcube);
+    PGX_CUDA(cudaGetLastError());
+    PGX_CUDA(cudaMemcpyAsync(inv, dinv, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (cube) PGX_CUDA(cudaMemcpyAsync(cube, dcube, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PGX_CUDA(cudaStreamSynchronize(s));
+    return PGX_OK;
+}
+
 } // namespace pgx
+

@@ -14,6 +14,8 @@
 #include <cmath>
 #include <cstdint>
 
+#include "rcp_fixed.h"
+
 namespace pgx
 {
 namespace dev
@@ -717,28 +719,31 @@ __device__ __forceinline__ double lj_rcp(double d)
     return (__double_as_longlong(y) << 1) == 0 ? y : r;
 }
 
-// The same reciprocal from a single-precision seed: d's exponent and leading
-// mantissa bits moved into a float with integer operations (relative error
-// below 2^-23), the FP32 approximate reciprocal (about 2^-23), the result
-// moved back the same way, then the cubic Newton step (error about 2^-66,
-// below the final rounding). Only the two Newton FMAs and the polynomial FMA
-// use the FP64 pipe. Distances outside 2^-100 .. 2^100, zero, infinities and
-// NaN take lj_rcp.
-__device__ __forceinline__ double lj_rcp_fs(double d)
+// 1/d and s = 1/d^3 without FP64 instructions: the FP32 approximate
+// reciprocal of m (d = m 2^k) as the seed, refined in integer fixed point and
+// cubed there (rcp_fixed.h: within 0.51 and 0.52 units of the last place).
+// The pair loops spent 21 FP64 instructions per pair (13 without the
+// gradient) on a pipe that retires two lanes per SM per clock; this moves the
+// reciprocal's three and the cube's two onto the integer pipes. Distances
+// outside 2^-100 .. 2^100, zero, infinities and NaN take lj_rcp and two FP64
+// multiplies.
+__device__ __forceinline__ void lj_rcp_cube(double d, double &inv, double &s)
 {
-    const unsigned hi = static_cast<unsigned>(__double2hiint(d));
+    const uint64_t b = static_cast<uint64_t>(__double_as_longlong(d));
+    const unsigned hi = static_cast<unsigned>(b >> 32);
     const unsigned ex = (hi >> 20) & 0x7ffu;
-    if (ex - (1023u - 100u) > 200u || (hi >> 31)) return lj_rcp(d);
-    const unsigned lo = static_cast<unsigned>(__double2loint(d));
-    const unsigned fb = ((ex - 1023u + 127u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    if (ex - (1023u - 100u) > 200u || (hi >> 31)) {
+        inv = lj_rcp(d);
+        s = inv * inv * inv;
+        return;
+    }
+    const uint64_t f = b & ((1ull << 52) - 1u);
     float yf;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(__uint_as_float(fb)));
-    const unsigned yb = __float_as_uint(yf);
-    const unsigned ye = (yb >> 23) & 0xffu;
-    const double y = __hiloint2double(static_cast<int>(((ye - 127u + 1023u) << 20) | ((yb & 0x7fffffu) >> 3)),
-                                      static_cast<int>((yb & 7u) << 29));
-    const double e = fma(-d, y, 1.0);
-    return fma(y, fma(e, e, e), y);
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(__uint_as_float(rcpfx::seed_input_bits(f))));
+    uint64_t ib, cb;
+    rcpfx::rcp_and_cube_bits(ex, f, rcpfx::seed_q32(__float_as_uint(yf)), &ib, &cb);
+    inv = __longlong_as_double(static_cast<long long>(ib));
+    s = __longlong_as_double(static_cast<long long>(cb));
 }
 
 __device__ __forceinline__ void lj_decode(const double *__restrict__ xr, uint32_t na, double *px, double *py,
@@ -812,8 +817,8 @@ __device__ __forceinline__ void lj_cluster_reg(const double *__restrict__ xr, ui
                 if (j >= na) j -= na;
                 const double dx = ox[m] - px[j], dy = oy[m] - py[j], dz = oz[m] - pz[j];
                 const double d = fma(dx, dx, fma(dy, dy, dz * dz));
-                const double inv = lj_rcp_fs(d);
-                const double s = inv * inv * inv;
+                double inv, s;
+                lj_rcp_cube(d, inv, s);
                 const double term = fma(s, s, -s);
                 if (__double_as_longlong(d) != 0)
                     e += term;
@@ -883,8 +888,8 @@ __device__ __forceinline__ void lj_cluster_flat(const double *__restrict__ xr, u
             dy = py[i] - py[j];
             dz = pz[i] - pz[j];
             const double d = fma(dx, dx, fma(dy, dy, dz * dz));
-            const double inv = lj_rcp_fs(d);
-            const double s = inv * inv * inv;
+            double inv, s;
+            lj_rcp_cube(d, inv, s);
             const double term = fma(s, s, -s);
             if (__double_as_longlong(d) != 0)
                 e += term;
@@ -954,8 +959,8 @@ __device__ __forceinline__ void lj_cluster_smem(const double *__restrict__ xr, u
                 dy = py[i] - py[j];
                 dz = pz[i] - pz[j];
                 const double d = fma(dx, dx, fma(dy, dy, dz * dz));
-                const double inv = lj_rcp_fs(d);
-                const double s = inv * inv * inv;
+                double inv, s;
+                lj_rcp_cube(d, inv, s);
                 const double term = fma(s, s, -s);
                 if (__double_as_longlong(d) != 0)
                     e += term;

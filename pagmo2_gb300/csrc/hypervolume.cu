@@ -9,8 +9,9 @@
 //  - 3D: with the points sorted by z, level i holds the 2D area A_i of the
 //    points up to level i, and HV = sum_i (z_{i+1} - z_i) A_i with z_n = r_z.
 //    Every level is an independent warp: over the points in y order, the
-//    running maximum of (r_x - x) among the points whose z rank is at most i
-//    times the y steps. O(n^2) work, all levels in parallel.
+//    running maximum of (r_x - x) among the points whose z rank is at most i,
+//    summed run by run between the points that widen it. O(n^2) integer work,
+//    FP64 only at those points, all levels in parallel.
 // Order: both sorts are counting ranks over the NaN-aware int64 order keys
 // (ties by index); a tie does not change any slab (its step is zero). The
 // widths r_x - x are non-negative on valid input, so their running maximum
@@ -48,20 +49,24 @@ __global__ void hv_keys_kernel(const double *__restrict__ pts, uint32_t n, uint3
     }
 }
 
-// rank[c * n + t]: position of point t when sorted by coordinate c + 1 (ties
-// by index); blockIdx.y = c, keys staged through shared memory
-__global__ void hv_rank_kernel(const long long *__restrict__ kyz, uint32_t n, int32_t *__restrict__ rank)
+// part[(q * nc + c) * n + t]: how many points of the q-th of gridDim.z
+// slices of the index range precede point t when sorted by coordinate c + 1
+// (ties by index); the slices add up to t's position. blockIdx.y = c, keys
+// staged through shared memory.
+__global__ void hv_rank_kernel(const long long *__restrict__ kyz, uint32_t n, int32_t *__restrict__ part)
 {
     __shared__ long long tile[1024];
-    const uint32_t c = blockIdx.y;
+    const uint32_t c = blockIdx.y, q = blockIdx.z, nq = gridDim.z;
     const long long *k = kyz + static_cast<uint64_t>(c) * n;
+    const uint32_t jb = static_cast<uint32_t>(static_cast<uint64_t>(n) * q / nq);
+    const uint32_t je = static_cast<uint32_t>(static_cast<uint64_t>(n) * (q + 1u) / nq);
     for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < n; b0 += gridDim.x * blockDim.x) {
         const uint32_t t = b0 + threadIdx.x;
         const bool act = t < n;
         const long long kt = act ? k[t] : 0;
         int r = 0;
-        for (uint32_t j0 = 0; j0 < n; j0 += 1024u) {
-            const uint32_t lim = n - j0 < 1024u ? n - j0 : 1024u;
+        for (uint32_t j0 = jb; j0 < je; j0 += 1024u) {
+            const uint32_t lim = je - j0 < 1024u ? je - j0 : 1024u;
             __syncthreads();
             for (uint32_t j = threadIdx.x; j < lim; j += blockDim.x) tile[j] = k[j0 + j];
             __syncthreads();
@@ -72,23 +77,28 @@ __global__ void hv_rank_kernel(const long long *__restrict__ kyz, uint32_t n, in
                 }
             }
         }
-        if (act) rank[static_cast<uint64_t>(c) * n + t] = r;
+        if (act) part[(static_cast<uint64_t>(q) * gridDim.y + c) * n + t] = r;
     }
 }
 
 // points into y order: ys, the widths r_x - x (as bits), and for 3D the z
-// rank of each y position and the z values in z order
+// rank of each y position and the z values in z order; the ranks are the
+// sums of the nq slice counts
 __global__ void hv_scatter_kernel(const double *__restrict__ pts, uint32_t n, uint32_t m, double rx,
-                                  const int32_t *__restrict__ rank, double *__restrict__ ys,
+                                  const int32_t *__restrict__ part, uint32_t nq, double *__restrict__ ys,
                                   long long *__restrict__ wbits, int32_t *__restrict__ zr, double *__restrict__ zs)
 {
+    const uint64_t stride = static_cast<uint64_t>(m - 1u) * n;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const double *p = pts + static_cast<uint64_t>(t) * m;
-        const int32_t ry = rank[t];
+        int32_t ry = 0, rz = 0;
+        for (uint32_t q = 0; q < nq; ++q) {
+            ry += part[q * stride + t];
+            if (m == 3u) rz += part[q * stride + n + t];
+        }
         ys[ry] = p[1];
         wbits[ry] = __double_as_longlong(rx - p[0]);
         if (m == 3u) {
-            const int32_t rz = rank[static_cast<uint64_t>(n) + t];
             zr[ry] = rz;
             zs[rz] = p[2];
         }
@@ -108,7 +118,10 @@ __device__ __forceinline__ long long warp_incl_max(long long v)
 
 // One warp per level i (3D) or a single level with every point (2D, zr null):
 // A = sum_t (y_{t+1} - y_t) * max_{t' <= t, zr[t'] <= i} w[t']; term[i] =
-// (z_{i+1} - z_i) * A (3D) or A (2D).
+// (z_{i+1} - z_i) * A (3D) or A (2D). The running maximum W changes only at
+// "records" (a point widening the staircase), so A is summed run by run,
+// W_run * (y at the next record - y at this record), the last run ending at
+// r_y: two FP64 operations per record instead of two per point.
 __global__ void hv_levels_kernel(const double *__restrict__ ys, const long long *__restrict__ wbits,
                                  const int32_t *__restrict__ zr, const double *__restrict__ zs, uint32_t n, double ry,
                                  double rz, uint32_t levels, double *__restrict__ term)
@@ -124,21 +137,34 @@ __global__ void hv_levels_kernel(const double *__restrict__ ys, const long long 
                 continue;
             }
         }
-        long long carry = 0; // bits of +0.0: no point yet
+        long long carry = 0;                // bits of the running maximum so far (+0.0: no point yet)
+        double pend_w = 0.0, pend_y = 0.0;  // the open run: its width and where it starts
         double a = 0.0;
         for (uint32_t t0 = 0; t0 < n; t0 += 32u) {
             const uint32_t t = t0 + lane;
+            const bool valid = t < n;
             long long v = 0;
-            double dy = 0.0;
-            if (t < n) {
-                if (!zr || static_cast<uint32_t>(zr[t]) <= i) v = wbits[t];
-                dy = (t + 1u < n ? ys[t + 1u] : ry) - ys[t];
-            }
+            if (valid && (!zr || static_cast<uint32_t>(zr[t]) <= i)) v = wbits[t];
             v = warp_incl_max(v);
             if (carry > v) v = carry;
+            long long prev = __shfl_up_sync(kFull, v, 1);
+            if (lane == 0) prev = carry;
+            const bool rec = valid && v != prev;
+            const uint32_t b = __ballot_sync(kFull, rec);
+            if (b) {
+                const double y = rec ? ys[t] : 0.0;
+                const double w = __longlong_as_double(v);
+                const uint32_t nb = b & ~((2u << lane) - 1u); // records after this lane
+                const double ynx = __shfl_sync(kFull, y, nb ? __ffs(nb) - 1 : static_cast<int>(lane));
+                if (rec && nb) a = fma(w, ynx - y, a);
+                if (static_cast<int>(lane) == __ffs(b) - 1 && pend_w > 0.0) a = fma(pend_w, y - pend_y, a);
+                const int last = 31 - __clz(b);
+                pend_w = __shfl_sync(kFull, w, last);
+                pend_y = __shfl_sync(kFull, y, last);
+            }
             carry = __shfl_sync(kFull, v, 31);
-            a = fma(dy, __longlong_as_double(v), a);
         }
+        if (lane == 0 && pend_w > 0.0) a = fma(pend_w, ry - pend_y, a);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
         if (lane == 0) term[i] = zr ? dz * a : a;
@@ -209,25 +235,29 @@ int launch_hypervolume(pgx_context *ctx, const double *d_pts, uint32_t n, uint32
                        double *d_out, cudaStream_t s)
 {
     const uint32_t nc = m - 1u;
-    const size_t b_keys = align256(static_cast<size_t>(n) * nc * 8u), b_rank = align256(static_cast<size_t>(n) * nc * 4u);
+    const int sms = ctx->num_sms;
+    const int g1 = static_cast<int>(std::min<uint64_t>((n + 255u) / 256u, static_cast<uint64_t>(sms) * 8u));
+    const int g2 = static_cast<int>(std::min<uint64_t>((n + 255u) / 256u, static_cast<uint64_t>(sms) * 4u));
+    // slices of the index range per rank count: about four blocks per SM in all
+    const uint32_t nq = static_cast<uint32_t>(std::max<int64_t>(
+        1, std::min<int64_t>(8, (4 * sms + g2 * static_cast<int>(nc) - 1) / (g2 * static_cast<int>(nc)))));
+    const size_t b_keys = align256(static_cast<size_t>(n) * nc * 8u);
+    const size_t b_rank = align256(static_cast<size_t>(n) * nc * nq * 4u);
     const size_t b_d = align256(static_cast<size_t>(n) * 8u), b_i = align256(static_cast<size_t>(n) * 4u);
     PGX_TRY(ctx->s_crowd.ensure(b_keys + b_rank + 4u * b_d + b_i + 256u));
     char *base = ctx->s_crowd.as<char>();
     long long *kyz = reinterpret_cast<long long *>(base);
-    int32_t *rank = reinterpret_cast<int32_t *>(base + b_keys);
+    int32_t *part = reinterpret_cast<int32_t *>(base + b_keys);
     double *ys = reinterpret_cast<double *>(base + b_keys + b_rank);
     long long *wbits = reinterpret_cast<long long *>(base + b_keys + b_rank + b_d);
     double *zs = reinterpret_cast<double *>(base + b_keys + b_rank + 2u * b_d);
     double *term = reinterpret_cast<double *>(base + b_keys + b_rank + 3u * b_d);
     int32_t *zr = reinterpret_cast<int32_t *>(base + b_keys + b_rank + 4u * b_d);
-    const int sms = ctx->num_sms;
-    const int g1 = static_cast<int>(std::min<uint64_t>((n + 255u) / 256u, static_cast<uint64_t>(sms) * 8u));
     hv_keys_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, kyz);
     PGX_CUDA(cudaGetLastError());
-    const int g2 = static_cast<int>(std::min<uint64_t>((n + 255u) / 256u, static_cast<uint64_t>(sms) * 4u));
-    hv_rank_kernel<<<dim3(g2, nc), 256, 0, s>>>(kyz, n, rank);
+    hv_rank_kernel<<<dim3(g2, nc, nq), 256, 0, s>>>(kyz, n, part);
     PGX_CUDA(cudaGetLastError());
-    hv_scatter_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, r[0], rank, ys, wbits, m == 3u ? zr : nullptr,
+    hv_scatter_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, r[0], part, nq, ys, wbits, m == 3u ? zr : nullptr,
                                          m == 3u ? zs : nullptr);
     PGX_CUDA(cudaGetLastError());
     const uint32_t levels = m == 3u ? n : 1u;

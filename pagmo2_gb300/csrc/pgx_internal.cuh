@@ -174,6 +174,8 @@ int launch_sort_pairs(pgx_context *ctx, long long *d_keys, int32_t *d_vals, uint
 size_t sort_pairs_state_bytes();
 // Self-test of the bounded grid barriers (one block never arrives).
 int run_barrier_timeout_test(pgx_context *ctx, uint64_t spin_limit, int32_t *timed_out);
+// Self-test of the Lennard-Jones pair loops' 1/d and 1/d^3 (host in, host out; cube may be null).
+int run_lj_reciprocal(pgx_context *ctx, const double *d, uint64_t n, double *inv, double *cube);
 
 // Reads the device status word of the last survival pass of shape (n, m) on
 // this context (after a stream synchronisation): PGX_ERR_TIMEOUT when a grid

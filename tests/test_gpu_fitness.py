@@ -222,6 +222,42 @@ def test_lj_coinciding_atoms_give_inf(ctx, orc):
     assert np.all(np.isnan(g[1, 3:6]))
 
 
+def test_lj_reciprocal_on_device(ctx):
+    """The pair loops' 1/d and 1/d^3 against the exact values (rational
+    arithmetic where 1/d differs from the correctly rounded 1.0 / d): in
+    2^-100 .. 2^100, the integer fixed-point path, 1/d within 0.5 + 2^-10
+    units of the last place (correctly rounded but within 2^-10 units of a
+    midpoint) and 1/d^3 within 0.5 + 2^-5 units; outside, the FP64 Newton
+    step from the FP64 approximate reciprocal, 1/d within one unit."""
+    from fractions import Fraction
+
+    rs = np.random.RandomState(11)
+    d = np.ldexp(1.0 + rs.random_sample(1_000_000), rs.randint(-100, 101, 1_000_000))
+    edges = np.array([0, 1, 2, (1 << 52) - 1, (1 << 52) - 2, 1 << 51, (1 << 29) - 1, 1 << 29], dtype=np.uint64)
+    ex = np.arange(-1021, 1022, dtype=np.int64)  # every binade with a normal reciprocal
+    e_bits = ((ex + 1023).astype(np.uint64) << np.uint64(52))[:, None] | edges[None, :]
+    d = np.concatenate([d, e_bits.ravel().view(np.float64), np.ldexp(1.0 + rs.random_sample(20000),
+                                                                      rs.randint(-1021, 1022, 20000))])
+    inv = np.empty_like(d)
+    cube = np.empty_like(d)
+    N.check(N.lib().pgx_selftest_lj_reciprocal(ctx.handle, d.ctypes.data, d.size, inv.ctypes.data,
+                                               cube.ctypes.data))
+    fast = (d >= 2.0 ** -100) & (d < 2.0 ** 101)
+    bad = np.nonzero(inv != 1.0 / d)[0]
+    assert np.count_nonzero(fast[bad]) <= np.count_nonzero(fast) // 10_000
+    for i in bad:
+        exact = 1 / Fraction(float(d[i]))
+        ulp = Fraction(2) ** (math.frexp(float(exact))[1] - 53)
+        bound = Fraction(1, 2) + Fraction(1, 1024) if fast[i] else Fraction(1)
+        assert abs(Fraction(float(inv[i])) - exact) <= bound * ulp, float(d[i]).hex()
+    # the cubes: exactly on a sample of the fast range, and every edge mantissa
+    idx = np.concatenate([np.arange(0, 1_000_000, 97), np.nonzero(fast)[0][1_000_000:]])
+    for i in idx:
+        exact = 1 / Fraction(float(d[i])) ** 3
+        ulp = Fraction(2) ** (math.frexp(float(exact))[1] - 53)
+        assert abs(Fraction(float(cube[i])) - exact) <= (Fraction(1, 2) + Fraction(1, 32)) * ulp, float(d[i]).hex()
+
+
 def test_nonfinite_inputs_propagate(ctx, orc):
     for kind, param in ((N.RASTRIGIN, 9), (N.ROSENBROCK, 9), (N.LENNARD_JONES, 5)):
         nx = N.problem_nx(kind, param)
