@@ -43,10 +43,14 @@ N_ROWS, DIM = 65536, 1000
 METRIC = "FP64 fitness+grad evals/s"
 UNIT = "evals/s"
 
-# FP64 flops per rosenbrock element in the implemented formulation
-# (FMA = 2): fitness t, sum t^2, (2x-2)^2 accumulate; gradient 2x, 2x-2,
-# t_prev - 2x t, 200 b + c -> 5 FMA + 2 add/sub = 12.
+# Algorithmic flops per rosenbrock element (FMA = 2): fitness t, sum t^2,
+# (2x-2)^2 accumulate; gradient 2x, 2x-2, t_prev - 2x t, 200 b + c -> 5 FMA +
+# 2 add/sub = 12. Of these the kernel runs 4 instructions on the FP64 pipe
+# (t, 2x-2, t_prev - 2x t, 200 b + c: 3 FMA + 1 add = 7 flops); 2x is an
+# exponent increment and the two sums of squares are exact integer
+# accumulations, on the integer pipes.
 ROS_FG_FLOPS_PER_ELEM = 12
+ROS_FG_FP64_INSTR_PER_ELEM = 4
 ROS_F_FLOPS_PER_ELEM = 7
 
 
@@ -324,6 +328,15 @@ def main():
                 "algorithmic": f"{ROS_FG_FLOPS_PER_ELEM} flops/element (FMA=2), {alg_bytes} bytes per launch",
                 "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
                         "peak_source": hbm_src}}
+    # the FP64 pipe itself: the instructions the kernel issues there, against
+    # the probe's DFMA rate (frac above 1.0 for the algorithmic flops because
+    # part of them runs on the integer pipes)
+    fp64_instr_rate = rows_n * (DIM - 1) * ROS_FG_FP64_INSTR_PER_ELEM / (ms * 1e-3)
+    roofline["fp64_pipe"] = {
+        "instructions_per_element": ROS_FG_FP64_INSTR_PER_ELEM,
+        "frac": fp64_instr_rate / (fp64_peak_tflops * 1e12 / 2.0),
+        "note": "2x by exponent increment and the sums of t^2 and (2x-2)^2 as exact integer accumulations "
+                "(integer pipes); the algorithmic frac counts those flops too"}
 
     # the opt-in double-float rows (not FP64 arithmetic), timed beside the headline
     os.environ["PGX_ROSENBROCK_DOUBLE_FLOAT"] = "1"

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdint>
 
+#include "isum.h"
 #include "rcp_fixed.h"
 
 namespace pgx
@@ -45,6 +46,22 @@ __device__ __forceinline__ double group_sum(double v, unsigned mask)
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, G);
     return v;
+}
+
+// Total of the integer sum-of-squares accumulators of a group of G lanes
+// (xor butterfly on integer shuffles: every lane gets the same total, no FP64
+// instruction).
+template <int G>
+__device__ __forceinline__ isum::sq_acc group_isum(isum::sq_acc a, unsigned mask)
+{
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+        const unsigned long long m = __shfl_xor_sync(mask, static_cast<unsigned long long>(a.m), o, G);
+        const int e = __shfl_xor_sync(mask, a.e, o, G);
+        a.flags |= __shfl_xor_sync(mask, a.flags, o, G);
+        isum::add(a, isum::sq_term{m, e});
+    }
+    return a;
 }
 
 // +1.0 or -1.0, and a constant with its sign flipped, built with integer
@@ -189,7 +206,8 @@ __device__ __forceinline__ void rosenbrock_row(const double *__restrict__ xr, ui
 {
     const unsigned sub = threadIdx.x & (G - 1);
     const unsigned mask = group_mask<G>();
-    double acc_t = 0.0, acc_u = 0.0, t_carry = 0.0;
+    isum::sq_acc acc_t = isum::make(), acc_u = isum::make();
+    double t_carry = 0.0;
     double x_cur = sub < nx ? __ldg(xr + sub) : 0.0;
     for (uint32_t base = 0; base < nx; base += G) {
         const uint32_t i = base + sub;
@@ -208,8 +226,8 @@ __device__ __forceinline__ void rosenbrock_row(const double *__restrict__ xr, ui
                 const double c = w - 2.0;
                 double gi;
                 if (has_next) {
-                    acc_t = fma(t, t, acc_t);
-                    acc_u = fma(c, c, acc_u);
+                    isum::add_square(acc_t, t);
+                    isum::add_square(acc_u, c);
                     gi = fma(200.0, fma(-w, t, t_prev), c);
                 } else {
                     gi = 200.0 * t_prev;
@@ -217,16 +235,15 @@ __device__ __forceinline__ void rosenbrock_row(const double *__restrict__ xr, ui
                 gr[i] = gi;
             }
         } else if (has_next) {
-            const double u = x_cur - 1.0;
-            acc_t = fma(t, t, acc_t);
-            acc_u = fma(u, u, acc_u);
+            isum::add_square(acc_t, t);
+            isum::add_square(acc_u, x_cur - 1.0);
         }
         x_cur = x_nxt;
     }
-    acc_t = group_sum<G>(acc_t, mask);
-    acc_u = group_sum<G>(acc_u, mask);
+    const double st = isum::value(group_isum<G>(acc_t, mask));
+    const double su = isum::value(group_isum<G>(acc_u, mask));
     // with the gradient the second sum is over c^2 = 4 (x-1)^2
-    if (sub == 0 && f_out) *f_out = GRAD ? fma(100.0, acc_t, 0.25 * acc_u) : fma(100.0, acc_t, acc_u);
+    if (sub == 0 && f_out) *f_out = GRAD ? fma(100.0, st, 0.25 * su) : fma(100.0, st, su);
 }
 
 // 2x by incrementing the exponent field: exact for normal x whose double is
@@ -253,7 +270,8 @@ __device__ __forceinline__ void rosenbrock_row_v4(const double *__restrict__ xr,
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t slots = nx >> 2;
     const double2 *x2 = reinterpret_cast<const double2 *>(xr);
-    double acc_t = 0.0, acc_u = 0.0, t_carry = 0.0;
+    isum::sq_acc acc_t = isum::make(), acc_u = isum::make();
+    double t_carry = 0.0;
     double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
     if (lane < slots) {
         a = __ldg(x2 + 2u * lane);
@@ -298,19 +316,19 @@ __device__ __forceinline__ void rosenbrock_row_v4(const double *__restrict__ xr,
             }
             if (act) {
                 const double c0 = w0 - 2.0, c1 = w1 - 2.0, c2 = w2 - 2.0, c3 = w3 - 2.0;
-                acc_t = fma(t0, t0, acc_t);
-                acc_t = fma(t1, t1, acc_t);
-                acc_t = fma(t2, t2, acc_t);
-                acc_u = fma(c0, c0, acc_u);
-                acc_u = fma(c1, c1, acc_u);
-                acc_u = fma(c2, c2, acc_u);
+                isum::add_square(acc_t, t0);
+                isum::add_square(acc_t, t1);
+                isum::add_square(acc_t, t2);
+                isum::add_square(acc_u, c0);
+                isum::add_square(acc_u, c1);
+                isum::add_square(acc_u, c2);
                 double2 g01, g23;
                 g01.x = fma(200.0, fma(-w0, t0, tp), c0);
                 g01.y = fma(200.0, fma(-w1, t1, t0), c1);
                 g23.x = fma(200.0, fma(-w2, t2, t1), c2);
                 if (last_has_next) {
-                    acc_t = fma(t3, t3, acc_t);
-                    acc_u = fma(c3, c3, acc_u);
+                    isum::add_square(acc_t, t3);
+                    isum::add_square(acc_u, c3);
                     g23.y = fma(200.0, fma(-w3, t3, t2), c3);
                 } else {
                     g23.y = 200.0 * t2;
@@ -320,25 +338,19 @@ __device__ __forceinline__ void rosenbrock_row_v4(const double *__restrict__ xr,
                 g2[2u * s + 1u] = g23;
             }
         } else if (act) {
-            const double u0 = x0 - 1.0, u1 = x1 - 1.0, u2 = x2v - 1.0;
-            acc_t = fma(t0, t0, acc_t);
-            acc_t = fma(t1, t1, acc_t);
-            acc_t = fma(t2, t2, acc_t);
-            acc_u = fma(u0, u0, acc_u);
-            acc_u = fma(u1, u1, acc_u);
-            acc_u = fma(u2, u2, acc_u);
-            if (last_has_next) {
-                const double u3 = x3 - 1.0;
-                acc_t = fma(t3, t3, acc_t);
-                acc_u = fma(u3, u3, acc_u);
-            }
+            isum::add(acc_t, isum::sum4(isum::square(t0, acc_t.flags), isum::square(t1, acc_t.flags),
+                                        isum::square(t2, acc_t.flags), isum::square(t3, acc_t.flags)));
+            isum::add(acc_u, isum::sum4(isum::square(x0 - 1.0, acc_u.flags), isum::square(x1 - 1.0, acc_u.flags),
+                                        isum::square(x2v - 1.0, acc_u.flags),
+                                        last_has_next ? isum::square(x3 - 1.0, acc_u.flags)
+                                                      : isum::sq_term{0u, isum::kEmptyExp}));
         }
         a = na;
         b = nb;
     }
-    acc_t = group_sum<32>(acc_t, kFull);
-    acc_u = group_sum<32>(acc_u, kFull);
-    if (lane == 0 && f_out) *f_out = GRAD ? fma(100.0, acc_t, 0.25 * acc_u) : fma(100.0, acc_t, acc_u);
+    const double st = isum::value(group_isum<32>(acc_t, kFull));
+    const double su = isum::value(group_isum<32>(acc_u, kFull));
+    if (lane == 0 && f_out) *f_out = GRAD ? fma(100.0, st, 0.25 * su) : fma(100.0, st, su);
 }
 
 // ------------------------------------------------ ackley, griewank, schwefel
