@@ -731,31 +731,114 @@ __device__ __forceinline__ double lj_rcp(double d)
     return (__double_as_longlong(y) << 1) == 0 ? y : r;
 }
 
-// 1/d and s = 1/d^3 without FP64 instructions: the FP32 approximate
-// reciprocal of m (d = m 2^k) as the seed, refined in integer fixed point and
-// cubed there (rcp_fixed.h: within 0.51 and 0.52 units of the last place).
-// The pair loops spent 21 FP64 instructions per pair (13 without the
-// gradient) on a pipe that retires two lanes per SM per clock; this moves the
-// reciprocal's three and the cube's two onto the integer pipes. Distances
-// outside 2^-100 .. 2^100, zero, infinities and NaN take lj_rcp and two FP64
+// Fixed-point 1/d and s = d^-3 for d = (u / 2^63) 2^k, 2^63 <= u < 2^64
+// (rcp_fixed.h): 1/d = z 2^(-64 - k), s = n3 2^(-64 - l3 - 3k) with
+// 2^63 <= n3 < 2^64. The seed is the FP32 approximate reciprocal of u's
+// leading bits.
+struct lj_fixed {
+    uint64_t z, n3;
+    int l3;
+};
+
+__device__ __forceinline__ lj_fixed lj_fixed_core(uint64_t u)
+{
+    float yf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(__uint_as_float(rcpfx::seed_input_bits_u(u))));
+    lj_fixed r;
+    r.z = rcpfx::rcp_q64_u(u, rcpfx::seed_q32(__float_as_uint(yf)));
+    const uint64_t z3 = rcpfx::mul_hi_u64(rcpfx::mul_hi_u64(r.z, r.z), r.z);
+    r.l3 = isum::clz64(z3);
+    r.n3 = z3 << r.l3;
+    return r;
+}
+
+// 1/d and s rounded to doubles (-100 <= k <= 100: both normal)
+__device__ __forceinline__ double lj_fixed_inv(const lj_fixed &r, int32_t k)
+{
+    return __longlong_as_double(
+        static_cast<long long>((static_cast<uint64_t>(1021 - k) << 52) + rcpfx::round_q64(r.z)));
+}
+
+__device__ __forceinline__ uint64_t lj_fixed_s_bits(const lj_fixed &r, int32_t k)
+{
+    return (static_cast<uint64_t>(1021 - 3 * k - r.l3) << 52) + rcpfx::round_q64(r.n3);
+}
+
+// The pair loops' 1/d and d^-3 for a double d (self-test): d = (u / 2^63) 2^k
+// with u from d's significand; outside 2^-100 .. 2^100, lj_rcp and two FP64
 // multiplies.
 __device__ __forceinline__ void lj_rcp_cube(double d, double &inv, double &s)
 {
     const uint64_t b = static_cast<uint64_t>(__double_as_longlong(d));
-    const unsigned hi = static_cast<unsigned>(b >> 32);
-    const unsigned ex = (hi >> 20) & 0x7ffu;
-    if (ex - (1023u - 100u) > 200u || (hi >> 31)) {
+    const int32_t k = static_cast<int32_t>((b >> 52) & 0x7ffu) - 1023;
+    if (k < -100 || k > 100 || (b >> 63)) {
         inv = lj_rcp(d);
         s = inv * inv * inv;
         return;
     }
-    const uint64_t f = b & ((1ull << 52) - 1u);
-    float yf;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(__uint_as_float(rcpfx::seed_input_bits(f))));
-    uint64_t ib, cb;
-    rcpfx::rcp_and_cube_bits(ex, f, rcpfx::seed_q32(__float_as_uint(yf)), &ib, &cb);
-    inv = __longlong_as_double(static_cast<long long>(ib));
-    s = __longlong_as_double(static_cast<long long>(cb));
+    const lj_fixed r = lj_fixed_core((1ull << 63) | (b << 11));
+    inv = lj_fixed_inv(r, k);
+    s = __longlong_as_double(static_cast<long long>(lj_fixed_s_bits(r, k)));
+}
+
+// One pair from its FP64 coordinate differences, with integer arithmetic
+// where it is exact or closer than FP64: d = dx^2 + dy^2 + dz^2 as the
+// aligned sum of the three squares (isum.h, within 2^-59 of the exact d), 1/d
+// and s = d^-3 in fixed point from that sum (rcp_fixed.h: Newton-Raphson
+// division seeded by the FP32 approximate reciprocal, then two 64 x 64-bit
+// products), and the energy as two integer sums E12 += s^2, E6 += s
+// (E = 4 (E12 - E6)). With the gradient, coef = (2 s^2 - s) / d, with 1/d and
+// s rounded to doubles: two FP64 instructions. The FP64 formulation spends 13
+// FP64 instructions per pair on the energy and 2 more on coef, on a pipe that
+// retires two lanes per SM per clock. Sums outside 2^-100 .. 2^100 and
+// infinite or NaN differences take the FP64 formulas (lj_rcp). A zero
+// distance sets *zero and gives coef = NaN (the reference's 1/0 in the
+// gradient).
+template <bool GRAD>
+__device__ __forceinline__ void lj_pair(double dx, double dy, double dz, isum::sq_acc &e12, isum::sq_acc &e6,
+                                        int &zero, double &coef)
+{
+    uint32_t fl = 0u;
+    const isum::sq_term d3 = isum::sum3(isum::square(dx, fl), isum::square(dy, fl), isum::square(dz, fl));
+    if (d3.p == 0u && fl == 0u) {
+        zero = 1;
+        if (GRAD) coef = __longlong_as_double(0x7ff8000000000000LL);
+        return;
+    }
+    const int lz = d3.p ? isum::clz64(d3.p) : 0;
+    const int32_t k = d3.q - lz + 63; // d = (u / 2^63) 2^k
+    if (fl != 0u || k < -100 || k > 100) {
+        const double d = fma(dx, dx, fma(dy, dy, dz * dz));
+        if (__double_as_longlong(d) == 0) {
+            zero = 1;
+            if (GRAD) coef = __longlong_as_double(0x7ff8000000000000LL);
+            return;
+        }
+        const double inv = lj_rcp(d);
+        const double s = inv * inv * inv;
+        isum::add_square(e12, s);
+        isum::add(e6, isum::magnitude(s, e6.flags));
+        if (GRAD) coef = fma(s + s, s, -s) * inv;
+        return;
+    }
+    const lj_fixed r = lj_fixed_core(d3.p << lz);
+    isum::add(e6, isum::sq_term{r.n3 >> 2, -62 - r.l3 - 3 * k});                                 // s
+    isum::add(e12, isum::sq_term{rcpfx::mul_hi_u64(r.n3, r.n3) >> 2, -62 - 2 * r.l3 - 6 * k}); // s^2
+    if (GRAD) {
+        const uint64_t sb = lj_fixed_s_bits(r, k);
+        const double sv = __longlong_as_double(static_cast<long long>(sb));
+        const double s2 = __longlong_as_double(static_cast<long long>(sb + (1ull << 52))); // 2s: s is normal here
+        coef = fma(s2, sv, -sv) * lj_fixed_inv(r, k);
+    }
+}
+
+// 4 (E12 - E6) over the warp, or +inf after a zero distance (NaN stays NaN).
+__device__ __forceinline__ double lj_energy(isum::sq_acc e12, isum::sq_acc e6, int zero)
+{
+    const double a = isum::value(group_isum<32>(e12, kFull));
+    const double b = isum::value(group_isum<32>(e6, kFull));
+    const double e = a - b;
+    return __any_sync(kFull, zero) ? (isnan(e) ? e : HUGE_VAL) : 4.0 * e;
 }
 
 __device__ __forceinline__ void lj_decode(const double *__restrict__ xr, uint32_t na, double *px, double *py,
@@ -796,8 +879,8 @@ __device__ __forceinline__ void lj_store_gradient(uint32_t nx, const double *gx,
 // Register variant (N <= 32*MA): lane l owns atoms l, l+32, ..., whose
 // positions and force sums stay in registers; only the reaction on the
 // partner atom goes through shared memory. Per pair, fitness + gradient:
-// 21 FP64 instructions (3 differences, r^2, reciprocal, r^-6, s^2-s, the
-// energy sum, the force coefficient, 3 own and 3 reaction FMAs); fitness only: 13.
+// 11 FP64 instructions (3 differences, the force coefficient, 3 own and 3
+// reaction FMAs; lj_pair does the rest on the integer pipes); fitness only: 3.
 template <int MA, bool GRAD>
 __device__ __forceinline__ void lj_cluster_reg(const double *__restrict__ xr, uint32_t na, uint32_t nx, double *sm,
                                                double *f_out, double *__restrict__ gr)
@@ -815,7 +898,7 @@ __device__ __forceinline__ void lj_cluster_reg(const double *__restrict__ xr, ui
         oz[m] = i < na ? pz[i] : 0.0;
         fx[m] = fy[m] = fz[m] = 0.0;
     }
-    double e = 0.0;
+    isum::sq_acc e12 = isum::make(), e6 = isum::make();
     int zero = 0;
     const bool even = (na & 1u) == 0u;
     const uint32_t kmax = na / 2u;
@@ -828,16 +911,9 @@ __device__ __forceinline__ void lj_cluster_reg(const double *__restrict__ xr, ui
                 uint32_t j = i + k;
                 if (j >= na) j -= na;
                 const double dx = ox[m] - px[j], dy = oy[m] - py[j], dz = oz[m] - pz[j];
-                const double d = fma(dx, dx, fma(dy, dy, dz * dz));
-                double inv, s;
-                lj_rcp_cube(d, inv, s);
-                const double term = fma(s, s, -s);
-                if (__double_as_longlong(d) != 0)
-                    e += term;
-                else
-                    zero = 1;
+                double coef = 0.0; // (2 s^2 - s) / r^2
+                lj_pair<GRAD>(dx, dy, dz, e12, e6, zero, coef);
                 if (GRAD) {
-                    const double coef = fma(s, s, term) * inv; // (2 s^2 - s) / r^2
                     fx[m] = fma(coef, dx, fx[m]);
                     fy[m] = fma(coef, dy, fy[m]);
                     fz[m] = fma(coef, dz, fz[m]);
@@ -850,10 +926,8 @@ __device__ __forceinline__ void lj_cluster_reg(const double *__restrict__ xr, ui
         // the partners of one step are distinct; the next step may revisit them
         if (GRAD) __syncwarp();
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(kFull, e, o);
-    zero = __any_sync(kFull, zero);
-    if (lane == 0 && f_out) *f_out = zero ? (isnan(e) ? e : HUGE_VAL) : 4.0 * e;
+    const double energy = lj_energy(e12, e6, zero);
+    if (lane == 0 && f_out) *f_out = energy;
     if (GRAD) {
 #pragma unroll
         for (int m = 0; m < MA; ++m) {
@@ -887,7 +961,7 @@ __device__ __forceinline__ void lj_cluster_flat(const double *__restrict__ xr, u
     const bool even = (na & 1u) == 0u;
     const uint32_t kmax = na / 2u;
     const uint32_t pairs = na * (na - 1u) / 2u;
-    double e = 0.0;
+    isum::sq_acc e12 = isum::make(), e6 = isum::make();
     int zero = 0;
     uint32_t k = 1u, i = lane; // pair number q0 + lane, q0 = 0
     for (uint32_t q0 = 0; q0 < pairs; q0 += 32u) {
@@ -899,15 +973,7 @@ __device__ __forceinline__ void lj_cluster_flat(const double *__restrict__ xr, u
             dx = px[i] - px[j];
             dy = py[i] - py[j];
             dz = pz[i] - pz[j];
-            const double d = fma(dx, dx, fma(dy, dy, dz * dz));
-            double inv, s;
-            lj_rcp_cube(d, inv, s);
-            const double term = fma(s, s, -s);
-            if (__double_as_longlong(d) != 0)
-                e += term;
-            else
-                zero = 1;
-            if (GRAD) coef = fma(s, s, term) * inv;
+            lj_pair<GRAD>(dx, dy, dz, e12, e6, zero, coef);
         }
         if (GRAD) {
             if (act) {
@@ -932,10 +998,8 @@ __device__ __forceinline__ void lj_cluster_flat(const double *__restrict__ xr, u
             ++k;
         }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(kFull, e, o);
-    zero = __any_sync(kFull, zero);
-    if (lane == 0 && f_out) *f_out = zero ? (isnan(e) ? e : HUGE_VAL) : 4.0 * e;
+    const double energy = lj_energy(e12, e6, zero);
+    if (lane == 0 && f_out) *f_out = energy;
     if (GRAD) {
         __syncwarp();
         lj_store_gradient(nx, gx, gy, gz, gr);
@@ -954,7 +1018,7 @@ __device__ __forceinline__ void lj_cluster_smem(const double *__restrict__ xr, u
     double *px = sm, *py = px + na, *pz = py + na;
     double *gx = pz + na, *gy = gx + na, *gz = gy + na;
     lj_decode(xr, na, px, py, pz, gx, gy, gz, GRAD);
-    double e = 0.0;
+    isum::sq_acc e12 = isum::make(), e6 = isum::make();
     int zero = 0;
     const bool even = (na & 1u) == 0u;
     const uint32_t kmax = na / 2u;
@@ -970,15 +1034,7 @@ __device__ __forceinline__ void lj_cluster_smem(const double *__restrict__ xr, u
                 dx = px[i] - px[j];
                 dy = py[i] - py[j];
                 dz = pz[i] - pz[j];
-                const double d = fma(dx, dx, fma(dy, dy, dz * dz));
-                double inv, s;
-                lj_rcp_cube(d, inv, s);
-                const double term = fma(s, s, -s);
-                if (__double_as_longlong(d) != 0)
-                    e += term;
-                else
-                    zero = 1;
-                if (GRAD) coef = fma(s, s, term) * inv;
+                lj_pair<GRAD>(dx, dy, dz, e12, e6, zero, coef);
             }
             if (GRAD) {
                 if (act) {
@@ -996,10 +1052,8 @@ __device__ __forceinline__ void lj_cluster_smem(const double *__restrict__ xr, u
             }
         }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(kFull, e, o);
-    zero = __any_sync(kFull, zero);
-    if (lane == 0 && f_out) *f_out = zero ? (isnan(e) ? e : HUGE_VAL) : 4.0 * e;
+    const double energy = lj_energy(e12, e6, zero);
+    if (lane == 0 && f_out) *f_out = energy;
     if (GRAD) {
         __syncwarp();
         lj_store_gradient(nx, gx, gy, gz, gr);

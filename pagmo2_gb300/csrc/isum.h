@@ -97,6 +97,30 @@ PGX_ISUM_HD sq_term square(double v, uint32_t &flags)
     return sq_term{p, 2 * static_cast<int32_t>(ex) - 2106};
 }
 
+// |v| = p 2^q (2^61 <= p < 2^62 for normal v, exact), for sums of
+// non-negative values; zero gives p = 0, infinity and NaN set the flags.
+PGX_ISUM_HD sq_term magnitude(double v, uint32_t &flags)
+{
+    const uint64_t b = bits_of(v);
+    const uint32_t ex = static_cast<uint32_t>(b >> 52) & 0x7ffu;
+    if (ex == 0x7ffu) {
+        flags |= (b << 12) != 0u ? 2u : 1u;
+        return sq_term{0u, kEmptyExp};
+    }
+    const uint64_t f = b & ((1ull << 52) - 1u);
+    if (ex == 0u) return sq_term{f << 9, -1083}; // subnormal (or zero): f 2^-1074
+    return sq_term{(f | (1ull << 52)) << 9, static_cast<int32_t>(ex) - 1084};
+}
+
+// a + b + c (each p < 2^62) aligned to the largest exponent, each truncated by
+// less than one unit: the result's p may reach 3 2^62 (below 2^64)
+PGX_ISUM_HD sq_term sum3(sq_term a, sq_term b, sq_term c)
+{
+    const int32_t qm = imax(imax(a.q, b.q), c.q);
+    const uint64_t s = (a.p >> imin(qm - a.q, 63)) + (b.p >> imin(qm - b.q, 63)) + (c.p >> imin(qm - c.q, 63));
+    return sq_term{s, qm};
+}
+
 // a + b + c + d aligned to the largest exponent (each truncated by less than
 // one unit), then brought below 2^62 (two more bits at most)
 PGX_ISUM_HD sq_term sum4(sq_term a, sq_term b, sq_term c, sq_term d)

@@ -81,17 +81,18 @@ PGX_RCP_HD uint32_t seed_q32(uint32_t y0_bits)
     return ((y0_bits & 0x7fffffu) | 0x800000u) << 8;
 }
 
-// The float whose value is m truncated to 23 fraction bits (the seed's input).
+// The float whose value is m = 1 + f52 2^-52 truncated to 23 fraction bits
+// (the seed's input).
 PGX_RCP_HD uint32_t seed_input_bits(uint64_t f52)
 {
     return 0x3f800000u | static_cast<uint32_t>(f52 >> 29);
 }
 
-// 1/m in Q64, 2^63 <= z < 2^64 (1/2 <= 1/m < 1 up to the error above; m = 1
-// gives 2^64 - 1). f52: m's fraction; y0q: the seed in Q32.
-PGX_RCP_HD uint64_t rcp_q64(uint64_t f52, uint32_t y0q)
+// 1/m in Q64 for m = u / 2^63, any 64-bit significand 2^63 <= u < 2^64:
+// 2^63 <= z < 2^64 (1/2 <= 1/m < 1 up to the error above; m = 1 gives
+// 2^64 - 1). y0q: the seed in Q32.
+PGX_RCP_HD uint64_t rcp_q64_u(uint64_t u, uint32_t y0q)
 {
-    const uint64_t u = (1ull << 63) | (f52 << 11);
     const uint64_t pl = static_cast<uint64_t>(static_cast<uint32_t>(u)) * y0q;
     const uint64_t ph = static_cast<uint64_t>(static_cast<uint32_t>(u >> 32)) * y0q + (pl >> 32);
     // D = 2^95 - u Y0 = T 2^32 - (pl mod 2^32); e = D / 2^95, ef = D / 2^12 = e 2^83
@@ -101,6 +102,18 @@ PGX_RCP_HD uint64_t rcp_q64(uint64_t f52, uint32_t y0q)
     const int64_t c = ef + ((eh * eh) >> 21);   // (e + e^2) 2^83
     const int64_t corr = mul_hi_s64(static_cast<int64_t>(static_cast<uint64_t>(y0q) << 31), c) >> 18; // y0 c 2^64
     return (static_cast<uint64_t>(y0q) << 32) + static_cast<uint64_t>(corr);
+}
+
+// The float whose value is u / 2^63 truncated to 23 fraction bits.
+PGX_RCP_HD uint32_t seed_input_bits_u(uint64_t u)
+{
+    return 0x3f800000u | (static_cast<uint32_t>(u >> 40) & 0x7fffffu);
+}
+
+// 1/m in Q64 for a double's significand m = 1 + f52 2^-52.
+PGX_RCP_HD uint64_t rcp_q64(uint64_t f52, uint32_t y0q)
+{
+    return rcp_q64_u((1ull << 63) | (f52 << 11), y0q);
 }
 
 // z in [2^63, 2^64) rounded to a 53-bit mantissa (implicit bit included):
