@@ -16,6 +16,7 @@
 
 #include "isum.h"
 #include "rcp_fixed.h"
+#include "trig_fixed.h"
 
 namespace pgx
 {
@@ -152,19 +153,45 @@ __device__ __forceinline__ double cos_2pi(double x, int &neg)
 // f = sum_i (x_i^2 - 10 cos(2 pi x_i)) + 10 n  (src/problems/rastrigin.cpp:62-72),
 // accumulated as sum x^2 and sum cos apart; g_i = 2 x_i + 10 omega sin(2 pi x_i)
 // (:98-107). One group of G lanes per row, lanes strided over coordinates.
-// FP64 instructions per element: fitness + gradient 21, fitness only 14.
+// For 2^-60 <= |x| < 2^40 (the usual case) sin and cos come from the integer
+// fixed-point routines of trig_fixed.h, sum x^2 is an exact integer sum
+// (isum.h) and 2x an exponent increment, so the FP64 instructions per element
+// are the cos sum and, with the gradient, its FMA: 2 with the gradient, 1
+// without (21 and 14 with FP64 polynomials). Other x take the FP64
+// polynomials (|x| < 2^-60) or CUDA's sincospi/cospi.
+
+// 2x exactly for zero or a normal x whose double 2x is finite
+__device__ __forceinline__ double twice_exact(double x)
+{
+    const long long b = __double_as_longlong(x);
+    return (b << 1) == 0 ? x : __longlong_as_double(b + (1LL << 52));
+}
+
 template <int G, bool GRAD>
 __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uint32_t nx, double *f_out,
                                               double *__restrict__ gr)
 {
     const unsigned sub = threadIdx.x & (G - 1);
     const unsigned mask = group_mask<G>();
-    double sx = 0.0, sc = 0.0;
+    isum::sq_acc sx = isum::make();
+    double sc = 0.0;
     // the next element's load is issued before this one's arithmetic
     double xn = sub < nx ? __ldg(xr + sub) : 0.0;
     for (uint32_t i = sub; i < nx; i += G) {
         const double xi = xn;
         if (i + G < nx) xn = __ldg(xr + i + G);
+        isum::add_square(sx, xi);
+        if (trigfx::in_range(xi)) {
+            if (GRAD) {
+                double s, c;
+                trigfx::sincos_2pi(xi, s, c);
+                sc += c;
+                gr[i] = fma(k10Omega, s, twice_exact(xi));
+            } else {
+                sc += trigfx::cos_2pi(xi);
+            }
+            continue;
+        }
         double s = 0.0, c;
         int s_neg = 0, c_neg = 0;
         if (fast_trig_arg(xi)) {
@@ -178,13 +205,12 @@ __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uin
             else
                 c = cospi(xi + xi);
         }
-        sx = fma(xi, xi, sx);
         sc = fma(c, unit_sign(c_neg), sc);
         if (GRAD) gr[i] = fma(signed_const(k10Omega, s_neg), s, xi + xi);
     }
-    sx = group_sum<G>(sx, mask);
+    const double sxv = isum::value(group_isum<G>(sx, mask));
     sc = group_sum<G>(sc, mask);
-    if (sub == 0 && f_out) *f_out = fma(-10.0, sc, sx) + 10.0 * static_cast<double>(nx);
+    if (sub == 0 && f_out) *f_out = fma(-10.0, sc, sxv) + 10.0 * static_cast<double>(nx);
 }
 
 // ----------------------------------------------------------------- rosenbrock
@@ -377,17 +403,22 @@ __device__ __forceinline__ void ackley_row(const double *__restrict__ xr, uint32
 {
     const unsigned sub = threadIdx.x & (G - 1);
     const unsigned mask = group_mask<G>();
-    double s1 = 0.0, s2 = 0.0;
+    isum::sq_acc sq = isum::make();
+    double s2 = 0.0;
     double xn = sub < nx ? __ldg(xr + sub) : 0.0;
     for (uint32_t i = sub; i < nx; i += G) {
         const double xi = xn;
         if (i + G < nx) xn = __ldg(xr + i + G);
-        int c_neg = 0;
-        const double c = fast_trig_arg(xi) ? cos_2pi(xi, c_neg) : cospi(xi + xi);
-        s1 = fma(xi, xi, s1);
-        s2 = fma(c, unit_sign(c_neg), s2);
+        isum::add_square(sq, xi);
+        if (trigfx::in_range(xi)) {
+            s2 += trigfx::cos_2pi(xi);
+        } else {
+            int c_neg = 0;
+            const double c = fast_trig_arg(xi) ? cos_2pi(xi, c_neg) : cospi(xi + xi);
+            s2 = fma(c, unit_sign(c_neg), s2);
+        }
     }
-    s1 = group_sum<G>(s1, mask);
+    const double s1 = isum::value(group_isum<G>(sq, mask));
     s2 = group_sum<G>(s2, mask);
     if (sub == 0 && f_out) {
         const double inv_n = 1.0 / static_cast<double>(nx);
