@@ -8,10 +8,11 @@
 //    y_n = r_y (hv2d's own sweep, summed as a tree).
 //  - 3D: with the points sorted by z, level i holds the 2D area A_i of the
 //    points up to level i, and HV = sum_i (z_{i+1} - z_i) A_i with z_n = r_z.
-//    Every level is an independent warp: over the points in y order, the
-//    running maximum of (r_x - x) among the points whose z rank is at most i,
-//    summed run by run between the points that widen it. O(n^2) integer work,
-//    FP64 only at those points, all levels in parallel.
+//    Every level is an independent thread: over the points in y order
+//    (staged through shared memory for a block of levels), the running
+//    maximum of (r_x - x) among the points whose z rank is at most i, summed
+//    run by run between the points that widen it. O(n^2) integer work, FP64
+//    only at those points, all levels in parallel.
 // Order: both sorts are counting ranks over the NaN-aware int64 order keys
 // (ties by index); a tie does not change any slab (its step is zero). The
 // widths r_x - x are non-negative on valid input, so their running maximum
@@ -81,12 +82,12 @@ __global__ void hv_rank_kernel(const long long *__restrict__ kyz, uint32_t n, in
     }
 }
 
-// points into y order: ys, the widths r_x - x (as bits), and for 3D the z
-// rank of each y position and the z values in z order; the ranks are the
+// points into y order: ys and the widths r_x - x (as bits; for 3D beside the
+// z rank of each y position, and the z values in z order); the ranks are the
 // sums of the nq slice counts
 __global__ void hv_scatter_kernel(const double *__restrict__ pts, uint32_t n, uint32_t m, double rx,
                                   const int32_t *__restrict__ part, uint32_t nq, double *__restrict__ ys,
-                                  long long *__restrict__ wbits, int32_t *__restrict__ zr, double *__restrict__ zs)
+                                  long long *__restrict__ wbits, longlong2 *__restrict__ wz, double *__restrict__ zs)
 {
     const uint64_t stride = static_cast<uint64_t>(m - 1u) * n;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
@@ -97,10 +98,12 @@ __global__ void hv_scatter_kernel(const double *__restrict__ pts, uint32_t n, ui
             if (m == 3u) rz += part[q * stride + n + t];
         }
         ys[ry] = p[1];
-        wbits[ry] = __double_as_longlong(rx - p[0]);
+        const long long w = __double_as_longlong(rx - p[0]);
         if (m == 3u) {
-            zr[ry] = rz;
+            wz[ry] = make_longlong2(w, rz);
             zs[rz] = p[2];
+        } else {
+            wbits[ry] = w;
         }
     }
 }
@@ -116,58 +119,130 @@ __device__ __forceinline__ long long warp_incl_max(long long v)
     return v;
 }
 
-// One warp per level i (3D) or a single level with every point (2D, zr null):
-// A = sum_t (y_{t+1} - y_t) * max_{t' <= t, zr[t'] <= i} w[t']; term[i] =
-// (z_{i+1} - z_i) * A (3D) or A (2D). The running maximum W changes only at
-// "records" (a point widening the staircase), so A is summed run by run,
-// W_run * (y at the next record - y at this record), the last run ending at
-// r_y: two FP64 operations per record instead of two per point.
-__global__ void hv_levels_kernel(const double *__restrict__ ys, const long long *__restrict__ wbits,
-                                 const int32_t *__restrict__ zr, const double *__restrict__ zs, uint32_t n, double ry,
-                                 double rz, uint32_t levels, double *__restrict__ term)
+// 2D, one warp: A = sum_t (y_{t+1} - y_t) * max_{t' <= t} w[t'] over the points
+// in y order (y_n = r_y). The running maximum W changes only at "records" (a
+// point widening the staircase), so A is summed run by run, W_run * (y at the
+// next record - y at this record), the last run ending at r_y: two FP64
+// operations per record instead of two per point.
+__global__ void hv_area2_kernel(const double *__restrict__ ys, const long long *__restrict__ wbits, uint32_t n,
+                                double ry, double *__restrict__ out)
 {
     const unsigned lane = threadIdx.x & 31u;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < levels; i += nw) {
-        double dz = 1.0;
-        if (zr) {
-            dz = (i + 1u < n ? zs[i + 1u] : rz) - zs[i];
-            if (dz == 0.0) { // a level of no thickness adds nothing
-                if (lane == 0) term[i] = 0.0;
-                continue;
-            }
+    long long carry = 0;               // bits of the running maximum so far (+0.0: no point yet)
+    double pend_w = 0.0, pend_y = 0.0; // the open run: its width and where it starts
+    double a = 0.0;
+    for (uint32_t t0 = 0; t0 < n; t0 += 32u) {
+        const uint32_t t = t0 + lane;
+        const bool valid = t < n;
+        long long v = valid ? wbits[t] : 0;
+        v = warp_incl_max(v);
+        if (carry > v) v = carry;
+        long long prev = __shfl_up_sync(kFull, v, 1);
+        if (lane == 0) prev = carry;
+        const bool rec = valid && v != prev;
+        const uint32_t b = __ballot_sync(kFull, rec);
+        if (b) {
+            const double y = rec ? ys[t] : 0.0;
+            const double w = __longlong_as_double(v);
+            const uint32_t nb = b & ~((2u << lane) - 1u); // records after this lane
+            const double ynx = __shfl_sync(kFull, y, nb ? __ffs(nb) - 1 : static_cast<int>(lane));
+            if (rec && nb) a = fma(w, ynx - y, a);
+            if (static_cast<int>(lane) == __ffs(b) - 1 && pend_w > 0.0) a = fma(pend_w, y - pend_y, a);
+            const int last = 31 - __clz(b);
+            pend_w = __shfl_sync(kFull, w, last);
+            pend_y = __shfl_sync(kFull, y, last);
         }
-        long long carry = 0;                // bits of the running maximum so far (+0.0: no point yet)
-        double pend_w = 0.0, pend_y = 0.0;  // the open run: its width and where it starts
-        double a = 0.0;
-        for (uint32_t t0 = 0; t0 < n; t0 += 32u) {
-            const uint32_t t = t0 + lane;
-            const bool valid = t < n;
-            long long v = 0;
-            if (valid && (!zr || static_cast<uint32_t>(zr[t]) <= i)) v = wbits[t];
-            v = warp_incl_max(v);
-            if (carry > v) v = carry;
-            long long prev = __shfl_up_sync(kFull, v, 1);
-            if (lane == 0) prev = carry;
-            const bool rec = valid && v != prev;
-            const uint32_t b = __ballot_sync(kFull, rec);
-            if (b) {
-                const double y = rec ? ys[t] : 0.0;
-                const double w = __longlong_as_double(v);
-                const uint32_t nb = b & ~((2u << lane) - 1u); // records after this lane
-                const double ynx = __shfl_sync(kFull, y, nb ? __ffs(nb) - 1 : static_cast<int>(lane));
-                if (rec && nb) a = fma(w, ynx - y, a);
-                if (static_cast<int>(lane) == __ffs(b) - 1 && pend_w > 0.0) a = fma(pend_w, y - pend_y, a);
-                const int last = 31 - __clz(b);
-                pend_w = __shfl_sync(kFull, w, last);
-                pend_y = __shfl_sync(kFull, y, last);
-            }
-            carry = __shfl_sync(kFull, v, 31);
-        }
-        if (lane == 0 && pend_w > 0.0) a = fma(pend_w, ry - pend_y, a);
+        carry = __shfl_sync(kFull, v, 31);
+    }
+    if (lane == 0 && pend_w > 0.0) a = fma(pend_w, ry - pend_y, a);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
-        if (lane == 0) term[i] = zr ? dz * a : a;
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
+    if (lane == 0) *out = a;
+}
+
+// 3D: one thread per level i (the points of z rank <= i), the points in y
+// order staged through shared memory for the whole block (asynchronous
+// copies, two tiles in flight): the same run-by-run sum as the 2D kernel,
+// with a warp covering 32 levels per point (a record, a point widening the
+// staircase, costs one FMA on its own lane).
+constexpr int kLevelThreads = 64;
+constexpr uint32_t kLevelTile = 1024;
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
+                 "l"(gmem));
+}
+
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
+                 "l"(gmem));
+}
+
+__global__ void __launch_bounds__(kLevelThreads)
+    hv_levels3_kernel(const double *__restrict__ ys, const longlong2 *__restrict__ wz, const double *__restrict__ zs,
+                      uint32_t n, double ry, double rz, double *__restrict__ term)
+{
+    __shared__ longlong2 s_wz[2][kLevelTile];
+    __shared__ double s_y[2][kLevelTile];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long lim = i < n ? static_cast<long long>(i) : -1; // z rank <= i
+    long long v = 0;                                              // running maximum (bits; +0.0: none)
+    double pend_w = 0.0, pend_y = 0.0, a = 0.0;
+    const uint32_t tiles = (n + kLevelTile - 1u) / kLevelTile;
+    auto stage = [&](uint32_t t, uint32_t buf) {
+        const uint32_t t0 = t * kLevelTile;
+        const uint32_t cnt = n - t0 < kLevelTile ? n - t0 : kLevelTile;
+        for (uint32_t j = threadIdx.x; j < cnt; j += blockDim.x) {
+            cp_async16(&s_wz[buf][j], wz + t0 + j);
+            cp_async8(&s_y[buf][j], ys + t0 + j);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    stage(0u, 0u);
+    for (uint32_t t = 0; t < tiles; ++t) {
+        const uint32_t buf = t & 1u;
+        if (t + 1u < tiles) {
+            stage(t + 1u, buf ^ 1u);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncthreads();
+        const uint32_t t0 = t * kLevelTile;
+        const uint32_t cnt = n - t0 < kLevelTile ? n - t0 : kLevelTile;
+        const longlong2 *w = s_wz[buf];
+        const double *yv = s_y[buf];
+        // four points per warp-uniform test; the records inside are rare
+        for (uint32_t j = 0; j < cnt; j += 4u) {
+            long long c[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t jq = j + q < cnt ? j + q : cnt - 1u;
+                const longlong2 e = w[jq];
+                c[q] = (j + q < cnt && e.y <= lim) ? e.x : 0;
+            }
+            const long long mx = max(max(c[0], c[1]), max(c[2], c[3]));
+            if (__any_sync(kFull, mx > v)) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (c[q] > v) {
+                        const double y = yv[j + q];
+                        if (pend_w > 0.0) a = fma(pend_w, y - pend_y, a);
+                        pend_w = __longlong_as_double(c[q]);
+                        pend_y = y;
+                        v = c[q];
+                    }
+                }
+            }
+        }
+        __syncthreads(); // the buffer is staged again two tiles on
+    }
+    if (i < n) {
+        if (pend_w > 0.0) a = fma(pend_w, ry - pend_y, a);
+        const double dz = (i + 1u < n ? zs[i + 1u] : rz) - zs[i];
+        term[i] = dz == 0.0 ? 0.0 : dz * a;
     }
 }
 
@@ -243,7 +318,7 @@ int launch_hypervolume(pgx_context *ctx, const double *d_pts, uint32_t n, uint32
         1, std::min<int64_t>(8, (4 * sms + g2 * static_cast<int>(nc) - 1) / (g2 * static_cast<int>(nc)))));
     const size_t b_keys = align256(static_cast<size_t>(n) * nc * 8u);
     const size_t b_rank = align256(static_cast<size_t>(n) * nc * nq * 4u);
-    const size_t b_d = align256(static_cast<size_t>(n) * 8u), b_i = align256(static_cast<size_t>(n) * 4u);
+    const size_t b_d = align256(static_cast<size_t>(n) * 8u), b_i = align256(static_cast<size_t>(n) * 16u);
     PGX_TRY(ctx->s_crowd.ensure(b_keys + b_rank + 4u * b_d + b_i + 256u));
     char *base = ctx->s_crowd.as<char>();
     long long *kyz = reinterpret_cast<long long *>(base);
@@ -252,23 +327,24 @@ int launch_hypervolume(pgx_context *ctx, const double *d_pts, uint32_t n, uint32
     long long *wbits = reinterpret_cast<long long *>(base + b_keys + b_rank + b_d);
     double *zs = reinterpret_cast<double *>(base + b_keys + b_rank + 2u * b_d);
     double *term = reinterpret_cast<double *>(base + b_keys + b_rank + 3u * b_d);
-    int32_t *zr = reinterpret_cast<int32_t *>(base + b_keys + b_rank + 4u * b_d);
+    longlong2 *wz = reinterpret_cast<longlong2 *>(base + b_keys + b_rank + 4u * b_d);
     hv_keys_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, kyz);
     PGX_CUDA(cudaGetLastError());
     hv_rank_kernel<<<dim3(g2, nc, nq), 256, 0, s>>>(kyz, n, part);
     PGX_CUDA(cudaGetLastError());
-    hv_scatter_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, r[0], part, nq, ys, wbits, m == 3u ? zr : nullptr,
+    hv_scatter_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, r[0], part, nq, ys, wbits, m == 3u ? wz : nullptr,
                                          m == 3u ? zs : nullptr);
     PGX_CUDA(cudaGetLastError());
-    const uint32_t levels = m == 3u ? n : 1u;
-    const int g3 = static_cast<int>(std::min<uint64_t>((static_cast<uint64_t>(levels) * 32u + 255u) / 256u,
-                                                       static_cast<uint64_t>(sms) * 8u));
-    hv_levels_kernel<<<g3, 256, 0, s>>>(ys, wbits, m == 3u ? zr : nullptr, m == 3u ? zs : nullptr, n, r[1],
-                                        m == 3u ? r[2] : 0.0, levels, term);
+    if (m == 3u) {
+        const int g3 = static_cast<int>((n + kLevelThreads - 1u) / kLevelThreads);
+        hv_levels3_kernel<<<g3, kLevelThreads, 0, s>>>(ys, wz, zs, n, r[1], r[2], term);
+        PGX_CUDA(cudaGetLastError());
+        hv_sum_kernel<<<1, 1024, 0, s>>>(term, n, d_out);
+    } else {
+        hv_area2_kernel<<<1, 32, 0, s>>>(ys, wbits, n, r[1], d_out);
+    }
     PGX_CUDA(cudaGetLastError());
-    hv_sum_kernel<<<1, 1024, 0, s>>>(term, levels, d_out);
-    PGX_CUDA(cudaGetLastError());
-    ctx->launches += 5;
+    ctx->launches += m == 3u ? 5 : 4;
     return PGX_OK;
 }
 

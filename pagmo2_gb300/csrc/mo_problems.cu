@@ -32,9 +32,11 @@ using dev::sincos_2pi;
 constexpr double kPi = 3.1415926535897932384626433832795028841971693993;
 constexpr double kPiHalf = kPi / 2.;
 
-// cos(2 pi t) with its sign applied.
+// cos(2 pi t) with its sign applied: the integer fixed-point routine for
+// 2^-60 <= |t| < 2^40 (trig_fixed.h), else the FP64 polynomial or cospi.
 __device__ __forceinline__ double cos_2pi_signed(double t)
 {
+    if (trigfx::in_range(t)) return trigfx::cos_2pi(t);
     if (!fast_trig_arg(t)) return cospi(t + t);
     int neg = 0;
     const double c = cos_2pi(t, neg);
