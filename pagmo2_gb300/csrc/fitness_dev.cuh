@@ -795,6 +795,27 @@ __device__ __forceinline__ uint64_t lj_fixed_s_bits(const lj_fixed &r, int32_t k
     return (static_cast<uint64_t>(1021 - 3 * k - r.l3) << 52) + rcpfx::round_q64(r.n3);
 }
 
+// The force coefficient (2 s^2 - s) / d = (2s - 1) s (1/d) in fixed point,
+// rounded to a double once. With s = n3 2^Es (Es = -64 - l3 - 3k), 2s - 1 is
+// formed exactly as W 2^Ec, Ec = max(Es + 3, -62) (the 1 drops below the last
+// unit only when 2s > 2^62), s (1/d) = pm 2^(-64 - l3 - 4k) with pm the high
+// half of n3 z, and the product's high half gives the result to within 2^-60
+// of max(2s, 1) s / d relative: as close as the FP64 fma(2s, s, -s) / d of
+// rounded s and 1/d, or closer.
+__device__ __forceinline__ double lj_fixed_coef(const lj_fixed &r, int32_t k)
+{
+    const int32_t es = -64 - r.l3 - 3 * k;
+    const int32_t ec = es + 3 > -62 ? es + 3 : -62;
+    const int sh = ec - es - 1 < 63 ? ec - es - 1 : 63;               // 2s = n3 2^(es+1) in units of 2^ec
+    const int64_t one = ec <= 0 ? (int64_t{1} << (-ec)) : 0;          // 1 in units of 2^ec
+    const int64_t w = static_cast<int64_t>(r.n3 >> sh) - one;         // (2s - 1) = w 2^ec
+    const uint64_t pm = rcpfx::mul_hi_u64(r.n3, r.z);                 // s (1/d) = pm 2^(-64 - l3 - 4k)
+    const int64_t q = rcpfx::mul_hi_s64(w, static_cast<int64_t>(pm >> 1)); // coef = q 2^(ec - l3 - 4k + 1)
+    if (q == 0) return 0.0;
+    const uint64_t mag = static_cast<uint64_t>(q < 0 ? -q : q);
+    return trigfx::to_double(mag, ec - r.l3 - 4 * k + 1, q < 0 ? 1u : 0u);
+}
+
 // The pair loops' 1/d and d^-3 for a double d (self-test): d = (u / 2^63) 2^k
 // with u from d's significand; outside 2^-100 .. 2^100, lj_rcp and two FP64
 // multiplies.
@@ -818,10 +839,10 @@ __device__ __forceinline__ void lj_rcp_cube(double d, double &inv, double &s)
 // and s = d^-3 in fixed point from that sum (rcp_fixed.h: Newton-Raphson
 // division seeded by the FP32 approximate reciprocal, then two 64 x 64-bit
 // products), and the energy as two integer sums E12 += s^2, E6 += s
-// (E = 4 (E12 - E6)). With the gradient, coef = (2 s^2 - s) / d, with 1/d and
-// s rounded to doubles: two FP64 instructions. The FP64 formulation spends 13
-// FP64 instructions per pair on the energy and 2 more on coef, on a pipe that
-// retires two lanes per SM per clock. Sums outside 2^-100 .. 2^100 and
+// (E = 4 (E12 - E6)). With the gradient, coef = (2 s^2 - s) / d in fixed point
+// as well (lj_fixed_coef). The FP64 formulation spends 13 FP64 instructions per
+// pair on the energy and 2 more on coef, on a pipe that retires two lanes per
+// SM per clock. Sums outside 2^-100 .. 2^100 and
 // infinite or NaN differences take the FP64 formulas (lj_rcp). A zero
 // distance sets *zero and gives coef = NaN (the reference's 1/0 in the
 // gradient).
@@ -855,12 +876,7 @@ __device__ __forceinline__ void lj_pair(double dx, double dy, double dz, isum::s
     const lj_fixed r = lj_fixed_core(d3.p << lz);
     isum::add(e6, isum::sq_term{r.n3 >> 2, -62 - r.l3 - 3 * k});                                 // s
     isum::add(e12, isum::sq_term{rcpfx::mul_hi_u64(r.n3, r.n3) >> 2, -62 - 2 * r.l3 - 6 * k}); // s^2
-    if (GRAD) {
-        const uint64_t sb = lj_fixed_s_bits(r, k);
-        const double sv = __longlong_as_double(static_cast<long long>(sb));
-        const double s2 = __longlong_as_double(static_cast<long long>(sb + (1ull << 52))); // 2s: s is normal here
-        coef = fma(s2, sv, -sv) * lj_fixed_inv(r, k);
-    }
+    if (GRAD) coef = lj_fixed_coef(r, k);
 }
 
 // 4 (E12 - E6) over the warp, or +inf after a zero distance (NaN stays NaN).
@@ -910,8 +926,8 @@ __device__ __forceinline__ void lj_store_gradient(uint32_t nx, const double *gx,
 // Register variant (N <= 32*MA): lane l owns atoms l, l+32, ..., whose
 // positions and force sums stay in registers; only the reaction on the
 // partner atom goes through shared memory. Per pair, fitness + gradient:
-// 11 FP64 instructions (3 differences, the force coefficient, 3 own and 3
-// reaction FMAs; lj_pair does the rest on the integer pipes); fitness only: 3.
+// 9 FP64 instructions (3 differences, 3 own and 3 reaction FMAs; lj_pair
+// does the rest on the integer pipes); fitness only: 3.
 template <int MA, bool GRAD>
 __device__ __forceinline__ void lj_cluster_reg(const double *__restrict__ xr, uint32_t na, uint32_t nx, double *sm,
                                                double *f_out, double *__restrict__ gr)
