@@ -258,6 +258,37 @@ def test_lj_reciprocal_on_device(ctx):
         assert abs(Fraction(float(cube[i])) - exact) <= (Fraction(1, 2) + Fraction(1, 32)) * ulp, float(d[i]).hex()
 
 
+def test_integer_paths_at_their_range_edges(ctx, orc):
+    """Inputs on both sides of the ranges the integer fixed-point paths take
+    (rastrigin/ackley trig for 2^-60 <= |x| < 2^40, the Lennard-Jones pair for
+    2^-100 <= r^2 < 2^101, the sums of squares over the whole double range),
+    against the long-double oracle: the fallbacks and the fixed-point code
+    agree with it alike."""
+    rs = np.random.RandomState(21)
+    # rastrigin / ackley: tiny, huge, exact multiples of 1/4 and 1/2 near 2^40, zeros
+    vals = np.array([1e-70, -3e-25, 1e-17, 2.0 ** -60, -(2.0 ** -61), 0.0, -0.0, 0.25, -0.75, 1.5,
+                     2.0 ** 40 - 0.5, -(2.0 ** 40) + 0.25, 2.0 ** 40, 1e13, -7.3e12, 123456.125])
+    x = rs.choice(vals, size=(64, 9))
+    x[:8] = rs.uniform(-5.12, 5.12, (8, 9))
+    check_against_oracle(orc, ctx, N.RASTRIGIN, 9, x)
+    check_against_oracle(orc, ctx, N.ACKLEY, 9, x, grad=False)
+    # rosenbrock: squares far above and below 1 (no overflow to inf)
+    x = rs.uniform(-5.0, 10.0, (32, 12))
+    x[::2, ::3] *= 1e60
+    x[1::2, 1::3] *= 1e-150
+    check_against_oracle(orc, ctx, N.ROSENBROCK, 12, x)
+    # lennard_jones, 6 atoms: clusters scaled so that some or all r^2 leave [2^-100, 2^101)
+    base = W.lj_lattice_batch(8, 6, seed=4)
+    rows = []
+    for scale in (1e-20, 1e-14, 1.0, 1e14, 1e16, 1e30):
+        rows.append(base * scale)
+    mixed = base.copy()
+    mixed[:, 3:6] *= 1e17  # atom 3 far out: its pairs on the slow path, the others not
+    rows.append(mixed)
+    x = np.concatenate(rows)
+    check_against_oracle(orc, ctx, N.LENNARD_JONES, 6, x)
+
+
 def test_nonfinite_inputs_propagate(ctx, orc):
     for kind, param in ((N.RASTRIGIN, 9), (N.ROSENBROCK, 9), (N.LENNARD_JONES, 5)):
         nx = N.problem_nx(kind, param)
