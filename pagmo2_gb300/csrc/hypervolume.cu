@@ -50,35 +50,73 @@ __global__ void hv_keys_kernel(const double *__restrict__ pts, uint32_t n, uint3
     }
 }
 
-// part[(q * nc + c) * n + t]: how many points of the q-th of gridDim.z
-// slices of the index range precede point t when sorted by coordinate c + 1
-// (ties by index); the slices add up to t's position. blockIdx.y = c, keys
-// staged through shared memory.
-__global__ void hv_rank_kernel(const long long *__restrict__ kyz, uint32_t n, int32_t *__restrict__ part)
+// Ranks by coordinate c + 1 (ties by index) in two steps. hv_runs_kernel:
+// block b sorts the (key, index) pairs of points [b R, (b + 1) R) (R =
+// kRun) by a bitonic network in shared memory, padding with (LLONG_MAX,
+// INT_MAX), which no point's pair exceeds, and writes the sorted run.
+// hv_rank_kernel: a point's rank is the number of pairs below its own, summed
+// over every run by binary search (pairs are distinct, so this is its
+// position). blockIdx.y = c.
+constexpr uint32_t kRun = 2048;
+
+struct key_idx {
+    long long k;
+    long long i;
+};
+
+__device__ __forceinline__ bool pair_less(const key_idx &a, const key_idx &b)
 {
-    __shared__ long long tile[1024];
-    const uint32_t c = blockIdx.y, q = blockIdx.z, nq = gridDim.z;
+    return a.k < b.k || (a.k == b.k && a.i < b.i);
+}
+
+__global__ void __launch_bounds__(1024) hv_runs_kernel(const long long *__restrict__ kyz, uint32_t n,
+                                                       key_idx *__restrict__ runs)
+{
+    __shared__ key_idx s[kRun];
+    const uint32_t c = blockIdx.y, nb = gridDim.x;
     const long long *k = kyz + static_cast<uint64_t>(c) * n;
-    const uint32_t jb = static_cast<uint32_t>(static_cast<uint64_t>(n) * q / nq);
-    const uint32_t je = static_cast<uint32_t>(static_cast<uint64_t>(n) * (q + 1u) / nq);
-    for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < n; b0 += gridDim.x * blockDim.x) {
-        const uint32_t t = b0 + threadIdx.x;
-        const bool act = t < n;
-        const long long kt = act ? k[t] : 0;
-        int r = 0;
-        for (uint32_t j0 = jb; j0 < je; j0 += 1024u) {
-            const uint32_t lim = je - j0 < 1024u ? je - j0 : 1024u;
-            __syncthreads();
-            for (uint32_t j = threadIdx.x; j < lim; j += blockDim.x) tile[j] = k[j0 + j];
-            __syncthreads();
-            if (act) {
-                for (uint32_t j = 0; j < lim; ++j) {
-                    const long long kj = tile[j];
-                    r += (kj < kt) | ((kj == kt) & (j0 + j < t));
+    const uint32_t t0 = blockIdx.x * kRun;
+    for (uint32_t j = threadIdx.x; j < kRun; j += blockDim.x) {
+        const uint32_t t = t0 + j;
+        s[j] = t < n ? key_idx{k[t], static_cast<long long>(t)} : key_idx{LLONG_MAX, INT_MAX};
+    }
+    __syncthreads();
+    for (uint32_t size = 2; size <= kRun; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t j = threadIdx.x; j < kRun / 2u; j += blockDim.x) {
+                const uint32_t lo = 2u * stride * (j / stride) + (j % stride), hi = lo + stride;
+                const bool up = (lo & size) == 0u;
+                const key_idx a = s[lo], b = s[hi];
+                if (pair_less(b, a) == up) {
+                    s[lo] = b;
+                    s[hi] = a;
                 }
             }
+            __syncthreads();
         }
-        if (act) part[(static_cast<uint64_t>(q) * gridDim.y + c) * n + t] = r;
+    }
+    key_idx *out = runs + (static_cast<uint64_t>(c) * nb + blockIdx.x) * kRun;
+    for (uint32_t j = threadIdx.x; j < kRun; j += blockDim.x) out[j] = s[j];
+}
+
+__global__ void hv_rank_kernel(const long long *__restrict__ kyz, uint32_t n, const key_idx *__restrict__ runs,
+                               uint32_t nb, int32_t *__restrict__ rank)
+{
+    const uint32_t c = blockIdx.y;
+    const long long *k = kyz + static_cast<uint64_t>(c) * n;
+    const key_idx *rc = runs + static_cast<uint64_t>(c) * nb * kRun;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const key_idx x{k[t], static_cast<long long>(t)};
+        uint32_t r = 0;
+        for (uint32_t b = 0; b < nb; ++b) {
+            const key_idx *run = rc + static_cast<uint64_t>(b) * kRun;
+            uint32_t pos = 0;
+#pragma unroll
+            for (uint32_t step = kRun / 2u; step > 0; step >>= 1)
+                if (pair_less(run[pos + step - 1u], x)) pos += step;
+            r += pos + (pair_less(run[pos], x) ? 1u : 0u) * (pos == kRun - 1u ? 1u : 0u);
+        }
+        rank[static_cast<uint64_t>(c) * n + t] = static_cast<int32_t>(r);
     }
 }
 
@@ -312,17 +350,18 @@ int launch_hypervolume(pgx_context *ctx, const double *d_pts, uint32_t n, uint32
     const uint32_t nc = m - 1u;
     const int sms = ctx->num_sms;
     const int g1 = static_cast<int>(std::min<uint64_t>((n + 255u) / 256u, static_cast<uint64_t>(sms) * 8u));
-    const int g2 = static_cast<int>(std::min<uint64_t>((n + 255u) / 256u, static_cast<uint64_t>(sms) * 4u));
-    // slices of the index range per rank count: about four blocks per SM in all
-    const uint32_t nq = static_cast<uint32_t>(std::max<int64_t>(
-        1, std::min<int64_t>(8, (4 * sms + g2 * static_cast<int>(nc) - 1) / (g2 * static_cast<int>(nc)))));
+    const uint32_t nb = (n + kRun - 1u) / kRun; // sorted runs per coordinate
+    const uint32_t nq = 1u;
     const size_t b_keys = align256(static_cast<size_t>(n) * nc * 8u);
-    const size_t b_rank = align256(static_cast<size_t>(n) * nc * nq * 4u);
+    const size_t b_rank = align256(static_cast<size_t>(n) * nc * 4u);
+    const size_t b_runs = align256(static_cast<size_t>(nb) * kRun * nc * sizeof(key_idx));
     const size_t b_d = align256(static_cast<size_t>(n) * 8u), b_i = align256(static_cast<size_t>(n) * 16u);
-    PGX_TRY(ctx->s_crowd.ensure(b_keys + b_rank + 4u * b_d + b_i + 256u));
+    PGX_TRY(ctx->s_crowd.ensure(b_keys + b_rank + b_runs + 4u * b_d + b_i + 256u));
     char *base = ctx->s_crowd.as<char>();
     long long *kyz = reinterpret_cast<long long *>(base);
     int32_t *part = reinterpret_cast<int32_t *>(base + b_keys);
+    key_idx *runs = reinterpret_cast<key_idx *>(base + b_keys + b_rank);
+    base += b_runs;
     double *ys = reinterpret_cast<double *>(base + b_keys + b_rank);
     long long *wbits = reinterpret_cast<long long *>(base + b_keys + b_rank + b_d);
     double *zs = reinterpret_cast<double *>(base + b_keys + b_rank + 2u * b_d);
@@ -330,7 +369,9 @@ int launch_hypervolume(pgx_context *ctx, const double *d_pts, uint32_t n, uint32
     longlong2 *wz = reinterpret_cast<longlong2 *>(base + b_keys + b_rank + 4u * b_d);
     hv_keys_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, kyz);
     PGX_CUDA(cudaGetLastError());
-    hv_rank_kernel<<<dim3(g2, nc, nq), 256, 0, s>>>(kyz, n, part);
+    hv_runs_kernel<<<dim3(nb, nc), 1024, 0, s>>>(kyz, n, runs);
+    PGX_CUDA(cudaGetLastError());
+    hv_rank_kernel<<<dim3(static_cast<unsigned>((n + 127u) / 128u), nc), 128, 0, s>>>(kyz, n, runs, nb, part);
     PGX_CUDA(cudaGetLastError());
     hv_scatter_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, r[0], part, nq, ys, wbits, m == 3u ? wz : nullptr,
                                          m == 3u ? zs : nullptr);
@@ -344,7 +385,7 @@ int launch_hypervolume(pgx_context *ctx, const double *d_pts, uint32_t n, uint32
         hv_area2_kernel<<<1, 32, 0, s>>>(ys, wbits, n, r[1], d_out);
     }
     PGX_CUDA(cudaGetLastError());
-    ctx->launches += m == 3u ? 5 : 4;
+    ctx->launches += m == 3u ? 6 : 5;
     return PGX_OK;
 }
 
