@@ -733,7 +733,9 @@ def run_archipelago(ctx, L, N, W, stream) -> dict:
             "e2e_speedup_pipelined_from_idle": ms_plain_e2e / ms_pipe_idle,
             "evals_per_s_fused_pipelined": rows / (ms_pipe * 1e-3),
             "plain": "one host-buffer batch call per island (pgx_batch_gradient from the islands' arrays), in order",
-            "fused": "all islands in one persistent kernel per epoch, CUDA graph over pinned staging (3 sets)"}
+            "fused": "all islands in one persistent kernel per epoch, one CUDA graph per set (3 sets); the kernel "
+                     "reads and writes the islands' arrays in place over NVLink-C2C where the device accesses "
+                     "pageable host memory (else pinned staging with packing and copies)"}
 
 
 if __name__ == "__main__":

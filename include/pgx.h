@@ -311,19 +311,28 @@ typedef struct pgx_request {
    once per (problem, dimension) and caches the choice. Host-to-device copy,
    one persistent fused kernel over all tiles and device-to-host copies are
    captured in CUDA graphs, one per pinned staging set (three sets, three
-   streams), so consecutive epochs overlap. Replaces the island-by-island
+   streams), so consecutive epochs overlap. On a device that accesses
+   pageable host memory coherently (cudaDevAttrPageableMemoryAccess, as GB300
+   with Grace over NVLink-C2C) a second graph per set lets the kernel read
+   the requests' dvs and write their fvs/grads in place, with no packing,
+   copies or unpacking; it is taken for every epoch whose arrays are 16-byte
+   aligned, unless PGX_EPOCH_STAGED=1. Replaces the island-by-island
    bfe calls of an archipelago epoch (src/archipelago.cpp:325-330 ->
    src/island.cpp:428-655 -> src/bfe.cpp:91-110). */
 PGX_API int pgx_epoch_create(pgx_context *ctx, const pgx_request *reqs, int n_reqs, pgx_epoch **out);
 
 /* One synchronous epoch: packs every request's dvs into the next staging
-   set, replays its graph, waits, unpacks fvs/grads. Shapes must match the
-   plan (PGX_ERR_INVALID otherwise). */
+   set, replays its graph, waits, unpacks fvs/grads (or evaluates the arrays
+   in place, see above). Shapes must match the plan (PGX_ERR_INVALID
+   otherwise). */
 PGX_API int pgx_epoch_run(pgx_epoch *ep, const pgx_request *reqs);
 
 /* Asynchronous pair over the staging sets: submit packs and launches
    one epoch and returns; collect waits for the oldest submitted epoch and
-   unpacks it into the pointers given at its submit. At most three in flight. */
+   unpacks it into the pointers given at its submit. At most three in flight.
+   Every array of a submitted request must stay allocated, and its dvs
+   unchanged, until the collect of that epoch returns: the kernel may read
+   and write them in place while the epoch runs. */
 PGX_API int pgx_epoch_submit(pgx_epoch *ep, const pgx_request *reqs);
 PGX_API int pgx_epoch_collect(pgx_epoch *ep);
 

@@ -1,6 +1,7 @@
 // Archipelago migration epochs: every island's batch request of one epoch is
 // evaluated by one persistent fused kernel, captured in a CUDA graph together
-// with its staging copies.
+// with its staging copies, or, where the device accesses pageable host memory
+// coherently (GB300 with Grace), reading and writing the islands' own arrays.
 //
 // In the reference, islands evolve asynchronously and each of their
 // algorithms calls bfe::operator() on its own (src/archipelago.cpp:325-330,
@@ -21,6 +22,7 @@
 #include <atomic>
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <fstream>
@@ -419,16 +421,26 @@ struct pgx_epoch {
     uint32_t sm_per_warp = 0;
     size_t smem = 0;
     struct set_t {
-        dbuf d_x, d_f, d_g, d_tiles, d_next;
-        hbuf h_x, h_f, h_g;
+        dbuf d_x, d_f, d_g, d_tiles, d_next, d_tiles_direct;
+        hbuf h_x, h_f, h_g, h_tiles_direct;
         cudaStream_t stream = nullptr;
-        cudaGraphExec_t graph = nullptr;
+        cudaGraphExec_t graph = nullptr;        // staged outputs: device buffers, then copies and unpacking
+        cudaGraphExec_t graph_direct = nullptr; // outputs stored by the kernel into the callers' arrays
         cudaEvent_t done = nullptr;
         std::vector<pgx_request> pending;
-        bool in_flight = false;
+        bool in_flight = false, direct = false;
     } sets[kSets];
     int next_set = 0;
     std::deque<int> fifo;
+    // Direct access: on a device that reads and writes pageable host memory
+    // through the host's page tables (Grace's NVLink-C2C), the kernel reads
+    // the callers' decision vectors and stores fitness and gradients straight
+    // into their arrays, so no packing, staging copies or unpacking are
+    // needed. PGX_EPOCH_STAGED=1 keeps the staged path.
+    bool direct_ok = false;
+    bool direct_inputs = false;
+    std::vector<tile_desc> tiles;                       // the staged tiles (inputs and shapes)
+    std::vector<std::pair<int, uint64_t>> tile_req_row; // request and first row of each tile
 };
 
 namespace pgx
@@ -468,6 +480,25 @@ int capture_set(pgx_epoch *ep, int si)
     const cudaError_t ie = cudaGraphInstantiate(&S.graph, graph, 0);
     cudaGraphDestroy(graph);
     if (ie != cudaSuccess) return cuda_status(ie, "cudaGraphInstantiate");
+    if (!ep->direct_ok) return PGX_OK;
+    // the direct variant: the tiles (with this epoch's output pointers) go up
+    // with the inputs, and nothing comes back by copy
+    PGX_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    if (ep->total_x && !ep->direct_inputs)
+        cudaMemcpyAsync(S.d_x.ptr, S.h_x.ptr, ep->total_x * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (ep->n_tiles)
+        cudaMemcpyAsync(S.d_tiles_direct.ptr, S.h_tiles_direct.ptr, ep->n_tiles * sizeof(tile_desc),
+                        cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(S.d_next.ptr, 0, sizeof(unsigned), s);
+    if (ep->n_tiles)
+        epoch_kernel<<<ep->grid, kWarpsPerBlock * 32, ep->smem, s>>>(S.d_tiles_direct.as<tile_desc>(), ep->n_tiles,
+                                                                     S.d_next.as<unsigned>(), ep->sm_per_warp);
+    graph = nullptr;
+    const cudaError_t ce2 = cudaStreamEndCapture(s, &graph);
+    if (ce2 != cudaSuccess) return cuda_status(ce2, "cudaStreamEndCapture");
+    const cudaError_t ie2 = cudaGraphInstantiate(&S.graph_direct, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie2 != cudaSuccess) return cuda_status(ie2, "cudaGraphInstantiate");
     return PGX_OK;
 }
 
@@ -544,6 +575,15 @@ int build_plan(pgx_epoch *ep, const pgx_request *reqs, int n_reqs)
     ep->n_tiles = static_cast<uint32_t>(tp.size());
     ep->grid = std::max(1, std::min(max_grid, static_cast<int>((tp.size() + kWarpsPerBlock - 1) / kWarpsPerBlock)));
 
+    {
+        int pageable = 0;
+        PGX_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, ctx->device));
+        const char *env = std::getenv("PGX_EPOCH_STAGED");
+        ep->direct_ok = pageable == 1 && !(env != nullptr && env[0] == '1');
+        ep->direct_inputs = ep->direct_ok;
+    }
+    ep->tile_req_row.resize(tp.size());
+    for (size_t t = 0; t < tp.size(); ++t) ep->tile_req_row[t] = {tp[t].req, tp[t].row0};
     for (int si = 0; si < kSets; ++si) {
         auto &S = ep->sets[si];
         PGX_CUDA(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
@@ -556,6 +596,10 @@ int build_plan(pgx_epoch *ep, const pgx_request *reqs, int n_reqs)
         PGX_TRY(S.h_x.ensure(std::max<uint64_t>(ep->total_x, 1) * sizeof(double)));
         PGX_TRY(S.h_f.ensure(std::max<uint64_t>(ep->total_f, 1) * sizeof(double)));
         PGX_TRY(S.h_g.ensure(std::max<uint64_t>(ep->total_g, 1) * sizeof(double)));
+        if (ep->direct_ok) {
+            PGX_TRY(S.d_tiles_direct.ensure(std::max<size_t>(tp.size(), 1) * sizeof(tile_desc)));
+            PGX_TRY(S.h_tiles_direct.ensure(std::max<size_t>(tp.size(), 1) * sizeof(tile_desc)));
+        }
         std::vector<tile_desc> td(tp.size());
         for (size_t t = 0; t < tp.size(); ++t) {
             const req_plan &p = ep->reqs[tp[t].req];
@@ -582,6 +626,7 @@ int build_plan(pgx_epoch *ep, const pgx_request *reqs, int n_reqs)
         }
         if (!td.empty())
             PGX_CUDA(cudaMemcpy(S.d_tiles.ptr, td.data(), td.size() * sizeof(tile_desc), cudaMemcpyHostToDevice));
+        if (si == 0) ep->tiles = td; // the shapes and row offsets are the same in every set
         PGX_TRY(capture_set(ep, si));
     }
     return PGX_OK;
@@ -593,14 +638,38 @@ int submit(pgx_epoch *ep, const pgx_request *reqs)
     const int si = ep->next_set;
     auto &S = ep->sets[si];
     PGX_CHECK(!S.in_flight, PGX_ERR_INVALID, "every staging set is in flight: collect an epoch first");
-    std::vector<copy_item> items;
-    for (size_t i = 0; i < ep->reqs.size(); ++i) {
-        const req_plan &p = ep->reqs[i];
-        if (p.n) items.push_back({S.h_x.as<double>() + p.off_x, reqs[i].dvs, p.n * p.nx * sizeof(double)});
+    // direct outputs when every output array can take the kernel's 16-byte
+    // stores (rows of the 4-wide variant): the tiles of this set point into
+    // them (a missing fitness array keeps the set's device buffer); direct
+    // inputs likewise need 16-byte aligned decision vectors
+    bool direct = ep->direct_ok;
+    for (size_t i = 0; direct && i < ep->reqs.size(); ++i)
+        direct = reinterpret_cast<uintptr_t>(reqs[i].fvs) % 16u == 0 && reinterpret_cast<uintptr_t>(reqs[i].grads) % 16u == 0
+                 && (!ep->direct_inputs || reinterpret_cast<uintptr_t>(reqs[i].dvs) % 16u == 0);
+    if (!(direct && ep->direct_inputs)) {
+        std::vector<copy_item> items;
+        for (size_t i = 0; i < ep->reqs.size(); ++i) {
+            const req_plan &p = ep->reqs[i];
+            if (p.n) items.push_back({S.h_x.as<double>() + p.off_x, reqs[i].dvs, p.n * p.nx * sizeof(double)});
+        }
+        parallel_copy(items);
     }
-    parallel_copy(items);
+    if (direct) {
+        tile_desc *ht = S.h_tiles_direct.as<tile_desc>();
+        for (size_t t = 0; t < ep->tiles.size(); ++t) {
+            const int ri = ep->tile_req_row[t].first;
+            const uint64_t row0 = ep->tile_req_row[t].second;
+            const req_plan &p = ep->reqs[ri];
+            tile_desc d = ep->tiles[t];
+            d.x = ep->direct_inputs ? reqs[ri].dvs + row0 * p.nx : S.d_x.as<double>() + p.off_x + row0 * p.nx;
+            d.f = reqs[ri].fvs ? reqs[ri].fvs + row0 : S.d_f.as<double>() + p.off_f + row0;
+            d.g = p.grad ? reqs[ri].grads + row0 * p.nx : nullptr;
+            ht[t] = d;
+        }
+    }
     PGX_TRY(use_device(ep->ctx));
-    PGX_CUDA(cudaGraphLaunch(S.graph, S.stream));
+    PGX_CUDA(cudaGraphLaunch(direct ? S.graph_direct : S.graph, S.stream));
+    S.direct = direct;
     PGX_CUDA(cudaEventRecord(S.done, S.stream));
     if (ep->n_tiles) ep->ctx->launches += 1;
     S.pending.assign(reqs, reqs + ep->reqs.size());
@@ -619,6 +688,7 @@ int collect(pgx_epoch *ep)
     ep->fifo.pop_front();
     S.in_flight = false;
     if (e != cudaSuccess) return cuda_status(e, "epoch");
+    if (S.direct) return PGX_OK; // the kernel stored the outputs in place
     std::vector<copy_item> items;
     for (size_t i = 0; i < ep->reqs.size(); ++i) {
         const req_plan &p = ep->reqs[i];
@@ -707,10 +777,11 @@ void pgx_epoch_destroy(pgx_epoch *ep)
     for (auto &S : ep->sets) {
         if (S.stream) cudaStreamSynchronize(S.stream);
         if (S.graph) cudaGraphExecDestroy(S.graph);
+        if (S.graph_direct) cudaGraphExecDestroy(S.graph_direct);
         if (S.done) cudaEventDestroy(S.done);
         if (S.stream) cudaStreamDestroy(S.stream);
-        for (pgx::dbuf *b : {&S.d_x, &S.d_f, &S.d_g, &S.d_tiles, &S.d_next}) b->release();
-        for (pgx::hbuf *b : {&S.h_x, &S.h_f, &S.h_g}) b->release();
+        for (pgx::dbuf *b : {&S.d_x, &S.d_f, &S.d_g, &S.d_tiles, &S.d_next, &S.d_tiles_direct}) b->release();
+        for (pgx::hbuf *b : {&S.h_x, &S.h_f, &S.h_g, &S.h_tiles_direct}) b->release();
     }
     delete ep;
 }

@@ -100,3 +100,45 @@ def test_collector_threads_on_gpu(ctx, orc):
         t.join(timeout=60)
     assert col.epochs_run == 1 and sorted(out) == list(range(6))
     check(orc, shapes, batches, [out[i] for i in range(6)])
+
+
+def test_in_place_staged_and_unaligned_epochs_agree(ctx, monkeypatch):
+    """The in-place epochs (the kernel reading and writing the islands' arrays
+    over NVLink-C2C), the staged ones (PGX_EPOCH_STAGED=1: packing, copies,
+    unpacking) and in-place plans handed arrays that are not 16-byte aligned
+    (they fall back to the staged graph) give bit-identical results: the same
+    kernel evaluates the same rows."""
+    shapes, batches = shapes_and_batches(islands=12, seed=11, grad_every=2)
+    ep = A.Epoch(shapes, ctx)
+    try:
+        direct = ep.run(batches)
+        # arrays at an 8-byte offset inside larger buffers: not 16-byte aligned
+        raw_x = [np.empty(x.size + 1) for x in batches]
+        shifted = []
+        for r, x in zip(raw_x, batches):
+            v = r[1:] if r.ctypes.data % 16 == 0 else r[:-1]
+            v[:] = x.ravel()
+            shifted.append(v.reshape(x.shape))
+        outs = []
+        for k, p, n, g in shapes:
+            rf = np.empty(n + 1)
+            f = rf[1:] if rf.ctypes.data % 16 == 0 else rf[:-1]
+            gr = None
+            if g:
+                nx = shifted[len(outs)].shape[1]
+                rg = np.empty(n * nx + 1)
+                gr = (rg[1:] if rg.ctypes.data % 16 == 0 else rg[:-1]).reshape(n, nx)
+            outs.append((f, gr))
+        unaligned = ep.run(shifted, outs)
+    finally:
+        ep.close()
+    monkeypatch.setenv("PGX_EPOCH_STAGED", "1")
+    ep = A.Epoch(shapes, ctx)
+    try:
+        staged = ep.run(batches)
+    finally:
+        ep.close()
+    for (f1, g1), (f2, g2), (f3, g3) in zip(direct, staged, unaligned):
+        assert np.array_equal(f1, f2) and np.array_equal(f1, f3)
+        if g1 is not None:
+            assert np.array_equal(g1, g2) and np.array_equal(g1, g3)
