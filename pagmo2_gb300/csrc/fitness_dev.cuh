@@ -1,7 +1,9 @@
 // Device routines of the batch fitness/gradient path, shared by the
 // per-problem kernels (fitness.cu) and the fused archipelago kernel
 // (epoch.cu). Every routine evaluates whole rows with a fixed group of lanes,
-// in FP64 arithmetic, except the opt-in rosenbrock_row_v4_ff, which works in
+// in FP64 arithmetic or in integer arithmetic that is exact or closer to the
+// exact result than the FP64 operations it replaces (isum.h, rcp_fixed.h,
+// trig_fixed.h), except the opt-in rosenbrock_row_v4_ff, which works in
 // double-float arithmetic on the FP32 pipe.
 //
 // GB300's FP64 pipe retires two lanes per SM per clock, so these routines are
@@ -219,9 +221,10 @@ __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uin
 //   f   = 100 sum t_i^2 + sum (x_i - 1)^2        (i < n-1)
 //   g_i = 200 (t_{i-1} - 2 x_i t_i) + c_i        (i < n-1, t_{-1} = 0)
 //   g_{n-1} = 200 t_{n-2}
-// Fitness + gradient: 7 FP64 instructions per element (t, sum t^2, 2x, 2x-2,
-// sum (2x-2)^2, t_{i-1} - 2x t, 200 b + c), 6 in the vector variant where 2x
-// is an integer exponent increment; fitness only: 4.
+// Fitness + gradient: 5 FP64 instructions per element (t, 2x, 2x-2,
+// t_{i-1} - 2x t, 200 b + c), 4 in the vector variant where 2x is an integer
+// exponent increment; fitness only: 2 (t, x-1). The sums of t^2 and
+// (2x-2)^2 or (x-1)^2 are exact integer accumulations (isum.h).
 
 // Scalar variant: one group of G lanes per row, element i in lane i mod G;
 // x_{i+1} from the next lane (the last lane takes the next chunk's head),
