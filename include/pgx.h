@@ -316,7 +316,8 @@ typedef struct pgx_request {
    with Grace over NVLink-C2C) a second graph per set lets the kernel read
    the requests' dvs and write their fvs/grads in place, with no packing,
    copies or unpacking; it is taken for every epoch whose arrays are 16-byte
-   aligned, unless PGX_EPOCH_STAGED=1. Replaces the island-by-island
+   aligned and whose outputs do not overlap its inputs, unless
+   PGX_EPOCH_STAGED=1. Replaces the island-by-island
    bfe calls of an archipelago epoch (src/archipelago.cpp:325-330 ->
    src/island.cpp:428-655 -> src/bfe.cpp:91-110). */
 PGX_API int pgx_epoch_create(pgx_context *ctx, const pgx_request *reqs, int n_reqs, pgx_epoch **out);

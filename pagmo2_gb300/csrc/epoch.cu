@@ -632,6 +632,40 @@ int build_plan(pgx_epoch *ep, const pgx_request *reqs, int n_reqs)
     return PGX_OK;
 }
 
+// True when an output array of the epoch overlaps a decision-vector array:
+// evaluating in place would then read values the kernel has overwritten (the
+// staged path reads every input before any output is written).
+bool outputs_overlap_inputs(const pgx_epoch *ep, const pgx_request *reqs)
+{
+    struct span {
+        uintptr_t lo, hi;
+    };
+    std::vector<span> in, out;
+    for (size_t i = 0; i < ep->reqs.size(); ++i) {
+        const req_plan &p = ep->reqs[i];
+        if (!p.n) continue;
+        const uintptr_t x = reinterpret_cast<uintptr_t>(reqs[i].dvs);
+        in.push_back({x, x + p.n * p.nx * sizeof(double)});
+        if (reqs[i].fvs) {
+            const uintptr_t f = reinterpret_cast<uintptr_t>(reqs[i].fvs);
+            out.push_back({f, f + p.n * sizeof(double)});
+        }
+        if (reqs[i].grads) {
+            const uintptr_t g = reinterpret_cast<uintptr_t>(reqs[i].grads);
+            out.push_back({g, g + p.n * p.nx * sizeof(double)});
+        }
+    }
+    auto by_lo = [](const span &a, const span &b) { return a.lo < b.lo; };
+    std::sort(in.begin(), in.end(), by_lo);
+    for (const span &o : out) {
+        // the first input span starting at or after o.hi cannot overlap; check the ones before it
+        auto it = std::lower_bound(in.begin(), in.end(), span{o.hi, o.hi}, by_lo);
+        for (auto j = in.begin(); j != it; ++j)
+            if (j->hi > o.lo) return true;
+    }
+    return false;
+}
+
 int submit(pgx_epoch *ep, const pgx_request *reqs)
 {
     PGX_TRY(check_shapes(ep, reqs));
@@ -646,6 +680,7 @@ int submit(pgx_epoch *ep, const pgx_request *reqs)
     for (size_t i = 0; direct && i < ep->reqs.size(); ++i)
         direct = reinterpret_cast<uintptr_t>(reqs[i].fvs) % 16u == 0 && reinterpret_cast<uintptr_t>(reqs[i].grads) % 16u == 0
                  && (!ep->direct_inputs || reinterpret_cast<uintptr_t>(reqs[i].dvs) % 16u == 0);
+    if (direct && ep->direct_inputs) direct = !outputs_overlap_inputs(ep, reqs); // in place needs disjoint arrays
     if (!(direct && ep->direct_inputs)) {
         std::vector<copy_item> items;
         for (size_t i = 0; i < ep->reqs.size(); ++i) {

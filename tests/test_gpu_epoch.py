@@ -142,3 +142,20 @@ def test_in_place_staged_and_unaligned_epochs_agree(ctx, monkeypatch):
         assert np.array_equal(f1, f2) and np.array_equal(f1, f3)
         if g1 is not None:
             assert np.array_equal(g1, g2) and np.array_equal(g1, g3)
+
+
+def test_gradients_written_over_their_inputs(ctx):
+    """A request whose gradient array is its own decision-vector array: the
+    epoch must read every input before writing (the in-place path detects the
+    overlap and takes the staged one)."""
+    shapes, batches = shapes_and_batches(islands=6, seed=13, grad_every=1)
+    ep = A.Epoch(shapes, ctx)
+    try:
+        want = ep.run(batches)
+        xs = [np.array(x, dtype=np.float64, copy=True) for x in batches]
+        outs = [(np.empty(n), xs[i]) for i, (k, p, n, g) in enumerate(shapes)]
+        got = ep.run(xs, outs)
+    finally:
+        ep.close()
+    for (f1, g1), (f2, g2) in zip(want, got):
+        assert np.array_equal(f1, f2) and np.array_equal(g1, g2)
