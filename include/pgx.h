@@ -135,10 +135,11 @@ PGX_API int pgx_selftest_barrier_timeout(pgx_context *ctx, uint64_t spin_limit, 
 
 /* Self-test of the reciprocal and its cube in the Lennard-Jones pair loops
    (no counterpart in the reference, whose pair sum divides and cubes in FP64:
-   src/problems/lennard_jones.cpp:83): inv[i] = the device's 1/d[i] and, when
-   inv_cube is not null, inv_cube[i] = its 1/d[i]^3, as those loops compute
-   them, for host arrays of n values. For 2^-100 <= d < 2^101 (integer fixed
-   point): 1/d within one half unit of the last place of the exact value plus
+   src/problems/lennard_jones.cpp:83): inv[i] = 1/d[i] and, when inv_cube is
+   not null, inv_cube[i] = 1/d[i]^3 from the fixed-point core those loops use
+   (the loops feed it the integer sum of the squared differences; here it
+   gets d's significand), for host arrays of n values. For 2^-100 <= d <
+   2^101: 1/d within one half unit of the last place of the exact value plus
    2^-10 units, 1/d^3 plus 2^-5 units; for the other positive normal d with a
    normal reciprocal (an FP64 Newton step, then two FP64 multiplies): 1/d
    within one unit. Other d are not covered (the pair loops flag d = 0 apart). */
