@@ -41,12 +41,17 @@ __device__ __forceinline__ long long hv_key(double v)
     return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
 }
 
-// keys of coordinates 1 (y) and, for 3D, 2 (z): kyz[c * n + t]
+// order keys kyz[c * n + t]: c = 0 the y coordinate; for 3D also c = 1 the z
+// coordinate and c = 2 the x coordinate
 __global__ void hv_keys_kernel(const double *__restrict__ pts, uint32_t n, uint32_t m, long long *__restrict__ kyz)
 {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        kyz[t] = hv_key(pts[static_cast<uint64_t>(t) * m + 1]);
-        if (m == 3u) kyz[static_cast<uint64_t>(n) + t] = hv_key(pts[static_cast<uint64_t>(t) * m + 2]);
+        const double *p = pts + static_cast<uint64_t>(t) * m;
+        kyz[t] = hv_key(p[1]);
+        if (m == 3u) {
+            kyz[static_cast<uint64_t>(n) + t] = hv_key(p[2]);
+            kyz[2ull * n + t] = hv_key(p[0]);
+        }
     }
 }
 
@@ -120,28 +125,27 @@ __global__ void hv_rank_kernel(const long long *__restrict__ kyz, uint32_t n, co
     }
 }
 
-// points into y order: ys and the widths r_x - x (as bits; for 3D beside the
-// z rank of each y position, and the z values in z order); the ranks are the
-// sums of the nq slice counts
+// points into y order: ys and, for 2D, the widths r_x - x as bits; for 3D
+// the 32-bit width keys (n - 1 - the x rank: a larger key never has a smaller
+// width) beside the z ranks, the widths as doubles, and the z values in z
+// order
 __global__ void hv_scatter_kernel(const double *__restrict__ pts, uint32_t n, uint32_t m, double rx,
-                                  const int32_t *__restrict__ part, uint32_t nq, double *__restrict__ ys,
-                                  long long *__restrict__ wbits, longlong2 *__restrict__ wz, double *__restrict__ zs)
+                                  const int32_t *__restrict__ rank, double *__restrict__ ys,
+                                  long long *__restrict__ wbits, int2 *__restrict__ wk, double *__restrict__ wv,
+                                  double *__restrict__ zs)
 {
-    const uint64_t stride = static_cast<uint64_t>(m - 1u) * n;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const double *p = pts + static_cast<uint64_t>(t) * m;
-        int32_t ry = 0, rz = 0;
-        for (uint32_t q = 0; q < nq; ++q) {
-            ry += part[q * stride + t];
-            if (m == 3u) rz += part[q * stride + n + t];
-        }
+        const int32_t ry = rank[t];
         ys[ry] = p[1];
-        const long long w = __double_as_longlong(rx - p[0]);
+        const double w = rx - p[0];
         if (m == 3u) {
-            wz[ry] = make_longlong2(w, rz);
+            const int32_t rz = rank[static_cast<uint64_t>(n) + t], rxk = rank[2ull * n + t];
+            wk[ry] = make_int2(static_cast<int>(n) - 1 - rxk, rz);
+            wv[ry] = w;
             zs[rz] = p[2];
         } else {
-            wbits[ry] = w;
+            wbits[ry] = __double_as_longlong(w);
         }
     }
 }
@@ -206,12 +210,6 @@ __global__ void hv_area2_kernel(const double *__restrict__ ys, const long long *
 constexpr int kLevelThreads = 64;
 constexpr uint32_t kLevelTile = 1024;
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
-                 "l"(gmem));
-}
-
 __device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
 {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
@@ -219,22 +217,24 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
 }
 
 __global__ void __launch_bounds__(kLevelThreads)
-    hv_levels3_kernel(const double *__restrict__ ys, const longlong2 *__restrict__ wz, const double *__restrict__ zs,
-                      uint32_t n, double ry, double rz, double *__restrict__ term)
+    hv_levels3_kernel(const double *__restrict__ ys, const int2 *__restrict__ wk, const double *__restrict__ wv,
+                      const double *__restrict__ zs, uint32_t n, double ry, double rz, double *__restrict__ term)
 {
-    __shared__ longlong2 s_wz[2][kLevelTile];
+    __shared__ __align__(16) int2 s_k[2][kLevelTile]; // read two entries at a time (16-byte loads)
     __shared__ double s_y[2][kLevelTile];
+    __shared__ double s_w[2][kLevelTile];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const long long lim = i < n ? static_cast<long long>(i) : -1; // z rank <= i
-    long long v = 0;                                              // running maximum (bits; +0.0: none)
+    const int lim = i < n ? static_cast<int>(i) : -1; // z rank <= i
+    int v = -1;                                       // running maximum width key (-1: no point yet)
     double pend_w = 0.0, pend_y = 0.0, a = 0.0;
     const uint32_t tiles = (n + kLevelTile - 1u) / kLevelTile;
     auto stage = [&](uint32_t t, uint32_t buf) {
         const uint32_t t0 = t * kLevelTile;
         const uint32_t cnt = n - t0 < kLevelTile ? n - t0 : kLevelTile;
         for (uint32_t j = threadIdx.x; j < cnt; j += blockDim.x) {
-            cp_async16(&s_wz[buf][j], wz + t0 + j);
+            cp_async8(&s_k[buf][j], wk + t0 + j);
             cp_async8(&s_y[buf][j], ys + t0 + j);
+            cp_async8(&s_w[buf][j], wv + t0 + j);
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
@@ -248,27 +248,24 @@ __global__ void __launch_bounds__(kLevelThreads)
             asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncthreads();
-        const uint32_t t0 = t * kLevelTile;
-        const uint32_t cnt = n - t0 < kLevelTile ? n - t0 : kLevelTile;
-        const longlong2 *w = s_wz[buf];
-        const double *yv = s_y[buf];
+        const uint32_t cnt = n - t * kLevelTile < kLevelTile ? n - t * kLevelTile : kLevelTile;
+        const int4 *k2 = reinterpret_cast<const int4 *>(s_k[buf]); // two points per 16-byte load
         // four points per warp-uniform test; the records inside are rare
         for (uint32_t j = 0; j < cnt; j += 4u) {
-            long long c[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const uint32_t jq = j + q < cnt ? j + q : cnt - 1u;
-                const longlong2 e = w[jq];
-                c[q] = (j + q < cnt && e.y <= lim) ? e.x : 0;
-            }
-            const long long mx = max(max(c[0], c[1]), max(c[2], c[3]));
+            const int4 e01 = k2[j >> 1], e23 = k2[(j >> 1) + 1u]; // staged past cnt: masked below
+            int c[4];
+            c[0] = e01.y <= lim ? e01.x : -1;
+            c[1] = (j + 1u < cnt && e01.w <= lim) ? e01.z : -1;
+            c[2] = (j + 2u < cnt && e23.y <= lim) ? e23.x : -1;
+            c[3] = (j + 3u < cnt && e23.w <= lim) ? e23.z : -1;
+            const int mx = max(max(c[0], c[1]), max(c[2], c[3]));
             if (__any_sync(kFull, mx > v)) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     if (c[q] > v) {
-                        const double y = yv[j + q];
+                        const double y = s_y[buf][j + q];
                         if (pend_w > 0.0) a = fma(pend_w, y - pend_y, a);
-                        pend_w = __longlong_as_double(c[q]);
+                        pend_w = s_w[buf][j + q];
                         pend_y = y;
                         v = c[q];
                     }
@@ -347,38 +344,38 @@ size_t align256(size_t b)
 int launch_hypervolume(pgx_context *ctx, const double *d_pts, uint32_t n, uint32_t m, const double *r,
                        double *d_out, cudaStream_t s)
 {
-    const uint32_t nc = m - 1u;
+    const uint32_t nc = m == 3u ? 3u : 1u; // coordinates ranked: y (and z, x for 3D)
     const int sms = ctx->num_sms;
     const int g1 = static_cast<int>(std::min<uint64_t>((n + 255u) / 256u, static_cast<uint64_t>(sms) * 8u));
     const uint32_t nb = (n + kRun - 1u) / kRun; // sorted runs per coordinate
-    const uint32_t nq = 1u;
     const size_t b_keys = align256(static_cast<size_t>(n) * nc * 8u);
     const size_t b_rank = align256(static_cast<size_t>(n) * nc * 4u);
     const size_t b_runs = align256(static_cast<size_t>(nb) * kRun * nc * sizeof(key_idx));
-    const size_t b_d = align256(static_cast<size_t>(n) * 8u), b_i = align256(static_cast<size_t>(n) * 16u);
-    PGX_TRY(ctx->s_crowd.ensure(b_keys + b_rank + b_runs + 4u * b_d + b_i + 256u));
+    const size_t b_d = align256(static_cast<size_t>(n) * 8u);
+    PGX_TRY(ctx->s_crowd.ensure(b_keys + b_rank + b_runs + 6u * b_d + 256u));
     char *base = ctx->s_crowd.as<char>();
     long long *kyz = reinterpret_cast<long long *>(base);
-    int32_t *part = reinterpret_cast<int32_t *>(base + b_keys);
+    int32_t *rank = reinterpret_cast<int32_t *>(base + b_keys);
     key_idx *runs = reinterpret_cast<key_idx *>(base + b_keys + b_rank);
-    base += b_runs;
-    double *ys = reinterpret_cast<double *>(base + b_keys + b_rank);
-    long long *wbits = reinterpret_cast<long long *>(base + b_keys + b_rank + b_d);
-    double *zs = reinterpret_cast<double *>(base + b_keys + b_rank + 2u * b_d);
-    double *term = reinterpret_cast<double *>(base + b_keys + b_rank + 3u * b_d);
-    longlong2 *wz = reinterpret_cast<longlong2 *>(base + b_keys + b_rank + 4u * b_d);
+    char *arr = base + b_keys + b_rank + b_runs; // six arrays of n doubles
+    double *ys = reinterpret_cast<double *>(arr);
+    long long *wbits = reinterpret_cast<long long *>(arr + b_d);
+    double *zs = reinterpret_cast<double *>(arr + 2u * b_d);
+    double *term = reinterpret_cast<double *>(arr + 3u * b_d);
+    int2 *wk = reinterpret_cast<int2 *>(arr + 4u * b_d);
+    double *wv = reinterpret_cast<double *>(arr + 5u * b_d);
     hv_keys_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, kyz);
     PGX_CUDA(cudaGetLastError());
     hv_runs_kernel<<<dim3(nb, nc), 1024, 0, s>>>(kyz, n, runs);
     PGX_CUDA(cudaGetLastError());
-    hv_rank_kernel<<<dim3(static_cast<unsigned>((n + 127u) / 128u), nc), 128, 0, s>>>(kyz, n, runs, nb, part);
+    hv_rank_kernel<<<dim3(static_cast<unsigned>((n + 127u) / 128u), nc), 128, 0, s>>>(kyz, n, runs, nb, rank);
     PGX_CUDA(cudaGetLastError());
-    hv_scatter_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, r[0], part, nq, ys, wbits, m == 3u ? wz : nullptr,
-                                         m == 3u ? zs : nullptr);
+    hv_scatter_kernel<<<g1, 256, 0, s>>>(d_pts, n, m, r[0], rank, ys, wbits, m == 3u ? wk : nullptr,
+                                         m == 3u ? wv : nullptr, m == 3u ? zs : nullptr);
     PGX_CUDA(cudaGetLastError());
     if (m == 3u) {
         const int g3 = static_cast<int>((n + kLevelThreads - 1u) / kLevelThreads);
-        hv_levels3_kernel<<<g3, kLevelThreads, 0, s>>>(ys, wz, zs, n, r[1], r[2], term);
+        hv_levels3_kernel<<<g3, kLevelThreads, 0, s>>>(ys, wk, wv, zs, n, r[1], r[2], term);
         PGX_CUDA(cudaGetLastError());
         hv_sum_kernel<<<1, 1024, 0, s>>>(term, n, d_out);
     } else {

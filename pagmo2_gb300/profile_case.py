@@ -17,6 +17,7 @@ profiler are not benchmark values). Cases:
   survival                      NSGA-II survival of --rows nested-front points x 3
   select_best                   select_best_N_mo(--rows nested-front points x 3, rows / 2)
   sort_population               sort_population_mo(--rows nested-front points x 3)
+  hypervolume                   hypervolume of --rows nested-front points x 3 (reference point max + 0.5)
   archipelago                   the fused kernel of a 64-island mixed epoch (--rows unused)
 """
 from __future__ import annotations
@@ -42,6 +43,7 @@ def main() -> None:
     ap.add_argument("--layers", type=int, default=30, help="nested fronts of the survival/select_best/sort cases")
     a = ap.parse_args()
 
+    import numpy as np
     import torch
 
     from pagmo2_gb300 import _native as N
@@ -71,6 +73,14 @@ def main() -> None:
         def run():
             N.check(L.pgx_nsga2_survival_device(ctx.handle, dp.data_ptr(), n, 3, rank.data_ptr(), dc.data_ptr(),
                                                 off.data_ptr(), idx.data_ptr(), nf.data_ptr(), cd.data_ptr(), sp))
+    elif a.case == "hypervolume":
+        p = W.nsga2_points(n, 3, layers=a.layers)
+        r = np.ascontiguousarray(p.max(axis=0) + 0.5)
+        dp = torch.from_numpy(np.ascontiguousarray(p)).cuda()
+        dhv = torch.empty(1, dtype=torch.float64, device="cuda")
+
+        def run():
+            N.check(L.pgx_hypervolume_device(ctx.handle, dp.data_ptr(), n, 3, N.ptr(r), dhv.data_ptr(), sp))
     elif a.case in ("select_best", "sort_population"):
         p = W.nsga2_points(n, 3, layers=a.layers)
         dp = torch.from_numpy(p).cuda()
