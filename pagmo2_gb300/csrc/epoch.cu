@@ -570,7 +570,35 @@ int build_plan(pgx_epoch *ep, const pgx_request *reqs, int n_reqs)
             ++p.tiles;
         }
     }
-    std::stable_sort(tp.begin(), tp.end(), [](const tile_plan &a, const tile_plan &b) { return a.cost > b.cost; });
+    // Costliest first within each pipe class, the classes interleaved in
+    // proportion to their total cost: Lennard-Jones and rosenbrock tiles load
+    // the FP64 pipe, rastrigin tiles (fixed-point sin/cos) the integer ALU,
+    // so warps running side by side on an SM keep both pipes busy, and both
+    // classes still end together with their small tiles.
+    {
+        std::vector<tile_plan> fp, alu;
+        for (const tile_plan &t : tp) (ep->reqs[t.req].kind == PGX_RASTRIGIN ? alu : fp).push_back(t);
+        auto by_cost = [](const tile_plan &a, const tile_plan &b) { return a.cost > b.cost; };
+        std::stable_sort(fp.begin(), fp.end(), by_cost);
+        std::stable_sort(alu.begin(), alu.end(), by_cost);
+        double tot_fp = 0, tot_alu = 0;
+        for (const tile_plan &t : fp) tot_fp += t.cost;
+        for (const tile_plan &t : alu) tot_alu += t.cost;
+        tp.clear();
+        size_t i = 0, j = 0;
+        double done_fp = 0, done_alu = 0;
+        while (i < fp.size() || j < alu.size()) {
+            const bool take_fp = j == alu.size()
+                                 || (i < fp.size() && done_fp / std::max(tot_fp, 1e-30) <= done_alu / std::max(tot_alu, 1e-30));
+            if (take_fp) {
+                done_fp += fp[i].cost;
+                tp.push_back(fp[i++]);
+            } else {
+                done_alu += alu[j].cost;
+                tp.push_back(alu[j++]);
+            }
+        }
+    }
     PGX_CHECK(tp.size() < (1ull << 31), PGX_ERR_CAPACITY, "too many tiles");
     ep->n_tiles = static_cast<uint32_t>(tp.size());
     ep->grid = std::max(1, std::min(max_grid, static_cast<int>((tp.size() + kWarpsPerBlock - 1) / kWarpsPerBlock)));
