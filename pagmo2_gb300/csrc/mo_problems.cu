@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(256) zdt_kernel(const double *__restrict__ x, 
         } else {
             // sum over x[1..nx-1]: of x (ZDT1-3, 6), of x^2 and cos(4 pi x) (ZDT4)
             double s1 = 0.0, s2 = 0.0;
+#pragma unroll 4
             for (uint32_t i = sub + 1u; i < nx; i += G) {
                 const double xi = __ldg(xr + i);
                 if constexpr (ID == 4) {
@@ -193,6 +194,7 @@ __global__ void __launch_bounds__(256) dtlz_kernel(const double *__restrict__ x,
         const double *xm = xr + (m - 1u);
         // distance function over x_M (dtlz.cpp:182-244)
         double s = 0.0, sc = 0.0;
+#pragma unroll 4
         for (uint32_t i = sub; i < k; i += G) {
             const double xi = __ldg(xm + i);
             if constexpr (ID == 1 || ID == 3) {
