@@ -67,6 +67,20 @@ __device__ __forceinline__ isum::sq_acc group_isum(isum::sq_acc a, unsigned mask
     return a;
 }
 
+// The same for the signed accumulators (isum::sg_acc).
+template <int G>
+__device__ __forceinline__ isum::sg_acc group_ssum(isum::sg_acc a, unsigned mask)
+{
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+        const long long m = __shfl_xor_sync(mask, static_cast<long long>(a.m), o, G);
+        const int e = __shfl_xor_sync(mask, a.e, o, G);
+        a.flags |= __shfl_xor_sync(mask, a.flags, o, G);
+        isum::add_signed(a, m, e);
+    }
+    return a;
+}
+
 // +1.0 or -1.0, and a constant with its sign flipped, built with integer
 // operations so that signs cost no FP64 instruction: callers fold them into
 // the FMA that consumes the value.

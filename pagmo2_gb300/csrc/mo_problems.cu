@@ -118,7 +118,11 @@ __global__ void __launch_bounds__(256) zdt_kernel(const double *__restrict__ x, 
             }
             continue;
         } else {
-            // sum over x[1..nx-1]: of x (ZDT1-3, 6), of x^2 and cos(4 pi x) (ZDT4)
+            // sum over x[1..nx-1]: of x (ZDT1-3, 6) in an integer accumulator
+            // (isum.h: within 2^-60 of the largest term per addition, rounded
+            // once); of x^2 and cos(4 pi x) (ZDT4) in FP64, where the
+            // fixed-point cosine already loads the integer pipes
+            isum::sg_acc a1 = isum::make_signed();
             double s1 = 0.0, s2 = 0.0;
 #pragma unroll 4
             for (uint32_t i = sub + 1u; i < nx; i += G) {
@@ -127,11 +131,15 @@ __global__ void __launch_bounds__(256) zdt_kernel(const double *__restrict__ x, 
                     s1 = fma(xi, xi, s1);
                     s2 += cos_2pi_signed(xi + xi);
                 } else {
-                    s1 += xi;
+                    isum::add_value(a1, xi);
                 }
             }
-            s1 = group_sum<G>(s1, mask);
-            if constexpr (ID == 4) s2 = group_sum<G>(s2, mask);
+            if constexpr (ID == 4) {
+                s1 = group_sum<G>(s1, mask);
+                s2 = group_sum<G>(s2, mask);
+            } else {
+                s1 = isum::value(dev::group_ssum<G>(a1, mask));
+            }
             if (sub != 0) continue;
             const double x0 = __ldg(xr);
             const double nm1 = static_cast<double>(nx - 1u);
@@ -193,27 +201,36 @@ __global__ void __launch_bounds__(256) dtlz_kernel(const double *__restrict__ x,
         const double *xr = x + row * nx;
         const double *xm = xr + (m - 1u);
         // distance function over x_M (dtlz.cpp:182-244)
-        double s = 0.0, sc = 0.0;
+        // sums as the problem takes them: of (x - 0.5)^2, of x and of x^0.1 in
+        // integer accumulators (isum.h), of cos(20 pi (x - 0.5)) in FP64
+        isum::sq_acc qs = isum::make();
+        isum::sg_acc as = isum::make_signed();
+        double sc = 0.0; // the cosines in FP64: their fixed-point evaluation already loads the integer pipes
 #pragma unroll 4
         for (uint32_t i = sub; i < k; i += G) {
             const double xi = __ldg(xm + i);
             if constexpr (ID == 1 || ID == 3) {
                 const double d = xi - 0.5;
-                s = fma(d, d, s);
+                isum::add_square(qs, d);
                 sc += cos_2pi_signed(10.0 * d); // cos(20 pi d)
             } else if constexpr (ID == 6) {
-                s += pow(xi, 0.1);
+                isum::add_value(as, pow(xi, 0.1));
             } else if constexpr (ID == 7) {
-                s += xi;
+                isum::add_value(as, xi);
             } else {
                 const double d = xi - 0.5;
-                s = fma(d, d, s);
+                isum::add_square(qs, d);
             }
         }
-        s = group_sum<G>(s, mask);
+        double s;
+        if constexpr (ID == 6 || ID == 7) {
+            s = isum::value(dev::group_ssum<G>(as, mask));
+        } else {
+            s = isum::value(dev::group_isum<G>(qs, mask));
+        }
+        if constexpr (ID == 1 || ID == 3) sc = group_sum<G>(sc, mask);
         double g;
         if constexpr (ID == 1 || ID == 3) {
-            sc = group_sum<G>(sc, mask);
             g = 100. * ((s - sc) + static_cast<double>(k));
         } else if constexpr (ID == 7) {
             g = (9. / static_cast<double>(k)) * s;

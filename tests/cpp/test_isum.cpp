@@ -3,9 +3,12 @@
 // spread over up to 2^200 in magnitude, 1..200 per sum, added one at a time
 // and four at a time (sum4); each sum must lie within 2^-53 + n 2^-60 of the
 // exact one (long double) relative, and the special values must follow FP64
-// semantics. Prints "<sums> <worst relative error>"; exit 1 on a violation.
+// semantics; signed sums within 2^-53 of the result plus n 2^-60 of the
+// largest magnitude. Prints "<sums> <worst relative error> <worst signed error
+// as a fraction of its bound>"; exit 1 on a violation.
 #include "isum.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <limits>
@@ -70,6 +73,48 @@ int main()
     add_square(a, -3.0);
     add_square(a, 4.0);
     violations += value(a) != 25.0;
-    std::printf("%ld %.3Le\n", sums, worst);
+    // signed sums: values of both signs over 2^-100 .. 2^100; the error is
+    // bounded by 2^-53 of the result plus n 2^-60 of the largest magnitude
+    long double worst_signed = 0;
+    for (int trial = 0; trial < 40000; ++trial) {
+        const int n = 1 + static_cast<int>(g() % 200u);
+        const int spread = (trial % 3 == 0) ? 200 : (trial % 3 == 1) ? 20 : 0;
+        sg_acc acc = make_signed();
+        long double exact = 0, big = 0;
+        for (int i = 0; i < n; ++i) {
+            const double v = std::ldexp(U(g), static_cast<int>(g() % static_cast<uint64_t>(spread + 1)) - spread / 2);
+            add_value(acc, v);
+            exact += v;
+            big = std::max<long double>(big, std::fabs(static_cast<long double>(v)));
+        }
+        const long double err = std::fabs(static_cast<long double>(value(acc)) - exact);
+        const long double bound = std::ldexp(1.0L, -53) * std::fabs(exact) + n * std::ldexp(1.0L, -60) * big;
+        if (bound > 0 && err / bound > worst_signed) worst_signed = err / bound;
+        if (err > bound) ++violations;
+    }
+    {
+        sg_acc a = make_signed();
+        add_value(a, 1.5);
+        add_value(a, -1.5);
+        violations += value(a) != 0.0;
+        a = make_signed();
+        add_value(a, std::numeric_limits<double>::infinity());
+        add_value(a, -std::numeric_limits<double>::infinity());
+        violations += !std::isnan(value(a));
+        a = make_signed();
+        add_value(a, -std::numeric_limits<double>::infinity());
+        add_value(a, 3.0);
+        violations += !(std::isinf(value(a)) && value(a) < 0);
+        a = make_signed();
+        add_value(a, 0.1);
+        add_value(a, 0.2);
+        add_value(a, -0.3);
+        violations += std::fabs(value(a)) > 1e-16;
+        a = make_signed();
+        add_value(a, -2.5);
+        add_value(a, 4.9e-324);
+        violations += value(a) != -2.5;
+    }
+    std::printf("%ld %.3Le %.3Le\n", sums, worst, worst_signed);
     return violations == 0 ? 0 : 1;
 }

@@ -10,7 +10,9 @@ the row loops, built with g++ (the headers compile as plain C++):
   (pagmo2_gb300/csrc/isum.h, tests/cpp/test_isum.cpp): 80 000 sums of 1..200
   squares spread over 2^200, one at a time and four at a time, within
   2^-53 + n 2^-60 of the exact sums; infinities, NaN, overflow, underflow
-  and subnormal squares as FP64 gives them;
+  and subnormal squares as FP64 gives them; and its signed variant (ZDT and
+  DTLZ sums): 40 000 sums of both signs within 2^-53 of the result plus
+  n 2^-60 of the largest magnitude, cancellation and infinities included;
 - the fixed-point sin/cos(2 pi x) of the rastrigin and ackley rows
   (pagmo2_gb300/csrc/trig_fixed.h, tests/cpp/test_trig_fixed.cpp): 2.8 million
   x over every binade of 2^-60 .. 2^40 and next to the multiples of 1/4,
@@ -42,9 +44,11 @@ def test_fixed_point_reciprocal_is_faithful(tmp_path):
 
 
 def test_integer_sum_of_squares(tmp_path):
-    sums, worst = build_and_run(tmp_path, "test_isum")
+    sums, worst, worst_signed = build_and_run(tmp_path, "test_isum")
     assert int(sums) == 80_000
     assert float(worst) <= 2.0 ** -53 + 200 * 2.0 ** -60
+    # signed sums: the worst error as a fraction of 2^-53 |sum| + n 2^-60 max |term|
+    assert float(worst_signed) <= 1.0
 
 
 def test_fixed_point_sin_cos_2pi(tmp_path):
