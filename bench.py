@@ -10,13 +10,17 @@ step = one batch. Prints one JSON line:
   e2e    the same metric through the public host-buffer entry point
          (pgx_batch_gradient) from pinned host memory, uploads and downloads
          inside the timed region
-  roofline  FP64 pipe of the rosenbrock kernel (peak measured in-run by a DFMA
-         probe; MEASURED_PEAKS.json has no FP64 figure) plus its HBM fraction
+  roofline  the rosenbrock kernel against the FP64 peak (measured in-run by a
+         DFMA probe; MEASURED_PEAKS.json has no FP64 figure): the algorithmic
+         flops, the FP64 pipe's own load (fp64_pipe: part of the algorithmic
+         flops run exactly on the integer pipes) and the HBM fraction
   cpu_baseline  the reference's CPU path (compiled reference where present,
          else the oracle's restatement of thread_bfe + gradient) on the host
   secondary  the other kernels of the path (rastrigin, lennard_jones, ackley,
-         griewank, schwefel, NSGA-II survival, select_best_N_mo,
-         sort_population_mo, the fused archipelago epoch) measured the same way
+         griewank, schwefel, ZDT/DTLZ, NSGA-II survival, select_best_N_mo,
+         sort_population_mo, one NSGA-II generation on ZDT1, hypervolume, the
+         fused archipelago epoch against one GPU bfe call per island) measured
+         the same way
 
 --impl reference times the reference's CPU implementation of the same step
 with every host thread. Multi-GPU (torchrun): every rank evaluates its own
