@@ -19,20 +19,47 @@ HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 ORACLE_SO = OUT / "liboracle.so"
 REF_SO = OUT / "libpagmo_ref.so"
-REF_ROOT = Path(os.environ.get("PGX_REFERENCE_ROOT", "/root/reference"))
+# The reference's sources: a pagmo 2.19.1 tree named by PGX_REFERENCE_ROOT, or
+# the copy `make -C oracle stage` leaves in baseline/_ref/pagmo2 (git-ignored;
+# it travels with the working tree). Neither present: the reference-pinned
+# tests skip.
+STAGED_ROOT = HERE.parent / "baseline" / "_ref" / "pagmo2"
+
+
+def _reference_root() -> Path | None:
+    env = os.environ.get("PGX_REFERENCE_ROOT")
+    if env:
+        return Path(env)
+    return STAGED_ROOT if (STAGED_ROOT / "src" / "problem.cpp").exists() else None
+
+
+REF_ROOT = _reference_root()
 
 _vp, _u64 = C.c_void_p, C.c_uint64
 
 
 def build(reference: bool | None = None) -> None:
-    """Compile the oracle (always) and the reference library (when its sources exist)."""
+    """Compile the oracle (always) and the reference library (when its sources exist).
+
+    With PGX_REFERENCE_ROOT set, the tree is first staged into baseline/_ref/pagmo2
+    so that later builds (also on machines without the tree) find it there."""
     r = subprocess.run(["make", "-s", "-C", str(HERE), "oracle"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    env = os.environ.get("PGX_REFERENCE_ROOT")
+    if env and Path(env).resolve() != STAGED_ROOT.resolve() and (Path(env) / "src" / "problem.cpp").exists():
+        r = subprocess.run(["make", "-s", "-C", str(HERE), "stage", f"PAGMO_SOURCE={env}"], capture_output=True,
+                           text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"staging the reference failed:\n{r.stdout}\n{r.stderr}")
+    root = STAGED_ROOT if (STAGED_ROOT / "src" / "problem.cpp").exists() else _reference_root()
     if reference is None:
-        reference = (REF_ROOT / "src" / "problem.cpp").exists()
+        reference = root is not None and (root / "src" / "problem.cpp").exists()
     if reference:
-        r = subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "ref", f"REF_ROOT={REF_ROOT}"],
+        if root is None:
+            raise RuntimeError("the reference's sources are not present (set PGX_REFERENCE_ROOT)")
+        jobs = str(max(2, os.cpu_count() or 2))
+        r = subprocess.run(["make", "-s", f"-j{jobs}", "-C", str(HERE), "ref", f"REF_ROOT={root}"],
                            capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference build failed:\n{r.stdout}\n{r.stderr}")

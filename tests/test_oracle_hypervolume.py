@@ -61,8 +61,8 @@ def read_cases(path):
 
 @pytest.mark.parametrize("name", ["c_max_t100_d2_n128", "c_max_t100_d3_n128", "c_max_t1_d3_n2048"])
 def test_reference_test_cases(orc, name):
-    path = oracle.REF_ROOT / "tests" / "hypervolume_test_data" / "testcases" / name
-    if not path.exists():
+    path = None if oracle.REF_ROOT is None else oracle.REF_ROOT / "tests" / "hypervolume_test_data" / "testcases" / name
+    if path is None or not path.exists():
         pytest.skip("the reference's test data is only present where its tree is")
     for p, r, want in read_cases(path):
         assert abs(orc.hypervolume(p, r) - want) < 1e-8, name
