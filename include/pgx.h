@@ -77,6 +77,11 @@ typedef struct pgx_epoch pgx_epoch;
 /* ABI version of the loaded library (PGX_ABI_VERSION at build time). */
 PGX_API int pgx_abi_version(void);
 
+/* Identity of this build of the library: a digest of its sources and compiler
+ * flags. The archipelago autotuner keys its cached choices by it, so a rebuilt
+ * library re-tunes. No counterpart in the reference. */
+PGX_API const char *pgx_build_id(void);
+
 /* Message of the calling thread's most recent failing call ("" if none). */
 PGX_API const char *pgx_last_error(void);
 
@@ -284,10 +289,14 @@ PGX_API int pgx_nsga2_survival_device(pgx_context *ctx, const double *d_points, 
    pgx_nsga2_survival_device, without a context: it runs on the current
    device, and its scratch is a fixed device array inside the library, so
    n <= 4096 and m <= 8, else PGX_ERR_CAPACITY. The first call on each device
-   looks up that array's device address (a one-time set-up); make that first
-   call before any stream capture. All calls share the array and it keeps the
-   last call's contents (each call re-initialises what it needs); calls whose
-   work overlaps on the GPU race on it and must be serialised by the caller. */
+   (and in each CUDA context) does a one-time set-up: it looks up that array's
+   device address and loads the library's survival code and data on the device
+   (under lazy module loading, the CUDA default, this is when the ~2.5 MB array
+   is allocated). Make that first call before another allocator reserves the
+   device's memory, and before any stream capture; later calls allocate
+   nothing. All calls share the array and it keeps the last call's contents
+   (each call re-initialises what it needs); calls whose work overlaps on the
+   GPU race on it and must be serialised by the caller. */
 PGX_API int pgx_nsga2_survival_device_noalloc(const double *d_points, uint64_t n, uint64_t m, int32_t *d_rank,
                                               int32_t *d_dom_count, int32_t *d_front_offsets,
                                               int32_t *d_front_indices, int32_t *d_n_fronts, double *d_crowding,

@@ -24,6 +24,7 @@ ZDT, DTLZ = 7, 8
 _vp, _u64, _i32, _d = C.c_void_p, C.c_uint64, C.c_int32, C.c_double
 SIGNATURES = {
     "pgx_abi_version": (C.c_int, []),
+    "pgx_build_id": (C.c_char_p, []),
     "pgx_last_error": (C.c_char_p, []),
     "pgx_context_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
     "pgx_context_destroy": (None, [_vp]),

@@ -59,9 +59,13 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     nvcc = _nvcc()
     objs = []
 
+    # the build's identity (a digest of every source and flag): the autotuner
+    # keys its cached choices by it, so a rebuilt library never reuses them
+    build_id = f'-DPGX_BUILD_ID="{fp[:16]}"'
+
     def compile_one(src: Path) -> Path:
         obj = OUT / (src.stem + ".o")
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, build_id, "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

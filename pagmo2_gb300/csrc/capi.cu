@@ -281,6 +281,11 @@ int pgx_abi_version(void)
     return PGX_ABI_VERSION;
 }
 
+const char *pgx_build_id(void)
+{
+    return PGX_BUILD_ID;
+}
+
 const char *pgx_last_error(void)
 {
     return get_error();

@@ -128,10 +128,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
 
 // ------------------------------------------------------------------ autotuner
 
-// Per (problem, dimension, gradient, device) choice of the row variant and its
-// measured cost per row at full-device throughput. Kept in memory and in a
-// text cache next to the library ("autotune.txt", one "key lanes ns" line per
-// entry); PGX_AUTOTUNE_CACHE overrides the path, "off" disables the file.
+// Per (build, problem, dimension, gradient, device) choice of the row variant
+// and its measured cost per row at full-device throughput. Kept in memory and
+// in a text cache next to the library ("autotune.txt", one "key lanes ns" line
+// per entry); PGX_AUTOTUNE_CACHE overrides the path, "off" disables the file.
+// Keys begin with the library's build identity (PGX_BUILD_ID): choices and
+// costs measured by another build of the kernels are never reused, and loading
+// the file drops their lines.
 struct tune_entry {
     int lanes; // rastrigin/rosenbrock: 1..32 lanes per row, 0 = 4-wide rosenbrock rows; lennard_jones: 32
     double ns_per_row;
@@ -153,16 +156,42 @@ std::string tune_path()
     return "";
 }
 
+std::string tune_key_prefix()
+{
+    return std::string(PGX_BUILD_ID) + "/";
+}
+
 void tune_load()
 {
     if (g_tune_loaded) return;
     g_tune_loaded = true;
     const std::string p = tune_path();
     if (p.empty() || p == "off") return;
-    std::ifstream in(p);
-    std::string key;
-    tune_entry e{};
-    while (in >> key >> e.lanes >> e.ns_per_row) g_tune[key] = e;
+    const std::string prefix = tune_key_prefix();
+    bool stale = false;
+    {
+        std::ifstream in(p);
+        std::string key;
+        tune_entry e{};
+        while (in >> key >> e.lanes >> e.ns_per_row) {
+            if (key.compare(0, prefix.size(), prefix) == 0) {
+                g_tune[key] = e;
+            } else {
+                stale = true;
+            }
+        }
+    }
+    if (stale) {
+        // rewrite the cache with this build's lines only (a temporary file
+        // renamed over it, so a concurrent reader sees one or the other)
+        const std::string tmp = p + ".tmp" + std::to_string(static_cast<long long>(getpid()));
+        {
+            std::ofstream out(tmp, std::ios::trunc);
+            if (!out) return;
+            for (const auto &kv : g_tune) out << kv.first << ' ' << kv.second.lanes << ' ' << kv.second.ns_per_row << '\n';
+        }
+        if (std::rename(tmp.c_str(), p.c_str()) != 0) std::remove(tmp.c_str());
+    }
 }
 
 void tune_store(const std::string &key, const tune_entry &e)
@@ -223,7 +252,7 @@ int tune(pgx_context *ctx, int kind, uint64_t param, uint64_t nx, bool grad, tun
     cudaDeviceProp prop{};
     PGX_CUDA(cudaGetDeviceProperties(&prop, ctx->device));
     std::ostringstream ks;
-    ks << kind << ':' << param << ':' << nx << ':' << (grad ? 1 : 0) << ':' << prop.multiProcessorCount << ':'
+    ks << tune_key_prefix() << kind << ':' << param << ':' << nx << ':' << (grad ? 1 : 0) << ':' << prop.multiProcessorCount << ':'
        << prop.major << prop.minor;
     const std::string key = ks.str();
     {

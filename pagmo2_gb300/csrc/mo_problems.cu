@@ -26,7 +26,6 @@ using dev::fast_trig_arg;
 using dev::group_mask;
 using dev::group_sum;
 using dev::signed_const;
-using dev::sincos_2pi;
 
 // The reference's pi and pi/2 (include/pagmo/detail/constants.hpp:37-44).
 constexpr double kPi = 3.1415926535897932384626433832795028841971693993;
@@ -43,27 +42,16 @@ __device__ __forceinline__ double cos_2pi_signed(double t)
     return signed_const(c, neg);
 }
 
-// sin and cos of (pi/2) a: the quarter a/4 is exact, so sincos_2pi(a/4)
-// evaluates the exact angle. Tiny a (where a/4 would lose bits) and huge or
-// non-finite a take other routes.
+// sin and cos of the reference's argument: a * (pi/2) rounded once to a
+// double (dtlz.cpp:303-314, 332-343 and 373-384 evaluate std::cos(a *
+// detail::pi_half())), then sin and cos of that double. Evaluating the exact
+// angle instead would give cos = 0 at a = 1 where the reference has
+// cos(fl(pi/2)) = 6.1e-17: individuals at the upper bound, which the variation
+// operators produce by clamping, would then tie where the reference ranks them
+// by g, and pagmo's algorithms would take other decisions.
 __device__ __forceinline__ void sincos_half_pi(double a, double &s, double &c)
 {
-    const unsigned e = (static_cast<unsigned>(__double2hiint(a)) >> 20) & 0x7ffu;
-    if (e < 1023u - 500u) {
-        s = a * kPiHalf;
-        c = 1.0;
-        return;
-    }
-    const double q = a * 0.25;
-    if (!fast_trig_arg(q)) {
-        sincospi(a * 0.5, &s, &c);
-        return;
-    }
-    double sv, cv;
-    int sn, cn;
-    sincos_2pi(q, sv, sn, cv, cn);
-    s = signed_const(sv, sn);
-    c = signed_const(cv, cn);
+    sincos(__dmul_rn(a, kPiHalf), &s, &c);
 }
 
 template <int G>
@@ -248,8 +236,8 @@ __global__ void __launch_bounds__(256) dtlz_kernel(const double *__restrict__ x,
             double y = 0.0;
             for (uint32_t i = sub; i + 1u < m; i += G) {
                 const double xi = __ldg(xr + i);
-                double sn, cs;
-                sincos_half_pi(6.0 * xi, sn, cs); // sin(3 pi x) = sin((pi/2) 6x)
+                // dtlz.cpp:253: std::sin(3 * detail::pi() * f[i]), 3 pi rounded first
+                const double sn = sin(__dmul_rn(3. * kPi, xi));
                 y += (xi / opg) * (1.0 + sn);
                 fr[i] = xi;
             }

@@ -12,6 +12,11 @@
 
 #include "../../include/pgx.h"
 
+// Digest of the sources and flags of this build, set by the build recipe.
+#ifndef PGX_BUILD_ID
+#define PGX_BUILD_ID "unversioned"
+#endif
+
 namespace pgx
 {
 

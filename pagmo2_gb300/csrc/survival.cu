@@ -2010,17 +2010,26 @@ int read_mo_status(pgx_context *ctx, uint64_t n, uint64_t m)
 // grows context buffers on demand, so this variant instead takes its scratch
 // (order keys, the dominance bit matrix, peel state, per-objective orders)
 // from one array compiled into the library: g_noalloc_scratch, sized for at
-// most kNoAllocMaxPoints points and kNoAllocMaxObjectives objectives
-// (about 2.5 MB, held by every GPU that loads the library until the process
-// exits). Larger inputs are rejected with PGX_ERR_CAPACITY.
+// most kNoAllocMaxPoints points and kNoAllocMaxObjectives objectives (about
+// 2.5 MB). Larger inputs are rejected with PGX_ERR_CAPACITY. The array is
+// device memory of the library's survival module: a device holds it from the
+// moment that module is loaded there (at the first call on the device under
+// lazy module loading, the default) until the process exits.
 //
 // Host code cannot use the array's name as a device address (it names a host
-// stand-in), so the first call on each device looks up its address with
-// cudaGetSymbolAddress, with that device current, and caches it; the kernels
-// then receive that pointer. All calls share the one array and it keeps the
-// last call's contents: every pass clears what must start at zero itself, and
-// calls whose work overlaps on the GPU (different streams, or different host
-// threads) race on the array and must be serialised by the caller.
+// stand-in), so the first call on each device does a set-up with that device
+// current: it looks up the array's address with cudaGetSymbolAddress (which
+// loads the module, allocating the array) and loads every kernel this pass can
+// launch (cudaFuncGetAttributes), so that no later call loads code or data and
+// allocates nothing. The set-up is keyed by the device, the current CUDA
+// context and the array's address: a call in another context (a driver-API
+// context, or the primary context re-created after cudaDeviceReset) repeats
+// it. Make the first call on a device before another allocator reserves that
+// device's memory and before any stream capture. All calls share the one array
+// and it keeps the last call's contents: every pass clears what must start at
+// zero itself, and calls whose work overlaps on the GPU (different streams, or
+// different host threads) race on the array and must be serialised by the
+// caller.
 namespace pgx
 {
 namespace
@@ -2034,24 +2043,74 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[survival_scratc
                                                                                         kNoAllocMaxObjectives)];
 
 struct noalloc_device {
-    void *scratch = nullptr; // device address of g_noalloc_scratch on this device
+    void *context = nullptr; // the CUDA context the set-up ran in
+    void *scratch = nullptr; // device address of g_noalloc_scratch in that context
     int num_sms = 0;
 };
 
 std::mutex g_noalloc_lock;
 noalloc_device g_noalloc_devices[kNoAllocMaxDevices];
 
-// One-time set-up per device, run with that device current.
+// The driver's cuCtxGetCurrent, reached through the runtime (no link-time
+// dependency on the driver library); null if unavailable.
+using ctx_get_current_fn = int (*)(void **);
+ctx_get_current_fn ctx_get_current()
+{
+    static const ctx_get_current_fn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess
+            || q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<ctx_get_current_fn>(p);
+    }();
+    return fn;
+}
+
+// Loads every kernel a survival pass of at most kNoAllocMaxPoints points can
+// launch, so that none is loaded (and allocated for) at a later call.
+int noalloc_load_kernels()
+{
+    const void *kernels[] = {
+        reinterpret_cast<const void *>(init_rem_kernel),
+        reinterpret_cast<const void *>(order_keys_kernel),
+        reinterpret_cast<const void *>(dominance_sym_kernel<1>),
+        reinterpret_cast<const void *>(dominance_sym_kernel<2>),
+        reinterpret_cast<const void *>(dominance_sym_kernel<3>),
+        reinterpret_cast<const void *>(dominance_sym_kernel<4>),
+        reinterpret_cast<const void *>(dominance_kernel<0>),
+        reinterpret_cast<const void *>(row_popcount_kernel),
+        reinterpret_cast<const void *>(peel2_kernel),
+        reinterpret_cast<const void *>(peel_kernel),
+        reinterpret_cast<const void *>(front_crowding_kernel),
+        reinterpret_cast<const void *>(big_crowding_kernel),
+    };
+    for (const void *k : kernels) {
+        cudaFuncAttributes a{};
+        PGX_CUDA(cudaFuncGetAttributes(&a, k));
+    }
+    return PGX_OK;
+}
+
+// Set-up per (device, context), run with that device current.
 int noalloc_setup(int device, noalloc_device *out)
 {
     std::lock_guard<std::mutex> g(g_noalloc_lock);
     noalloc_device &d = g_noalloc_devices[device];
-    if (d.scratch == nullptr) {
-        void *p = nullptr;
-        PGX_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    void *context = nullptr;
+    if (const ctx_get_current_fn get = ctx_get_current()) {
+        if (get(&context) != 0) context = nullptr;
+    }
+    void *p = nullptr;
+    PGX_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    if (d.scratch != p || d.context != context || d.num_sms == 0) {
+        PGX_TRY(noalloc_load_kernels());
         int sms = 0;
         PGX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
         d.num_sms = sms;
+        d.context = context;
         d.scratch = p;
     }
     *out = d;

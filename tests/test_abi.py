@@ -109,3 +109,12 @@ def test_lj_encode_preserves_energy(orc):
     e = 4 * np.sum(s * s - s)
     fl, _ = orc.batch_fitness_ld(3, 12, dv[None, :])
     assert abs(fl[0] - e) <= 1e-12 * np.sum(s * s + s) * 4
+
+
+def test_build_id_is_this_builds_digest():
+    """The library reports the digest its build recipe stamped it with (the
+    autotuner's cache key starts with it)."""
+    from pagmo2_gb300 import build as B
+
+    bid = N.lib().pgx_build_id().decode()
+    assert bid == (B.OUT / "libpgx.stamp").read_text()[:16]

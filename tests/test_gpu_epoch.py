@@ -1,5 +1,7 @@
 """The fused archipelago epoch (through the C ABI) against the island-by-island
 path and the long-double oracle, including two epochs in flight."""
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -159,3 +161,37 @@ def test_gradients_written_over_their_inputs(ctx):
         ep.close()
     for (f1, g1), (f2, g2) in zip(want, got):
         assert np.array_equal(f1, f2) and np.array_equal(g1, g2)
+
+
+def test_autotune_cache_is_keyed_by_the_build(tmp_path):
+    """The autotuner's cached choices carry the library's build identity: a
+    line written by another build of the kernels is neither used nor kept (the
+    shape is re-tuned), a line of this build is used as written. Runs in a
+    fresh process, since a process loads the cache file once."""
+    import os
+    import subprocess
+    import sys
+
+    import torch
+
+    bid = N.lib().pgx_build_id().decode()
+    prop = torch.cuda.get_device_properties(0)
+    tail = f"{prop.multi_processor_count}:{prop.major}{prop.minor}"
+    stale_key = f"0123456789abcdef/{N.RASTRIGIN}:37:37:1:{tail}"
+    fresh_key = f"{bid}/{N.ROSENBROCK}:41:41:1:{tail}"
+    cache = tmp_path / "autotune.txt"
+    cache.write_text(f"{stale_key} 2 1\n{fresh_key} 4 1\n")
+    code = ("from pagmo2_gb300 import archipelago as A, _native as N\n"
+            "ep = A.Epoch([(N.RASTRIGIN, 37, 100, True), (N.ROSENBROCK, 41, 100, True)])\n"
+            "print('LANES', ep.info(0)[0], ep.info(1)[0])\n"
+            "ep.close()\n")
+    root = Path(__file__).resolve().parents[1]
+    env = dict(os.environ, PGX_AUTOTUNE_CACHE=str(cache), PYTHONPATH=str(root))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=300, cwd=root)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lanes = [int(v) for v in r.stdout.split("LANES")[1].split()]
+    assert lanes[1] == 4  # this build's cached choice
+    lines = cache.read_text().splitlines()
+    assert not any(ln.startswith("0123456789abcdef/") for ln in lines)
+    assert any(ln.startswith(f"{bid}/{N.RASTRIGIN}:37:37:1:") for ln in lines)  # re-tuned and stored
+    assert any(ln.startswith(fresh_key + " 4 ") for ln in lines)
