@@ -15,6 +15,14 @@
 // 1e-13 of the error scale), and the same decisions show that no selection
 // turned on such a difference. Exit status 0 = every case passed.
 //
+// Each run's initial population is evaluated by the run's own batch evaluator
+// (pagmo's population(problem, bfe, size, seed) constructor, same decision
+// vectors for both): NSGA-II copies offspring that neither crossover nor
+// mutation changed, and such a clone must tie with its parent. A GPU run that
+// started from parents evaluated by problem::fitness on the CPU would compare
+// GPU clones with CPU parents, whose values can differ in the last bit, and
+// pagmo's dominance test would then rank one above the other.
+//
 // Without PGX_TEST_HAVE_GPU=1 only the thread_bfe runs are made (the GPU bfe
 // is then expected to fail loudly, which the other adaptor test checks).
 #include <cmath>
@@ -46,6 +54,7 @@
 #include <pagmo/problems/zdt.hpp>
 
 #include <pagmo_gb300/gpu_bfe.hpp>
+#include <pagmo_gb300/gpu_problems.hpp>
 #include <pagmo_gb300/s11n_implement.hpp>
 
 namespace
@@ -111,9 +120,11 @@ int failures = 0;
 
 template <typename UDA, typename Make>
 void compare(const char *name, Make make, const pagmo::problem &prob, pagmo::population::size_type np,
-             unsigned pop_seed, bool have_gpu)
+             unsigned pop_seed, bool have_gpu, const pagmo::problem *prob_gpu_udp = nullptr)
 {
-    const pagmo::population pop{prob, np, pop_seed};
+    // prob_gpu_udp: the GPU run on a GPU UDP (every problem::fitness call on
+    // the GPU too) instead of on the reference's own UDP
+    const pagmo::population pop{prob, pagmo::bfe{pagmo::thread_bfe{}}, np, pop_seed};
     UDA cpu = make();
     cpu.set_verbosity(1u);
     cpu.set_bfe(pagmo::bfe{pagmo::thread_bfe{}});
@@ -127,13 +138,20 @@ void compare(const char *name, Make make, const pagmo::problem &prob, pagmo::pop
                     static_cast<unsigned long long>(p_cpu.get_problem().get_fevals()));
         return;
     }
+    const pagmo::population pop_gpu{prob_gpu_udp ? *prob_gpu_udp : prob, pagmo::bfe{pagmo_gb300::gpu_bfe{}}, np,
+                                    pop_seed};
+    if (pop_gpu.get_x() != pop.get_x()) {
+        std::printf("case %-34s initial populations differ -> FAILED\n", name);
+        ++failures;
+        return;
+    }
     UDA gpu = make();
     gpu.set_verbosity(1u);
     gpu.set_bfe(pagmo::bfe{pagmo_gb300::gpu_bfe{}});
     pagmo::population p_gpu;
     {
         Quiet q;
-        p_gpu = gpu.evolve(pop);
+        p_gpu = gpu.evolve(pop_gpu);
     }
     Diff log_d, f_d;
     const auto &l1 = cpu.get_log();
@@ -207,6 +225,11 @@ int main()
     compare<nspso>("nspso dtlz2(12,3) 24x10",
                    [] { return nspso{10u, 0.6, 2.0, 2.0, 1.0, 0.5, 60u, "crowding distance", false, 23u}; },
                    problem{dtlz{2u, 12u, 3u}}, 24u, 32u, have_gpu);
+    {
+        const problem gp{pagmo_gb300::gpu_dtlz{2u, 12u, 3u}};
+        compare<nsga2>("nsga2 gpu_dtlz2(12,3) UDP 92x30", [] { return nsga2{30u, 0.95, 10., 0.01, 50., 11u}; },
+                       problem{dtlz{2u, 12u, 3u}}, 92u, 12u, have_gpu, &gp);
+    }
     compare<maco>("maco dtlz1(10,2) 43x10", [] { return maco{10u, 43u, 1.0, 1u, 7u, 100000u, 0., false, 23u}; },
                   problem{dtlz{1u, 10u, 2u}}, 43u, 32u, have_gpu);
     // PSO (generational) and GACO: single objective, the three hot-path UDPs
