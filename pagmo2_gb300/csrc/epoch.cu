@@ -65,10 +65,14 @@ __device__ __forceinline__ void tile_rows(const tile_desc &d)
             const double *xr = d.x + static_cast<uint64_t>(r) * d.nx;
             double *gr = GRAD ? d.g + static_cast<uint64_t>(r) * d.nx : nullptr;
             double *fo = d.f + r;
-            if (d.kind == PGX_RASTRIGIN)
-                rastrigin_row<G, GRAD>(xr, d.nx, fo, gr);
-            else
-                rosenbrock_row<G, GRAD>(xr, d.nx, fo, gr);
+            if constexpr (G >= 4) {
+                if (d.kind == PGX_RASTRIGIN) {
+                    rastrigin_row<G, GRAD>(xr, d.nx, fo, gr);
+                    continue;
+                }
+            }
+            // rastrigin tiles never take fewer than 4 lanes (the plan's choice)
+            rosenbrock_row<G, GRAD>(xr, d.nx, fo, gr);
         }
     }
 }
@@ -294,9 +298,12 @@ int tune(pgx_context *ctx, int kind, uint64_t param, uint64_t nx, bool grad, tun
         if (kind == PGX_LENNARD_JONES) {
             cands.push_back(32);
         } else {
-            cands.push_back(lanes_per_row(static_cast<uint32_t>(nx)));
+            const int own = lanes_per_row(static_cast<uint32_t>(nx));
+            // rastrigin rows take 4 to 32 lanes, with identical results for each
+            cands.push_back(kind == PGX_RASTRIGIN && own < 4 ? 4 : own);
             for (int g : {32, 16, 8, 4})
-                if (static_cast<uint64_t>(g) <= nx && std::find(cands.begin(), cands.end(), g) == cands.end())
+                if ((static_cast<uint64_t>(g) <= nx || kind == PGX_RASTRIGIN)
+                    && std::find(cands.begin(), cands.end(), g) == cands.end())
                     cands.push_back(g);
             if (kind == PGX_ROSENBROCK && nx % 4 == 0 && nx >= 128) cands.push_back(0);
         }

@@ -166,8 +166,13 @@ int launch_rows(int kind, bool grad, const double *x, uint64_t n, uint32_t nx, d
     constexpr int pb = G; // lanes per row
     switch (kind) {
         case PGX_RASTRIGIN:
-            return grad ? launch_simple(rastrigin_kernel<G, true>, pb, x, n, nx, f, g, s, num_sms)
-                        : launch_simple(rastrigin_kernel<G, false>, pb, x, n, nx, f, g, s, num_sms);
+            if constexpr (G >= 4) {
+                return grad ? launch_simple(rastrigin_kernel<G, true>, pb, x, n, nx, f, g, s, num_sms)
+                            : launch_simple(rastrigin_kernel<G, false>, pb, x, n, nx, f, g, s, num_sms);
+            } else {
+                set_error("rastrigin rows take 4, 8, 16 or 32 lanes");
+                return PGX_ERR_INVALID;
+            }
         case PGX_ROSENBROCK:
             return grad ? launch_simple(rosenbrock_kernel<G, true>, pb, x, n, nx, f, g, s, num_sms)
                         : launch_simple(rosenbrock_kernel<G, false>, pb, x, n, nx, f, g, s, num_sms);
@@ -264,7 +269,9 @@ int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64
                || kind == PGX_SCHWEFEL) {
         PGX_CHECK(!grad || kind <= PGX_ROSENBROCK, PGX_ERR_NOTIMPL,
                   "The gradient has been requested but it is not implemented in the UDP");
-        switch (lanes_per_row(nx32)) {
+        const int lanes = kind == PGX_RASTRIGIN ? dev::rastrigin_lanes(lanes_per_row(nx32), n, num_sms)
+                                                : lanes_per_row(nx32);
+        switch (lanes) {
             case 32: st = launch_rows<32>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;
             case 16: st = launch_rows<16>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;
             case 8: st = launch_rows<8>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;

@@ -183,50 +183,124 @@ __device__ __forceinline__ double twice_exact(double x)
     return (b << 1) == 0 ? x : __longlong_as_double(b + (1LL << 52));
 }
 
+// One element's contribution: x^2 into sx, cos(2 pi x) into sc and, with the
+// gradient, g = 2x + 10 omega sin(2 pi x) stored.
+template <bool GRAD>
+__device__ __forceinline__ void rastrigin_element(double xi, isum::sq_acc &sx, double &sc, double *gi)
+{
+    isum::add_square(sx, xi);
+    if (trigfx::in_range(xi)) {
+        if (GRAD) {
+            double s, c;
+            trigfx::sincos_2pi(xi, s, c);
+            sc += c;
+            *gi = fma(k10Omega, s, twice_exact(xi));
+        } else {
+            sc += trigfx::cos_2pi(xi);
+        }
+        return;
+    }
+    double s = 0.0, c;
+    int s_neg = 0, c_neg = 0;
+    if (fast_trig_arg(xi)) {
+        if (GRAD)
+            sincos_2pi(xi, s, s_neg, c, c_neg);
+        else
+            c = cos_2pi(xi, c_neg);
+    } else {
+        if (GRAD)
+            sincospi(xi + xi, &s, &c);
+        else
+            c = cospi(xi + xi);
+    }
+    sc = fma(c, unit_sign(c_neg), sc);
+    if (GRAD) *gi = fma(signed_const(k10Omega, s_neg), s, xi + xi);
+}
+
+// A row's two sums in one fixed order, whatever the number of lanes G that
+// evaluates it (G = 4, 8, 16 or 32): element i belongs to virtual lane
+// v = i mod 32, each virtual lane sums its elements in index order, and the 32
+// partial sums are combined by the butterfly of a 32-lane xor reduction
+// (offsets 16, 8, 4, 2, 1; each step adds the partner's sum to one's own).
+// Lane `sub` of a group holds the J = 32/G virtual lanes sub + G j: the
+// butterfly's steps with offsets >= G pair them inside the thread (offset
+// G h joins j and j + h), the others cross the group by shuffles. Inside the
+// thread the virtual lanes are visited in bit-reversed order of j and merged
+// like a binary counter, which adds exactly the butterfly's pairs while at
+// most log2(J) + 1 partial sums are live. Empty virtual lanes (v >= nx) hold
+// +0, which every step adds exactly. The result is therefore bit-identical
+// for every G, and the number of lanes can follow the batch size (many per
+// row for small batches) without changing any value.
+struct rastrigin_part {
+    isum::sq_acc sx; // sum of x^2 (flags kept apart: OR-ed, order-free)
+    double sc;       // sum of cos(2 pi x)
+};
+
+__device__ __forceinline__ void rastrigin_join(rastrigin_part &a, const rastrigin_part &b)
+{
+    isum::add(a.sx, isum::sq_term{b.sx.m, b.sx.e});
+    a.sc = a.sc + b.sc;
+}
+
+template <int J>
+__device__ __forceinline__ constexpr int bit_reverse(int t)
+{
+    int r = 0;
+    for (int b = 1; b < J; b <<= 1) r = (r << 1) | ((t & b) ? 1 : 0);
+    return r;
+}
+
 template <int G, bool GRAD>
 __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uint32_t nx, double *f_out,
                                               double *__restrict__ gr)
 {
+    static_assert(G >= 4 && G <= 32 && (G & (G - 1)) == 0, "rastrigin rows take 4, 8, 16 or 32 lanes");
+    constexpr int J = 32 / G;
+    constexpr int D = J == 1 ? 1 : (J == 2 ? 2 : (J == 4 ? 3 : 4)); // log2(J) + 1
     const unsigned sub = threadIdx.x & (G - 1);
     const unsigned mask = group_mask<G>();
-    isum::sq_acc sx = isum::make();
-    double sc = 0.0;
-    // the next element's load is issued before this one's arithmetic
-    double xn = sub < nx ? __ldg(xr + sub) : 0.0;
-    for (uint32_t i = sub; i < nx; i += G) {
-        const double xi = xn;
-        if (i + G < nx) xn = __ldg(xr + i + G);
-        isum::add_square(sx, xi);
-        if (trigfx::in_range(xi)) {
-            if (GRAD) {
-                double s, c;
-                trigfx::sincos_2pi(xi, s, c);
-                sc += c;
-                gr[i] = fma(k10Omega, s, twice_exact(xi));
-            } else {
-                sc += trigfx::cos_2pi(xi);
-            }
-            continue;
+    uint32_t flags = 0u;
+    rastrigin_part stack[D];
+#pragma unroll
+    for (int t = 0; t < J; ++t) {
+        const uint32_t v = sub + static_cast<uint32_t>(G * bit_reverse<J>(t));
+        rastrigin_part a{isum::make(), 0.0};
+        // virtual lane v: elements v, v + 32, ... in order; the next load is
+        // issued before this element's arithmetic
+        double xn = v < nx ? __ldg(xr + v) : 0.0;
+        for (uint32_t i = v; i < nx; i += 32u) {
+            const double xi = xn;
+            if (i + 32u < nx) xn = __ldg(xr + i + 32u);
+            rastrigin_element<GRAD>(xi, a.sx, a.sc, GRAD ? gr + i : nullptr);
         }
-        double s = 0.0, c;
-        int s_neg = 0, c_neg = 0;
-        if (fast_trig_arg(xi)) {
-            if (GRAD)
-                sincos_2pi(xi, s, s_neg, c, c_neg);
-            else
-                c = cos_2pi(xi, c_neg);
-        } else {
-            if (GRAD)
-                sincospi(xi + xi, &s, &c);
-            else
-                c = cospi(xi + xi);
+        flags |= a.sx.flags;
+        // binary-counter merge: t's trailing ones are the completed pairs
+        int level = 0;
+#pragma unroll
+        for (int k = t; k & 1; k >>= 1) {
+            rastrigin_join(stack[level], a);
+            a = stack[level];
+            ++level;
         }
-        sc = fma(c, unit_sign(c_neg), sc);
-        if (GRAD) gr[i] = fma(signed_const(k10Omega, s_neg), s, xi + xi);
+        stack[level] = a;
     }
-    const double sxv = isum::value(group_isum<G>(sx, mask));
-    sc = group_sum<G>(sc, mask);
-    if (sub == 0 && f_out) *f_out = fma(-10.0, sc, sxv) + 10.0 * static_cast<double>(nx);
+    rastrigin_part r = stack[D - 1];
+    r.sx.flags = flags;
+    // offsets G/2 .. 1 across the group
+    const double sxv = isum::value(group_isum<G>(r.sx, mask));
+    const double scv = group_sum<G>(r.sc, mask);
+    if (sub == 0 && f_out) *f_out = fma(-10.0, scv, sxv) + 10.0 * static_cast<double>(nx);
+}
+
+// Lanes per rastrigin row: the group the dimension alone would take (at least
+// 4), widened for batches too small to fill the device, as long as all rows'
+// lanes fit on it at once (2048 threads per SM). Results do not depend on it.
+__host__ __device__ inline int rastrigin_lanes(int lanes_for_dim, uint64_t n, int num_sms)
+{
+    int g = lanes_for_dim < 4 ? 4 : (lanes_for_dim > 32 ? 32 : lanes_for_dim);
+    const uint64_t cap = static_cast<uint64_t>(num_sms > 0 ? num_sms : 1) * 2048u;
+    while (g < 32 && n * static_cast<uint64_t>(2 * g) <= cap) g *= 2;
+    return g;
 }
 
 // ----------------------------------------------------------------- rosenbrock

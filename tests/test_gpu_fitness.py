@@ -107,6 +107,23 @@ def test_lennard_jones_atoms(ctx, orc, atoms):
     check_against_oracle(orc, ctx, N.LENNARD_JONES, atoms, W.lj_lattice_batch(n // 2 + 1, atoms, seed=atoms))
 
 
+@pytest.mark.parametrize("dim", [3, 7, 20, 50, 100])
+def test_rastrigin_rows_do_not_depend_on_the_batch(ctx, dim):
+    """A rastrigin row gives bit-identical fitness and gradient whatever batch
+    it is evaluated in: small batches take 32 lanes per row, larger ones 16, 8
+    or 4 (rows of 1 to 262144 here), and every lane count sums a row in the
+    same order. The fitness-only kernel gives the same fitness too."""
+    x = W.uniform_batch(N.RASTRIGIN, dim, 262144, seed=100 + dim)
+    udp = P.rastrigin(dim, ctx)
+    f_all, g_all = udp.batch_gradient(x)
+    assert np.array_equal(udp.batch_fitness(x), f_all)
+    for n in (1, 100, 4096, 10000, 20000, 65536):
+        f, g = udp.batch_gradient(x[:n])
+        assert np.array_equal(f, f_all[:n]), (dim, n)
+        assert np.array_equal(g, g_all[:n]), (dim, n)
+        assert np.array_equal(udp.batch_fitness(x[:n]), f_all[:n]), (dim, n)
+
+
 def test_config1_rastrigin_full(ctx, orc):
     x = W.rastrigin_batch()  # 4096 x 50, the reference's CPU-runnable case
     f, g = check_against_oracle(orc, ctx, N.RASTRIGIN, 50, x)
