@@ -49,7 +49,17 @@ struct tile_desc {
     double *g; // null: fitness only
     uint32_t rows, nx, param;
     uint8_t kind, lanes, variant, ma;
+    uint8_t width; // rastrigin: the canonical width of its rows (dev::rastrigin_width)
 };
+
+// rastrigin rows of width V on G lanes; only the pairs the plan gives (at most
+// two virtual lanes per physical lane, which keeps the kernel's registers) are
+// compiled into the epoch kernel
+template <int V, int G, bool GRAD>
+__device__ __forceinline__ void tile_rastrigin_row(const double *xr, uint32_t nx, double *fo, double *gr)
+{
+    if constexpr (G >= 4 && G <= V && V / G <= 2) rastrigin_row<V, G, GRAD>(xr, nx, fo, gr);
+}
 
 constexpr int kWarpsPerBlock = 4;
 constexpr int kSets = 3; // pinned staging sets: packing of later epochs never waits for the GPU
@@ -65,13 +75,14 @@ __device__ __forceinline__ void tile_rows(const tile_desc &d)
             const double *xr = d.x + static_cast<uint64_t>(r) * d.nx;
             double *gr = GRAD ? d.g + static_cast<uint64_t>(r) * d.nx : nullptr;
             double *fo = d.f + r;
-            if constexpr (G >= 4) {
-                if (d.kind == PGX_RASTRIGIN) {
-                    rastrigin_row<G, GRAD>(xr, d.nx, fo, gr);
-                    continue;
+            if (d.kind == PGX_RASTRIGIN) {
+                switch (d.width) {
+                    case 8: tile_rastrigin_row<8, G, GRAD>(xr, d.nx, fo, gr); break;
+                    case 16: tile_rastrigin_row<16, G, GRAD>(xr, d.nx, fo, gr); break;
+                    default: tile_rastrigin_row<32, G, GRAD>(xr, d.nx, fo, gr); break;
                 }
+                continue;
             }
-            // rastrigin tiles never take fewer than 4 lanes (the plan's choice)
             rosenbrock_row<G, GRAD>(xr, d.nx, fo, gr);
         }
     }
@@ -299,12 +310,18 @@ int tune(pgx_context *ctx, int kind, uint64_t param, uint64_t nx, bool grad, tun
             cands.push_back(32);
         } else {
             const int own = lanes_per_row(static_cast<uint32_t>(nx));
-            // rastrigin rows take 4 to 32 lanes, with identical results for each
-            cands.push_back(kind == PGX_RASTRIGIN && own < 4 ? 4 : own);
-            for (int g : {32, 16, 8, 4})
-                if ((static_cast<uint64_t>(g) <= nx || kind == PGX_RASTRIGIN)
-                    && std::find(cands.begin(), cands.end(), g) == cands.end())
-                    cands.push_back(g);
+            if (kind == PGX_RASTRIGIN) {
+                // the dimension's lanes (at least 4) and the full width: the
+                // pairs the epoch kernel holds, with identical results
+                const int v = dev::rastrigin_width(own);
+                cands.push_back(own < 4 ? 4 : (own > v ? v : own));
+                if (cands[0] != v) cands.push_back(v);
+            } else {
+                cands.push_back(own);
+                for (int g : {32, 16, 8, 4})
+                    if (static_cast<uint64_t>(g) <= nx && std::find(cands.begin(), cands.end(), g) == cands.end())
+                        cands.push_back(g);
+            }
             if (kind == PGX_ROSENBROCK && nx % 4 == 0 && nx >= 128) cands.push_back(0);
         }
         tune_entry best{cands[0], 1e30};
@@ -685,6 +702,11 @@ int build_plan(pgx_epoch *ep, const pgx_request *reqs, int n_reqs)
             } else {
                 d.variant = kRows;
                 d.lanes = static_cast<uint8_t>(p.tune.lanes);
+                if (p.kind == PGX_RASTRIGIN) {
+                    d.width = static_cast<uint8_t>(dev::rastrigin_width(lanes_per_row(d.nx)));
+                    PGX_CHECK(d.lanes >= 4 && d.lanes <= d.width && d.width <= 2 * d.lanes, PGX_ERR_INVALID,
+                              "rastrigin epoch tile: unsupported lane count");
+                }
             }
             td[t] = d;
         }

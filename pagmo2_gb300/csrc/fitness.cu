@@ -33,13 +33,13 @@ namespace
 
 using namespace dev;
 
-template <int G, bool GRAD>
+template <int V, int G, bool GRAD>
 __global__ void __launch_bounds__(256) rastrigin_kernel(const double *__restrict__ x, uint64_t n, uint32_t nx,
                                                         double *__restrict__ f, double *__restrict__ g)
 {
     const uint64_t stride = static_cast<uint64_t>(gridDim.x) * (blockDim.x / G);
     for (uint64_t row = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / G; row < n; row += stride)
-        rastrigin_row<G, GRAD>(x + row * nx, nx, f ? f + row : nullptr, GRAD ? g + row * nx : nullptr);
+        rastrigin_row<V, G, GRAD>(x + row * nx, nx, f ? f + row : nullptr, GRAD ? g + row * nx : nullptr);
 }
 
 template <int G, bool GRAD>
@@ -165,14 +165,6 @@ int launch_rows(int kind, bool grad, const double *x, uint64_t n, uint32_t nx, d
 {
     constexpr int pb = G; // lanes per row
     switch (kind) {
-        case PGX_RASTRIGIN:
-            if constexpr (G >= 4) {
-                return grad ? launch_simple(rastrigin_kernel<G, true>, pb, x, n, nx, f, g, s, num_sms)
-                            : launch_simple(rastrigin_kernel<G, false>, pb, x, n, nx, f, g, s, num_sms);
-            } else {
-                set_error("rastrigin rows take 4, 8, 16 or 32 lanes");
-                return PGX_ERR_INVALID;
-            }
         case PGX_ROSENBROCK:
             return grad ? launch_simple(rosenbrock_kernel<G, true>, pb, x, n, nx, f, g, s, num_sms)
                         : launch_simple(rosenbrock_kernel<G, false>, pb, x, n, nx, f, g, s, num_sms);
@@ -182,6 +174,34 @@ int launch_rows(int kind, bool grad, const double *x, uint64_t n, uint32_t nx, d
             return launch_simple(row_f_kernel<G, PGX_GRIEWANK>, pb, x, n, nx, f, nullptr, s, num_sms);
         default:
             return launch_simple(row_f_kernel<G, PGX_SCHWEFEL>, pb, x, n, nx, f, nullptr, s, num_sms);
+    }
+}
+
+template <int V, int G>
+int launch_rastrigin_vg(bool grad, const double *x, uint64_t n, uint32_t nx, double *f, double *g, cudaStream_t s,
+                        int num_sms)
+{
+    return grad ? launch_simple(rastrigin_kernel<V, G, true>, G, x, n, nx, f, g, s, num_sms)
+                : launch_simple(rastrigin_kernel<V, G, false>, G, x, n, nx, f, g, s, num_sms);
+}
+
+// rastrigin rows of canonical width V (8, 16, 32) on G lanes (4 <= G <= V)
+int launch_rastrigin(int V, int G, bool grad, const double *x, uint64_t n, uint32_t nx, double *f, double *g,
+                     cudaStream_t s, int num_sms)
+{
+    switch (V * 64 + G) {
+        case 8 * 64 + 4: return launch_rastrigin_vg<8, 4>(grad, x, n, nx, f, g, s, num_sms);
+        case 8 * 64 + 8: return launch_rastrigin_vg<8, 8>(grad, x, n, nx, f, g, s, num_sms);
+        case 16 * 64 + 4: return launch_rastrigin_vg<16, 4>(grad, x, n, nx, f, g, s, num_sms);
+        case 16 * 64 + 8: return launch_rastrigin_vg<16, 8>(grad, x, n, nx, f, g, s, num_sms);
+        case 16 * 64 + 16: return launch_rastrigin_vg<16, 16>(grad, x, n, nx, f, g, s, num_sms);
+        case 32 * 64 + 4: return launch_rastrigin_vg<32, 4>(grad, x, n, nx, f, g, s, num_sms);
+        case 32 * 64 + 8: return launch_rastrigin_vg<32, 8>(grad, x, n, nx, f, g, s, num_sms);
+        case 32 * 64 + 16: return launch_rastrigin_vg<32, 16>(grad, x, n, nx, f, g, s, num_sms);
+        case 32 * 64 + 32: return launch_rastrigin_vg<32, 32>(grad, x, n, nx, f, g, s, num_sms);
+        default:
+            set_error("rastrigin rows: " + std::to_string(G) + " lanes for width " + std::to_string(V));
+            return PGX_ERR_INVALID;
     }
 }
 
@@ -269,9 +289,14 @@ int launch_eval(int kind, uint64_t param, uint64_t nx, const double *d_x, uint64
                || kind == PGX_SCHWEFEL) {
         PGX_CHECK(!grad || kind <= PGX_ROSENBROCK, PGX_ERR_NOTIMPL,
                   "The gradient has been requested but it is not implemented in the UDP");
-        const int lanes = kind == PGX_RASTRIGIN ? dev::rastrigin_lanes(lanes_per_row(nx32), n, num_sms)
-                                                : lanes_per_row(nx32);
-        switch (lanes) {
+        if (kind == PGX_RASTRIGIN) {
+            const int own = lanes_per_row(nx32);
+            st = launch_rastrigin(dev::rastrigin_width(own), dev::rastrigin_lanes(own, n, num_sms), grad, d_x, n, nx32,
+                                  d_f, d_g, stream, num_sms);
+            if (st == PGX_OK && launches) ++*launches;
+            return st;
+        }
+        switch (lanes_per_row(nx32)) {
             case 32: st = launch_rows<32>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;
             case 16: st = launch_rows<16>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;
             case 8: st = launch_rows<8>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms); break;
@@ -326,6 +351,9 @@ int launch_rows_variant(int kind, uint64_t nx, const double *d_x, uint64_t n, do
         return grad ? launch_simple(rosenbrock_v4_kernel<true>, 32, d_x, n, nx32, d_f, d_g, stream, num_sms)
                     : launch_simple(rosenbrock_v4_kernel<false>, 32, d_x, n, nx32, d_f, d_g, stream, num_sms);
     }
+    if (kind == PGX_RASTRIGIN)
+        return launch_rastrigin(dev::rastrigin_width(lanes_per_row(nx32)), lanes, grad, d_x, n, nx32, d_f, d_g, stream,
+                                num_sms);
     switch (lanes) {
         case 32: return launch_rows<32>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);
         case 16: return launch_rows<16>(kind, grad, d_x, n, nx32, d_f, d_g, stream, num_sms);

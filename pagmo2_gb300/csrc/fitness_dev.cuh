@@ -218,21 +218,19 @@ __device__ __forceinline__ void rastrigin_element(double xi, isum::sq_acc &sx, d
 }
 
 // A row's two sums in one fixed order, whatever the number of lanes G that
-// evaluates it (G = 4, 8, 16 or 32): element i belongs to virtual lane
-// v = i mod 32, each virtual lane sums its elements in index order, and the 32
-// partial sums are combined by the butterfly of a 32-lane xor reduction
-// (offsets 16, 8, 4, 2, 1; each step adds the partner's sum to one's own).
-// Lane `sub` of a group holds the J = 32/G virtual lanes sub + G j: the
-// butterfly's steps with offsets >= G pair them inside the thread (offset
-// G h joins j and j + h), the others cross the group by shuffles. Inside the
-// thread the virtual lanes are visited in bit-reversed order of j and merged
-// like a binary counter, which adds exactly the butterfly's pairs while at
-// most log2(J) + 1 partial sums are live. Empty virtual lanes (v >= nx) hold
-// +0, which every step adds exactly. The result is therefore bit-identical
-// for every G, and the number of lanes can follow the batch size (many per
-// row for small batches) without changing any value.
+// evaluates it: element i belongs to virtual lane v = i mod V, each virtual
+// lane sums its elements in index order, and the V partial sums are combined
+// by the butterfly of a V-lane xor reduction (offsets V/2, ..., 1; each step
+// adds the partner's sum to one's own). V depends on the dimension only
+// (rastrigin_width). Lane `sub` of a group of G | V lanes holds the J = V/G
+// virtual lanes sub + G j: the butterfly's steps with offsets >= G join them
+// inside the thread (offset G h joins j and j + h), the others cross the group
+// by shuffles. Empty virtual lanes (v >= nx) hold +0, which every step adds
+// exactly. The result is therefore bit-identical for every G, and the number
+// of lanes follows the batch size (more per row for small batches) without
+// changing any value.
 struct rastrigin_part {
-    isum::sq_acc sx; // sum of x^2 (flags kept apart: OR-ed, order-free)
+    isum::sq_acc sx; // sum of x^2 (its flags are OR-ed apart: order-free)
     double sc;       // sum of cos(2 pi x)
 };
 
@@ -242,65 +240,63 @@ __device__ __forceinline__ void rastrigin_join(rastrigin_part &a, const rastrigi
     a.sc = a.sc + b.sc;
 }
 
-template <int J>
-__device__ __forceinline__ constexpr int bit_reverse(int t)
-{
-    int r = 0;
-    for (int b = 1; b < J; b <<= 1) r = (r << 1) | ((t & b) ? 1 : 0);
-    return r;
-}
-
-template <int G, bool GRAD>
+template <int V, int G, bool GRAD>
 __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uint32_t nx, double *f_out,
                                               double *__restrict__ gr)
 {
-    static_assert(G >= 4 && G <= 32 && (G & (G - 1)) == 0, "rastrigin rows take 4, 8, 16 or 32 lanes");
-    constexpr int J = 32 / G;
-    constexpr int D = J == 1 ? 1 : (J == 2 ? 2 : (J == 4 ? 3 : 4)); // log2(J) + 1
+    static_assert(G >= 4 && G <= V && V <= 32 && (G & (G - 1)) == 0 && (V & (V - 1)) == 0,
+                  "rastrigin rows: 4 <= G <= V <= 32, powers of two");
+    constexpr int J = V / G;
     const unsigned sub = threadIdx.x & (G - 1);
     const unsigned mask = group_mask<G>();
-    uint32_t flags = 0u;
-    rastrigin_part stack[D];
+    rastrigin_part acc[J];
 #pragma unroll
-    for (int t = 0; t < J; ++t) {
-        const uint32_t v = sub + static_cast<uint32_t>(G * bit_reverse<J>(t));
-        rastrigin_part a{isum::make(), 0.0};
-        // virtual lane v: elements v, v + 32, ... in order; the next load is
-        // issued before this element's arithmetic
-        double xn = v < nx ? __ldg(xr + v) : 0.0;
-        for (uint32_t i = v; i < nx; i += 32u) {
+    for (int j = 0; j < J; ++j) acc[j] = rastrigin_part{isum::make(), 0.0};
+    // chunks of V elements; the next element's load is issued before this
+    // one's arithmetic
+    double xn = sub < nx ? __ldg(xr + sub) : 0.0;
+    for (uint32_t base = 0; base < nx; base += V) {
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+            const uint32_t i = base + sub + static_cast<uint32_t>(G * j);
             const double xi = xn;
-            if (i + 32u < nx) xn = __ldg(xr + i + 32u);
-            rastrigin_element<GRAD>(xi, a.sx, a.sc, GRAD ? gr + i : nullptr);
+            const uint32_t inext = j + 1 < J ? i + G : base + V + sub;
+            if (inext < nx) xn = __ldg(xr + inext);
+            if (i < nx) rastrigin_element<GRAD>(xi, acc[j].sx, acc[j].sc, GRAD ? gr + i : nullptr);
         }
-        flags |= a.sx.flags;
-        // binary-counter merge: t's trailing ones are the completed pairs
-        int level = 0;
-#pragma unroll
-        for (int k = t; k & 1; k >>= 1) {
-            rastrigin_join(stack[level], a);
-            a = stack[level];
-            ++level;
-        }
-        stack[level] = a;
     }
-    rastrigin_part r = stack[D - 1];
-    r.sx.flags = flags;
-    // offsets G/2 .. 1 across the group
-    const double sxv = isum::value(group_isum<G>(r.sx, mask));
-    const double scv = group_sum<G>(r.sc, mask);
+    uint32_t flags = 0u;
+#pragma unroll
+    for (int j = 0; j < J; ++j) flags |= acc[j].sx.flags;
+#pragma unroll
+    for (int h = J / 2; h >= 1; h >>= 1) {
+#pragma unroll
+        for (int j = 0; j < h; ++j) rastrigin_join(acc[j], acc[j + h]);
+    }
+    acc[0].sx.flags = flags;
+    const double sxv = isum::value(group_isum<G>(acc[0].sx, mask));
+    const double scv = group_sum<G>(acc[0].sc, mask);
     if (sub == 0 && f_out) *f_out = fma(-10.0, scv, sxv) + 10.0 * static_cast<double>(nx);
 }
 
-// Lanes per rastrigin row: the group the dimension alone would take (at least
-// 4), widened for batches too small to fill the device, as long as all rows'
-// lanes fit on it at once (2048 threads per SM). Results do not depend on it.
+// The canonical width V of a rastrigin row, from its dimension alone: the
+// lanes the dimension would take by itself (lanes_for_dim) when that is 16 or
+// 32, else 8.
+__host__ __device__ inline int rastrigin_width(int lanes_for_dim)
+{
+    return lanes_for_dim >= 16 ? (lanes_for_dim >= 32 ? 32 : 16) : 8;
+}
+
+// Lanes per rastrigin row for a batch of n rows: all V for batches of at most
+// one 256-thread block's worth of lanes per SM (latency-bound: shorter chains
+// per lane), else the dimension's own choice (at least 4). Results do not
+// depend on it.
 __host__ __device__ inline int rastrigin_lanes(int lanes_for_dim, uint64_t n, int num_sms)
 {
-    int g = lanes_for_dim < 4 ? 4 : (lanes_for_dim > 32 ? 32 : lanes_for_dim);
-    const uint64_t cap = static_cast<uint64_t>(num_sms > 0 ? num_sms : 1) * 2048u;
-    while (g < 32 && n * static_cast<uint64_t>(2 * g) <= cap) g *= 2;
-    return g;
+    const int v = rastrigin_width(lanes_for_dim);
+    const uint64_t cap = static_cast<uint64_t>(num_sms > 0 ? num_sms : 1) * 256u;
+    if (n * static_cast<uint64_t>(v) <= cap) return v;
+    return lanes_for_dim < 4 ? 4 : (lanes_for_dim > v ? v : lanes_for_dim);
 }
 
 // ----------------------------------------------------------------- rosenbrock
