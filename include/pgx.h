@@ -362,6 +362,45 @@ PGX_API void pgx_epoch_destroy(pgx_epoch *ep);
    NULL). */
 PGX_API int pgx_requests_run_plain(pgx_context *ctx, const pgx_request *reqs, int n_reqs);
 
+/* ------------------------------------------------ batched local refinement */
+
+/* Parameters of pgx_refine_batch (see there). */
+typedef struct pgx_refine_params {
+    uint32_t hops;   /* at most this many perturb-and-descend trials per individual */
+    uint32_t stop;   /* an individual's chain ends after this many trials in a row without improvement
+                        (mbh's stop, src/algorithms/mbh.cpp:150-190) */
+    uint32_t steps;  /* projected-gradient steps per trial */
+    double perturb;  /* perturbation half-width as a fraction of (ub - lb), in ]0, 1] (mbh's perturb) */
+    double step0;    /* first step length of a descent, in box-scaled units, in ]0, 1] */
+    double step_min; /* a descent ends when its step length falls below this (0 < step_min <= step0) */
+    uint64_t seed;   /* the perturbations are a function of (seed, individual, trial, coordinate) */
+} pgx_refine_params;
+
+/* Monotonic basin hopping on every individual of a batch at once, with the
+   batched adjoint driving a projected-gradient local descent: the scheme of
+   mbh::evolve (src/algorithms/mbh.cpp:102-200) applied to each individual as
+   its own chain, with gradient descent as the inner optimiser (mbh takes a
+   pagmo algorithm and accepts a whole population when its best improves; it
+   has no batched counterpart). Per individual, starting from its decision
+   vector x_best: each trial perturbs x_best uniformly within
+   [max(x - perturb (ub - lb), lb), min(x + perturb (ub - lb), ub)] per
+   coordinate, takes up to `steps` steps x <- clamp(x - eta s d / |d|, lb, ub)
+   with s = ub - lb and d = s * gradient (a step is kept when it lowers the
+   fitness, eta then doubling up to 1, else eta halves; the descent ends when
+   eta < step_min), and replaces x_best when it ends lower. Kinds with a
+   gradient only (rastrigin, rosenbrock, lennard_jones; else PGX_ERR_NOTIMPL).
+   dvs (n_dvs x nx) is overwritten with the best points, fvs (n_dvs) receives
+   their fitness, *evals (nullable) the number of fitness + gradient
+   evaluations made. Synchronous. */
+PGX_API int pgx_refine_batch(pgx_context *ctx, int kind, uint64_t param, const pgx_refine_params *params, double *dvs,
+                             uint64_t n_dvs, double *fvs, uint64_t *evals);
+
+/* The same on device buffers, asynchronous on `stream`: *d_evals (device,
+   zeroed by the caller) accumulates the evaluations. */
+PGX_API int pgx_refine_batch_device(pgx_context *ctx, int kind, uint64_t param, const pgx_refine_params *params,
+                                    double *d_dvs, uint64_t n_dvs, double *d_fvs, unsigned long long *d_evals,
+                                    void *stream);
+
 /* ------------------------------------------------------------ measurement */
 
 /* FP64 FMA throughput of the device in GFLOP/s (FMA = 2 flops), measured by a

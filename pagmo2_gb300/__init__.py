@@ -14,9 +14,12 @@ plugin interface for the batch-fitness path:
   multi_objective:  fast_non_dominated_sorting, crowding_distance,
                     nsga2_survival, select_best_N_mo, sort_population_mo,
                     hypervolume (2 or 3 objectives)
+  algorithms:       gpu_mbh (monotonic basin hopping with gradient descent on
+                    every individual of a batch at once)
   workloads:        seeded synthetic inputs
 """
 from ._native import Context, default_context  # noqa: F401
+from .algorithms import gpu_mbh  # noqa: F401
 from .batch_evaluators import bfe, gpu_bfe, problem  # noqa: F401
 from .multi_objective import (crowding_distance, fast_non_dominated_sorting, hypervolume,  # noqa: F401
                               nsga2_survival, select_best_N_mo, sort_population_mo)

@@ -45,6 +45,8 @@ SIGNATURES = {
     "pgx_nsga2_survival": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp]),
     "pgx_nsga2_survival_device": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "pgx_measure_fp64_peak": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "pgx_refine_batch": (C.c_int, [_vp, C.c_int, _u64, _vp, _vp, _u64, _vp, _vp]),
+    "pgx_refine_batch_device": (C.c_int, [_vp, C.c_int, _u64, _vp, _vp, _u64, _vp, _vp, _vp]),
     "pgx_nsga2_survival_device_noalloc": (C.c_int, [_vp, _u64, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "pgx_epoch_create": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(_vp)]),
     "pgx_epoch_run": (C.c_int, [_vp, _vp]),
@@ -76,6 +78,12 @@ class pgx_mo_problem(C.Structure):
     """struct pgx_mo_problem of include/pgx.h: zdt(prob_id, param) or dtlz(prob_id, dim=param, fdim, alpha)."""
     _fields_ = [("kind", C.c_int), ("prob_id", C.c_uint32), ("param", C.c_uint64), ("fdim", C.c_uint64),
                 ("alpha", C.c_uint32)]
+
+
+class pgx_refine_params(C.Structure):
+    """struct pgx_refine_params of include/pgx.h."""
+    _fields_ = [("hops", C.c_uint32), ("stop", C.c_uint32), ("steps", C.c_uint32), ("perturb", C.c_double),
+                ("step0", C.c_double), ("step_min", C.c_double), ("seed", C.c_uint64)]
 
 
 _lib = None

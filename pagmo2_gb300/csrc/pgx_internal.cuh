@@ -92,6 +92,8 @@ struct pgx_context {
     std::vector<cudaEvent_t> chunk_ev;
     // survival: inputs/outputs of host calls, the scratch of a pass, small outputs
     pgx::dbuf s_points, s_state, s_outs, s_crowd;
+    // batched refinement: per-individual working points and gradients
+    pgx::dbuf r_work;
 };
 
 namespace pgx

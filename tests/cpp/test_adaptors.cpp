@@ -11,14 +11,17 @@
 #include <string>
 #include <vector>
 
+#include <pagmo/algorithm.hpp>
 #include <pagmo/batch_evaluators/member_bfe.hpp>
 #include <pagmo/batch_evaluators/thread_bfe.hpp>
 #include <pagmo/bfe.hpp>
+#include <pagmo/population.hpp>
 #include <pagmo/problem.hpp>
 #include <pagmo/exceptions.hpp>
 #include <pagmo/problems/ackley.hpp>
 #include <pagmo/problems/dtlz.hpp>
 #include <pagmo/problems/griewank.hpp>
+#include <pagmo/problems/lennard_jones.hpp>
 #include <pagmo/problems/null_problem.hpp>
 #include <pagmo/problems/rastrigin.hpp>
 #include <pagmo/problems/rosenbrock.hpp>
@@ -28,6 +31,7 @@
 #include <pagmo/utils/multi_objective.hpp>
 
 #include <pagmo_gb300/gpu_bfe.hpp>
+#include <pagmo_gb300/gpu_mbh.hpp>
 #include <pagmo_gb300/gpu_problems.hpp>
 #include <pagmo_gb300/multi_objective.hpp>
 #include <pagmo_gb300/s11n_implement.hpp>
@@ -235,7 +239,35 @@ int main()
             CHECK(fg.size() == fr.size());
             for (size_t i = 0; i < fr.size(); ++i) CHECK(std::abs(fg[i] - fr[i]) <= 1e-12 * (1.0 + std::abs(fr[i])));
         }
+        // gpu_mbh through pagmo's algorithm: no individual gets worse, most improve,
+        // the stored fitness is the problem's fitness of the stored point, fevals grow
+        for (auto prob : {pagmo::problem{pagmo::rosenbrock{10u}}, pagmo::problem{gpu_rastrigin{20u}},
+                          pagmo::problem{pagmo::lennard_jones{8u}}}) {
+            pagmo::population pop{prob, 64u, 17u};
+            const auto f0 = pop.get_f();
+            const auto fe0 = pop.get_problem().get_fevals();
+            pagmo::algorithm algo{gpu_mbh{4u, 3u, 10u, 0.05, 0.05, 1e-6, 3u}};
+            CHECK(algo.get_name().find("GB300") != std::string::npos);
+            pop = algo.evolve(pop);
+            int better = 0;
+            for (size_t i = 0; i < f0.size(); ++i) {
+                CHECK(pop.get_f()[i][0] <= f0[i][0]);
+                better += pop.get_f()[i][0] < f0[i][0];
+                const double fx = pagmo::problem{prob}.fitness(pop.get_x()[i])[0];
+                CHECK(std::abs(fx - pop.get_f()[i][0]) <= 1e-12 * (1.0 + std::abs(fx)));
+            }
+            CHECK(better > 32);
+            CHECK(pop.get_problem().get_fevals() > fe0 + 64u);
+        }
     }
+    // gpu_mbh refuses problems it cannot refine (no CPU fallback) and bad perturbations
+    CHECK(throws_with<std::invalid_argument>([] { gpu_mbh{10u, 5u, 20u, 0.0}; }, "The perturbation must be in ]0,1]"));
+    CHECK(throws_with<std::invalid_argument>(
+        [] {
+            pagmo::population pop{pagmo::problem{pagmo::ackley{3u}}, 4u, 1u};
+            gpu_mbh{}.evolve(pop);
+        },
+        "Cannot use gpu_mbh"));
     if (failures) {
         std::fprintf(stderr, "%d check(s) failed\n", failures);
         return 1;
