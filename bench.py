@@ -11,16 +11,20 @@ step = one batch. Prints one JSON line:
          (pgx_batch_gradient) from pinned host memory, uploads and downloads
          inside the timed region
   roofline  the rosenbrock kernel against the FP64 peak (measured in-run by a
-         DFMA probe; MEASURED_PEAKS.json has no FP64 figure): the algorithmic
-         flops, the FP64 pipe's own load (fp64_pipe: part of the algorithmic
-         flops run exactly on the integer pipes) and the HBM fraction
+         DFMA probe; MEASURED_PEAKS.json has no FP64 figure): frac is the FP64
+         pipe's load (the kernel's FP64 instructions at 2 flops each), the
+         binding pipe; beside it the reference formulas' algorithmic flops
+         (18 per element, 14 of them exact on the integer pipes) and the HBM
+         fraction of the algorithmic bytes
   cpu_baseline  the reference's CPU path (compiled reference where present,
          else the oracle's restatement of thread_bfe + gradient) on the host
   secondary  the other kernels of the path (rastrigin, lennard_jones, ackley,
          griewank, schwefel, ZDT/DTLZ, NSGA-II survival, select_best_N_mo,
          sort_population_mo, one NSGA-II generation on ZDT1, hypervolume, the
-         fused archipelago epoch against one GPU bfe call per island) measured
-         the same way
+         fused archipelago epoch against one GPU bfe call per island, batched
+         basin-hopping refinement) measured the same way; rastrigin 4096 x 50
+         and lennard_jones 16384 x 150 also through the host-buffer entry
+         points (e2e), survival as e2e_ms
 
 --impl reference times the reference's CPU implementation of the same step
 with every host thread. Multi-GPU (torchrun): every rank evaluates its own
@@ -47,15 +51,16 @@ N_ROWS, DIM = 65536, 1000
 METRIC = "FP64 fitness+grad evals/s"
 UNIT = "evals/s"
 
-# Algorithmic flops per rosenbrock element (FMA = 2): fitness t, sum t^2,
-# (2x-2)^2 accumulate; gradient 2x, 2x-2, t_prev - 2x t, 200 b + c -> 5 FMA +
-# 2 add/sub = 12. Of these the kernel runs 4 instructions on the FP64 pipe
-# (t, 2x-2, t_prev - 2x t, 200 b + c: 3 FMA + 1 add = 7 flops); 2x is an
-# exponent increment and the two sums of squares are exact integer
-# accumulations, on the integer pipes.
-ROS_FG_FLOPS_PER_ELEM = 12
+# Work per rosenbrock element of the fitness + gradient batch. Algorithmic
+# flops, counted on the reference's own formulas (add/sub/mul = 1, FMA = 2):
+# fitness 8 (x^2, x^2 - x', its square, x 100, x - 1, its square, two adds),
+# gradient 10: 18. The kernel issues 4 instructions per element on the FP64
+# pipe (t = x' - x^2, 2x - 2, t_prev - 2x t, 200 b + c); the rest is exact on
+# the integer pipes (2x by an exponent increment, the sums of t^2 and
+# (2x - 2)^2 as integer accumulations), so the FP64 pipe's load, not the
+# algorithmic flops, measures the distance to the ceiling.
+ROS_FG_FLOPS_PER_ELEM = 18
 ROS_FG_FP64_INSTR_PER_ELEM = 4
-ROS_F_FLOPS_PER_ELEM = 7
 
 
 def parse():
@@ -327,8 +332,11 @@ def main():
     fp = C.c_double()
     N.check(L.pgx_measure_fp64_peak(ctx.handle, C.byref(fp)))
     fp64_peak_tflops = fp.value / 1e3
-    flops = rows_n * ((DIM - 1) * ROS_FG_FLOPS_PER_ELEM + 2)
-    achieved_tflops = flops / (ms * 1e-3) / 1e12
+    alg_flops = rows_n * (DIM - 1) * ROS_FG_FLOPS_PER_ELEM
+    alg_tflops = alg_flops / (ms * 1e-3) / 1e12
+    # the binding pipe: FP64 instructions issued, at 2 flops each (the DFMA
+    # rate the peak probe measures)
+    pipe_tflops = rows_n * (DIM - 1) * ROS_FG_FP64_INSTR_PER_ELEM * 2 / (ms * 1e-3) / 1e12
     alg_bytes = rows_n * (DIM * 8 * 2 + 8)
     peaks = measured_peaks()
     hbm_peak = peaks.get("hbm_gbs")
@@ -336,23 +344,19 @@ def main():
                else "6800 GB/s (of fallback: MEASURED_PEAKS.json absent)")
     hbm_peak = hbm_peak or 6800.0
     achieved_gbs = alg_bytes / (ms * 1e-3) / 1e9
-    roofline = {"bound": "fp64", "achieved": achieved_tflops, "peak": fp64_peak_tflops, "unit": "TFLOP/s",
-                "frac": achieved_tflops / fp64_peak_tflops, "traffic": ncu_traffic("rosenbrock_fg_65536x1000"),
+    roofline = {"bound": "fp64", "achieved": pipe_tflops, "peak": fp64_peak_tflops, "unit": "TFLOP/s",
+                "frac": pipe_tflops / fp64_peak_tflops, "traffic": ncu_traffic("rosenbrock_fg_65536x1000"),
                 "kernel": "rosenbrock_v4_kernel<true>",
-                "peak_source": "in-run DFMA throughput probe (pgx_measure_fp64_peak); no FP64 figure in "
-                               "MEASURED_PEAKS.json",
-                "algorithmic": f"{ROS_FG_FLOPS_PER_ELEM} flops/element (FMA=2), {alg_bytes} bytes per launch",
+                "achieved_is": f"the FP64 pipe's load: {ROS_FG_FP64_INSTR_PER_ELEM} FP64 instructions per element "
+                               "x 2 flops, per launch, over the launch's CUDA-event time",
+                "peak_source": "in-run DFMA throughput probe (pgx_measure_fp64_peak; MEASURED_PEAKS.json has no "
+                               "FP64 figure), of measured",
+                "algorithmic": {"flops_per_element": ROS_FG_FLOPS_PER_ELEM, "achieved": alg_tflops,
+                                "unit": "TFLOP/s", "frac_of_fp64_peak": alg_tflops / fp64_peak_tflops,
+                                "note": "the reference formulas' flops; above the FP64 peak because 14 of the 18 "
+                                        "run exactly on the integer pipes"},
                 "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
-                        "peak_source": hbm_src}}
-    # the FP64 pipe itself: the instructions the kernel issues there, against
-    # the probe's DFMA rate (frac above 1.0 for the algorithmic flops because
-    # part of them runs on the integer pipes)
-    fp64_instr_rate = rows_n * (DIM - 1) * ROS_FG_FP64_INSTR_PER_ELEM / (ms * 1e-3)
-    roofline["fp64_pipe"] = {
-        "instructions_per_element": ROS_FG_FP64_INSTR_PER_ELEM,
-        "frac": fp64_instr_rate / (fp64_peak_tflops * 1e12 / 2.0),
-        "note": "2x by exponent increment and the sums of t^2 and (2x-2)^2 as exact integer accumulations "
-                "(integer pipes); the algorithmic frac counts those flops too"}
+                        "bytes_per_launch": alg_bytes, "peak_source": hbm_src}}
 
     # the opt-in double-float rows (not FP64 arithmetic), timed beside the headline
     os.environ["PGX_ROSENBROCK_DOUBLE_FLOAT"] = "1"
@@ -485,7 +489,7 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops, cpu_ok=True) -> dict:
             ts.append(e0.elapsed_time(e1))
         return float(np.median(ts))
 
-    def fitness_case(name, kind, param, x, grad):
+    def fitness_case(name, kind, param, x, grad, e2e=False):
         n, nx = x.shape
         dx = torch.from_numpy(x).cuda()
         df = torch.empty(n, dtype=torch.float64, device="cuda")
@@ -497,9 +501,32 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops, cpu_ok=True) -> dict:
         ms = timed(fn)
         bytes_ = n * nx * 8 * (2 if grad else 1) + n * 8
         out[name] = {"evals_per_s": n / (ms * 1e-3), "ms": ms, "hbm_gbs": bytes_ / (ms * 1e-3) / 1e9}
+        if e2e:
+            # the same batch through the host-buffer entry point (pinned buffers;
+            # uploads and downloads inside the timed region), wall clock
+            hx = torch.from_numpy(x).pin_memory()
+            hf = torch.empty(n, dtype=torch.float64).pin_memory()
+            hg = torch.empty((n, nx), dtype=torch.float64).pin_memory() if grad else None
 
-    fitness_case("rastrigin_fg_4096x50", N.RASTRIGIN, 50, W.rastrigin_batch(), True)
-    fitness_case("rastrigin_f_4096x50", N.RASTRIGIN, 50, W.rastrigin_batch(), False)
+            def host():
+                if grad:
+                    N.check(L.pgx_batch_gradient(ctx.handle, kind, param, hx.data_ptr(), n, hf.data_ptr(),
+                                                 hg.data_ptr()))
+                else:
+                    N.check(L.pgx_batch_fitness(ctx.handle, kind, param, hx.data_ptr(), n, hf.data_ptr()))
+            for _ in range(3):
+                host()
+            reps = 20
+            t = time.perf_counter()
+            for _ in range(reps):
+                host()
+            e2e_s = (time.perf_counter() - t) / reps
+            out[name]["e2e"] = {"ms": e2e_s * 1e3, "evals_per_s": n / e2e_s,
+                                "h2d_bytes": n * nx * 8, "d2h_bytes": n * 8 + (n * nx * 8 if grad else 0),
+                                "entry_point": "pgx_batch_gradient" if grad else "pgx_batch_fitness"}
+
+    fitness_case("rastrigin_fg_4096x50", N.RASTRIGIN, 50, W.rastrigin_batch(), True, e2e=True)
+    fitness_case("rastrigin_f_4096x50", N.RASTRIGIN, 50, W.rastrigin_batch(), False, e2e=True)
     fitness_case("rastrigin_fg_1048576x50", N.RASTRIGIN, 50, W.rastrigin_batch(1 << 20, 50), True)
     fitness_case("rosenbrock_f_65536x1000", N.ROSENBROCK, 1000, W.rosenbrock_batch(), False)
     for kind, name in ((N.ACKLEY, "ackley"), (N.GRIEWANK, "griewank"), (N.SCHWEFEL, "schwefel")):
@@ -524,7 +551,7 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops, cpu_ok=True) -> dict:
     for pid in (1, 2, 4, 6, 7):
         mo_case(f"dtlz{pid}_f_1048576x12_m3", N.DTLZ, pid, 12, 1 << 20, fdim=3)
     lj = W.lj_batch()
-    fitness_case("lj_fg_16384x150", N.LENNARD_JONES, 150, lj, True)
+    fitness_case("lj_fg_16384x150", N.LENNARD_JONES, 150, lj, True, e2e=True)
     fitness_case("lj_f_16384x150", N.LENNARD_JONES, 150, lj, False)
     pairs = 16384 * 150 * 149 // 2
     for k in ("lj_fg_16384x150", "lj_f_16384x150"):
@@ -645,6 +672,50 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops, cpu_ok=True) -> dict:
         out[name] = rec
     out["sort_population_mo_20000x3"] = {"ms": timed(sortpop, reps=10, flush_l2=False)}
     out["archipelago_64_islands"] = run_archipelago(ctx, L, N, W, stream)
+    out.update(run_refine(ctx, L, N, W, stream))
+    return out
+
+
+def run_refine(ctx, L, N, W, stream) -> dict:
+    """Batched basin hopping with gradient descent (pgx_refine_batch_device):
+    every individual of a batch refined in one launch; device time (CUDA
+    events) and the fitness + gradient evaluations it made per second."""
+    import ctypes as C
+
+    import torch
+
+    out = {}
+    sp = stream.cuda_stream
+    params = N.pgx_refine_params(10, 5, 20, 0.02, 0.05, 1e-7, 7)
+    for name, kind, param, x in (("refine_rastrigin_4096x50", N.RASTRIGIN, 50, W.rastrigin_batch()),
+                                 ("refine_rosenbrock_4096x1000", N.ROSENBROCK, 1000, W.rosenbrock_batch(4096, 1000)),
+                                 ("refine_lennard_jones_1024x150", N.LENNARD_JONES, 150, W.lj_batch(1024, 150))):
+        n = x.shape[0]
+        d0 = torch.from_numpy(x).cuda()
+        dx = torch.empty_like(d0)
+        df = torch.empty(n, dtype=torch.float64, device="cuda")
+        de = torch.zeros(1, dtype=torch.int64, device="cuda")
+
+        def fn():
+            dx.copy_(d0)
+            de.zero_()
+            N.check(L.pgx_refine_batch_device(ctx.handle, kind, param, C.byref(params), dx.data_ptr(), n,
+                                              df.data_ptr(), de.data_ptr(), sp))
+        with torch.cuda.stream(stream):
+            fn()
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        evals = int(de.item())
+        out[name] = {"ms": ms, "evals": evals, "evals_per_s": evals / (ms * 1e-3), "individuals": n,
+                     "params": {"hops": 10, "stop": 5, "steps": 20, "perturb": 0.02, "step0": 0.05,
+                                "step_min": 1e-7}}
     return out
 
 

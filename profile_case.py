@@ -1,8 +1,8 @@
-"""Runs one kernel of the path on a chosen workload, for profilers.
+"""Runs one kernel of the batch-evaluation path on a chosen workload, for profilers.
 
-    python -m pagmo2_gb300.profile_case --case rosenbrock_fg --rows 16384
+    python profile_case.py --case rosenbrock_fg --rows 16384
     ncu --set full --clock-control none -k regex:rosenbrock -s 2 -c 1 \
-        python -m pagmo2_gb300.profile_case --case rosenbrock_fg --rows 16384
+        python profile_case.py --case rosenbrock_fg --rows 16384
 
 Inputs are seeded synthetic batches resident on the device; --warmup launches
 are followed by --launches timed ones (CUDA events; numbers printed under a
@@ -26,7 +26,7 @@ import argparse
 import sys
 from pathlib import Path
 
-ROOT = Path(__file__).resolve().parents[1]
+ROOT = Path(__file__).resolve().parent
 if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
