@@ -14,8 +14,8 @@ step = one batch. Prints one JSON line:
          DFMA probe; MEASURED_PEAKS.json has no FP64 figure): frac is the FP64
          pipe's load (the kernel's FP64 instructions at 2 flops each), the
          binding pipe; beside it the reference formulas' algorithmic flops
-         (18 per element, 14 of them exact on the integer pipes) and the HBM
-         fraction of the algorithmic bytes
+         (18 per element, for which the kernel issues 4 FP64 instructions) and
+         the HBM fraction of the algorithmic bytes
   cpu_baseline  the reference's CPU path (compiled reference where present,
          else the oracle's restatement of thread_bfe + gradient) on the host
   secondary  the other kernels of the path (rastrigin, lennard_jones, ackley,
@@ -353,8 +353,9 @@ def main():
                                "FP64 figure), of measured",
                 "algorithmic": {"flops_per_element": ROS_FG_FLOPS_PER_ELEM, "achieved": alg_tflops,
                                 "unit": "TFLOP/s", "frac_of_fp64_peak": alg_tflops / fp64_peak_tflops,
-                                "note": "the reference formulas' flops; above the FP64 peak because 14 of the 18 "
-                                        "run exactly on the integer pipes"},
+                                "note": "the reference formulas' flops; above the FP64 peak because the kernel "
+                                        "issues 4 FP64 instructions for them (the sums of squares and 2x are exact "
+                                        "on the integer pipes)"},
                 "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
                         "bytes_per_launch": alg_bytes, "peak_source": hbm_src}}
 
