@@ -453,12 +453,17 @@ __global__ void __launch_bounds__(kPeelThreads) peel_kernel(const uint32_t *__re
 // order (the reference's first front), come from the dom_count == 0 bit set
 // and its prefix popcounts, which every block computes for itself.
 // For k >= 1, Phase A finds the members of front k. Each unassigned point j
-// keeps a witness wit[j], an unassigned dominator found earlier: while the
-// witness stays unassigned, j is settled by one shared-memory bit test. When
-// the witness is peeled, j's row of Dt is scanned again from the witness's
-// word (the words before it held no unassigned dominator then, and the
+// keeps a witness wit[j], an unassigned dominator found earlier, and the
+// resume word res[j], the first word of its row that held an unassigned
+// dominator then (both in the shared memory of the block that owns j's word):
+// while the witness stays unassigned, j is settled by one shared-memory bit
+// test. When the witness is peeled, j's row of Dt is scanned again from
+// res[j] (the words before it held no unassigned dominator, and the
 // unassigned set only shrinks); no unassigned dominator left makes j a member
-// of front k. A block first tests the witnesses of the points of its own rem
+// of front k. Otherwise every lane proposes one unassigned dominator from the
+// first nonzero word of its part of the scanned window and the new witness is
+// the proposal with the most dominators itself, which is likely peeled late,
+// so that j is rescanned seldom. A block first tests the witnesses of the points of its own rem
 // words, queueing the points that need a scan, then its warps scan the queue.
 // A member's ordering key is the highest position, in front k-1, of one of
 // its dominators (the reference appends q when its last dominator in front
@@ -473,12 +478,17 @@ __global__ void __launch_bounds__(kPeelThreads) peel_kernel(const uint32_t *__re
 // before the next barrier. A front larger than kTile takes the grid-wide
 // counting of peel_kernel and a second barrier instead.
 constexpr int kQueue = 4096; // witness rescans queued per block and front
+// Up to this many points every block keeps the previous front's membership
+// bits and each member's position there (16 bits) in shared memory, and a
+// member's key comes out of its own row scan (no second pass over the row).
+constexpr uint32_t kPosPoints = 32768;
 
 struct peel2_args {
     const uint32_t *Dt;
     const int32_t *dom_count;
     uint32_t n, W, W8;
-    int32_t *wit;       // n witnesses (-1: none yet)
+    int32_t *wit;       // n first witnesses (-1: none) and
+    int32_t *res;       // n their resume words, from witness_init_kernel
     int32_t *list;      // 2 n: members of fronts k (parity k & 1)
     int32_t *keyv;      // 2 n: their ordering keys
     int32_t *cnt;       // n + 2 per-front member counters, zeroed
@@ -527,6 +537,88 @@ __device__ __forceinline__ bool bit_of(const uint32_t *s, int32_t q)
     return (s[q >> 5] >> (q & 31)) & 1u;
 }
 
+// rem (the valid points) minus front 0 (the points without dominators): the
+// unassigned set when front 1 is peeled.
+__global__ void rem_outside_front0_kernel(const int32_t *__restrict__ dom_count, uint32_t n, uint32_t W,
+                                          uint32_t *__restrict__ rem)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < W; w += warps) {
+        const uint32_t q = w * 32u + lane;
+        const uint32_t z = __ballot_sync(kFull, q < n && __ldg(dom_count + q) == 0);
+        if (lane == 0) rem[w] &= ~z;
+    }
+}
+
+// Every point's first witness and resume word, before the peel and on every
+// SM at full occupancy (one warp per point): the first word of its row of Dt
+// holding a dominator outside front 0 is the resume word, and the witness is,
+// of one such dominator per lane (from the lane's first nonzero word), the one
+// with the most dominators itself, as the peel's rescans choose. Points with
+// no dominator outside front 0 (front 1) and front 0 itself get -1.
+__global__ void __launch_bounds__(256) witness_init_kernel(const uint32_t *__restrict__ Dt,
+                                                           const int32_t *__restrict__ dom_count,
+                                                           const uint32_t *__restrict__ rem, uint32_t n, uint32_t W,
+                                                           uint32_t W8, int32_t *__restrict__ wit,
+                                                           int32_t *__restrict__ res)
+{
+    extern __shared__ uint32_t s_u[]; // W8 words: rem (words from W on are zero)
+    for (uint32_t w = threadIdx.x; w < W8; w += blockDim.x) s_u[w] = w < W ? __ldg(rem + w) : 0u;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < n; j += warps) {
+        int32_t found = -1, resume = -1;
+        if (__ldg(dom_count + j) > 0) {
+            const uint32_t *row = Dt + static_cast<uint64_t>(j) * W8;
+            for (uint32_t base = 0; base < W && found < 0; base += 512u) {
+                uint4 x[4];
+#pragma unroll
+                for (uint32_t u = 0; u < 4u; ++u) {
+                    const uint32_t wi = base + 4u * (u * 32u + lane);
+                    x[u] = make_uint4(0u, 0u, 0u, 0u);
+                    if (wi < W) {
+                        const uint4 d = __ldg(reinterpret_cast<const uint4 *>(row + wi));
+                        const uint4 r = *reinterpret_cast<const uint4 *>(s_u + wi);
+                        x[u] = make_uint4(d.x & r.x, d.y & r.y, d.z & r.z, d.w & r.w);
+                    }
+                }
+                int cand = -1;
+#pragma unroll
+                for (uint32_t u = 0; u < 4u; ++u) {
+                    const uint32_t c = x[u].x ? 0u : (x[u].y ? 1u : (x[u].z ? 2u : 3u));
+                    const uint32_t xv = x[u].x ? x[u].x : (x[u].y ? x[u].y : (x[u].z ? x[u].z : x[u].w));
+                    if (cand < 0 && xv)
+                        cand = static_cast<int>((base + 4u * (u * 32u + lane) + c) * 32u) + (31 - __clz(xv));
+                    const uint32_t bb = __ballot_sync(kFull, xv != 0u);
+                    if (resume < 0 && bb) {
+                        const int l0 = __ffs(bb) - 1;
+                        const uint32_t cl = __shfl_sync(kFull, c, l0);
+                        resume = static_cast<int32_t>(base + 4u * (u * 32u + static_cast<uint32_t>(l0)) + cl);
+                    }
+                }
+                if (resume >= 0) {
+                    int best = cand >= 0 ? __ldg(dom_count + cand) : -1, bq = cand;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const int ob = __shfl_xor_sync(kFull, best, o), oq = __shfl_xor_sync(kFull, bq, o);
+                        if (ob > best || (ob == best && oq < bq)) {
+                            best = ob;
+                            bq = oq;
+                        }
+                    }
+                    found = bq;
+                }
+            }
+        }
+        if (lane == 0) {
+            wit[j] = found;
+            res[j] = resume;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
 {
     extern __shared__ uint32_t dyn[];
@@ -538,6 +630,11 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
     int32_t *s_key = s_prev + 2 * kTile;                            // kTile
     int32_t *s_idx = s_key + kTile;                                 // kTile
     int32_t *s_queue = s_idx + kTile;                               // kQueue
+    int32_t *s_wit = s_queue + kQueue;                              // 32 wpb: witnesses of this block's points
+    int32_t *s_res = s_wit + 32u * ((W + gridDim.x - 1u) / gridDim.x); // 32 wpb: their rescans' resume words
+    uint32_t *s_pbits = reinterpret_cast<uint32_t *>(s_res + 32u * ((W + gridDim.x - 1u) / gridDim.x)); // W
+    uint16_t *s_pos = reinterpret_cast<uint16_t *>(s_pbits + W); // n: positions in the previous front
+    const bool pos_maps = n <= kPosPoints;
     __shared__ int32_t s_list[kLocalMembers], s_lkey[kLocalMembers];
     __shared__ int s_cnt, s_base, s_qn, s_wtot[32];
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -546,6 +643,12 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
     // this block's rem words in Phase A
     const uint32_t wpb = (W + gridDim.x - 1u) / gridDim.x;
     const uint32_t w_lo = min(W, blockIdx.x * wpb), w_hi = min(W, w_lo + wpb);
+    const int32_t j_lo = static_cast<int32_t>(32u * w_lo); // this block's points: [j_lo, 32 w_hi)
+    for (uint32_t t = threadIdx.x; t < 32u * wpb; t += blockDim.x) {
+        const uint32_t j = static_cast<uint32_t>(j_lo) + t;
+        s_wit[t] = j < n ? __ldg(a.wit + j) : -1;
+        s_res[t] = j < n ? __ldg(a.res + j) : -1;
+    }
 
     // ---- front 0 from dom_count (every block for itself)
     for (uint32_t w = warp; w < W; w += nwarp_b) {
@@ -602,8 +705,17 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
         }
     }
     if (tid == 0) a.front_offsets[1] = L0;
+    if (pos_maps) {
+        // front 0's membership bits and positions (every block for itself)
+        for (uint32_t w = threadIdx.x; w < W; w += blockDim.x) s_pbits[w] = s_Z[w];
+        for (uint32_t w = warp; w < W; w += nwarp_b) {
+            const uint32_t z = s_Z[w];
+            if ((z >> lane) & 1u) s_pos[w * 32u + lane] = static_cast<uint16_t>(s_Zp[w] + __popc(z & ((1u << lane) - 1u)));
+        }
+    }
     int off = L0, off_prev = 0, size_prev = L0;
     bool prev_global = false; // front k-1 by position only in global memory (a large front)
+    bool pos_ok = pos_maps;   // front k-1's bits and positions are in s_pbits / s_pos
     int k = 1;
     for (; off < static_cast<int>(n); ++k) {
         if (threadIdx.x == 0) {
@@ -623,7 +735,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
             const bool cand = (bits >> lane) & 1u;
             bool need = false;
             if (cand) {
-                const int32_t wj = __ldcg(a.wit + j);
+                const int32_t wj = s_wit[j - j_lo];
                 need = !(wj >= 0 && bit_of(s_rem, wj));
             }
             const uint32_t b = __ballot_sync(kFull, need);
@@ -640,11 +752,12 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
         for (int t = static_cast<int>(warp); t < qn; t += static_cast<int>(nwarp_b)) {
             const int32_t j = s_queue[t];
             const uint32_t *row = a.Dt + static_cast<uint64_t>(j) * a.W8;
-            const int32_t wj = __ldcg(a.wit + j);
-            // 512 words per round, four per 16-byte load (rows start on 32-byte
-            // boundaries; words from W on are masked)
-            const uint32_t ws = (wj >= 0 ? static_cast<uint32_t>(wj) >> 5 : 0u) & ~3u;
-            int32_t found = -1;
+            // 512 words per round from the resume word, four per 16-byte load
+            // (rows start on 32-byte boundaries; words from W on are masked)
+            const int32_t rj = s_res[j - j_lo];
+            const uint32_t ws = (rj >= 0 ? static_cast<uint32_t>(rj) : 0u) & ~3u;
+            int32_t found = -1, resume = -1;
+            int pkey = -1; // this lane's highest position in front k-1 among the dominators seen
             for (uint32_t base = ws; base < W && found < 0; base += 512u) {
                 uint4 x[4];
 #pragma unroll
@@ -658,29 +771,69 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
                         x[u].y = wi + 1u < W ? d.y & r.y : 0u;
                         x[u].z = wi + 2u < W ? d.z & r.z : 0u;
                         x[u].w = wi + 3u < W ? d.w & r.w : 0u;
+                        if (pos_ok) {
+                            // dominators in front k-1 (all at or after the resume
+                            // word: they were unassigned at every earlier scan)
+                            const uint32_t dw[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+                            for (uint32_t c = 0; c < 4u; ++c) {
+                                uint32_t pb = wi + c < W ? dw[c] & s_pbits[wi + c] : 0u;
+                                while (pb) {
+                                    const int b = __ffs(pb) - 1;
+                                    pkey = max(pkey, static_cast<int>(s_pos[(wi + c) * 32u + static_cast<uint32_t>(b)]));
+                                    pb &= pb - 1u;
+                                }
+                            }
+                        }
                     }
                 }
+                // the first word holding an unassigned dominator: rescans resume there
+                // (the words before it hold none, and the unassigned set only shrinks)
+                int cand = -1; // this lane's proposal: a dominator from its first nonzero word
 #pragma unroll
                 for (uint32_t u = 0; u < 4u; ++u) {
-                    const uint32_t bb = __ballot_sync(kFull, (x[u].x | x[u].y | x[u].z | x[u].w) != 0u);
-                    if (found < 0 && bb) {
+                    const uint32_t c = x[u].x ? 0u : (x[u].y ? 1u : (x[u].z ? 2u : 3u));
+                    const uint32_t xv = x[u].x ? x[u].x : (x[u].y ? x[u].y : (x[u].z ? x[u].z : x[u].w));
+                    if (cand < 0 && xv)
+                        cand = static_cast<int>((base + 4u * (u * 32u + lane) + c) * 32u) + (31 - __clz(xv));
+                    const uint32_t bb = __ballot_sync(kFull, xv != 0u);
+                    if (resume < 0 && bb) {
                         const int l0 = __ffs(bb) - 1;
-                        const uint32_t c0 = __shfl_sync(kFull, x[u].x, l0), c1 = __shfl_sync(kFull, x[u].y, l0);
-                        const uint32_t c2 = __shfl_sync(kFull, x[u].z, l0), c3 = __shfl_sync(kFull, x[u].w, l0);
-                        const uint32_t c = c0 ? 0u : (c1 ? 1u : (c2 ? 2u : 3u));
-                        const uint32_t xv = c0 ? c0 : (c1 ? c1 : (c2 ? c2 : c3));
-                        const uint32_t word = base + 4u * (u * 32u + static_cast<uint32_t>(l0)) + c;
-                        found = static_cast<int32_t>(word * 32u) + __ffs(xv) - 1;
+                        const uint32_t cl = __shfl_sync(kFull, c, l0);
+                        resume = static_cast<int32_t>(base + 4u * (u * 32u + static_cast<uint32_t>(l0)) + cl);
                     }
+                }
+                if (resume >= 0) {
+                    // the witness: of the lanes' proposals, the dominator with the
+                    // most dominators itself (likely in a later front, so j is
+                    // rescanned less often)
+                    int best = cand >= 0 ? __ldg(a.dom_count + cand) : -1, bq = cand;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const int ob = __shfl_xor_sync(kFull, best, o), oq = __shfl_xor_sync(kFull, bq, o);
+                        if (ob > best || (ob == best && oq < bq)) {
+                            best = ob;
+                            bq = oq;
+                        }
+                    }
+                    found = bq;
                 }
             }
             if (found >= 0) {
-                if (lane == 0) a.wit[j] = found;
+                if (lane == 0) {
+                    s_wit[j - j_lo] = found;
+                    s_res[j - j_lo] = resume;
+                }
                 continue;
             }
             // a member of front k: its key
             int key = -1;
-            if (k == 1) {
+            if (pos_ok) {
+                // the scan above read every word that can hold its front k-1 dominators
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) pkey = max(pkey, __shfl_xor_sync(kFull, pkey, o));
+                key = pkey;
+            } else if (k == 1) {
                 // the highest-index dominator among front 0 (positions follow indices there)
                 for (int top = static_cast<int>(W) - 1; top >= 0 && key < 0; top -= 256) {
                     uint32_t x[8];
@@ -702,22 +855,26 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
                     }
                 }
             } else {
-                for (int top = size_prev - 1; top >= 0 && key < 0; top -= 128) {
-                    unsigned bal[4];
+                // 256 positions per round: every lane's 8 row-word loads are in
+                // flight together, then the ballots
+                for (int top = size_prev - 1; top >= 0 && key < 0; top -= 256) {
+                    uint32_t hw[8], hb[8];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
+                    for (int u = 0; u < 8; ++u) {
                         const int p = top - 32 * u - static_cast<int>(lane);
-                        bool h = false;
+                        hw[u] = 0u;
+                        hb[u] = 0u;
                         if (p >= 0) {
                             const uint32_t d = static_cast<uint32_t>(prev_in_smem ? s_prev[p]
                                                                                   : __ldcg(a.front_indices + off_prev + p));
-                            h = (__ldg(row + (d >> 5)) >> (d & 31u)) & 1u;
+                            hw[u] = __ldg(row + (d >> 5));
+                            hb[u] = d & 31u;
                         }
-                        bal[u] = __ballot_sync(kFull, h);
                     }
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        if (key < 0 && bal[u]) key = top - 32 * u - (__ffs(bal[u]) - 1);
+                    for (int u = 0; u < 8; ++u) {
+                        const unsigned bal = __ballot_sync(kFull, (hw[u] >> hb[u]) & 1u);
+                        if (key < 0 && bal) key = top - 32 * u - (__ffs(bal) - 1);
                     }
                 }
             }
@@ -756,6 +913,8 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
             int32_t *h = s_queue;              // R bucket counters, then bucket starts / ends
             int32_t *s_blist = s_prev + kTile; // members in bucket order
             for (int t = threadIdx.x; t < R; t += blockDim.x) h[t] = 0;
+            if (pos_maps)
+                for (uint32_t w = threadIdx.x; w < W; w += blockDim.x) s_pbits[w] = 0u;
             for (int t = threadIdx.x; t < L; t += blockDim.x) {
                 int kq = __ldcg(kv + t);
                 if (kq < 0 || kq >= R) { // a member without a dominator in front k-1: never expected
@@ -802,6 +961,10 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
                     const int q = s_idx[t], p = pos[i];
                     s_prev[p] = q; // front k by position, for the keys of front k+1
                     atomicAnd(s_rem + (q >> 5), ~(1u << (q & 31)));
+                    if (pos_maps) {
+                        s_pos[q] = static_cast<uint16_t>(p);
+                        atomicOr(s_pbits + (q >> 5), 1u << (q & 31));
+                    }
                     if (p % static_cast<int>(gridDim.x) == static_cast<int>(blockIdx.x)) {
                         a.front_indices[off + p] = q;
                         a.rank[q] = k;
@@ -809,6 +972,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
                 }
             }
             prev_global = false;
+            pos_ok = pos_maps;
         } else {
             // ---- a large front: block b ranks members [m_lo, m_hi), one warp per
             // member, lanes splitting the comparisons against shared-memory tiles;
@@ -848,6 +1012,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
                 a.rank[q] = k;
             }
             prev_global = true;
+            pos_ok = false;
             if (!grid_sync(a.st)) {
                 if (threadIdx.x == 0) atomicExch(&a.st->n_fronts, -1);
                 return;
@@ -1682,15 +1847,28 @@ int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n,
     const uint32_t wpb = (W + static_cast<uint32_t>(num_sms) - 1u) / static_cast<uint32_t>(num_sms);
     if (W <= static_cast<uint32_t>(kRemWords) && 32u * wpb <= static_cast<uint32_t>(kQueue)
         && n <= static_cast<uint64_t>(kQueue) * static_cast<uint32_t>(num_sms)) {
-        const size_t smem2 = (3u * static_cast<size_t>(W) + 4u * kTile + kQueue) * sizeof(int32_t);
+        const size_t smem2 = (3u * static_cast<size_t>(W) + 4u * kTile + kQueue + 64u * wpb) * sizeof(int32_t)
+                             + (n <= kPosPoints ? static_cast<size_t>(W) * 4u + ((static_cast<size_t>(n) * 2u + 3u) & ~size_t(3))
+                                                : 0u);
         PGX_CUDA(cudaFuncSetAttribute(peel2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(smem2)));
         int occ2 = 0;
         PGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, peel2_kernel, kPeelThreads, smem2));
         PGX_CHECK(occ2 >= 1, PGX_ERR_CUDA, "peel kernel cannot be resident");
-        PGX_CUDA(cudaMemsetAsync(sc.wit, 0xff, static_cast<size_t>(n) * sizeof(int32_t), s));
         PGX_CUDA(cudaMemsetAsync(sc.cnt, 0, (static_cast<size_t>(n) + 2u) * sizeof(int32_t), s));
-        peel2_args pa{sc.Dt, out.dom_count, n, W, W8, sc.wit, sc.list, sc.keyv, sc.cnt,
+        // first witnesses, on every SM (sc.widx holds their resume words until the crowding sorts)
+        rem_outside_front0_kernel<<<blocks_for(static_cast<uint64_t>(W) * 32u, 256, num_sms), 256, 0, s>>>(
+            out.dom_count, n, W, sc.rem);
+        PGX_CUDA(cudaGetLastError());
+        {
+            const uint64_t wblocks = std::min<uint64_t>((static_cast<uint64_t>(n) + 7u) / 8u,
+                                                        static_cast<uint64_t>(num_sms) * 8u);
+            witness_init_kernel<<<static_cast<unsigned>(wblocks), 256, static_cast<size_t>(W8) * 4u, s>>>(
+                sc.Dt, out.dom_count, sc.rem, n, W, W8, sc.wit, sc.widx);
+            PGX_CUDA(cudaGetLastError());
+        }
+        *launches += 2;
+        peel2_args pa{sc.Dt, out.dom_count, n, W, W8, sc.wit, sc.widx, sc.list, sc.keyv, sc.cnt,
                       out.rank, out.front_offsets, out.front_indices, sc.st};
         void *args2[] = {&pa};
         PGX_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(peel2_kernel), dim3(num_sms),
@@ -2082,6 +2260,8 @@ int noalloc_load_kernels()
         reinterpret_cast<const void *>(dominance_sym_kernel<4>),
         reinterpret_cast<const void *>(dominance_kernel<0>),
         reinterpret_cast<const void *>(row_popcount_kernel),
+        reinterpret_cast<const void *>(rem_outside_front0_kernel),
+        reinterpret_cast<const void *>(witness_init_kernel),
         reinterpret_cast<const void *>(peel2_kernel),
         reinterpret_cast<const void *>(peel_kernel),
         reinterpret_cast<const void *>(front_crowding_kernel),
