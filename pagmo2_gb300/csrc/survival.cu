@@ -147,6 +147,134 @@ __global__ void row_popcount_kernel(const uint32_t *__restrict__ Dt, uint32_t n,
     }
 }
 
+// ------------------------------------------------ packed-rank dominance
+//
+// For n <= kRankPoints and m <= 4 the dominance tiles compare ranks instead of
+// 64-bit order keys: the rank of a point in objective k is the number of
+// points with a smaller key there (equal keys, equal ranks, so the order and
+// the ties of every objective are kept, and with them the dominance relation).
+// Ranks are below 2^15; two share a 32-bit word as 16-bit fields whose top bit
+// is a guard: for words a and b, ((b | G) - a) & G == G exactly when no field
+// of a exceeds b's (a field's subtraction borrows from its guard bit only
+// then, and never from the next field). So "no objective worse" costs one
+// OR, one subtraction and one AND per word, for both directions of a pair.
+constexpr uint32_t kRankPoints = 32768;
+constexpr uint32_t kRankRun = 1024; // keys per sorted run
+constexpr uint32_t kRankGuard = 0x80008000u;
+
+// Sorted runs of kRankRun keys of each objective (bitonic network in shared
+// memory; grid: runs x objectives).
+__global__ void __launch_bounds__(kRankRun / 2) rank_runs_kernel(const long long *__restrict__ keys, uint32_t n,
+                                                                 long long *__restrict__ runs)
+{
+    __shared__ long long sk[kRankRun];
+    const uint32_t k = blockIdx.y, nb = gridDim.x;
+    const uint32_t t0 = blockIdx.x * kRankRun;
+    for (uint32_t j = threadIdx.x; j < kRankRun; j += blockDim.x) {
+        const uint32_t t = t0 + j;
+        sk[j] = t < n ? keys[static_cast<uint64_t>(k) * n + t] : LLONG_MAX;
+    }
+    __syncthreads();
+    for (uint32_t size = 2; size <= kRankRun; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t j = threadIdx.x; j < kRankRun / 2u; j += blockDim.x) {
+                const uint32_t lo = 2u * stride * (j / stride) + (j % stride), hi = lo + stride;
+                const bool up = (lo & size) == 0u;
+                const long long a = sk[lo], b = sk[hi];
+                if ((b < a) == up) {
+                    sk[lo] = b;
+                    sk[hi] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    long long *out = runs + (static_cast<uint64_t>(k) * nb + blockIdx.x) * kRankRun;
+    for (uint32_t j = threadIdx.x; j < kRankRun; j += blockDim.x) out[j] = sk[j];
+}
+
+// Each point's ranks (keys below its own, summed over the runs), added into
+// the packed words pa = r0 | r1 << 16, pb = r2 | r3 << 16 (zeroed before):
+// block (run b of objective k, chunk c of the points) holds the run in shared
+// memory and counts, for each point of the chunk, the run's keys below the
+// point's key by binary search (the padding keys LLONG_MAX are never below a
+// point's key: NaN's key is LLONG_MAX too). A field's sum is the rank, below
+// 2^15, so the additions never carry into the next field.
+__global__ void __launch_bounds__(256) rank_search_kernel(const long long *__restrict__ keys, uint32_t n,
+                                                          const long long *__restrict__ runs, uint32_t nb,
+                                                          uint32_t *__restrict__ pa, uint32_t *__restrict__ pb)
+{
+    __shared__ long long sk[kRankRun];
+    const uint32_t k = blockIdx.y / nb, b = blockIdx.y - k * nb;
+    const long long *run = runs + (static_cast<uint64_t>(k) * nb + b) * kRankRun;
+    for (uint32_t j = threadIdx.x; j < kRankRun; j += blockDim.x) sk[j] = run[j];
+    __syncthreads();
+    uint32_t *dst = (k >> 1) ? pb : pa;
+    const uint32_t shift = 16u * (k & 1u);
+    const uint32_t t1 = min(n, (blockIdx.x + 1u) * 1024u);
+    for (uint32_t t = blockIdx.x * 1024u + threadIdx.x; t < t1; t += blockDim.x) {
+        const long long x = keys[static_cast<uint64_t>(k) * n + t];
+        uint32_t lo = 0;
+#pragma unroll
+        for (uint32_t step = kRankRun / 2u; step > 0; step >>= 1)
+            if (sk[lo + step - 1u] < x) lo += step;
+        lo += sk[lo] < x ? 1u : 0u;
+        if (lo) atomicAdd(dst + t, lo << shift);
+    }
+}
+
+// dominance_sym_kernel on packed ranks (NW = 1: m <= 2, NW = 2: m <= 4).
+template <int NW>
+__global__ void __launch_bounds__(256) dominance_sym_packed_kernel(const uint32_t *__restrict__ pa,
+                                                                   const uint32_t *__restrict__ pb, uint32_t n,
+                                                                   uint32_t W8, uint32_t *__restrict__ Dt)
+{
+    __shared__ uint32_t ja[32], jb[32];
+    __shared__ uint32_t tile[32][9];
+    const uint32_t bj = blockIdx.y;
+    const uint32_t bi0 = blockIdx.x * 8u;
+    if (bi0 > bj) return;
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t J0 = bj * 32u;
+    if (threadIdx.x < 32u) {
+        const uint32_t j = J0 + threadIdx.x;
+        ja[threadIdx.x] = j < n ? pa[j] : 0u;
+        jb[threadIdx.x] = j < n && NW == 2 ? pb[j] : 0u;
+    }
+    __syncthreads();
+    const uint32_t bi = bi0 + warp;
+    const bool active = bi <= bj;
+    const uint32_t i = bi * 32u + lane;
+    const bool iv = active && i < n;
+    const uint32_t ia = iv ? pa[i] : 0u, ib = iv && NW == 2 ? pb[i] : 0u;
+    const uint32_t iag = ia | kRankGuard, ibg = ib | kRankGuard;
+    uint32_t row_i = 0u;
+    if (active) {
+        for (unsigned jj = 0; jj < 32u; ++jj) {
+            const uint32_t a = ja[jj], b = jb[jj];
+            uint32_t le_ij = (a | kRankGuard) - ia; // i no worse than j in the fields of word a
+            uint32_t le_ji = iag - a;               // j no worse than i
+            bool ne = ia != a;
+            if (NW == 2) {
+                le_ij &= (b | kRankGuard) - ib;
+                le_ji &= ibg - b;
+                ne |= ib != b;
+            }
+            const bool valid = iv && J0 + jj < n && ne;
+            const bool i_dom_j = valid && (le_ij & kRankGuard) == kRankGuard;
+            const bool j_dom_i = valid && (le_ji & kRankGuard) == kRankGuard;
+            const unsigned word = __ballot_sync(kFull, i_dom_j);
+            if (lane == 0) tile[jj][warp] = word;
+            row_i |= static_cast<uint32_t>(j_dom_i) << jj;
+        }
+        if (bi != bj && i < n) Dt[static_cast<uint64_t>(i) * W8 + bj] = row_i;
+    }
+    __syncthreads();
+    const unsigned jj = threadIdx.x >> 3, ww = threadIdx.x & 7u;
+    const uint32_t j = J0 + jj;
+    if (j < n && bi0 + ww <= bj) Dt[static_cast<uint64_t>(j) * W8 + bi0 + ww] = tile[jj][ww];
+}
+
 // CTA tile: 32 dominated candidates j (rows of Dt) x 256 dominators i (8 words).
 // Warp w tests i = 32*(w0+w) + lane against each j and ballots the row word.
 // M > 0: objectives in registers; M == 0: runtime m, keys read from global.
@@ -1655,8 +1783,33 @@ int blocks_for(uint64_t work, int threads, int num_sms)
 }
 
 int launch_dominance(const long long *keys, uint32_t n, uint32_t m, uint32_t W, uint32_t W8, uint32_t *Dt,
-                     int32_t *dom_count, cudaStream_t s)
+                     int32_t *dom_count, long long *runs, uint32_t *packed, int num_sms, cudaStream_t s,
+                     uint64_t *launches)
 {
+    if (m >= 1u && m <= 4u && n <= kRankPoints && runs != nullptr) {
+        if (W8 > W)
+            PGX_CUDA(cudaMemset2DAsync(Dt + W, static_cast<size_t>(W8) * 4u, 0, static_cast<size_t>(W8 - W) * 4u, n,
+                                       s));
+        const uint32_t nb = (n + kRankRun - 1u) / kRankRun;
+        rank_runs_kernel<<<dim3(nb, m), kRankRun / 2u, 0, s>>>(keys, n, runs);
+        PGX_CUDA(cudaGetLastError());
+        uint32_t *pa = packed, *pb = packed + n;
+        PGX_CUDA(cudaMemsetAsync(packed, 0, 2u * static_cast<size_t>(n) * sizeof(uint32_t), s));
+        rank_search_kernel<<<dim3((n + 1023u) / 1024u, nb * m), 256, 0, s>>>(keys, n, runs, nb, pa, pb);
+        PGX_CUDA(cudaGetLastError());
+        dim3 grid((W + 7u) / 8u, W);
+        if (m <= 2u)
+            dominance_sym_packed_kernel<1><<<grid, 256, 0, s>>>(pa, pb, n, W8, Dt);
+        else
+            dominance_sym_packed_kernel<2><<<grid, 256, 0, s>>>(pa, pb, n, W8, Dt);
+        PGX_CUDA(cudaGetLastError());
+        const int blocks = static_cast<int>(std::min<uint64_t>((static_cast<uint64_t>(n) + 7u) / 8u, 65535u));
+        row_popcount_kernel<<<blocks, 256, 0, s>>>(Dt, n, W8, dom_count);
+        PGX_CUDA(cudaGetLastError());
+        *launches += 4;
+        return PGX_OK;
+    }
+    *launches += m <= 4u ? 2 : 1; // dominance tiles (+ row popcounts)
     if (m >= 1u && m <= 4u) {
         // symmetric tiles cover words 0 .. W-1 of every row; zero the padding words W .. W8-1
         if (W8 > W)
@@ -1732,7 +1885,13 @@ struct survival_scratch {
     int2 *wlist;         // n sort ranges
     int32_t *wpos;       // 2 n sort stopper positions
     double *wcd;         // n crowding distances (select_best_N_mo, sort_population_mo)
+    long long *runs;     // m * ceil(n / kRankRun) * kRankRun sorted key runs (n <= kRankPoints, m <= 4)
 };
+
+constexpr uint64_t rank_runs_bytes(uint64_t n, uint64_t m)
+{
+    return n <= kRankPoints && m >= 1u && m <= 4u ? m * ((n + kRankRun - 1u) / kRankRun) * kRankRun * 8u : 0u;
+}
 
 constexpr size_t survival_scratch_bytes(uint64_t n, uint64_t m)
 {
@@ -1740,7 +1899,8 @@ constexpr size_t survival_scratch_bytes(uint64_t n, uint64_t m)
            + align256(n * ((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u) + align256(sizeof(peel_state))
            + align256(((((n + 31u) / 32u) + 7u) & ~uint64_t(7)) * 4u) + 2u * align256(2u * n * 4u)
            + align256(n * 4u) + align256((n + 2u) * 4u) + align256(n * 16u)
-           + align256(n * 4u) + align256(n * sizeof(int2)) + align256(2u * n * 4u) + align256(n * sizeof(double));
+           + align256(n * 4u) + align256(n * sizeof(int2)) + align256(2u * n * 4u) + align256(n * sizeof(double))
+           + align256(rank_runs_bytes(n, m));
 }
 
 survival_scratch carve_survival_scratch(void *base, uint64_t n, uint64_t m)
@@ -1774,6 +1934,8 @@ survival_scratch carve_survival_scratch(void *base, uint64_t n, uint64_t m)
     s.wpos = reinterpret_cast<int32_t *>(p);
     p += align256(2u * n * 4u);
     s.wcd = reinterpret_cast<double *>(p);
+    p += align256(n * sizeof(double));
+    s.runs = rank_runs_bytes(n, m) ? reinterpret_cast<long long *>(p) : nullptr;
     return s;
 }
 
@@ -1837,8 +1999,10 @@ int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n,
         order_keys_kernel<<<blocks_for(static_cast<uint64_t>(n) * m, 256, num_sms), 256, 0, s>>>(d_points, n, m,
                                                                                                  sc.keys);
         PGX_CUDA(cudaGetLastError());
-        PGX_TRY(launch_dominance(sc.keys, n, m, W, W8, sc.Dt, out.dom_count, s));
-        *launches += m <= 4u ? 3 : 2; // keys, dominance tiles (+ row popcounts)
+        // the packed ranks borrow the keyv area (2 n words), free until the peel
+        PGX_TRY(launch_dominance(sc.keys, n, m, W, W8, sc.Dt, out.dom_count, sc.runs,
+                                 reinterpret_cast<uint32_t *>(sc.keyv), num_sms, s, launches));
+        *launches += 1; // keys
     } else {
         PGX_CUDA(cudaMemsetAsync(sc.Dt, 0, static_cast<size_t>(n) * W8 * sizeof(uint32_t), s));
     }
@@ -2217,8 +2381,13 @@ constexpr uint64_t kNoAllocMaxPoints = 4096;
 constexpr uint64_t kNoAllocMaxObjectives = 8;
 constexpr int kNoAllocMaxDevices = 64;
 
-static __device__ __align__(256) unsigned char g_noalloc_scratch[survival_scratch_bytes(kNoAllocMaxPoints,
-                                                                                        kNoAllocMaxObjectives)];
+// the largest layout of at most kNoAllocMaxPoints points and kNoAllocMaxObjectives
+// objectives (up to 4 objectives the layout adds the sorted rank runs)
+constexpr size_t kNoAllocBytes = survival_scratch_bytes(kNoAllocMaxPoints, kNoAllocMaxObjectives)
+                                         > survival_scratch_bytes(kNoAllocMaxPoints, 4)
+                                     ? survival_scratch_bytes(kNoAllocMaxPoints, kNoAllocMaxObjectives)
+                                     : survival_scratch_bytes(kNoAllocMaxPoints, 4);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 struct noalloc_device {
     void *context = nullptr; // the CUDA context the set-up ran in
@@ -2260,6 +2429,10 @@ int noalloc_load_kernels()
         reinterpret_cast<const void *>(dominance_sym_kernel<4>),
         reinterpret_cast<const void *>(dominance_kernel<0>),
         reinterpret_cast<const void *>(row_popcount_kernel),
+        reinterpret_cast<const void *>(rank_runs_kernel),
+        reinterpret_cast<const void *>(rank_search_kernel),
+        reinterpret_cast<const void *>(dominance_sym_packed_kernel<1>),
+        reinterpret_cast<const void *>(dominance_sym_packed_kernel<2>),
         reinterpret_cast<const void *>(rem_outside_front0_kernel),
         reinterpret_cast<const void *>(witness_init_kernel),
         reinterpret_cast<const void *>(peel2_kernel),
