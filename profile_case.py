@@ -19,6 +19,8 @@ profiler are not benchmark values). Cases:
   sort_population               sort_population_mo(--rows nested-front points x 3)
   hypervolume                   hypervolume of --rows nested-front points x 3 (reference point max + 0.5)
   archipelago                   the fused kernel of a 64-island mixed epoch (--rows unused)
+  refine_rastrigin / refine_rosenbrock / refine_lj   batched basin hopping with gradient descent
+                                (10 trials, stop 5, 20 steps) on --rows individuals
 """
 from __future__ import annotations
 
@@ -63,6 +65,24 @@ def main() -> None:
 
         def run():
             ep.launch_device(sp)
+    elif a.case.startswith("refine_"):
+        import ctypes as C
+
+        kind, param, x = {"refine_rastrigin": (N.RASTRIGIN, a.dim or 50, lambda: W.rastrigin_batch(n, a.dim or 50)),
+                          "refine_rosenbrock": (N.ROSENBROCK, a.dim or 1000,
+                                                lambda: W.rosenbrock_batch(n, a.dim or 1000)),
+                          "refine_lj": (N.LENNARD_JONES, a.atoms, lambda: W.lj_batch(n, a.atoms))}[a.case]
+        d0 = torch.from_numpy(x()).cuda()
+        dx = torch.empty_like(d0)
+        df = torch.empty(n, dtype=torch.float64, device="cuda")
+        de = torch.zeros(1, dtype=torch.int64, device="cuda")
+        params = N.pgx_refine_params(10, 5, 20, 0.02, 0.05, 1e-7, 7)
+
+        def run():
+            with torch.cuda.stream(stream):
+                dx.copy_(d0)
+            N.check(L.pgx_refine_batch_device(ctx.handle, kind, param, C.byref(params), dx.data_ptr(), n,
+                                              df.data_ptr(), de.data_ptr(), sp))
     elif a.case == "survival":
         p = W.nsga2_points(n, 3, layers=a.layers)
         dp = torch.from_numpy(p).cuda()
