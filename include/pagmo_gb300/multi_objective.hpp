@@ -156,12 +156,11 @@ inline nsga2_survival_result nsga2_survival(const std::vector<pagmo::vector_doub
     return r;
 }
 
-// hypervolume(points).compute(ref) for 2 or 3 objectives
-// (src/utils/hypervolume.cpp:203-228, hv2d / hv3d) on the GPU, with the
-// reference's checks and messages; 4 or more objectives throw
-// pagmo::not_implemented_error.
-inline double hypervolume_compute(const std::vector<pagmo::vector_double> &points, const pagmo::vector_double &ref,
-                                  int device = 0)
+namespace detail
+{
+// The points row-major, after hypervolume's construction and dimension checks
+// (src/utils/hypervolume.cpp:406-449).
+inline std::vector<double> hv_rows(const std::vector<pagmo::vector_double> &points, const pagmo::vector_double &ref)
 {
     if (points.empty()) throw std::invalid_argument("Point set cannot be empty.");
     const auto m = points[0].size();
@@ -174,9 +173,66 @@ inline double hypervolume_compute(const std::vector<pagmo::vector_double> &point
     }
     if (ref.size() != m)
         throw std::invalid_argument("Point set dimensions and reference point dimension must be equal.");
+    return flat;
+}
+} // namespace detail
+
+// hypervolume(points).compute(ref) (src/utils/hypervolume.cpp:203-228) on the
+// GPU for 2 to 16 objectives (hv2d / hv3d's value, hvwfg's bit for bit from 4
+// objectives on), with the reference's checks and messages; more than 16
+// objectives throw pagmo::not_implemented_error.
+inline double hypervolume_compute(const std::vector<pagmo::vector_double> &points, const pagmo::vector_double &ref,
+                                  int device = 0)
+{
+    const auto flat = detail::hv_rows(points, ref);
     double out = 0.0;
-    check(pgx_hypervolume(device_context(device), flat.data(), points.size(), m, ref.data(), &out));
+    check(pgx_hypervolume(device_context(device), flat.data(), points.size(), ref.size(), ref.data(), &out));
     return out;
+}
+
+// hypervolume(points).exclusive(p_idx, ref) (hypervolume.cpp:249-272).
+inline double hypervolume_exclusive(const std::vector<pagmo::vector_double> &points, unsigned p_idx,
+                                    const pagmo::vector_double &ref, int device = 0)
+{
+    const auto flat = detail::hv_rows(points, ref);
+    double out = 0.0;
+    check(pgx_hypervolume_exclusive(device_context(device), flat.data(), points.size(), ref.size(), ref.data(), p_idx,
+                                    &out));
+    return out;
+}
+
+// hypervolume(points).contributions(ref) (hypervolume.cpp:293-320), by
+// hvwfg's limit sets.
+inline std::vector<double> hypervolume_contributions(const std::vector<pagmo::vector_double> &points,
+                                                     const pagmo::vector_double &ref, int device = 0)
+{
+    const auto flat = detail::hv_rows(points, ref);
+    std::vector<double> out(points.size());
+    check(pgx_hypervolume_contributions(device_context(device), flat.data(), points.size(), ref.size(), ref.data(),
+                                        out.data()));
+    return out;
+}
+
+// hypervolume(points).least_contributor(ref) / greatest_contributor(ref)
+// (hypervolume.cpp:333-401).
+inline unsigned long long hypervolume_least_contributor(const std::vector<pagmo::vector_double> &points,
+                                                        const pagmo::vector_double &ref, int device = 0)
+{
+    const auto flat = detail::hv_rows(points, ref);
+    std::uint64_t idx = 0;
+    check(pgx_hypervolume_extreme_contributor(device_context(device), flat.data(), points.size(), ref.size(),
+                                              ref.data(), 0, &idx));
+    return idx;
+}
+
+inline unsigned long long hypervolume_greatest_contributor(const std::vector<pagmo::vector_double> &points,
+                                                           const pagmo::vector_double &ref, int device = 0)
+{
+    const auto flat = detail::hv_rows(points, ref);
+    std::uint64_t idx = 0;
+    check(pgx_hypervolume_extreme_contributor(device_context(device), flat.data(), points.size(), ref.size(),
+                                              ref.data(), 1, &idx));
+    return idx;
 }
 
 } // namespace pagmo_gb300

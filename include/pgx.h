@@ -192,15 +192,17 @@ PGX_API int pgx_mo_p_distance(pgx_context *ctx, const pgx_mo_problem *p, const d
 
 /* ------------------------------------------------------------- hypervolume */
 
-/* hypervolume(points).compute(ref) for 2 or 3 objectives
-   (src/utils/hypervolume.cpp:203-228 with hv2d / hv3d,
-   src/utils/hv_algos/hv_hv2d.cpp:48-68, hv_hv3d.cpp:75-116): the measure of
-   the region the n points (row-major, m = 2 or 3) dominate, bounded by ref.
-   The reference's checks and messages (hypervolume.cpp:406-449,
-   hv_algorithm.cpp:226-258: empty set, NaN, a point outside or equal to the
-   reference point) give PGX_ERR_INVALID; 4 or more objectives (pagmo's hvwfg)
-   give PGX_ERR_NOTIMPL. FP64; the value differs from the reference's sweep
-   by summation order only (non-negative slabs, no cancellation). */
+/* hypervolume(points).compute(ref) (src/utils/hypervolume.cpp:203-228,
+   with the algorithm the reference picks: hv2d, hv3d or hvwfg,
+   src/utils/hv_algos/hv_hv2d.cpp:48-68, hv_hv3d.cpp:75-116,
+   hv_hvwfg.cpp:64-69): the measure of the region the n points (row-major, m
+   objectives) dominate, bounded by ref. The reference's checks and messages
+   (hypervolume.cpp:406-449, hv_algorithm.cpp:226-258: empty set, NaN, a point
+   outside or equal to the reference point) give PGX_ERR_INVALID; more than
+   16 objectives give PGX_ERR_NOTIMPL. FP64. For 2 and 3 objectives the value
+   differs from the reference's sweep by summation order only (non-negative
+   slabs, no cancellation); for 4 to 16 it is the reference's hvwfg value bit
+   for bit. */
 PGX_API int pgx_hypervolume(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, const double *ref,
                             double *out);
 
@@ -210,6 +212,43 @@ PGX_API int pgx_hypervolume(pgx_context *ctx, const double *points, uint64_t n, 
    caller's. */
 PGX_API int pgx_hypervolume_device(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m,
                                    const double *ref, double *d_out, void *stream);
+
+/* hypervolume(points).exclusive(p_idx, ref) (hypervolume.cpp:249-272 with
+   hv_algorithm::exclusive, hv_algorithm.cpp:93-106): the volume of all the
+   points minus the volume without point p_idx, both on the GPU (a lone
+   point: its volume). The reference's checks come first, then an index
+   p_idx >= n gives PGX_ERR_INVALID ("Index of the individual is out of
+   bounds."). */
+PGX_API int pgx_hypervolume_exclusive(pgx_context *ctx, const double *points, uint64_t n, uint64_t m,
+                                      const double *ref, uint64_t p_idx, double *out);
+
+/* hypervolume(points).contributions(ref) (hypervolume.cpp:293-320): out[i] =
+   the volume only point i dominates, by hvwfg's contributions
+   (hv_hvwfg.cpp:79-105): vol(p_i) - hv(limit set of p_i). For 4 to 16
+   objectives this is the algorithm the reference picks and the values are
+   its bit for bit; for 3 objectives the reference's hv3d (HyCon3D,
+   hv_hv3d.cpp:170-300) sums boxes instead and falls back to the same hvwfg
+   when a point is dominated; for 2, hv2d hands hv3d the points with a third
+   coordinate 0 and a reference 1, and so does this call. A lone point: its
+   volume |prod (p_c - r_c)| (hypervolume.cpp:303-307). Checks as
+   pgx_hypervolume. */
+PGX_API int pgx_hypervolume_contributions(pgx_context *ctx, const double *points, uint64_t n, uint64_t m,
+                                          const double *ref, double *out);
+
+/* Device-resident variant: d_points and d_out (n doubles) on the device, ref
+   on the host, asynchronous on `stream`. A NaN in d_out marks a point whose
+   warp ran out of frame buffers (cannot happen with the fixed pool of m
+   frames of n rows per warp; the host variant reports it). */
+PGX_API int pgx_hypervolume_contributions_device(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m,
+                                                 const double *ref, double *d_out, void *stream);
+
+/* least_contributor(ref) (greatest = 0) or greatest_contributor(ref)
+   (greatest = 1) (hypervolume.cpp:333-401, hv_algorithm.cpp:136-157 and
+   329-349): the first index of the smallest / largest contribution, the
+   contributions as pgx_hypervolume_contributions computes them; 0 for a
+   lone point. */
+PGX_API int pgx_hypervolume_extreme_contributor(pgx_context *ctx, const double *points, uint64_t n, uint64_t m,
+                                                const double *ref, int greatest, uint64_t *idx);
 
 /* --------------------------------------------------- NSGA-II survival (MO) */
 

@@ -121,6 +121,8 @@ class _Oracle:
         h.orc_zdt_p_distance.restype = C.c_double
         h.orc_zdt_p_distance.argtypes = [C.c_uint, _vp, _u64]
         h.orc_hypervolume_ld.argtypes = [_vp, _u64, _u64, _vp, _vp]
+        h.orc_hvwfg.argtypes = [_vp, _u64, _u64, _vp, _vp]
+        h.orc_hvwfg_contributions.argtypes = [_vp, _u64, _u64, _vp, _vp]
         h.orc_mo_dims.argtypes = [C.c_int, C.c_uint, _u64, _u64, _vp, _vp]
         h.orc_mo_batch_fitness.argtypes = [C.c_int, C.c_uint, _u64, _u64, C.c_uint, _vp, _u64, _u64, _vp, C.c_int]
         h.orc_mo_batch_fitness_ld.argtypes = [C.c_int, C.c_uint, _u64, _u64, C.c_uint, _vp, _u64, _u64, _vp, _vp,
@@ -259,6 +261,24 @@ class _Oracle:
             raise ValueError("hypervolume oracle: 2 or 3 objectives and at least one point")
         return out.value
 
+    def hvwfg(self, pts, ref):
+        """WFG hypervolume in double, the reference's operation order (any m >= 2)."""
+        p = _pts2d(pts)
+        r = np.ascontiguousarray(ref, dtype=np.float64)
+        out = C.c_double()
+        if self.h.orc_hvwfg(_p(p), p.shape[0], p.shape[1], _p(r), C.byref(out)) != 0:
+            raise ValueError("hvwfg oracle: at least one point of 2 or more objectives")
+        return out.value
+
+    def hvwfg_contributions(self, pts, ref):
+        """Every point's exclusive contribution, WFG in double (any m >= 2)."""
+        p = _pts2d(pts)
+        r = np.ascontiguousarray(ref, dtype=np.float64)
+        out = np.empty(p.shape[0])
+        if self.h.orc_hvwfg_contributions(_p(p), p.shape[0], p.shape[1], _p(r), _p(out)) != 0:
+            raise ValueError("hvwfg oracle: at least one point of 2 or more objectives")
+        return out
+
     # ZDT / DTLZ ------------------------------------------------------------------
     # spec = (family, prob_id, param, fdim, alpha): family 7 = zdt{prob_id, param},
     # family 8 = dtlz{prob_id, dim=param, fdim, alpha} (the GPU library's kinds).
@@ -324,6 +344,10 @@ class _Reference:
         h.ref_sort_population_mo.argtypes = [_vp, _u64, _u64, _vp]
         mo = [C.c_int, C.c_uint, _u64, _u64, C.c_uint]
         h.ref_hypervolume.argtypes = [_vp, _u64, _u64, _vp, _vp]
+        h.ref_hv_exclusive.argtypes = [_vp, _u64, _u64, _vp, _u64, _vp]
+        h.ref_hv_contributions.argtypes = [_vp, _u64, _u64, _vp, C.c_int, _vp]
+        h.ref_hv_extreme.argtypes = [_vp, _u64, _u64, _vp, C.c_int, _vp]
+        h.ref_hvwfg_compute.argtypes = [_vp, _u64, _u64, _vp, _vp]
         h.ref_mo_dims.argtypes = mo + [_vp, _vp, _vp]
         h.ref_mo_bounds.argtypes = mo + [_vp, _vp]
         h.ref_mo_thread_bfe.argtypes = mo + [_vp, _u64, _u64, _vp]
@@ -433,6 +457,38 @@ class _Reference:
         r = np.ascontiguousarray(ref, dtype=np.float64)
         out = C.c_double()
         self._chk(self.h.ref_hypervolume(_p(p), p.shape[0], p.shape[1], _p(r), C.byref(out)))
+        return out.value
+
+    def hv_exclusive(self, pts, ref, p_idx):
+        """hypervolume(points, true).exclusive(p_idx, ref) of the reference."""
+        p = _pts2d(pts)
+        r = np.ascontiguousarray(ref, dtype=np.float64)
+        out = C.c_double()
+        self._chk(self.h.ref_hv_exclusive(_p(p), p.shape[0], p.shape[1], _p(r), int(p_idx), C.byref(out)))
+        return out.value
+
+    def hv_contributions(self, pts, ref, wfg=False):
+        """hypervolume(points, true).contributions(ref) of the reference (hvwfg() given explicitly with wfg)."""
+        p = _pts2d(pts)
+        r = np.ascontiguousarray(ref, dtype=np.float64)
+        out = np.empty(p.shape[0])
+        self._chk(self.h.ref_hv_contributions(_p(p), p.shape[0], p.shape[1], _p(r), int(bool(wfg)), _p(out)))
+        return out
+
+    def hv_extreme(self, pts, ref, greatest):
+        """least_contributor(ref) / greatest_contributor(ref) of the reference."""
+        p = _pts2d(pts)
+        r = np.ascontiguousarray(ref, dtype=np.float64)
+        out = C.c_uint64()
+        self._chk(self.h.ref_hv_extreme(_p(p), p.shape[0], p.shape[1], _p(r), int(bool(greatest)), C.byref(out)))
+        return out.value
+
+    def hvwfg(self, pts, ref):
+        """hypervolume(points, true).compute(ref, hvwfg()) of the reference."""
+        p = _pts2d(pts)
+        r = np.ascontiguousarray(ref, dtype=np.float64)
+        out = C.c_double()
+        self._chk(self.h.ref_hvwfg_compute(_p(p), p.shape[0], p.shape[1], _p(r), C.byref(out)))
         return out.value
 
     # ZDT / DTLZ (spec as in the oracle) ---------------------------------------------

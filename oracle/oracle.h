@@ -127,6 +127,11 @@ int orc_mo_batch_p_distance(int family, unsigned prob_id, uint64_t param, uint64
 /* ---- hypervolume of 2 or 3 objectives, long double (hypervolume.cpp) ---- */
 int orc_hypervolume_ld(const double *pts, uint64_t n, uint64_t m, const double *ref, double *out);
 
+/* ---- WFG (hvwfg, stop dimension 2) in double, the reference's operation
+   order: the volume, and every point's exclusive contribution ---- */
+int orc_hvwfg(const double *pts, uint64_t n, uint64_t m, const double *ref, double *out);
+int orc_hvwfg_contributions(const double *pts, uint64_t n, uint64_t m, const double *ref, double *out);
+
 #ifdef __cplusplus
 }
 #endif

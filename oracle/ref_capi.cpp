@@ -5,6 +5,7 @@
 // Every function catches exceptions and returns a status (0 = ok, 1 = the
 // reference threw std::invalid_argument, 2 = any other exception); the
 // message of the last error is available from ref_last_error().
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <exception>
@@ -24,6 +25,7 @@
 #include <pagmo/problems/rosenbrock.hpp>
 #include <pagmo/problems/schwefel.hpp>
 #include <pagmo/problems/zdt.hpp>
+#include <pagmo/utils/hv_algos/hv_hvwfg.hpp>
 #include <pagmo/utils/hypervolume.hpp>
 #include <pagmo/utils/multi_objective.hpp>
 
@@ -207,6 +209,49 @@ int ref_hypervolume(const double *pts, std::uint64_t n, std::uint64_t m, const d
     return guard([&] {
         pagmo::hypervolume hv(rows(pts, n, m), true);
         *out = hv.compute(pagmo::vector_double(r, r + m));
+    });
+}
+
+// hypervolume(points, true).exclusive(p_idx, ref), .contributions(ref),
+// .least_contributor(ref), .greatest_contributor(ref)
+// (src/utils/hypervolume.cpp:249-401), each with the algorithm the reference
+// picks for the dimension; with wfg != 0, hvwfg() given explicitly.
+int ref_hv_exclusive(const double *pts, std::uint64_t n, std::uint64_t m, const double *r, std::uint64_t p_idx,
+                     double *out)
+{
+    return guard([&] {
+        pagmo::hypervolume hv(rows(pts, n, m), true);
+        *out = hv.exclusive(static_cast<unsigned>(p_idx), pagmo::vector_double(r, r + m));
+    });
+}
+
+int ref_hv_contributions(const double *pts, std::uint64_t n, std::uint64_t m, const double *r, int wfg, double *out)
+{
+    return guard([&] {
+        pagmo::hypervolume hv(rows(pts, n, m), true);
+        const pagmo::vector_double rv(r, r + m);
+        pagmo::hvwfg algo;
+        const auto c = wfg ? hv.contributions(rv, algo) : hv.contributions(rv);
+        std::copy(c.begin(), c.end(), out);
+    });
+}
+
+int ref_hv_extreme(const double *pts, std::uint64_t n, std::uint64_t m, const double *r, int greatest,
+                   std::uint64_t *idx)
+{
+    return guard([&] {
+        pagmo::hypervolume hv(rows(pts, n, m), true);
+        const pagmo::vector_double rv(r, r + m);
+        *idx = greatest ? hv.greatest_contributor(rv) : hv.least_contributor(rv);
+    });
+}
+
+int ref_hvwfg_compute(const double *pts, std::uint64_t n, std::uint64_t m, const double *r, double *out)
+{
+    return guard([&] {
+        pagmo::hypervolume hv(rows(pts, n, m), true);
+        pagmo::hvwfg algo;
+        *out = hv.compute(pagmo::vector_double(r, r + m), algo);
     });
 }
 

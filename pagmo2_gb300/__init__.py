@@ -13,7 +13,8 @@ plugin interface for the batch-fitness path:
                     pagmo's input/output checks and fevals accounting
   multi_objective:  fast_non_dominated_sorting, crowding_distance,
                     nsga2_survival, select_best_N_mo, sort_population_mo,
-                    hypervolume (2 or 3 objectives)
+                    hypervolume (2 to 16 objectives: compute, exclusive,
+                    contributions, least / greatest contributor)
   algorithms:       gpu_mbh (monotonic basin hopping with gradient descent on
                     every individual of a batch at once)
   workloads:        seeded synthetic inputs

@@ -65,6 +65,10 @@ SIGNATURES = {
     "pgx_selftest_lj_reciprocal": (C.c_int, [_vp, _vp, _u64, _vp, _vp]),
     "pgx_hypervolume": (C.c_int, [_vp, _vp, _u64, _u64, _vp, C.POINTER(C.c_double)]),
     "pgx_hypervolume_device": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp]),
+    "pgx_hypervolume_exclusive": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _u64, C.POINTER(C.c_double)]),
+    "pgx_hypervolume_contributions": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp]),
+    "pgx_hypervolume_contributions_device": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp]),
+    "pgx_hypervolume_extreme_contributor": (C.c_int, [_vp, _vp, _u64, _u64, _vp, C.c_int, C.POINTER(_u64)]),
 }
 
 

@@ -341,7 +341,7 @@ void pgx_context_destroy(pgx_context *ctx)
     for (auto &ev : ctx->chunk_ev)
         if (ev) cudaEventDestroy(ev);
     for (pgx::dbuf *b : {&ctx->d_in, &ctx->d_out, &ctx->d_grad, &ctx->s_points,
-                         &ctx->s_state, &ctx->s_outs, &ctx->s_crowd, &ctx->r_work})
+                         &ctx->s_state, &ctx->s_outs, &ctx->s_crowd, &ctx->r_work, &ctx->h_wfg})
         b->release();
     for (cudaStream_t s : {ctx->stream, ctx->h2d, ctx->d2h})
         if (s) cudaStreamDestroy(s);

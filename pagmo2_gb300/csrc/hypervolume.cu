@@ -1,6 +1,9 @@
 // Hypervolume of 2 or 3 objectives on the GPU (pagmo's hypervolume::compute,
 // src/utils/hypervolume.cpp:203-228, which picks hv2d for two objectives and
-// hv3d for three: src/utils/hv_algos/hv_hv2d.cpp:48-68, hv_hv3d.cpp:75-116).
+// hv3d for three: src/utils/hv_algos/hv_hv2d.cpp:48-68, hv_hv3d.cpp:75-116),
+// and the C ABI of the hypervolume queries: compute (4 or more objectives by
+// hvwfg in hv_wfg.cu), exclusive, contributions and the least and greatest
+// contributors (hypervolume.cpp:249-401).
 //
 // The dominated region is summed as non-negative slabs (no cancellation):
 //  - 2D: with the points sorted by y, the staircase width W(t) = max over the
@@ -306,8 +309,9 @@ int hv_check(const double *pts, uint64_t n, uint64_t m, const double *r)
     for (uint64_t i = 0; i < n * m; ++i)
         PGX_CHECK(!std::isnan(pts[i]), PGX_ERR_INVALID,
                   "A nan value has been encountered in the hypervolume points. Cannot construct the hypervolume object");
-    PGX_CHECK(m == 2u || m == 3u, PGX_ERR_NOTIMPL,
-              "hypervolume on the GPU: 2 or 3 objectives (pagmo's hv2d and hv3d); " + std::to_string(m) + " given");
+    PGX_CHECK(m <= kWfgMaxObjectives, PGX_ERR_NOTIMPL,
+              "hypervolume on the GPU: at most " + std::to_string(kWfgMaxObjectives) + " objectives; " +
+                  std::to_string(m) + " given");
     for (uint64_t i = 0; i < n; ++i) {
         bool outside = false, all_equal = true;
         for (uint64_t k = 0; k < m; ++k) {
@@ -340,10 +344,12 @@ size_t align256(size_t b)
     return (b + 255u) & ~size_t(255);
 }
 
-// All kernels on stream s over device points; *d_out receives the volume.
+// All kernels on stream s over device points; *d_out receives the volume
+// (4 or more objectives: hvwfg, hv_wfg.cu).
 int launch_hypervolume(pgx_context *ctx, const double *d_pts, uint32_t n, uint32_t m, const double *r,
                        double *d_out, cudaStream_t s)
 {
+    if (m >= 4u) return launch_wfg_compute(ctx, d_pts, n, m, r, d_out, s);
     const uint32_t nc = m == 3u ? 3u : 1u; // coordinates ranked: y (and z, x for 3D)
     const int sms = ctx->num_sms;
     const int g1 = static_cast<int>(std::min<uint64_t>((n + 255u) / 256u, static_cast<uint64_t>(sms) * 8u));
@@ -386,6 +392,78 @@ int launch_hypervolume(pgx_context *ctx, const double *d_pts, uint32_t n, uint32
     return PGX_OK;
 }
 
+// *out = a - b
+__global__ void hv_sub_kernel(const double *__restrict__ a, const double *__restrict__ b, double *__restrict__ out)
+{
+    if (threadIdx.x == 0) *out = __dsub_rn(*a, *b);
+}
+
+// *idx = the first index of the smallest (greatest = 0) or largest
+// (greatest = 1) of c[0 .. n): hv_algorithm::extreme_contributor's strict
+// scan from index 0 (hv_algorithm.cpp:329-349), as a reduction that prefers
+// the lower index on ties.
+__global__ void __launch_bounds__(1024) hv_extreme_kernel(const double *__restrict__ c, uint32_t n, int greatest,
+                                                          unsigned long long *__restrict__ idx)
+{
+    __shared__ double sv[1024];
+    __shared__ uint32_t si[1024];
+    double best = 0.0;
+    uint32_t bi = UINT32_MAX;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double v = c[i];
+        if (bi == UINT32_MAX || (greatest ? v > best : v < best)) {
+            best = v;
+            bi = i;
+        }
+    }
+    sv[threadIdx.x] = best;
+    si[threadIdx.x] = bi;
+    __syncthreads();
+    for (unsigned h = blockDim.x / 2u; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            const double v = sv[threadIdx.x + h];
+            const uint32_t j = si[threadIdx.x + h];
+            const uint32_t i = si[threadIdx.x];
+            const bool take = j != UINT32_MAX &&
+                              (i == UINT32_MAX || (greatest ? v > sv[threadIdx.x] : v < sv[threadIdx.x]) ||
+                               (v == sv[threadIdx.x] && j < i));
+            if (take) {
+                sv[threadIdx.x] = v;
+                si[threadIdx.x] = j;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *idx = si[0];
+}
+
+// The checks of hypervolume's construction and compute on host data, the
+// point count and the device, then the points on the device (s_points):
+// returns their address; tail_bytes more are reserved after them.
+int upload_points(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, const double *ref,
+                  size_t tail_bytes, double **dp, char **tail)
+{
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    PGX_CHECK((points != nullptr || n == 0) && ref != nullptr, PGX_ERR_INVALID, "null buffer");
+    PGX_TRY(hv_check(points, n, m, ref));
+    PGX_CHECK(n < (1u << 24), PGX_ERR_CAPACITY, "hypervolume: more than 2^24 points");
+    PGX_TRY(use_device(ctx));
+    const size_t bp = align256(static_cast<size_t>(n) * m * 8u);
+    PGX_TRY(ctx->s_points.ensure(bp + tail_bytes));
+    *dp = ctx->s_points.as<double>();
+    *tail = ctx->s_points.as<char>() + bp;
+    PGX_CUDA(cudaMemcpyAsync(*dp, points, static_cast<size_t>(n) * m * 8u, cudaMemcpyHostToDevice, ctx->stream));
+    return PGX_OK;
+}
+
+int wfg_ok(pgx_context *ctx)
+{
+    unsigned st = 0;
+    PGX_TRY(wfg_status(ctx, &st));
+    PGX_CHECK(st == 0u, PGX_ERR_CAPACITY, "hypervolume (WFG): a warp ran out of frame buffers");
+    return PGX_OK;
+}
+
 } // namespace
 } // namespace pgx
 
@@ -420,13 +498,113 @@ int pgx_hypervolume_device(pgx_context *ctx, const double *d_points, uint64_t n,
     PGX_CHECK(d_points != nullptr && d_out != nullptr && ref != nullptr, PGX_ERR_INVALID, "null buffer");
     PGX_CHECK(n > 0u, PGX_ERR_INVALID, "Point set cannot be empty.");
     PGX_CHECK(m > 1u, PGX_ERR_INVALID, "Points of dimension > 1 required.");
-    PGX_CHECK(m == 2u || m == 3u, PGX_ERR_NOTIMPL,
-              "hypervolume on the GPU: 2 or 3 objectives (pagmo's hv2d and hv3d); " + std::to_string(m) + " given");
+    PGX_CHECK(m <= kWfgMaxObjectives, PGX_ERR_NOTIMPL,
+              "hypervolume on the GPU: at most " + std::to_string(kWfgMaxObjectives) + " objectives; " +
+                  std::to_string(m) + " given");
     PGX_CHECK(n < (1u << 24), PGX_ERR_CAPACITY, "hypervolume: more than 2^24 points");
     std::lock_guard<std::mutex> g(ctx->lock);
     PGX_TRY(use_device(ctx));
     return launch_hypervolume(ctx, d_points, static_cast<uint32_t>(n), static_cast<uint32_t>(m), ref, d_out,
                               static_cast<cudaStream_t>(stream));
+}
+
+int pgx_hypervolume_exclusive(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, const double *ref,
+                              uint64_t p_idx, double *out)
+{
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    PGX_CHECK(out != nullptr && (points != nullptr || n == 0) && ref != nullptr, PGX_ERR_INVALID, "null buffer");
+    PGX_TRY(hv_check(points, n, m, ref)); // before the index, as hypervolume::exclusive (hypervolume.cpp:251-256)
+    PGX_CHECK(p_idx < n, PGX_ERR_INVALID, "Index of the individual is out of bounds.");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    const size_t bl = align256(static_cast<size_t>(n) * m * 8u);
+    double *dp = nullptr;
+    char *tail = nullptr;
+    PGX_TRY(upload_points(ctx, points, n, m, ref, bl + 256u, &dp, &tail));
+    double *less = reinterpret_cast<double *>(tail);
+    double *d3 = reinterpret_cast<double *>(tail + bl); // volume of all, of all but p_idx, their difference
+    cudaStream_t s = ctx->stream;
+    const auto nn = static_cast<uint32_t>(n), mm = static_cast<uint32_t>(m);
+    if (n == 1u) {
+        // hv_algorithm::exclusive of a lone point: the volume (hv_algorithm.cpp:96-98)
+        PGX_TRY(launch_hypervolume(ctx, dp, nn, mm, ref, d3 + 2, s));
+    } else {
+        const size_t row = static_cast<size_t>(m) * 8u;
+        if (p_idx > 0u) PGX_CUDA(cudaMemcpyAsync(less, dp, p_idx * row, cudaMemcpyDeviceToDevice, s));
+        if (p_idx + 1u < n)
+            PGX_CUDA(cudaMemcpyAsync(less + p_idx * m, dp + (p_idx + 1u) * m, (n - p_idx - 1u) * row,
+                                     cudaMemcpyDeviceToDevice, s));
+        PGX_TRY(launch_hypervolume(ctx, dp, nn, mm, ref, d3, s));
+        PGX_TRY(launch_hypervolume(ctx, less, nn - 1u, mm, ref, d3 + 1, s));
+        hv_sub_kernel<<<1, 32, 0, s>>>(d3, d3 + 1, d3 + 2);
+        PGX_CUDA(cudaGetLastError());
+        ++ctx->launches;
+    }
+    PGX_CUDA(cudaMemcpyAsync(out, d3 + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
+    PGX_CUDA(cudaStreamSynchronize(s));
+    if (m >= 4u) PGX_TRY(wfg_ok(ctx));
+    return PGX_OK;
+}
+
+int pgx_hypervolume_contributions(pgx_context *ctx, const double *points, uint64_t n, uint64_t m, const double *ref,
+                                  double *out)
+{
+    PGX_CHECK(out != nullptr, PGX_ERR_INVALID, "null buffer");
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    const size_t bo = align256(static_cast<size_t>(n) * 8u);
+    double *dp = nullptr;
+    char *tail = nullptr;
+    PGX_TRY(upload_points(ctx, points, n, m, ref, bo, &dp, &tail));
+    double *dc = reinterpret_cast<double *>(tail);
+    PGX_TRY(launch_wfg_contributions(ctx, dp, static_cast<uint32_t>(n), static_cast<uint32_t>(m), ref, dc,
+                                     ctx->stream));
+    PGX_CUDA(cudaMemcpyAsync(out, dc, static_cast<size_t>(n) * 8u, cudaMemcpyDeviceToHost, ctx->stream));
+    return wfg_ok(ctx);
+}
+
+int pgx_hypervolume_contributions_device(pgx_context *ctx, const double *d_points, uint64_t n, uint64_t m,
+                                         const double *ref, double *d_out, void *stream)
+{
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    PGX_CHECK(d_points != nullptr && d_out != nullptr && ref != nullptr, PGX_ERR_INVALID, "null buffer");
+    PGX_CHECK(n > 0u, PGX_ERR_INVALID, "Point set cannot be empty.");
+    PGX_CHECK(m > 1u, PGX_ERR_INVALID, "Points of dimension > 1 required.");
+    PGX_CHECK(m <= kWfgMaxObjectives, PGX_ERR_NOTIMPL,
+              "hypervolume on the GPU: at most " + std::to_string(kWfgMaxObjectives) + " objectives; " +
+                  std::to_string(m) + " given");
+    PGX_CHECK(n < (1u << 24), PGX_ERR_CAPACITY, "hypervolume: more than 2^24 points");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    PGX_TRY(use_device(ctx));
+    return launch_wfg_contributions(ctx, d_points, static_cast<uint32_t>(n), static_cast<uint32_t>(m), ref, d_out,
+                                    static_cast<cudaStream_t>(stream));
+}
+
+int pgx_hypervolume_extreme_contributor(pgx_context *ctx, const double *points, uint64_t n, uint64_t m,
+                                        const double *ref, int greatest, uint64_t *idx)
+{
+    PGX_CHECK(idx != nullptr, PGX_ERR_INVALID, "null buffer");
+    PGX_CHECK(ctx != nullptr, PGX_ERR_INVALID, "null context");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    const size_t bo = align256(static_cast<size_t>(n) * 8u);
+    double *dp = nullptr;
+    char *tail = nullptr;
+    PGX_TRY(upload_points(ctx, points, n, m, ref, bo + 256u, &dp, &tail));
+    if (n == 1u) { // hypervolume.cpp:339-342, hv_algorithm.cpp:332-335
+        *idx = 0;
+        return PGX_OK;
+    }
+    double *dc = reinterpret_cast<double *>(tail);
+    auto *di = reinterpret_cast<unsigned long long *>(tail + bo);
+    cudaStream_t s = ctx->stream;
+    PGX_TRY(launch_wfg_contributions(ctx, dp, static_cast<uint32_t>(n), static_cast<uint32_t>(m), ref, dc, s));
+    hv_extreme_kernel<<<1, 1024, 0, s>>>(dc, static_cast<uint32_t>(n), greatest ? 1 : 0, di);
+    PGX_CUDA(cudaGetLastError());
+    ++ctx->launches;
+    unsigned long long h = 0;
+    PGX_CUDA(cudaMemcpyAsync(&h, di, sizeof(h), cudaMemcpyDeviceToHost, s));
+    PGX_TRY(wfg_ok(ctx));
+    *idx = h;
+    return PGX_OK;
 }
 
 } // extern "C"

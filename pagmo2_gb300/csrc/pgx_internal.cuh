@@ -94,6 +94,8 @@ struct pgx_context {
     pgx::dbuf s_points, s_state, s_outs, s_crowd;
     // batched refinement: per-individual working points and gradients
     pgx::dbuf r_work;
+    // WFG hypervolume: work counter, status and the warps' frame pools
+    pgx::dbuf h_wfg;
 };
 
 namespace pgx
@@ -116,6 +118,24 @@ int host_rows(pgx_context *ctx, uint64_t nx, uint64_t out_w, const double *dvs, 
 // ------------------------------------------------------------ problem facts
 
 int problem_nx(int kind, uint64_t param, uint64_t *nx);
+
+// ------------------------------------------------------ WFG hypervolume
+
+// Most objectives the WFG kernels take (hv_wfg.cu).
+constexpr uint32_t kWfgMaxObjectives = 16;
+// The volume of n >= 1 device points of 2 <= m <= kWfgMaxObjectives
+// objectives by pagmo's hvwfg (stop dimension 2), r on the host; *d_out on
+// stream s. Bit-exact with the reference.
+int launch_wfg_compute(pgx_context *ctx, const double *d_pts, uint32_t n, uint32_t m, const double *r,
+                       double *d_out, cudaStream_t s);
+// Every point's exclusive contribution (d_out[n]) as pagmo's
+// hypervolume::contributions computes it for m >= 4 (hvwfg), and as hv3d /
+// hv2d's contributions do when they fall back to hvwfg for m = 3 / 2.
+int launch_wfg_contributions(pgx_context *ctx, const double *d_pts, uint32_t n, uint32_t m, const double *r,
+                             double *d_out, cudaStream_t s);
+// Synchronises ctx->stream and reads the status word of the last WFG warp
+// kernel (nonzero: a warp ran out of frame buffers; its outputs are NaN).
+int wfg_status(pgx_context *ctx, unsigned *status);
 
 // -------------------------------------------------------------- launchers
 

@@ -151,10 +151,13 @@ def std_sort_keys(keys, values=None, ctx: _nat.Context | None = None):
 
 
 class hypervolume:
-    """pagmo's hypervolume indicator (src/utils/hypervolume.cpp) for 2 or 3 objectives: compute(ref) is the
-    measure of the region the points dominate, bounded by the reference point, on the GPU (hv2d / hv3d's
-    result; 4 or more objectives, pagmo's hvwfg, raise NotImplementedError). Construction checks the points as
-    the reference does (hypervolume.cpp:406-432)."""
+    """pagmo's hypervolume indicator (src/utils/hypervolume.cpp) on the GPU, 2 to 16 objectives:
+    compute(ref) is the measure of the region the points dominate, bounded by the reference point (hv2d /
+    hv3d's result for 2 and 3 objectives, hvwfg's bit for bit for 4 and more); exclusive(p_idx, ref),
+    contributions(ref), least_contributor(ref) and greatest_contributor(ref) are the reference's queries
+    (hypervolume.cpp:249-401), the contributions by hvwfg's limit sets. Construction checks the points as the
+    reference does (hypervolume.cpp:406-432); every query checks the reference point
+    (hv_algorithm.cpp:226-258)."""
 
     def __init__(self, points, verify: bool = True, context: N.Context | None = None):
         rows = points.get_f() if hasattr(points, "get_f") else points
@@ -189,3 +192,48 @@ class hypervolume:
         out = C.c_double()
         N.check(N.lib().pgx_hypervolume(ctx.handle, N.ptr(self._points), n, m, N.ptr(r), C.byref(out)))
         return out.value
+
+    def _ref(self, ref):
+        r = np.ascontiguousarray(np.asarray(ref, dtype=np.float64).reshape(-1))
+        if r.size != self._points.shape[1]:
+            raise ValueError("Point set dimensions and reference point dimension must be equal.")
+        return r, (self._ctx if self._ctx is not None else N.default_context())
+
+    def refpoint(self, offset: float = 0.0) -> np.ndarray:
+        """The componentwise maximum of the points plus offset (hypervolume.cpp:160-180)."""
+        return self._points.max(axis=0) + float(offset)
+
+    def exclusive(self, p_idx: int, ref) -> float:
+        """The volume only point p_idx dominates: compute(ref) minus the volume without it."""
+        r, ctx = self._ref(ref)
+        n, m = self._points.shape
+        if int(p_idx) < 0:
+            raise ValueError("Index of the individual is out of bounds.")
+        out = C.c_double()
+        N.check(N.lib().pgx_hypervolume_exclusive(ctx.handle, N.ptr(self._points), n, m, N.ptr(r), int(p_idx),
+                                                  C.byref(out)))
+        return out.value
+
+    def contributions(self, ref) -> np.ndarray:
+        """Every point's exclusive contribution."""
+        r, ctx = self._ref(ref)
+        n, m = self._points.shape
+        out = np.empty(n)
+        N.check(N.lib().pgx_hypervolume_contributions(ctx.handle, N.ptr(self._points), n, m, N.ptr(r), N.ptr(out)))
+        return out
+
+    def _extreme(self, ref, greatest: bool) -> int:
+        r, ctx = self._ref(ref)
+        n, m = self._points.shape
+        out = C.c_uint64()
+        N.check(N.lib().pgx_hypervolume_extreme_contributor(ctx.handle, N.ptr(self._points), n, m, N.ptr(r),
+                                                            int(greatest), C.byref(out)))
+        return out.value
+
+    def least_contributor(self, ref) -> int:
+        """The first index of the smallest contribution."""
+        return self._extreme(ref, False)
+
+    def greatest_contributor(self, ref) -> int:
+        """The first index of the largest contribution."""
+        return self._extreme(ref, True)

@@ -28,6 +28,7 @@
 #include <pagmo/problems/schwefel.hpp>
 #include <pagmo/problems/translate.hpp>
 #include <pagmo/problems/zdt.hpp>
+#include <pagmo/utils/hypervolume.hpp>
 #include <pagmo/utils/multi_objective.hpp>
 
 #include <pagmo_gb300/gpu_bfe.hpp>
@@ -258,6 +259,24 @@ int main()
             }
             CHECK(better > 32);
             CHECK(pop.get_problem().get_fevals() > fe0 + 64u);
+        }
+        // hypervolume queries against pagmo::hypervolume: 5 objectives (hvwfg) bit for bit
+        {
+            std::vector<pagmo::vector_double> pts;
+            for (unsigned i = 0; i < 40u; ++i) {
+                pagmo::vector_double q(5);
+                for (unsigned k = 0; k < 5u; ++k) q[k] = std::fmod(0.37 * (i + 1u) * (k + 2u) + 0.11 * k * k, 1.0);
+                pts.push_back(q);
+            }
+            const pagmo::vector_double r(5, 1.5);
+            pagmo::hypervolume h(pts);
+            CHECK(hypervolume_compute(pts, r) == h.compute(r));
+            CHECK(hypervolume_contributions(pts, r) == h.contributions(r));
+            CHECK(hypervolume_exclusive(pts, 7u, r) == h.exclusive(7u, r));
+            CHECK(hypervolume_least_contributor(pts, r) == h.least_contributor(r));
+            CHECK(hypervolume_greatest_contributor(pts, r) == h.greatest_contributor(r));
+            CHECK(throws_with<std::invalid_argument>([&] { hypervolume_exclusive(pts, 40u, r); },
+                                                     "Index of the individual is out of bounds."));
         }
     }
     // gpu_mbh refuses problems it cannot refine (no CPU fallback) and bad perturbations
