@@ -25,7 +25,9 @@
 #include <pagmo/problems/rastrigin.hpp>
 #include <pagmo/problems/rosenbrock.hpp>
 #include <pagmo/problems/schwefel.hpp>
+#include <pagmo/problems/hock_schittkowski_71.hpp>
 #include <pagmo/problems/translate.hpp>
+#include <pagmo/problems/unconstrain.hpp>
 #include <pagmo/problems/zdt.hpp>
 #include <pagmo/threading.hpp>
 #include <pagmo/types.hpp>
@@ -51,7 +53,25 @@ public:
         if (const auto *g = p.extract<gpu_schwefel>()) return g->batch_fitness(dvs);
         if (const auto *g = p.extract<gpu_zdt>()) return g->batch_fitness(dvs);
         if (const auto *g = p.extract<gpu_dtlz>()) return g->batch_fitness(dvs);
+        if (const auto *g = p.extract<gpu_hock_schittkowski_71>()) return g->batch_fitness(dvs);
         if (p.extract<pagmo::zdt>() || p.extract<pagmo::dtlz>()) return mo_fitness(p, dvs);
+        if (p.extract<pagmo::hock_schittkowski_71>()) {
+            const std::uint64_t n = dvs.size() / 4u; // pagmo::bfe checked divisibility
+            pagmo::vector_double fvs(3u * n);
+            if (n)
+                check(pgx_constrained_batch_fitness(device_context(m_device), PGX_HS71, 0u, dvs.data(), n,
+                                                    fvs.data()));
+            return fvs;
+        }
+        if (const auto *u = p.extract<pagmo::unconstrain>()) {
+            // unconstrain::batch_fitness (src/problems/unconstrain.cpp:245-266):
+            // the inner problem's batch evaluation (on the GPU for a GPU UDP),
+            // then pagmo's own penalty; its method and weights are private
+            if (u->get_inner_problem().has_batch_fitness()) return u->batch_fitness(dvs);
+            throw std::invalid_argument("Cannot use a gpu_bfe on '" + p.get_name()
+                                        + "': wrap a GPU UDP with batch_fitness (gpu_hock_schittkowski_71) "
+                                          "in the unconstrain");
+        }
         if (const auto *t = p.extract<pagmo::translate>()) {
             // translate::batch_fitness (src/problems/translate.cpp:118-146): the
             // decision vectors shifted back, then the inner problem's evaluation
@@ -79,7 +99,7 @@ public:
         } else {
             throw std::invalid_argument("Cannot use a gpu_bfe on the problem '" + p.get_name()
                                         + "': only rastrigin, rosenbrock, lennard_jones, ackley, griewank, "
-                                          "schwefel, zdt and dtlz are evaluated on the GPU");
+                                          "schwefel, zdt, dtlz and hock_schittkowski_71 are evaluated on the GPU");
         }
         const std::uint64_t n = dvs.size() / p.get_nx(); // pagmo::bfe checked divisibility
         pagmo::vector_double fvs(n);

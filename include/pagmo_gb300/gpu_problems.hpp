@@ -371,6 +371,64 @@ public:
     }
 };
 
+// hock_schittkowski_71: four variables in [1, 5], one objective, one equality
+// and one inequality constraint (src/problems/hock_schittkowski_71.cpp:48-69);
+// batch_fitness on the GPU (n rows of [f, ceq, cineq], the reference's values
+// bit for bit). Inside pagmo's unconstrain, whose batch_fitness forwards to the
+// inner problem's (src/problems/unconstrain.cpp:245-266), the evaluations run
+// on the GPU. pagmo's gradient and hessians of this UDP are not provided.
+class gpu_hock_schittkowski_71
+{
+public:
+    explicit gpu_hock_schittkowski_71(int device = 0) : m_device(device) {}
+    pagmo::vector_double fitness(const pagmo::vector_double &x) const
+    {
+        return batch_fitness(x);
+    }
+    pagmo::vector_double batch_fitness(const pagmo::vector_double &dvs) const
+    {
+        if (dvs.size() % 4u)
+            throw std::invalid_argument("Invalid argument for a batch fitness evaluation: the length of the vector "
+                                        "representing the decision vectors, "
+                                        + std::to_string(dvs.size())
+                                        + ", is not an exact multiple of the dimension of the problem, 4");
+        const std::uint64_t n = dvs.size() / 4u;
+        pagmo::vector_double f(3u * n);
+        if (n) check(pgx_constrained_batch_fitness(device_context(m_device), PGX_HS71, 0u, dvs.data(), n, f.data()));
+        return f;
+    }
+    std::pair<pagmo::vector_double, pagmo::vector_double> get_bounds() const
+    {
+        std::pair<pagmo::vector_double, pagmo::vector_double> b{pagmo::vector_double(4), pagmo::vector_double(4)};
+        check(pgx_constrained_bounds(PGX_HS71, 0u, b.first.data(), b.second.data()));
+        return b;
+    }
+    pagmo::vector_double::size_type get_nec() const
+    {
+        return 1u;
+    }
+    pagmo::vector_double::size_type get_nic() const
+    {
+        return 1u;
+    }
+    std::string get_name() const
+    {
+        return "Hock Schittkowski 71";
+    }
+    pagmo::thread_safety get_thread_safety() const
+    {
+        return pagmo::thread_safety::constant;
+    }
+    template <typename Archive>
+    void serialize(Archive &ar, unsigned)
+    {
+        ar &m_device;
+    }
+
+private:
+    int m_device = 0;
+};
+
 } // namespace pagmo_gb300
 
 // Registration with pagmo's Boost.Serialization machinery (include/pagmo/problem.hpp:67-76):
@@ -383,5 +441,6 @@ PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_griewank)
 PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_schwefel)
 PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_zdt)
 PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_dtlz)
+PAGMO_S11N_PROBLEM_EXPORT_KEY(pagmo_gb300::gpu_hock_schittkowski_71)
 
 #endif

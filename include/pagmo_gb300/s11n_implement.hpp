@@ -20,5 +20,6 @@ PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_griewank)
 PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_schwefel)
 PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_zdt)
 PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_dtlz)
+PAGMO_S11N_PROBLEM_IMPLEMENT(pagmo_gb300::gpu_hock_schittkowski_71)
 
 #endif

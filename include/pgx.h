@@ -250,6 +250,43 @@ PGX_API int pgx_hypervolume_contributions_device(pgx_context *ctx, const double 
 PGX_API int pgx_hypervolume_extreme_contributor(pgx_context *ctx, const double *points, uint64_t n, uint64_t m,
                                                 const double *ref, int greatest, uint64_t *idx);
 
+/* ---------------------------------- constrained problems and unconstrain */
+
+#define PGX_HS71 9 /* src/problems/hock_schittkowski_71.cpp: nx 4, one objective, one equality, one inequality */
+
+/* hock_schittkowski_71 (param unused): dimensions and bounds [1, 5]^4
+   (hock_schittkowski_71.cpp:66-69), and the batch fitness, n rows of
+   [f, ceq, cineq] (pagmo's fvs layout, :48-55), bit for bit the reference's. */
+PGX_API int pgx_constrained_dims(int kind, uint64_t param, uint64_t *nx, uint64_t *nobj, uint64_t *nec,
+                                 uint64_t *nic);
+PGX_API int pgx_constrained_bounds(int kind, uint64_t param, double *lb, double *ub);
+PGX_API int pgx_constrained_batch_fitness(pgx_context *ctx, int kind, uint64_t param, const double *dvs,
+                                          uint64_t n_dvs, double *fvs);
+
+/* unconstrain{inner, method, weights} (src/problems/unconstrain.cpp): the
+   methods "death penalty", "kuri", "weighted", "ignore_c", "ignore_o"; weights
+   (n_weights = nec + nic) for "weighted" only; c_tol the inner problem's
+   constraint tolerances (NULL: all 0, pagmo's default). */
+#define PGX_UNCONSTRAIN_DEATH 0
+#define PGX_UNCONSTRAIN_KURI 1
+#define PGX_UNCONSTRAIN_WEIGHTED 2
+#define PGX_UNCONSTRAIN_IGNORE_C 3
+#define PGX_UNCONSTRAIN_IGNORE_O 4
+typedef struct pgx_unconstrain {
+    int method;
+    const double *weights;
+    uint64_t n_weights;
+    const double *c_tol;
+} pgx_unconstrain;
+
+/* unconstrain::batch_fitness (unconstrain.cpp:245-266): the inner problem's
+   batch fitness and unconstrain::penalize (:130-225) of every row in one
+   kernel; out n rows of the inner problem's nobj objectives (one for
+   "ignore_o"), bit for bit the reference's. The constructor's checks and
+   messages (:66-100) give PGX_ERR_INVALID. */
+PGX_API int pgx_unconstrain_batch_fitness(pgx_context *ctx, int kind, uint64_t param, const pgx_unconstrain *u,
+                                          const double *dvs, uint64_t n_dvs, double *fvs);
+
 /* --------------------------------------------------- NSGA-II survival (MO) */
 
 /* fast_non_dominated_sorting (src/utils/multi_objective.cpp:200-257) over n

@@ -123,6 +123,9 @@ class _Oracle:
         h.orc_hypervolume_ld.argtypes = [_vp, _u64, _u64, _vp, _vp]
         h.orc_hvwfg.argtypes = [_vp, _u64, _u64, _vp, _vp]
         h.orc_hvwfg_contributions.argtypes = [_vp, _u64, _u64, _vp, _vp]
+        h.orc_hs71_fitness.argtypes = [_vp, _u64, _vp]
+        h.orc_hs71_fitness.restype = None
+        h.orc_unconstrain_penalize.argtypes = [_vp, _u64, _u64, _u64, _u64, C.c_int, _vp, _vp, _vp]
         h.orc_mo_dims.argtypes = [C.c_int, C.c_uint, _u64, _u64, _vp, _vp]
         h.orc_mo_batch_fitness.argtypes = [C.c_int, C.c_uint, _u64, _u64, C.c_uint, _vp, _u64, _u64, _vp, C.c_int]
         h.orc_mo_batch_fitness_ld.argtypes = [C.c_int, C.c_uint, _u64, _u64, C.c_uint, _vp, _u64, _u64, _vp, _vp,
@@ -270,6 +273,24 @@ class _Oracle:
             raise ValueError("hvwfg oracle: at least one point of 2 or more objectives")
         return out.value
 
+    def hs71_fitness(self, dvs):
+        """hock_schittkowski_71 rows [f, ceq, cineq], the reference's double arithmetic."""
+        x = np.ascontiguousarray(dvs, dtype=np.float64).reshape(-1, 4)
+        out = np.empty((x.shape[0], 3))
+        self.h.orc_hs71_fitness(_p(x), x.shape[0], _p(out))
+        return out
+
+    def unconstrain_hs71(self, method, dvs, weights=(), c_tol=None):
+        """unconstrain{hock_schittkowski_71, method, weights} rows, the reference's double arithmetic."""
+        codes = {"death penalty": 0, "kuri": 1, "weighted": 2, "ignore_c": 3, "ignore_o": 4}
+        f = self.hs71_fitness(dvs)
+        w = np.ascontiguousarray(weights if len(weights) else np.zeros(2), dtype=np.float64)
+        tol = np.zeros(2) if c_tol is None else np.ascontiguousarray(c_tol, dtype=np.float64)
+        out = np.empty(f.shape[0])
+        if self.h.orc_unconstrain_penalize(_p(f), f.shape[0], 1, 1, 1, codes[method], _p(w), _p(tol), _p(out)):
+            raise ValueError(method)
+        return out
+
     def hvwfg_contributions(self, pts, ref):
         """Every point's exclusive contribution, WFG in double (any m >= 2)."""
         p = _pts2d(pts)
@@ -348,6 +369,8 @@ class _Reference:
         h.ref_hv_contributions.argtypes = [_vp, _u64, _u64, _vp, C.c_int, _vp]
         h.ref_hv_extreme.argtypes = [_vp, _u64, _u64, _vp, C.c_int, _vp]
         h.ref_hvwfg_compute.argtypes = [_vp, _u64, _u64, _vp, _vp]
+        h.ref_hs71_fitness.argtypes = [_vp, _u64, _vp]
+        h.ref_unconstrain_hs71.argtypes = [C.c_char_p, _vp, _u64, _vp, _vp, _u64, _vp]
         h.ref_mo_dims.argtypes = mo + [_vp, _vp, _vp]
         h.ref_mo_bounds.argtypes = mo + [_vp, _vp]
         h.ref_mo_thread_bfe.argtypes = mo + [_vp, _u64, _u64, _vp]
@@ -482,6 +505,23 @@ class _Reference:
         out = C.c_uint64()
         self._chk(self.h.ref_hv_extreme(_p(p), p.shape[0], p.shape[1], _p(r), int(bool(greatest)), C.byref(out)))
         return out.value
+
+    def hs71_fitness(self, dvs):
+        """problem{hock_schittkowski_71{}}.fitness per row of the reference."""
+        x = np.ascontiguousarray(dvs, dtype=np.float64).reshape(-1, 4)
+        out = np.empty((x.shape[0], 3))
+        self._chk(self.h.ref_hs71_fitness(_p(x), x.shape[0], _p(out)))
+        return out
+
+    def unconstrain_hs71(self, method, dvs, weights=(), c_tol=None):
+        """problem{unconstrain{hock_schittkowski_71 (with c_tol), method, weights}}.fitness per row."""
+        x = np.ascontiguousarray(dvs, dtype=np.float64).reshape(-1, 4)
+        w = np.ascontiguousarray(weights, dtype=np.float64).reshape(-1)
+        tol = None if c_tol is None else np.ascontiguousarray(c_tol, dtype=np.float64)
+        out = np.empty(x.shape[0])
+        self._chk(self.h.ref_unconstrain_hs71(method.encode(), _p(w) if w.size else None, w.size, _p(tol), _p(x),
+                                              x.shape[0], _p(out)))
+        return out
 
     def hvwfg(self, pts, ref):
         """hypervolume(points, true).compute(ref, hvwfg()) of the reference."""

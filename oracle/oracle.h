@@ -132,6 +132,13 @@ int orc_hypervolume_ld(const double *pts, uint64_t n, uint64_t m, const double *
 int orc_hvwfg(const double *pts, uint64_t n, uint64_t m, const double *ref, double *out);
 int orc_hvwfg_contributions(const double *pts, uint64_t n, uint64_t m, const double *ref, double *out);
 
+/* ---- hock_schittkowski_71 and unconstrain's penalties, double, the
+   reference's operation order (constrained.cpp); method 0..4 = death penalty,
+   kuri, weighted, ignore_c, ignore_o ---- */
+void orc_hs71_fitness(const double *x, uint64_t n, double *f);
+int orc_unconstrain_penalize(const double *f, uint64_t n, uint64_t nobj, uint64_t nec, uint64_t nic, int method,
+                             const double *weights, const double *tol, double *out);
+
 #ifdef __cplusplus
 }
 #endif

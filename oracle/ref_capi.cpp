@@ -20,10 +20,12 @@
 #include <pagmo/problems/ackley.hpp>
 #include <pagmo/problems/dtlz.hpp>
 #include <pagmo/problems/griewank.hpp>
+#include <pagmo/problems/hock_schittkowski_71.hpp>
 #include <pagmo/problems/lennard_jones.hpp>
 #include <pagmo/problems/rastrigin.hpp>
 #include <pagmo/problems/rosenbrock.hpp>
 #include <pagmo/problems/schwefel.hpp>
+#include <pagmo/problems/unconstrain.hpp>
 #include <pagmo/problems/zdt.hpp>
 #include <pagmo/utils/hv_algos/hv_hvwfg.hpp>
 #include <pagmo/utils/hypervolume.hpp>
@@ -243,6 +245,35 @@ int ref_hv_extreme(const double *pts, std::uint64_t n, std::uint64_t m, const do
         pagmo::hypervolume hv(rows(pts, n, m), true);
         const pagmo::vector_double rv(r, r + m);
         *idx = greatest ? hv.greatest_contributor(rv) : hv.least_contributor(rv);
+    });
+}
+
+// hock_schittkowski_71::fitness per row, and problem{unconstrain{problem with
+// hock_schittkowski_71 and c_tol, method, weights}}.fitness per row
+// (src/problems/unconstrain.cpp:104-225); method as its string.
+int ref_hs71_fitness(const double *x, std::uint64_t n, double *out)
+{
+    return guard([&] {
+        pagmo::problem p{pagmo::hock_schittkowski_71{}};
+        for (std::uint64_t r = 0; r < n; ++r) {
+            const auto f = p.fitness(pagmo::vector_double(x + 4u * r, x + 4u * r + 4u));
+            std::copy(f.begin(), f.end(), out + 3u * r);
+        }
+    });
+}
+
+int ref_unconstrain_hs71(const char *method, const double *weights, std::uint64_t n_weights, const double *c_tol,
+                         const double *x, std::uint64_t n, double *out)
+{
+    return guard([&] {
+        pagmo::problem inner{pagmo::hock_schittkowski_71{}};
+        if (c_tol) inner.set_c_tol(pagmo::vector_double(c_tol, c_tol + 2));
+        pagmo::problem p{pagmo::unconstrain{inner, method, pagmo::vector_double(weights, weights + n_weights)}};
+        const auto w = p.get_nf();
+        for (std::uint64_t r = 0; r < n; ++r) {
+            const auto f = p.fitness(pagmo::vector_double(x + 4u * r, x + 4u * r + 4u));
+            std::copy(f.begin(), f.end(), out + w * r);
+        }
     });
 }
 

@@ -8,7 +8,8 @@ plugin interface for the batch-fitness path:
                     batch_fitness, gradient and batch_gradient); ackley,
                     griewank, schwefel (batch_fitness; no gradient, as in
                     the reference); zdt, dtlz (multi-objective batch_fitness
-                    and p_distance)
+                    and p_distance); hock_schittkowski_71 (constrained) and
+                    the unconstrain meta-problem around it; translate
   batch_evaluators: gpu_bfe (the UDBFE) and a bfe/problem pair reproducing
                     pagmo's input/output checks and fevals accounting
   multi_objective:  fast_non_dominated_sorting, crowding_distance,
@@ -24,5 +25,5 @@ from .algorithms import gpu_mbh  # noqa: F401
 from .batch_evaluators import bfe, gpu_bfe, problem  # noqa: F401
 from .multi_objective import (crowding_distance, fast_non_dominated_sorting, hypervolume,  # noqa: F401
                               nsga2_survival, select_best_N_mo, sort_population_mo)
-from .problems import (ackley, dtlz, griewank, lennard_jones, rastrigin, rosenbrock, schwefel,  # noqa: F401
-                       translate, zdt)
+from .problems import (ackley, dtlz, griewank, hock_schittkowski_71, lennard_jones, rastrigin,  # noqa: F401
+                       rosenbrock, schwefel, translate, unconstrain, zdt)

@@ -19,6 +19,8 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpgx.so"
 OK, ERR_INVALID, ERR_CUDA, ERR_TIMEOUT, ERR_CAPACITY, ERR_NODEVICE, ERR_NOTIMPL = 0, 1, 2, 3, 4, 5, 6
 RASTRIGIN, ROSENBROCK, LENNARD_JONES, ACKLEY, GRIEWANK, SCHWEFEL = 1, 2, 3, 4, 5, 6
 ZDT, DTLZ = 7, 8
+HS71 = 9
+UNCONSTRAIN_METHODS = {"death penalty": 0, "kuri": 1, "weighted": 2, "ignore_c": 3, "ignore_o": 4}
 
 # Exported symbols and their signatures (kept in step with include/pgx.h).
 _vp, _u64, _i32, _d = C.c_void_p, C.c_uint64, C.c_int32, C.c_double
@@ -65,6 +67,10 @@ SIGNATURES = {
     "pgx_selftest_lj_reciprocal": (C.c_int, [_vp, _vp, _u64, _vp, _vp]),
     "pgx_hypervolume": (C.c_int, [_vp, _vp, _u64, _u64, _vp, C.POINTER(C.c_double)]),
     "pgx_hypervolume_device": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp]),
+    "pgx_constrained_dims": (C.c_int, [C.c_int, _u64, _vp, _vp, _vp, _vp]),
+    "pgx_constrained_bounds": (C.c_int, [C.c_int, _u64, _vp, _vp]),
+    "pgx_constrained_batch_fitness": (C.c_int, [_vp, C.c_int, _u64, _vp, _u64, _vp]),
+    "pgx_unconstrain_batch_fitness": (C.c_int, [_vp, C.c_int, _u64, _vp, _vp, _u64, _vp]),
     "pgx_hypervolume_exclusive": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _u64, C.POINTER(C.c_double)]),
     "pgx_hypervolume_contributions": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp]),
     "pgx_hypervolume_contributions_device": (C.c_int, [_vp, _vp, _u64, _u64, _vp, _vp, _vp]),
@@ -82,6 +88,11 @@ class pgx_mo_problem(C.Structure):
     """struct pgx_mo_problem of include/pgx.h: zdt(prob_id, param) or dtlz(prob_id, dim=param, fdim, alpha)."""
     _fields_ = [("kind", C.c_int), ("prob_id", C.c_uint32), ("param", C.c_uint64), ("fdim", C.c_uint64),
                 ("alpha", C.c_uint32)]
+
+
+class pgx_unconstrain(C.Structure):
+    """struct pgx_unconstrain of include/pgx.h: unconstrain's method code, weights and the inner tolerances."""
+    _fields_ = [("method", C.c_int), ("weights", C.c_void_p), ("n_weights", C.c_uint64), ("c_tol", C.c_void_p)]
 
 
 class pgx_refine_params(C.Structure):

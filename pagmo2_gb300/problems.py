@@ -306,6 +306,136 @@ class dtlz(_gpu_mo_udp):
         return f"DTLZ{self.prob_id}"
 
 
+class hock_schittkowski_71:
+    """hock_schittkowski_71 (src/problems/hock_schittkowski_71.cpp) on the GPU: four variables in [1, 5], one
+    objective, one equality and one inequality constraint; batch_fitness gives n rows of [f, ceq, cineq], the
+    reference's values bit for bit. pagmo's gradient and hessians of this UDP are not provided."""
+    thread_safety = "constant"
+
+    def __init__(self, context: N.Context | None = None):
+        self._ctx = context
+        self.kind, self.param = N.HS71, 0
+
+    @property
+    def ctx(self) -> N.Context:
+        return self._ctx if self._ctx is not None else N.default_context()
+
+    def get_nx(self) -> int:
+        return 4
+
+    def get_nobj(self) -> int:
+        return 1
+
+    def get_nec(self) -> int:
+        return 1
+
+    def get_nic(self) -> int:
+        return 1
+
+    def get_nf(self) -> int:
+        return 3
+
+    def get_bounds(self):
+        lb, ub = np.empty(4), np.empty(4)
+        N.check(N.lib().pgx_constrained_bounds(N.HS71, 0, N.ptr(lb), N.ptr(ub)))
+        return lb, ub
+
+    def get_name(self) -> str:
+        return "Hock Schittkowski 71"
+
+    def get_thread_safety(self) -> str:
+        return self.thread_safety
+
+    def has_gradient(self) -> bool:
+        return False
+
+    def batch_fitness(self, dvs) -> np.ndarray:
+        x = _as_rows(dvs, 4)
+        n = x.size // 4
+        f = np.empty(3 * n)
+        if n:
+            N.check(N.lib().pgx_constrained_batch_fitness(self.ctx.handle, N.HS71, 0, N.ptr(x), n, N.ptr(f)))
+        return f
+
+    def fitness(self, x) -> np.ndarray:
+        x = np.asarray(x, dtype=np.float64)
+        if x.size != 4:
+            raise ValueError(f"A decision vector is incompatible with a problem of type '{self.get_name()}': the "
+                             f"number of dimensions of the problem is 4, while the decision vector has a size of "
+                             f"{x.size} (the two values should be equal)")
+        return self.batch_fitness(x)
+
+
+class unconstrain:
+    """unconstrain{udp, method, weights} (src/problems/unconstrain.cpp) around a constrained GPU UDP: the inner
+    batch fitness and every row's penalty ("death penalty", "kuri", "weighted", "ignore_c", "ignore_o";
+    unconstrain::penalize, :130-225) in one GPU pass, the reference's values bit for bit. c_tol: the inner
+    problem's constraint tolerances (pagmo's problem::set_c_tol; default 0). Constructor checks and messages as
+    the reference's (:66-100)."""
+
+    def __init__(self, udp, method: str = "death penalty", weights=(), c_tol=None):
+        nc = udp.get_nec() + udp.get_nic() if hasattr(udp, "get_nec") else 0
+        if nc == 0:
+            raise ValueError(f"Unconstrain can only be applied to constrained problems, the instance of "
+                             f"{udp.get_name()} is not one.")
+        w = np.ascontiguousarray(np.asarray(weights, dtype=np.float64).reshape(-1))
+        if w.size != nc and method == "weighted":
+            raise ValueError(f"Length of weight vector is: {w.size} while the problem constraints are: {nc}")
+        if method not in N.UNCONSTRAIN_METHODS:
+            raise ValueError(f"The method {method} is not supported (did you misspell?)")
+        if w.size != 0 and method != "weighted":
+            raise ValueError(f"The weight vector needs to be empty to use the unconstrain method {method}")
+        if not hasattr(udp, "kind") or udp.kind != N.HS71:
+            raise NotImplementedError(f"unconstrain on the GPU: the inner problem must be a constrained GPU UDP "
+                                      f"(hock_schittkowski_71), not {udp.get_name()}")
+        self.inner, self.method, self.weights = udp, method, w
+        self.c_tol = np.zeros(nc) if c_tol is None else np.ascontiguousarray(np.asarray(c_tol, dtype=np.float64))
+        if self.c_tol.size != nc:  # problem::set_c_tol's checks (src/problem.cpp:620-636)
+            raise ValueError(f"The tolerance vector size should be: {nc}, while a size of: {self.c_tol.size} was "
+                             f"detected.")
+        for i, t in enumerate(self.c_tol):
+            if np.isnan(t):
+                raise ValueError(f"The tolerance vector has a NaN value at the index {i}")
+            if t < 0:
+                raise ValueError(f"The tolerance vector has a negative value at the index {i}")
+        self._desc = N.pgx_unconstrain(N.UNCONSTRAIN_METHODS[method], N.ptr(self.weights) if w.size else None,
+                                       w.size, N.ptr(self.c_tol))
+
+    def get_nx(self) -> int:
+        return self.inner.get_nx()
+
+    def get_nobj(self) -> int:
+        return 1 if self.method == "ignore_o" else self.inner.get_nobj()
+
+    def get_nf(self) -> int:
+        return self.get_nobj()
+
+    def get_bounds(self):
+        return self.inner.get_bounds()
+
+    def get_name(self) -> str:
+        return self.inner.get_name() + " [unconstrained]"
+
+    def get_thread_safety(self) -> str:
+        return self.inner.get_thread_safety()
+
+    def has_gradient(self) -> bool:
+        return False
+
+    def batch_fitness(self, dvs) -> np.ndarray:
+        nx = self.get_nx()
+        x = _as_rows(dvs, nx)
+        n = x.size // nx
+        f = np.empty(n * self.get_nobj())
+        if n:
+            N.check(N.lib().pgx_unconstrain_batch_fitness(self.inner.ctx.handle, self.inner.kind, self.inner.param,
+                                                          C.byref(self._desc), N.ptr(x), n, N.ptr(f)))
+        return f
+
+    def fitness(self, x) -> np.ndarray:
+        return self.batch_fitness(np.asarray(x, dtype=np.float64).reshape(1, -1))
+
+
 class translate:
     """translate{udp, translation} (src/problems/translate.cpp): f(x) = inner(x - translation), bounds shifted by
     the translation; batch_fitness shifts the whole batch back and forwards it to the inner problem's batch_fitness

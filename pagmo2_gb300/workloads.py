@@ -15,6 +15,8 @@ Workloads (sizes as benchmarked):
   nsga2       20000 points x 3 objectives: 30 nested simplex layers of radius
               1 + 0.1 k with N(0, 1e-3) jitter, plus 5 % exact duplicates,
               shuffled,                                        seed 4
+  sphere      points on the positive orthant of the unit sphere (hypervolume
+              of 4+ objectives),                               seed 6
   archipelago 64 islands, population log-uniform in [32, 4096], dimension
               uniform in [10, 500], problems round-robin over the three
               (lennard_jones gets N = round((dim + 6) / 3) atoms), seed 5
@@ -148,6 +150,13 @@ class island_request:
     @property
     def nx(self) -> int:
         return nx_of(self.kind, self.param)
+
+
+def sphere_front(n: int = 2000, m: int = 5, seed: int = 6) -> np.ndarray:
+    """n points of m objectives on the positive orthant of the unit sphere (squared uniform directions,
+    normalised): a front on which most points are non-dominated, the hard case of the WFG hypervolume."""
+    w = np.random.default_rng(seed).random((n, m)) ** 2
+    return np.ascontiguousarray(w / np.linalg.norm(w, axis=1, keepdims=True))
 
 
 def archipelago(islands: int = 64, seed: int = 5, pop_lo: int = 32, pop_hi: int = 4096, dim_lo: int = 10,

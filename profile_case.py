@@ -18,6 +18,8 @@ profiler are not benchmark values). Cases:
   select_best                   select_best_N_mo(--rows nested-front points x 3, rows / 2)
   sort_population               sort_population_mo(--rows nested-front points x 3)
   hypervolume                   hypervolume of --rows nested-front points x 3 (reference point max + 0.5)
+  hv_wfg / hv_contributions     hypervolume / every point's contribution of --rows points on a sphere front of
+                                --fdim objectives (default 5; reference point 1.1)
   archipelago                   the fused kernel of a 64-island mixed epoch (--rows unused)
   refine_rastrigin / refine_rosenbrock / refine_lj   batched basin hopping with gradient descent
                                 (10 trials, stop 5, 20 steps) on --rows individuals
@@ -101,6 +103,19 @@ def main() -> None:
 
         def run():
             N.check(L.pgx_hypervolume_device(ctx.handle, dp.data_ptr(), n, 3, N.ptr(r), dhv.data_ptr(), sp))
+    elif a.case in ("hv_wfg", "hv_contributions"):
+        m = a.fdim if a.fdim != 3 else 5
+        p = W.sphere_front(n, m)
+        r = np.full(m, 1.1)
+        dp = torch.from_numpy(p).cuda()
+        dout = torch.empty(n, dtype=torch.float64, device="cuda")
+
+        def run():
+            if a.case == "hv_wfg":
+                N.check(L.pgx_hypervolume_device(ctx.handle, dp.data_ptr(), n, m, N.ptr(r), dout.data_ptr(), sp))
+            else:
+                N.check(L.pgx_hypervolume_contributions_device(ctx.handle, dp.data_ptr(), n, m, N.ptr(r),
+                                                               dout.data_ptr(), sp))
     elif a.case in ("select_best", "sort_population"):
         p = W.nsga2_points(n, 3, layers=a.layers)
         dp = torch.from_numpy(p).cuda()

@@ -21,12 +21,14 @@
 #include <pagmo/problems/ackley.hpp>
 #include <pagmo/problems/dtlz.hpp>
 #include <pagmo/problems/griewank.hpp>
+#include <pagmo/problems/hock_schittkowski_71.hpp>
 #include <pagmo/problems/lennard_jones.hpp>
 #include <pagmo/problems/null_problem.hpp>
 #include <pagmo/problems/rastrigin.hpp>
 #include <pagmo/problems/rosenbrock.hpp>
 #include <pagmo/problems/schwefel.hpp>
 #include <pagmo/problems/translate.hpp>
+#include <pagmo/problems/unconstrain.hpp>
 #include <pagmo/problems/zdt.hpp>
 #include <pagmo/utils/hypervolume.hpp>
 #include <pagmo/utils/multi_objective.hpp>
@@ -70,6 +72,7 @@ static_assert(pagmo::has_gradient<gpu_rosenbrock>::value, "gradient hook");
 static_assert(pagmo::has_gradient<gpu_lennard_jones>::value, "gradient hook");
 static_assert(pagmo::has_batch_fitness<pagmo::translate>::value, "translate forwards batch_fitness");
 static_assert(pagmo::is_udp<gpu_zdt>::value && pagmo::is_udp<gpu_dtlz>::value, "gpu_zdt / gpu_dtlz must be UDPs");
+static_assert(pagmo::is_udp<gpu_hock_schittkowski_71>::value, "gpu_hock_schittkowski_71 must be a UDP");
 static_assert(pagmo::has_batch_fitness<gpu_zdt>::value && pagmo::has_batch_fitness<gpu_dtlz>::value,
               "batch_fitness hook of the multi-objective UDPs");
 static_assert(!pagmo::has_gradient<gpu_zdt>::value && !pagmo::has_gradient<gpu_dtlz>::value,
@@ -259,6 +262,28 @@ int main()
             }
             CHECK(better > 32);
             CHECK(pop.get_problem().get_fevals() > fe0 + 64u);
+        }
+        // hock_schittkowski_71 through bfe{gpu_bfe}, and pagmo's unconstrain around the GPU UDP (its
+        // batch_fitness forwards to the GPU) against the reference's own problems, bit for bit
+        {
+            std::vector<double> hx(4 * 50);
+            for (size_t i = 0; i < hx.size(); ++i) hx[i] = 1.0 + std::fmod(0.731 * static_cast<double>(i * i + 3u), 4.0);
+            pagmo::problem hr{pagmo::hock_schittkowski_71{}}, hg{gpu_hock_schittkowski_71{}};
+            const auto fr = pagmo::bfe{pagmo::thread_bfe{}}(hr, hx);
+            CHECK(b(hr, hx) == fr);
+            CHECK(pagmo::bfe{pagmo::member_bfe{}}(hg, hx) == fr);
+            for (const char *m : {"death penalty", "kuri", "ignore_c", "ignore_o"}) {
+                pagmo::problem ur{pagmo::unconstrain{pagmo::hock_schittkowski_71{}, m}};
+                pagmo::problem ug{pagmo::unconstrain{gpu_hock_schittkowski_71{}, m}};
+                CHECK(ug.has_batch_fitness());
+                const auto want = pagmo::bfe{pagmo::thread_bfe{}}(ur, hx);
+                CHECK(pagmo::bfe{pagmo::member_bfe{}}(ug, hx) == want);
+                CHECK(b(ug, hx) == want);
+            }
+            pagmo::problem uw{pagmo::unconstrain{gpu_hock_schittkowski_71{}, "weighted", {2.0, 0.5}}};
+            CHECK(b(uw, hx)
+                  == pagmo::bfe{pagmo::thread_bfe{}}(
+                      pagmo::problem{pagmo::unconstrain{pagmo::hock_schittkowski_71{}, "weighted", {2.0, 0.5}}}, hx));
         }
         // hypervolume queries against pagmo::hypervolume: 5 objectives (hvwfg) bit for bit
         {
