@@ -25,14 +25,19 @@
 // against each other, then the kept points the survivors cover are removed),
 // the counting-rank sorts of a frame and the closed forms; the recursion
 // below the top level runs on an explicit stack, its frames in the warp's
-// slice of a scratch pool (m buffers of n rows). A frame's kept set is the
-// unique non-dominated subset of its candidates whatever order they are
-// filtered in, every frame of more than two points is sorted by a strict
-// order before it is used, and the two-point form is symmetric, so the
-// arithmetic is the reference's: every operation is the reference's
-// IEEE double operation in the reference's order (explicit round-to-nearest
-// intrinsics: no contraction into FMA), and the volumes and contributions
-// equal the reference's bit for bit.
+// slice of a scratch pool (m buffers of n rows); the top level's frames are
+// split into one work item per sub-term (see wfg_args). Every comparison (limit
+// sets, sorts, maxima) runs on 64-bit integer order keys of the coordinates
+// (the IEEE bit pattern with negatives mirrored, -0.0 read as +0.0, which the
+// reference compares equal): the frames hold keys, and only the volumes and
+// terms turn them back into doubles (GB300's FP64 pipe is far too narrow for
+// the comparisons). A frame's kept set is the unique non-dominated subset of
+// its candidates whatever order they are filtered in, every frame of more than
+// two points is sorted by a strict order before it is used, and the two-point
+// form is symmetric, so the arithmetic is the reference's: every operation is
+// the reference's IEEE double operation in the reference's order (explicit
+// round-to-nearest intrinsics: no contraction into FMA), and the volumes and
+// contributions equal the reference's bit for bit.
 #include "pgx_internal.cuh"
 
 #include <algorithm>
@@ -49,6 +54,19 @@ struct wfg_ref {
     double r[kWfgMaxObjectives];
 };
 
+using okey = long long; // order key of a coordinate
+
+__device__ __forceinline__ okey to_key(double v)
+{
+    const long long b = __double_as_longlong(v == 0.0 ? 0.0 : v);
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+
+__device__ __forceinline__ double from_key(okey k)
+{
+    return __longlong_as_double(k >= 0 ? k : (k ^ 0x7fffffffffffffffLL));
+}
+
 __device__ __forceinline__ double std_max(double a, double b)
 {
     return a < b ? b : a; // std::max(a, b)
@@ -56,7 +74,15 @@ __device__ __forceinline__ double std_max(double a, double b)
 
 // |prod over c = d-1 .. 0 of (r_c - p_c)| (hv_algorithm::volume_between on
 // pointers, hv_algorithm.cpp:73-82)
-__device__ __forceinline__ double vol(const double *r, const double *p, uint32_t d)
+__device__ __forceinline__ double vol(const double *r, const okey *p, uint32_t d)
+{
+    double v = 1.0;
+    for (int c = static_cast<int>(d) - 1; c >= 0; --c) v = __dmul_rn(v, __dsub_rn(r[c], from_key(p[c])));
+    return v < 0.0 ? -v : v;
+}
+
+// the same on plain doubles
+__device__ __forceinline__ double vol_d(const double *r, const double *p, uint32_t d)
 {
     double v = 1.0;
     for (int c = static_cast<int>(d) - 1; c >= 0; --c) v = __dmul_rn(v, __dsub_rn(r[c], p[c]));
@@ -73,23 +99,22 @@ __device__ __forceinline__ unsigned lanes_below(unsigned lane)
 // the non-dominated ones with one copy of equal points, written to dst
 // (stride dc). Returns the number kept. Warp-uniform arguments.
 template <int DM>
-__device__ uint32_t limit_set(const double *src, uint32_t src_stride, uint32_t begin, uint32_t end, uint32_t skip,
-                              const double *p, uint32_t dc, double *dst, unsigned lane)
+__device__ uint32_t limit_set(const okey *src, uint32_t src_stride, uint32_t begin, uint32_t end, uint32_t skip,
+                              const okey *p, uint32_t dc, okey *dst, unsigned lane)
 {
     uint32_t K = 0;
     for (uint32_t base = begin; base < end; base += 32u) {
         const uint32_t t = base + lane;
         const bool valid = t < end && t != skip;
-        double s[DM];
+        okey s[DM];
 #pragma unroll
         for (int c = 0; c < DM; ++c)
-            s[c] = (valid && c < static_cast<int>(dc)) ? std_max(src[static_cast<uint64_t>(t) * src_stride + c], p[c])
-                                                       : 0.0;
+            s[c] = (valid && c < static_cast<int>(dc)) ? max(src[static_cast<uint64_t>(t) * src_stride + c], p[c]) : 0;
         bool alive = valid;
         // a kept point <= s in every coordinate (dominating or equal): s goes
         for (uint32_t q = 0; q < K; ++q) {
             if (!__any_sync(kMask, alive)) break;
-            const double *kq = dst + static_cast<uint64_t>(q) * dc;
+            const okey *kq = dst + static_cast<uint64_t>(q) * dc;
             bool le = true;
 #pragma unroll
             for (int c = 0; c < DM; ++c)
@@ -107,7 +132,7 @@ __device__ uint32_t limit_set(const double *src, uint32_t src_stride, uint32_t b
 #pragma unroll
                 for (int c = 0; c < DM; ++c) {
                     if (c < static_cast<int>(dc)) {
-                        const double su = __shfl_sync(kMask, s[c], u);
+                        const okey su = __shfl_sync(kMask, s[c], u);
                         le &= su <= s[c];
                         lt |= su < s[c];
                     }
@@ -123,10 +148,10 @@ __device__ uint32_t limit_set(const double *src, uint32_t src_stride, uint32_t b
         for (uint32_t c0 = 0; c0 < K; c0 += 32u) {
             const uint32_t q = c0 + lane;
             const bool has = q < K;
-            double qr[DM];
+            okey qr[DM];
 #pragma unroll
             for (int c = 0; c < DM; ++c)
-                qr[c] = (has && c < static_cast<int>(dc)) ? dst[static_cast<uint64_t>(q) * dc + c] : 0.0;
+                qr[c] = (has && c < static_cast<int>(dc)) ? dst[static_cast<uint64_t>(q) * dc + c] : 0;
             bool keep = has;
             for (unsigned rs = surv; rs; rs &= rs - 1u) {
                 const int u = __ffs(rs) - 1;
@@ -139,7 +164,7 @@ __device__ uint32_t limit_set(const double *src, uint32_t src_stride, uint32_t b
             const unsigned km = __ballot_sync(kMask, keep);
             __syncwarp();
             if (keep) {
-                double *o = dst + static_cast<uint64_t>(nk + __popc(km & lanes_below(lane))) * dc;
+                okey *o = dst + static_cast<uint64_t>(nk + __popc(km & lanes_below(lane))) * dc;
 #pragma unroll
                 for (int c = 0; c < DM; ++c)
                     if (c < static_cast<int>(dc)) o[c] = qr[c];
@@ -148,7 +173,7 @@ __device__ uint32_t limit_set(const double *src, uint32_t src_stride, uint32_t b
             __syncwarp();
         }
         if (alive) {
-            double *o = dst + static_cast<uint64_t>(nk + __popc(surv & lanes_below(lane))) * dc;
+            okey *o = dst + static_cast<uint64_t>(nk + __popc(surv & lanes_below(lane))) * dc;
 #pragma unroll
             for (int c = 0; c < DM; ++c)
                 if (c < static_cast<int>(dc)) o[c] = s[c];
@@ -164,27 +189,27 @@ __device__ uint32_t limit_set(const double *src, uint32_t src_stride, uint32_t b
 // ascending second coordinate (hv2d, hv_hv2d.cpp:79-81). Ties by row index
 // (a frame's rows are distinct, so they never decide an order there).
 template <int DM>
-__device__ void sort_rows(const double *src, uint32_t K, uint32_t d, bool by_y, double *dst, unsigned lane)
+__device__ void sort_rows(const okey *src, uint32_t K, uint32_t d, bool by_y, okey *dst, unsigned lane)
 {
     for (uint32_t i0 = 0; i0 < K; i0 += 32u) {
         const uint32_t i = i0 + lane;
         const bool has = i < K;
-        double mine[DM];
+        okey mine[DM];
 #pragma unroll
         for (int c = 0; c < DM; ++c)
-            mine[c] = (has && c < static_cast<int>(d)) ? src[static_cast<uint64_t>(i) * d + c] : 0.0;
+            mine[c] = (has && c < static_cast<int>(d)) ? src[static_cast<uint64_t>(i) * d + c] : 0;
         uint32_t rank = 0;
         for (uint32_t j = 0; j < K; ++j) {
-            const double *rj = src + static_cast<uint64_t>(j) * d;
+            const okey *rj = src + static_cast<uint64_t>(j) * d;
             int dec = 0; // +1: row j first, -1: this row first
             if (by_y) {
-                const double a = rj[1];
+                const okey a = rj[1];
                 dec = a < mine[1] ? 1 : (a > mine[1] ? -1 : 0);
             } else {
 #pragma unroll
                 for (int c = DM - 1; c >= 0; --c) {
                     if (c < static_cast<int>(d) && dec == 0) {
-                        const double a = rj[c];
+                        const okey a = rj[c];
                         dec = a > mine[c] ? 1 : (a < mine[c] ? -1 : 0);
                     }
                 }
@@ -192,7 +217,7 @@ __device__ void sort_rows(const double *src, uint32_t K, uint32_t d, bool by_y, 
             rank += (dec > 0 || (dec == 0 && j < i)) ? 1u : 0u;
         }
         if (has) {
-            double *o = dst + static_cast<uint64_t>(rank) * d;
+            okey *o = dst + static_cast<uint64_t>(rank) * d;
 #pragma unroll
             for (int c = 0; c < DM; ++c)
                 if (c < static_cast<int>(d)) o[c] = mine[c];
@@ -203,7 +228,7 @@ __device__ void sort_rows(const double *src, uint32_t K, uint32_t d, bool by_y, 
 
 // The frames of a warp: m buffers of bd doubles, taken and given back by bit.
 struct frame_pool {
-    double *base;
+    okey *base;
     uint64_t bd;
     unsigned free;
 
@@ -218,7 +243,7 @@ struct frame_pool {
     {
         free |= 1u << b;
     }
-    __device__ double *at(int b) const
+    __device__ okey *at(int b) const
     {
         return base + static_cast<uint64_t>(b) * bd;
     }
@@ -227,28 +252,28 @@ struct frame_pool {
 // hv of a frame of 1 or 2 points, or of 2 coordinates (tmp: a free buffer
 // for the sort by y when k > 2)
 template <int DM>
-__device__ double closed_form(const double *r, const double *f, uint32_t K, uint32_t d, double *tmp, unsigned lane)
+__device__ double closed_form(const double *r, const okey *f, uint32_t K, uint32_t d, okey *tmp, unsigned lane)
 {
     if (K == 1u) return vol(r, f, d);
     if (K == 2u) {
         const double h = __dadd_rn(vol(r, f, d), vol(r, f + d, d));
         double isect = 1.0;
-        for (uint32_t c = 0; c < d; ++c) isect = __dmul_rn(isect, __dsub_rn(r[c], std_max(f[c], f[d + c])));
+        for (uint32_t c = 0; c < d; ++c) isect = __dmul_rn(isect, __dsub_rn(r[c], from_key(max(f[c], f[d + c]))));
         return __dsub_rn(h, isect);
     }
     sort_rows<DM>(f, K, 2u, true, tmp, lane);
-    double area = 0.0, w = __dsub_rn(r[0], tmp[0]);
+    double area = 0.0, w = __dsub_rn(r[0], from_key(tmp[0]));
     for (uint32_t t = 0; t + 1u < K; ++t) {
-        area = __dadd_rn(area, __dmul_rn(__dsub_rn(tmp[2u * (t + 1u) + 1u], tmp[2u * t + 1u]), w));
-        w = std_max(w, __dsub_rn(r[0], tmp[2u * (t + 1u)]));
+        area = __dadd_rn(area, __dmul_rn(__dsub_rn(from_key(tmp[2u * (t + 1u) + 1u]), from_key(tmp[2u * t + 1u])), w));
+        w = std_max(w, __dsub_rn(r[0], from_key(tmp[2u * (t + 1u)])));
     }
-    return __dadd_rn(area, __dmul_rn(__dsub_rn(r[1], tmp[2u * (K - 1u) + 1u]), w));
+    return __dadd_rn(area, __dmul_rn(__dsub_rn(r[1], from_key(tmp[2u * (K - 1u) + 1u])), w));
 }
 
 // |(p[d-1] - r[d-1]) * ex|, the term a point of a frame of d coordinates adds
-__device__ __forceinline__ double slice_term(const double *r, const double *p, uint32_t d, double ex)
+__device__ __forceinline__ double slice_term(const double *r, const okey *p, uint32_t d, double ex)
 {
-    return fabs(__dmul_rn(__dsub_rn(p[d - 1u], r[d - 1u]), ex));
+    return fabs(__dmul_rn(__dsub_rn(from_key(p[d - 1u]), r[d - 1u]), ex));
 }
 
 // hv of the frame in buffer `buf` (K points of d coordinates, K >= 1); the
@@ -272,7 +297,7 @@ __device__ double frame_hv(const double *r, frame_pool &pool, int buf, uint32_t 
     for (;;) {
         const int j = st_j[sp];
         const uint32_t kk = st_k[sp], dd = st_d[sp];
-        const double *f = pool.at(st_buf[sp]);
+        const okey *f = pool.at(st_buf[sp]);
         double val;
         if (j < 0) {
             if (kk <= 2u || dd == 2u) {
@@ -297,13 +322,13 @@ __device__ double frame_hv(const double *r, frame_pool &pool, int buf, uint32_t 
                 continue;
             }
         } else if (static_cast<uint32_t>(j) < kk) {
-            const double *p = f + static_cast<uint64_t>(j) * dd;
+            const okey *p = f + static_cast<uint64_t>(j) * dd;
             const int cb = pool.take();
             if (cb < 0) {
                 *fail = true;
                 return 0.0;
             }
-            double *child = pool.at(cb);
+            okey *child = pool.at(cb);
             const uint32_t ck = limit_set<DM>(f, dd, static_cast<uint32_t>(j) + 1u, kk, kk, p, dd - 1u, child, lane);
             if (ck <= 1u) {
                 double ex = vol(r, p, dd - 1u);
@@ -329,25 +354,51 @@ __device__ double frame_hv(const double *r, frame_pool &pool, int buf, uint32_t 
         --sp;
         const uint32_t pd = st_d[sp];
         const int pj = st_j[sp];
-        const double *p = pool.at(st_buf[sp]) + static_cast<uint64_t>(pj) * pd;
+        const okey *p = pool.at(st_buf[sp]) + static_cast<uint64_t>(pj) * pd;
         st_h[sp] = __dadd_rn(st_h[sp], slice_term(r, p, pd, __dsub_rn(vol(r, p, pd - 1u), val)));
         st_j[sp] = pj + 1;
     }
 }
 
+// The work of one volume or one set of contributions is split in two levels:
+// wfg_top_kernel takes the items (the top-level terms of a volume, or the
+// points of the contributions), builds each item's limit set (its "frame")
+// and finishes the items whose frame has at most two points or two
+// coordinates; every other frame is sorted into a global frame list, one row
+// per sub-term. wfg_sub_kernel takes the rows: row j of an item's frame gives
+// the sub-term |(f_j[d-1] - r_{d-1}) * (vol_{d-1}(f_j) - hv(limit set of f_j
+// over the rows after it))|, with the recursion below it on the warp's own
+// stack. wfg_join_kernel adds each item's sub-terms in order (compute_hv's
+// H += ..., hv_hvwfg.cpp:262-266) and finishes the item. The operations and
+// their order are those of one recursion, split between warps.
 struct wfg_args {
-    const double *pts;  // n rows of m; sorted by cmp_points for the terms of a volume
+    const okey *pts;    // n rows of m keys; sorted by cmp_points for the terms of a volume
     uint32_t n, m;
     int contributions;  // 0: out[i] = the top-level term of sorted point i; 1: the contribution of point i
     double *out;        // n
-    double *pool;       // per warp: m buffers of bd doubles
+    okey *pool;         // per warp: m buffers of bd keys
     uint64_t bd;
-    unsigned *next;     // work counter (zero at launch)
+    unsigned *next;     // work counters (zero at launch): [0] items, [2] rows
     unsigned *status;   // set when a warp's pool ran dry
+    unsigned long long *rows_used; // frame rows handed out (zero at launch)
+    uint64_t row_cap;   // rows of the frame list
+    okey *frames;       // the sorted frames, rows of dc keys
+    uint32_t *row_item; // the item of each row
+    double *row_term;   // the sub-term of each row
+    uint32_t *frame_k;  // per item: rows of its frame in the list (0: the item is finished)
+    unsigned long long *frame_off; // per item: its first row
 };
 
+__device__ __forceinline__ void mark_failed(const wfg_args &a, uint32_t item, unsigned lane)
+{
+    if (lane == 0) {
+        atomicOr(a.status, 1u);
+        a.out[item] = __longlong_as_double(0x7ff8000000000000LL);
+    }
+}
+
 template <int DM>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) wfg_kernel(wfg_args a, wfg_ref ref)
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) wfg_top_kernel(wfg_args a, wfg_ref ref)
 {
     __shared__ double s_r[DM];
     if (threadIdx.x < DM) s_r[threadIdx.x] = threadIdx.x < a.m ? ref.r[threadIdx.x] : 0.0;
@@ -362,7 +413,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) wfg_kernel(wfg_args a, wf
         if (lane == 0) item = atomicAdd(a.next, 1u);
         item = __shfl_sync(kMask, item, 0);
         if (item >= a.n) break;
-        const double *p = a.pts + static_cast<uint64_t>(item) * m;
+        const okey *p = a.pts + static_cast<uint64_t>(item) * m;
         const int b0 = pool.take(); // the pool is full here
         const uint32_t k0 = a.contributions ? limit_set<DM>(a.pts, m, 0u, a.n, item, p, dc, pool.at(b0), lane)
                                             : limit_set<DM>(a.pts, m, item + 1u, a.n, a.n, p, dc, pool.at(b0), lane);
@@ -370,62 +421,182 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) wfg_kernel(wfg_args a, wf
         bool fail = false;
         if (k0 == 0u) {
             pool.give(b0);
+        } else if (k0 <= 2u || dc == 2u) {
+            const int tb = k0 > 2u ? pool.take() : -1;
+            ex = __dsub_rn(ex, closed_form<DM>(s_r, pool.at(b0), k0, dc, tb >= 0 ? pool.at(tb) : nullptr, lane));
+            if (tb >= 0) pool.give(tb);
+            pool.give(b0);
         } else {
+            unsigned long long row0 = 0;
+            if (lane == 0) row0 = atomicAdd(a.rows_used, static_cast<unsigned long long>(k0));
+            row0 = __shfl_sync(kMask, row0, 0);
+            if (row0 + k0 <= a.row_cap) {
+                sort_rows<DM>(pool.at(b0), k0, dc, false, a.frames + row0 * dc, lane);
+                for (uint32_t t = lane; t < k0; t += 32u) a.row_item[row0 + t] = item;
+                if (lane == 0) {
+                    a.frame_k[item] = k0;
+                    a.frame_off[item] = row0;
+                }
+                pool.give(b0);
+                continue;
+            }
+            // the frame list is full: this warp finishes the item alone
             ex = __dsub_rn(ex, frame_hv<DM>(s_r, pool, b0, k0, dc, lane, &fail));
+        }
+        if (fail) {
+            mark_failed(a, item, lane);
+            if (lane == 0) a.frame_k[item] = 0;
+            pool.free = (1u << m) - 1u;
+            continue;
+        }
+        if (lane == 0) {
+            a.frame_k[item] = 0;
+            a.out[item] = a.contributions ? ex : slice_term(s_r, p, m, ex);
+        }
+    }
+}
+
+template <int DM>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) wfg_sub_kernel(wfg_args a, wfg_ref ref)
+{
+    __shared__ double s_r[DM];
+    if (threadIdx.x < DM) s_r[threadIdx.x] = threadIdx.x < a.m ? ref.r[threadIdx.x] : 0.0;
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t gw = static_cast<uint64_t>(blockIdx.x) * kWarpsPerBlock + (threadIdx.x >> 5);
+    const uint32_t m = a.m;
+    const uint32_t dc = a.contributions ? m : m - 1u;
+    const unsigned long long used = *a.rows_used;
+    const unsigned long long rows = used < a.row_cap ? used : a.row_cap;
+    frame_pool pool{a.pool + gw * m * a.bd, a.bd, (1u << m) - 1u};
+    for (;;) {
+        unsigned g = 0;
+        if (lane == 0) g = atomicAdd(a.next + 2, 1u);
+        g = __shfl_sync(kMask, g, 0);
+        if (g >= rows) break;
+        const uint32_t item = a.row_item[g]; // unwritten (any value) for rows of a frame past the list's end
+        if (item >= a.n) continue;
+        const uint32_t k0 = a.frame_k[item];
+        const unsigned long long off = a.frame_off[item];
+        if (k0 == 0u || g < off || g >= off + k0) continue; // rows of a frame past the list's end
+        const uint32_t j = static_cast<uint32_t>(g - off);
+        const okey *f = a.frames + off * dc;
+        const okey *p = f + static_cast<uint64_t>(j) * dc;
+        const int cb = pool.take();
+        const uint32_t ck = limit_set<DM>(f, dc, j + 1u, k0, k0, p, dc - 1u, pool.at(cb), lane);
+        double ex = vol(s_r, p, dc - 1u);
+        bool fail = false;
+        if (ck == 0u) {
+            pool.give(cb);
+        } else {
+            ex = __dsub_rn(ex, frame_hv<DM>(s_r, pool, cb, ck, dc - 1u, lane, &fail));
         }
         if (fail) {
             if (lane == 0) {
                 atomicOr(a.status, 1u);
-                a.out[item] = __longlong_as_double(0x7ff8000000000000LL);
+                a.row_term[g] = __longlong_as_double(0x7ff8000000000000LL);
             }
             pool.free = (1u << m) - 1u;
             continue;
         }
-        if (lane == 0) a.out[item] = a.contributions ? ex : slice_term(s_r, p, m, ex);
+        if (lane == 0) a.row_term[g] = slice_term(s_r, p, dc, ex);
     }
 }
 
-// Ranks of the points by hvwfg::cmp_points over m coordinates (ties by index)
-// and the points written in that order: one thread per point, the others
-// staged through shared memory.
-constexpr int kRankThreads = 128;
+// The items with a frame in the list: H = the sum of their rows' sub-terms in
+// order from 0.0, then the item's value as wfg_top_kernel would give it.
+__global__ void wfg_join_kernel(wfg_args a, wfg_ref ref)
+{
+    const uint32_t m = a.m;
+    const uint32_t dc = a.contributions ? m : m - 1u;
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < a.n; item += gridDim.x * blockDim.x) {
+        const uint32_t k0 = a.frame_k[item];
+        if (k0 == 0u) continue;
+        const unsigned long long off = a.frame_off[item];
+        double h = 0.0;
+        for (uint32_t j = 0; j < k0; ++j) h = __dadd_rn(h, a.row_term[off + j]);
+        const okey *p = a.pts + static_cast<uint64_t>(item) * m;
+        const double ex = __dsub_rn(vol(ref.r, p, dc), h);
+        a.out[item] = a.contributions ? ex : slice_term(ref.r, p, m, ex);
+    }
+}
+
+// The points as order keys (keys[i * m + c]).
+__global__ void wfg_keys_kernel(const double *__restrict__ pts, uint64_t total, okey *__restrict__ keys)
+{
+    for (uint64_t e = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        keys[e] = to_key(pts[e]);
+}
+
+// Ranks of the points by hvwfg::cmp_points over m coordinates (ties by
+// index): block (x, y) counts, for its 64 points, the points of slice y of
+// the others that come first (staged in shared memory), added to rank[]
+// (zero at launch).
+constexpr int kRankThreads = 64;
+constexpr uint32_t kRankSlices = 8;
 
 __global__ void __launch_bounds__(kRankThreads)
-    wfg_sort_points_kernel(const double *__restrict__ pts, uint32_t n, uint32_t m, double *__restrict__ sorted)
+    wfg_rank_kernel(const okey *__restrict__ keys, uint32_t n, uint32_t m, unsigned *__restrict__ rank)
 {
-    __shared__ double tile[kRankThreads * kWfgMaxObjectives];
+    __shared__ okey tile[kRankThreads * kWfgMaxObjectives];
     const uint32_t i = blockIdx.x * kRankThreads + threadIdx.x;
-    double mine[kWfgMaxObjectives];
-    for (uint32_t c = 0; c < m; ++c) mine[c] = i < n ? pts[static_cast<uint64_t>(i) * m + c] : 0.0;
-    uint32_t rank = 0;
-    for (uint32_t j0 = 0; j0 < n; j0 += kRankThreads) {
-        const uint32_t cnt = min(static_cast<uint32_t>(kRankThreads), n - j0);
+    okey mine[kWfgMaxObjectives];
+    for (uint32_t c = 0; c < m; ++c) mine[c] = i < n ? keys[static_cast<uint64_t>(i) * m + c] : 0;
+    const uint32_t per = (n + kRankSlices - 1u) / kRankSlices;
+    const uint32_t j_begin = blockIdx.y * per, j_end = min(n, j_begin + per);
+    uint32_t cnt = 0;
+    for (uint32_t j0 = j_begin; j0 < j_end; j0 += kRankThreads) {
+        const uint32_t len = min(static_cast<uint32_t>(kRankThreads), j_end - j0);
         __syncthreads();
-        for (uint32_t e = threadIdx.x; e < cnt * m; e += kRankThreads)
-            tile[e] = pts[static_cast<uint64_t>(j0) * m + e];
+        for (uint32_t e = threadIdx.x; e < len * m; e += kRankThreads) tile[e] = keys[static_cast<uint64_t>(j0) * m + e];
         __syncthreads();
         if (i < n) {
-            for (uint32_t jj = 0; jj < cnt; ++jj) {
-                const double *rj = tile + jj * m;
+            for (uint32_t jj = 0; jj < len; ++jj) {
+                const okey *rj = tile + jj * m;
                 int dec = 0;
                 for (int c = static_cast<int>(m) - 1; c >= 0 && dec == 0; --c)
                     dec = rj[c] > mine[c] ? 1 : (rj[c] < mine[c] ? -1 : 0);
-                rank += (dec > 0 || (dec == 0 && j0 + jj < i)) ? 1u : 0u;
+                cnt += (dec > 0 || (dec == 0 && j0 + jj < i)) ? 1u : 0u;
             }
         }
     }
-    if (i < n)
-        for (uint32_t c = 0; c < m; ++c) sorted[static_cast<uint64_t>(rank) * m + c] = mine[c];
+    if (i < n && cnt) atomicAdd(rank + i, cnt);
+}
+
+// sorted[rank[i]] = keys[i] (rows of m)
+__global__ void wfg_scatter_kernel(const okey *__restrict__ keys, uint32_t n, uint32_t m,
+                                   const unsigned *__restrict__ rank, okey *__restrict__ sorted)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        for (uint32_t c = 0; c < m; ++c) sorted[static_cast<uint64_t>(rank[i]) * m + c] = keys[static_cast<uint64_t>(i) * m + c];
 }
 
 // out = the sum of term[0 .. n) in index order from 0.0 (compute_hv's
-// H += ..., hv_hvwfg.cpp:262-266)
-__global__ void wfg_sum_kernel(const double *__restrict__ term, uint32_t n, double *__restrict__ out)
+// H += ..., hv_hvwfg.cpp:262-266): the block stages the terms in shared
+// memory, one thread adds them in order.
+constexpr int kSumThreads = 1024;
+
+__global__ void __launch_bounds__(kSumThreads) wfg_sum_kernel(const double *__restrict__ term, uint32_t n,
+                                                              double *__restrict__ out)
 {
-    if (threadIdx.x != 0) return;
+    __shared__ double s[kSumThreads];
     double h = 0.0;
-    for (uint32_t i = 0; i < n; ++i) h = __dadd_rn(h, term[i]);
-    *out = h;
+    for (uint32_t base = 0; base < n; base += kSumThreads) {
+        const uint32_t len = min(static_cast<uint32_t>(kSumThreads), n - base);
+        __syncthreads();
+        if (threadIdx.x < len) s[threadIdx.x] = term[base + threadIdx.x];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (; t + 4u <= len; t += 4u) {
+                const double a = s[t], b = s[t + 1u], c = s[t + 2u], d = s[t + 3u];
+                h = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(h, a), b), c), d);
+            }
+            for (; t < len; ++t) h = __dadd_rn(h, s[t]);
+        }
+    }
+    if (threadIdx.x == 0) *out = h;
 }
 
 // The volume of one or two points (compute_hv's inclusion-exclusion,
@@ -445,23 +616,23 @@ __global__ void wfg_small_kernel(const double *__restrict__ pts, uint32_t n, uin
         return;
     }
     if (n == 1u) {
-        *out = vol(r, pts, m);
+        *out = vol_d(r, pts, m);
         return;
     }
-    const double h = __dadd_rn(vol(r, pts, m), vol(r, pts + m, m));
+    const double h = __dadd_rn(vol_d(r, pts, m), vol_d(r, pts + m, m));
     double isect = 1.0;
     for (uint32_t c = 0; c < m; ++c) isect = __dmul_rn(isect, __dsub_rn(r[c], std_max(pts[c], pts[m + c])));
     *out = __dsub_rn(h, isect);
 }
 
-// 2-objective points as hv2d::contributions hands them to hv3d: a third
-// coordinate 0 (hv_hv2d.cpp:135-143)
-__global__ void wfg_lift2_kernel(const double *__restrict__ pts, uint32_t n, double *__restrict__ out)
+// 2-objective points as hv2d::contributions hands them to hv3d, as keys: a
+// third coordinate 0 (hv_hv2d.cpp:135-143)
+__global__ void wfg_lift2_kernel(const double *__restrict__ pts, uint32_t n, okey *__restrict__ out)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        out[3ull * i] = pts[2ull * i];
-        out[3ull * i + 1u] = pts[2ull * i + 1u];
-        out[3ull * i + 2u] = 0.0;
+        out[3ull * i] = to_key(pts[2ull * i]);
+        out[3ull * i + 1u] = to_key(pts[2ull * i + 1u]);
+        out[3ull * i + 2u] = to_key(0.0);
     }
 }
 
@@ -470,47 +641,73 @@ size_t round256(size_t b)
     return (b + 255u) & ~size_t(255);
 }
 
-// Scratch of the warp kernel over n points of m coordinates: [points n*m |
-// out n | counter, status | pool]; the number of warps fits the pool in
+// Scratch of the split kernels over n points of m coordinates: [counters,
+// status | per item: frame rows, first row | per row: item, sub-term, dc keys
+// | pool]; the frame list holds up to kRowCap rows (past it, a frame is
+// finished by the warp that built it), the number of warps fits the pool in
 // kPoolBytes (at least one warp).
 constexpr size_t kPoolBytes = size_t(1) << 30;
+constexpr uint64_t kRowCap = uint64_t(1) << 22;
 
-int run_warps(pgx_context *ctx, const double *d_pts, uint32_t n, uint32_t m, const wfg_ref &ref, int contributions,
+int run_warps(pgx_context *ctx, const okey *d_keys, uint32_t n, uint32_t m, const wfg_ref &ref, int contributions,
               double *d_out, cudaStream_t s)
 {
     const uint64_t bd = static_cast<uint64_t>(n) * m; // a frame: at most n rows of at most m coordinates
-    const size_t per_warp = static_cast<size_t>(m) * bd * sizeof(double);
+    const size_t per_warp = static_cast<size_t>(m) * bd * sizeof(okey);
     PGX_CHECK(per_warp <= (size_t(4) << 30), PGX_ERR_CAPACITY,
               "hypervolume (WFG): " + std::to_string(n) + " points of " + std::to_string(m) +
                   " objectives need more than 4 GiB of frames per warp");
-    const uint64_t want = std::min<uint64_t>(n, static_cast<uint64_t>(ctx->num_sms) * 16u);
+    const uint32_t dc = contributions ? m : m - 1u;
+    const uint64_t row_cap = std::max<uint64_t>(1u, std::min<uint64_t>(static_cast<uint64_t>(n) * (n - 1u) / 2u + n,
+                                                                        kRowCap));
+    const uint64_t want = std::min<uint64_t>(std::max<uint64_t>(n, 1024u), static_cast<uint64_t>(ctx->num_sms) * 16u);
     const uint64_t fit = std::max<uint64_t>(1u, kPoolBytes / per_warp);
     uint64_t warps = std::min(want, fit);
     const unsigned blocks = static_cast<unsigned>((warps + kWarpsPerBlock - 1u) / kWarpsPerBlock);
     warps = static_cast<uint64_t>(blocks) * kWarpsPerBlock; // every warp of the grid has its slice
     const size_t b_ctl = 256u;
-    PGX_TRY(ctx->h_wfg.ensure(b_ctl + warps * per_warp));
-    unsigned *ctl = ctx->h_wfg.as<unsigned>();
+    const size_t b_k = round256(static_cast<size_t>(n) * sizeof(uint32_t));
+    const size_t b_off = round256(static_cast<size_t>(n) * sizeof(unsigned long long));
+    const size_t b_ri = round256(row_cap * sizeof(uint32_t));
+    const size_t b_rt = round256(row_cap * sizeof(double));
+    const size_t b_fr = round256(row_cap * dc * sizeof(okey));
+    const size_t head = b_ctl + b_k + b_off + b_ri + b_rt + b_fr;
+    PGX_TRY(ctx->h_wfg.ensure(head + warps * per_warp));
+    char *base = ctx->h_wfg.as<char>();
+    unsigned *ctl = reinterpret_cast<unsigned *>(base);
     PGX_CUDA(cudaMemsetAsync(ctl, 0, b_ctl, s));
     wfg_args a{};
-    a.pts = d_pts;
+    a.pts = d_keys;
     a.n = n;
     a.m = m;
     a.contributions = contributions;
     a.out = d_out;
-    a.pool = reinterpret_cast<double *>(ctx->h_wfg.as<char>() + b_ctl);
+    a.pool = reinterpret_cast<okey *>(base + head);
     a.bd = bd;
     a.next = ctl;
     a.status = ctl + 1;
+    a.rows_used = reinterpret_cast<unsigned long long *>(ctl + 4);
+    a.row_cap = row_cap;
+    a.frame_k = reinterpret_cast<uint32_t *>(base + b_ctl);
+    a.frame_off = reinterpret_cast<unsigned long long *>(base + b_ctl + b_k);
+    a.row_item = reinterpret_cast<uint32_t *>(base + b_ctl + b_k + b_off);
+    a.row_term = reinterpret_cast<double *>(base + b_ctl + b_k + b_off + b_ri);
+    a.frames = reinterpret_cast<okey *>(base + b_ctl + b_k + b_off + b_ri + b_rt);
+    const int threads = kWarpsPerBlock * 32;
     if (m <= 4u) {
-        wfg_kernel<4><<<blocks, kWarpsPerBlock * 32, 0, s>>>(a, ref);
+        wfg_top_kernel<4><<<blocks, threads, 0, s>>>(a, ref);
+        wfg_sub_kernel<4><<<blocks, threads, 0, s>>>(a, ref);
     } else if (m <= 8u) {
-        wfg_kernel<8><<<blocks, kWarpsPerBlock * 32, 0, s>>>(a, ref);
+        wfg_top_kernel<8><<<blocks, threads, 0, s>>>(a, ref);
+        wfg_sub_kernel<8><<<blocks, threads, 0, s>>>(a, ref);
     } else {
-        wfg_kernel<16><<<blocks, kWarpsPerBlock * 32, 0, s>>>(a, ref);
+        wfg_top_kernel<16><<<blocks, threads, 0, s>>>(a, ref);
+        wfg_sub_kernel<16><<<blocks, threads, 0, s>>>(a, ref);
     }
     PGX_CUDA(cudaGetLastError());
-    ++ctx->launches;
+    wfg_join_kernel<<<(n + 127u) / 128u, 128, 0, s>>>(a, ref);
+    PGX_CUDA(cudaGetLastError());
+    ctx->launches += 3;
     return PGX_OK;
 }
 
@@ -544,17 +741,30 @@ int launch_wfg_compute(pgx_context *ctx, const double *d_pts, uint32_t n, uint32
         ++ctx->launches;
         return PGX_OK;
     }
-    const size_t b_pts = round256(static_cast<size_t>(n) * m * sizeof(double));
+    // keys | sorted keys | ranks | terms
+    const size_t b_keys = round256(static_cast<size_t>(n) * m * sizeof(okey));
+    const size_t b_rank = round256(static_cast<size_t>(n) * sizeof(unsigned));
     const size_t b_terms = round256(static_cast<size_t>(n) * sizeof(double));
-    PGX_TRY(ctx->s_crowd.ensure(b_pts + b_terms));
-    double *sorted = ctx->s_crowd.as<double>();
-    double *terms = reinterpret_cast<double *>(ctx->s_crowd.as<char>() + b_pts);
-    wfg_sort_points_kernel<<<(n + kRankThreads - 1u) / kRankThreads, kRankThreads, 0, s>>>(d_pts, n, m, sorted);
+    PGX_TRY(ctx->s_crowd.ensure(2u * b_keys + b_rank + b_terms));
+    char *base = ctx->s_crowd.as<char>();
+    okey *keys = reinterpret_cast<okey *>(base);
+    okey *sorted = reinterpret_cast<okey *>(base + b_keys);
+    unsigned *rank = reinterpret_cast<unsigned *>(base + 2u * b_keys);
+    double *terms = reinterpret_cast<double *>(base + 2u * b_keys + b_rank);
+    const uint64_t total = static_cast<uint64_t>(n) * m;
+    const unsigned g = static_cast<unsigned>(std::min<uint64_t>((total + 255u) / 256u, 8192u));
+    wfg_keys_kernel<<<g, 256, 0, s>>>(d_pts, total, keys);
+    PGX_CUDA(cudaGetLastError());
+    PGX_CUDA(cudaMemsetAsync(rank, 0, static_cast<size_t>(n) * sizeof(unsigned), s));
+    wfg_rank_kernel<<<dim3((n + kRankThreads - 1u) / kRankThreads, kRankSlices), kRankThreads, 0, s>>>(keys, n, m,
+                                                                                                     rank);
+    PGX_CUDA(cudaGetLastError());
+    wfg_scatter_kernel<<<(n + 255u) / 256u, 256, 0, s>>>(keys, n, m, rank, sorted);
     PGX_CUDA(cudaGetLastError());
     PGX_TRY(run_warps(ctx, sorted, n, m, ref, 0, terms, s));
-    wfg_sum_kernel<<<1, 32, 0, s>>>(terms, n, d_out);
+    wfg_sum_kernel<<<1, kSumThreads, 0, s>>>(terms, n, d_out);
     PGX_CUDA(cudaGetLastError());
-    ctx->launches += 2;
+    ctx->launches += 4;
     return PGX_OK;
 }
 
@@ -571,17 +781,23 @@ int launch_wfg_contributions(pgx_context *ctx, const double *d_pts, uint32_t n, 
         ++ctx->launches;
         return PGX_OK;
     }
+    const uint32_t mk = m == 2u ? 3u : m; // 2 objectives: hv3d's points with a third coordinate 0
+    PGX_TRY(ctx->s_crowd.ensure(static_cast<size_t>(n) * mk * sizeof(okey)));
+    okey *keys = ctx->s_crowd.as<okey>();
     if (m == 2u) {
-        PGX_TRY(ctx->s_crowd.ensure(static_cast<size_t>(n) * 3u * sizeof(double)));
-        double *lifted = ctx->s_crowd.as<double>();
         const unsigned g = static_cast<unsigned>(std::min<uint64_t>((n + 255u) / 256u, 4096u));
-        wfg_lift2_kernel<<<g, 256, 0, s>>>(d_pts, n, lifted);
+        wfg_lift2_kernel<<<g, 256, 0, s>>>(d_pts, n, keys);
         PGX_CUDA(cudaGetLastError());
         ++ctx->launches;
         const double r3[3] = {r[0], r[1], 1.0};
-        return run_warps(ctx, lifted, n, 3u, make_ref(r3, 3u), 1, d_out, s);
+        return run_warps(ctx, keys, n, 3u, make_ref(r3, 3u), 1, d_out, s);
     }
-    return run_warps(ctx, d_pts, n, m, make_ref(r, m), 1, d_out, s);
+    const uint64_t total = static_cast<uint64_t>(n) * m;
+    const unsigned g = static_cast<unsigned>(std::min<uint64_t>((total + 255u) / 256u, 8192u));
+    wfg_keys_kernel<<<g, 256, 0, s>>>(d_pts, total, keys);
+    PGX_CUDA(cudaGetLastError());
+    ++ctx->launches;
+    return run_warps(ctx, keys, n, m, make_ref(r, m), 1, d_out, s);
 }
 
 int wfg_status(pgx_context *ctx, unsigned *status)
