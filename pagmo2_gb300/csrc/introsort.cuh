@@ -20,21 +20,17 @@
 //  - Ranges are processed level by level (a level = one recursion depth), each
 //    range by one warp; the ranges of a level are disjoint, so the order in
 //    which warps take them does not change the result.
-//  - A warp partitions its range without scratch: the sequential loop swaps
-//    the i-th "left stopper" (position p > first with !(x[p] < pivot), in
-//    ascending order) with the i-th "right stopper" (!(pivot < x[p]), in
-//    descending order) for as long as the former lies below the latter, and
-//    returns min(next left stopper, last swapped right stopper) -- the first
-//    left stopper if nothing was swapped. The warp finds the stoppers with
-//    ballots over 32-position chunks taken alternately from both ends (each
-//    chunk clipped, when it is loaded, to positions no swap has touched, so
-//    its flags are those of the original values) and pairs them in order.
-//  - Ranges longer than kBlockRange are partitioned by the whole block instead:
-//    every left and right stopper of the range is compacted in position order
-//    (block scans over the original values), K = the number of pairs i with
-//    left[i] < right[i] (a prefix of i), the K swaps run in parallel, and the
-//    cut is min(left[K], right[K-1]) (left[0] when K = 0) -- the same pairs
-//    and cut as the sequential loop.
+//  - The sequential loop swaps the i-th "left stopper" (position p > first
+//    with !(x[p] < pivot), in ascending order) with the i-th "right stopper"
+//    (!(pivot < x[p]), in descending order) for as long as the former lies
+//    below the latter, and returns min(next left stopper, last swapped right
+//    stopper) -- the first left stopper if nothing was swapped. A partition
+//    here compacts every left and right stopper of the range in position order
+//    (ballots over the original values: by one warp for ranges up to
+//    kBlockRange, by block scans for longer ones), K = the number of pairs i
+//    with left[i] < right[i] (a prefix of i), the K swaps run in parallel, and
+//    the cut is min(left[K], right[K-1]) (left[0] when K = 0) -- the same
+//    pairs and cut as the sequential loop.
 //  - Ranges of 16 or fewer elements are final: the closing insertion sort of
 //    the whole array moves no element across a partition boundary, so it
 //    equals a stable sort of each such range, which a half warp computes by
@@ -320,78 +316,57 @@ __device__ int block_partition(const sort_view<K> &x, int first, int last, const
 }
 
 // One warp: median-of-three into `first`, then the Hoare partition of
-// [first+1, last) around it; returns the cut. `slots` is 64 ints of this
-// warp's shared memory. All 32 lanes call it with the same arguments.
+// [first+1, last) around it from compacted stopper lists, as block_partition
+// does with the whole block: one sweep of ballots over 32-position chunks
+// lists every left stopper (!(x[p] < pivot)) and right stopper
+// (!(pivot < x[p])) in position order into pos_l / pos_r at offset `first`
+// (the ranges a level's warps hold are disjoint, so are these areas), the
+// swappable pairs are a prefix counted by ballots, the swaps run on all lanes,
+// and the cut is min(left[K], right[K-1]) (left[0] when K = 0). All 32 lanes
+// call it with the same arguments; returns the cut.
 template <typename K>
-__device__ int warp_partition(const sort_view<K> &x, int first, int last, int *slots, int *err)
+__device__ int warp_partition(const sort_view<K> &x, int first, int last, const sort_work &w, int *err)
 {
     const unsigned lane = threadIdx.x & 31u;
+    const unsigned below = (1u << lane) - 1u;
     if (lane == 0) median_to_first(x, first, first + 1, first + (last - first) / 2, last - 1);
     __syncwarp();
     const K pv = x.k[first];
-    int lo = first + 1, hi = last - 1; // next unscanned position from each end
-    int lastL = first, lastR = last;   // last swapped left / right stopper
-    unsigned lmask = 0u, rmask = 0u;   // unpaired stoppers of the current chunks
-    int lbase = 0, rbase = 0;
-    const unsigned below = (1u << lane) - 1u;
-    // every pass either pairs a stopper or returns; chunk loads advance lo/hi
-    for (int pass = 0; pass <= last - first; ++pass) {
-        while (lmask == 0u && lo < lastR) {
-            const int p = lo + static_cast<int>(lane);
-            const bool st = p < lastR && !key_less(x.k[p], pv);
-            lmask = __ballot_sync(kSortFull, st);
-            lbase = lo;
-            lo = min(lo + 32, lastR);
+    int *pl = w.pos_l + first, *pr = w.pos_r + first;
+    int nl = 0, nr = 0;
+    for (int t0 = first + 1; t0 < last; t0 += 32) {
+        const int p = t0 + static_cast<int>(lane);
+        bool fl = false, fr = false;
+        if (p < last) {
+            const K kp = x.k[p];
+            fl = !key_less(kp, pv);
+            fr = !key_less(pv, kp);
         }
-        if (lmask == 0u) {
-            // no left stopper below the last swapped right stopper
-            if (lastR == last) {
-                if (lane == 0) atomicExch(err, kSortErrNoSentinel);
-                return last - 1;
-            }
-            return lastR;
-        }
-        while (rmask == 0u && hi > lastL) {
-            const int p = hi - static_cast<int>(lane);
-            const bool st = p > lastL && !key_less(pv, x.k[p]);
-            rmask = __ballot_sync(kSortFull, st);
-            rbase = hi;
-            hi = max(hi - 32, lastL);
-        }
-        if (rmask == 0u) return min(lbase + __ffs(lmask) - 1, lastR);
-        const int mm = min(__popc(lmask), __popc(rmask));
-        if ((lmask >> lane) & 1u) {
-            const int r = __popc(lmask & below);
-            if (r < mm) slots[r] = lbase + static_cast<int>(lane);
-        }
-        if ((rmask >> lane) & 1u) {
-            const int r = __popc(rmask & below);
-            if (r < mm) slots[32 + r] = rbase - static_cast<int>(lane);
-        }
-        __syncwarp();
-        int lp = 0, rp = 0;
-        bool ok = false;
-        if (static_cast<int>(lane) < mm) {
-            lp = slots[lane];
-            rp = slots[32 + lane];
-            ok = lp < rp;
-        }
-        // left positions ascend and right ones descend with the pair index, so
-        // the pairs that may swap are a prefix
-        const int v = __popc(__ballot_sync(kSortFull, ok));
-        if (ok) x.swap(lp, rp);
-        __syncwarp();
-        if (v > 0) {
-            lastL = __shfl_sync(kSortFull, lp, v - 1);
-            lastR = __shfl_sync(kSortFull, rp, v - 1);
-        }
-        if (v < mm) return min(__shfl_sync(kSortFull, lp, v), lastR);
-        // drop the mm paired (lowest) stoppers of each mask
-        lmask &= ~__ballot_sync(kSortFull, ((lmask >> lane) & 1u) && __popc(lmask & below) < mm);
-        rmask &= ~__ballot_sync(kSortFull, ((rmask >> lane) & 1u) && __popc(rmask & below) < mm);
+        const unsigned bl = __ballot_sync(kSortFull, fl), br = __ballot_sync(kSortFull, fr);
+        if (fl) pl[nl + __popc(bl & below)] = p;
+        if (fr) pr[nr + __popc(br & below)] = p;
+        nl += __popc(bl);
+        nr += __popc(br);
     }
-    if (lane == 0) atomicExch(err, kSortErrGuard);
-    return last - 1;
+    __syncwarp();
+    // pair i = (pl[i], pr[nr-1-i]); the swappable pairs are a prefix
+    const int mx = min(nl, nr);
+    int kk = 0;
+    for (int i0 = 0; i0 < mx; i0 += 32) {
+        const int i = i0 + static_cast<int>(lane);
+        const unsigned b = __ballot_sync(kSortFull, i < mx && pl[i] < pr[nr - 1 - i]);
+        kk += __popc(b);
+        if (b != kSortFull) break;
+    }
+    for (int i = static_cast<int>(lane); i < kk; i += 32) x.swap(pl[i], pr[nr - 1 - i]);
+    __syncwarp();
+    if (nl == 0) {
+        if (lane == 0) atomicExch(err, kSortErrNoSentinel);
+        return last - 1;
+    }
+    if (kk == 0) return pl[0];
+    const int cut = pr[nr - kk];
+    return kk < nl ? min(cut, pl[kk]) : cut;
 }
 
 // Ranges of 17..kBlockRange elements wait in a ring of int4 (first, last,
@@ -456,7 +431,6 @@ __device__ void block_std_sort(const sort_view<K> &x, int n, const sort_work &w,
 {
     const unsigned lane = threadIdx.x & 31u;
     const int warp = static_cast<int>(threadIdx.x >> 5);
-    int *slots = slots_all + warp * 64;
     if (n <= 16) {
         if (warp == 0) halfwarp_leaf_sort(x, 0, lane < 16u ? n : 0);
         __syncthreads();
@@ -548,7 +522,7 @@ __device__ void block_std_sort(const sort_view<K> &x, int n, const sort_work &w,
             if (lane == 0) heap_sort(x, a, b);
             __syncwarp();
         } else {
-            const int cut = warp_partition(x, a, b, slots, err);
+            const int cut = warp_partition(x, a, b, w, err);
             if (lane == 0) place_child(a, cut, d - 1, big_next, w, ring, cap, ctl, err);
             if (lane == 1) place_child(cut, b, d - 1, big_next, w, ring, cap, ctl, err);
             const int la = lane < 16u ? a : cut, len = lane < 16u ? cut - a : b - cut;

@@ -767,7 +767,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
     __shared__ int s_cnt, s_base, s_qn, s_wtot[32];
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const unsigned nwarp_b = blockDim.x >> 5;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     // this block's rem words in Phase A
     const uint32_t wpb = (W + gridDim.x - 1u) / gridDim.x;
     const uint32_t w_lo = min(W, blockIdx.x * wpb), w_hi = min(W, w_lo + wpb);
