@@ -346,13 +346,16 @@ struct peel_state {
     int status;   // kStatusNeedTwoObjectives: crowding over fewer than two objectives
     int sort_err; // broken invariant of the device sort (never expected)
     int gs[72];   // grid sort: [0] shared-memory ranges, [1 + level] block-partitioned ranges per level
+    int fronts_done; // fused crowding: fronts whose members and offsets are complete
+    int peel_done;   // fused crowding: the peel has ended (n_fronts final)
 };
 
 constexpr int kStatusNeedTwoObjectives = 1;
 
-// Grid-wide barrier for a cooperative launch; gives up (and flags st->err)
-// after about a second (spin_limit polls) instead of waiting forever.
-__device__ bool grid_sync(peel_state *st, unsigned long long spin_limit = kSpinLimit)
+// Grid-wide barrier for a cooperative launch (of its first nblocks blocks, all
+// of them when 0); gives up (and flags st->err) after about a second
+// (spin_limit polls) instead of waiting forever.
+__device__ bool grid_sync(peel_state *st, unsigned long long spin_limit = kSpinLimit, unsigned nblocks = 0)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -360,7 +363,7 @@ __device__ bool grid_sync(peel_state *st, unsigned long long spin_limit = kSpinL
         const unsigned g0 = *vgen;
         __threadfence();
         const unsigned arrived = atomicAdd(&st->bar_count, 1u);
-        if (arrived == gridDim.x - 1u) {
+        if (arrived == (nblocks ? nblocks : gridDim.x) - 1u) {
             atomicExch(&st->bar_count, 0u);
             __threadfence();
             atomicAdd(&st->bar_gen, 1u);
@@ -611,6 +614,102 @@ constexpr int kQueue = 4096; // witness rescans queued per block and front
 // member's key comes out of its own row scan (no second pass over the row).
 constexpr uint32_t kPosPoints = 32768;
 
+// ------------------------------------------------------------ crowding and orders
+
+constexpr int kSortThreads = 1024;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortSmemCap = 4096;                                // (key, value) pairs kept in shared memory
+constexpr int kSortSmemSmall = kSortSmemCap / 16 + 2;             // short ranges per level list
+constexpr int kSortSmemBig = kSortSmemCap / dev::kBlockRange + 2; // block-partitioned ranges per level list
+constexpr size_t kSortSmemBytes = static_cast<size_t>(kSortSmemCap) * (sizeof(dev::key2) + 3u * sizeof(int32_t))
+                                  + 2u * (kSortSmemSmall + kSortSmemBig) * sizeof(int2);
+
+// Where one block sorts L pairs: its shared memory when they fit, else the
+// caller's slices of the global work arrays (L keys, L values, L ranges, 2 L
+// positions).
+template <typename K>
+struct sort_area {
+    K *k;
+    int32_t *v;
+    dev::sort_work w;
+};
+
+template <typename K>
+__device__ sort_area<K> pick_area(unsigned char *smem, int L, K *gk, int32_t *gv, int2 *gl, int32_t *gpos)
+{
+    sort_area<K> a;
+    if (L <= kSortSmemCap) {
+        unsigned char *q = smem;
+        a.k = reinterpret_cast<K *>(q);
+        q += kSortSmemCap * sizeof(dev::key2);
+        a.w.small = reinterpret_cast<int2 *>(q);
+        a.w.small_cap = kSortSmemSmall;
+        q += 2u * kSortSmemSmall * sizeof(int2);
+        a.w.big = reinterpret_cast<int2 *>(q);
+        a.w.big_cap = kSortSmemBig;
+        q += 2u * kSortSmemBig * sizeof(int2);
+        a.v = reinterpret_cast<int32_t *>(q);
+        q += kSortSmemCap * sizeof(int32_t);
+        a.w.pos_l = reinterpret_cast<int *>(q);
+        q += kSortSmemCap * sizeof(int32_t);
+        a.w.pos_r = reinterpret_cast<int *>(q);
+    } else {
+        a.k = gk;
+        a.v = gv;
+        // the small-range list doubles as a ring of int4: start it on a 16-byte boundary
+        int2 *g0 = gl + ((reinterpret_cast<uintptr_t>(gl) & 15u) ? 1 : 0);
+        a.w.big_cap = L / dev::kBlockRange + 2;
+        a.w.small_cap = (L - 1 - 2 * a.w.big_cap) / 2;
+        a.w.small = g0;
+        a.w.big = g0 + 2 * a.w.small_cap;
+        a.w.pos_l = gpos;
+        a.w.pos_r = gpos + L;
+    }
+    return a;
+}
+
+// crowding_distance (multi_objective.cpp:280-315) of one front of L >= 2
+// members (point indices, in front order), by one block, into cd[point]. Per
+// objective: std::sort of the member list by that objective (starting from the
+// previous objective's order), ends := +inf, interior += (f[next] - f[prev]) /
+// (f[last] - f[first]).
+__device__ void front_crowding(const double *__restrict__ pts, uint32_t n, uint32_t m,
+                               const long long *__restrict__ keys, const int32_t *members, int L,
+                               const sort_area<long long> &a, dev::sort_ctl *ctl, int *slots, int *err, double *cd)
+{
+    for (int p = threadIdx.x; p < L; p += blockDim.x) {
+        const int32_t q = __ldcg(members + p); // written by other blocks of a fused peel
+        a.v[p] = q;
+        cd[q] = 0.0;
+    }
+    __syncthreads();
+    for (uint32_t k = 0; k < m; ++k) {
+        const long long *kk = keys + static_cast<uint64_t>(k) * n;
+        for (int p = threadIdx.x; p < L; p += blockDim.x) a.k[p] = kk[a.v[p]];
+        __syncthreads();
+        dev::block_std_sort(dev::sort_view<long long>{a.k, a.v}, L, a.w, ctl, slots, err);
+        const int32_t q0 = a.v[0], q1 = a.v[L - 1];
+        const double df = pts[static_cast<uint64_t>(q1) * m + k] - pts[static_cast<uint64_t>(q0) * m + k];
+        for (int p = 1 + static_cast<int>(threadIdx.x); p < L - 1; p += blockDim.x) {
+            const int32_t q = a.v[p];
+            cd[q] += (pts[static_cast<uint64_t>(a.v[p + 1]) * m + k] - pts[static_cast<uint64_t>(a.v[p - 1]) * m + k])
+                     / df;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            cd[q0] = HUGE_VAL;
+            cd[q1] = HUGE_VAL;
+        }
+        __syncthreads();
+    }
+}
+
+// How fronts of one and two points are treated.
+enum : int {
+    kCrowdNsga2 = 0,         // nsga2.cpp:188-193: +inf for fronts of 1 or 2 points
+    kCrowdSortPopulation = 1 // multi_objective.cpp:441-446: 0 for a single point, else crowding_distance
+};
+
 struct peel2_args {
     const uint32_t *Dt;
     const int32_t *dom_count;
@@ -622,7 +721,61 @@ struct peel2_args {
     int32_t *cnt;       // n + 2 per-front member counters, zeroed
     int32_t *rank, *front_offsets, *front_indices;
     peel_state *st;
+    // blocks [0, npeel) peel; with crowding (cd set), blocks [npeel, gridDim.x)
+    // compute the crowding distances of the fronts of up to kSortSmemCap
+    // members as the peel completes them (longer fronts: big_crowding_kernel)
+    uint32_t npeel;
+    const double *pts;
+    uint32_t m;
+    const long long *keys;
+    double *cd;
+    int crowd_mode;
 };
+
+// Blocks of the fused peel that compute crowding distances.
+constexpr int kCrowdBlocks = 16;
+
+// The crowding blocks of peel2_kernel: block c of C takes fronts c, c + C, ...,
+// each once the peel has published it (st->fronts_done), with a bounded wait.
+__device__ void crowd_role(const peel2_args &a, int c, int C)
+{
+    extern __shared__ __align__(16) unsigned char sort_smem[];
+    __shared__ dev::sort_ctl ctl;
+    __shared__ int slots[kSortWarps * 64];
+    __shared__ int s_go;
+    for (int f = c;; f += C) {
+        if (threadIdx.x == 0) {
+            int go = 0;
+            volatile int *vd = &a.st->fronts_done, *vp = &a.st->peel_done, *ve = &a.st->err, *vn = &a.st->n_fronts;
+            for (unsigned long long spins = 0;; ++spins) {
+                if (*vd > f) {
+                    go = 1;
+                    break;
+                }
+                if (*ve) break;
+                if (*vp && *vn <= f) break;
+                if (spins > kSpinLimit) {
+                    atomicExch(&a.st->err, 1);
+                    break;
+                }
+                __nanosleep(256);
+            }
+            __threadfence();
+            s_go = go;
+        }
+        __syncthreads();
+        if (!s_go) return;
+        const int off = __ldcg(a.front_offsets + f), L = __ldcg(a.front_offsets + f + 1) - off;
+        const int32_t *mem = a.front_indices + off;
+        if (L == 1 || (L == 2 && a.crowd_mode == kCrowdNsga2)) {
+            if (static_cast<int>(threadIdx.x) < L) a.cd[__ldcg(mem + threadIdx.x)] = a.crowd_mode == kCrowdNsga2 ? HUGE_VAL : 0.0;
+        } else if (L <= kSortSmemCap) {
+            const sort_area<long long> area = pick_area<long long>(sort_smem, L, nullptr, nullptr, nullptr, nullptr);
+            front_crowding(a.pts, a.n, a.m, a.keys, mem, L, area, &ctl, slots, &a.st->sort_err, a.cd);
+        }
+        __syncthreads();
+    }
+}
 
 // In-place exclusive prefix sum of h[0, R) by the whole block (R <= 4
 // entries per thread here); wtot holds 32 ints of scratch.
@@ -749,7 +902,12 @@ __global__ void __launch_bounds__(256) witness_init_kernel(const uint32_t *__res
 
 __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
 {
-    extern __shared__ uint32_t dyn[];
+    if (blockIdx.x >= a.npeel) {
+        crowd_role(a, static_cast<int>(blockIdx.x - a.npeel), static_cast<int>(gridDim.x - a.npeel));
+        return;
+    }
+    const uint32_t P = a.npeel; // the peeling blocks
+    extern __shared__ __align__(16) uint32_t dyn[];
     const uint32_t W = a.W, n = a.n;
     uint32_t *s_rem = dyn;                                          // W
     uint32_t *s_Z = s_rem + W;                                      // W: front 0
@@ -759,8 +917,8 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
     int32_t *s_idx = s_key + kTile;                                 // kTile
     int32_t *s_queue = s_idx + kTile;                               // kQueue
     int32_t *s_wit = s_queue + kQueue;                              // 32 wpb: witnesses of this block's points
-    int32_t *s_res = s_wit + 32u * ((W + gridDim.x - 1u) / gridDim.x); // 32 wpb: their rescans' resume words
-    uint32_t *s_pbits = reinterpret_cast<uint32_t *>(s_res + 32u * ((W + gridDim.x - 1u) / gridDim.x)); // W
+    int32_t *s_res = s_wit + 32u * ((W + P - 1u) / P); // 32 wpb: their rescans' resume words
+    uint32_t *s_pbits = reinterpret_cast<uint32_t *>(s_res + 32u * ((W + P - 1u) / P)); // W
     uint16_t *s_pos = reinterpret_cast<uint16_t *>(s_pbits + W); // n: positions in the previous front
     const bool pos_maps = n <= kPosPoints;
     __shared__ int32_t s_list[kLocalMembers], s_lkey[kLocalMembers];
@@ -769,7 +927,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
     const unsigned nwarp_b = blockDim.x >> 5;
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     // this block's rem words in Phase A
-    const uint32_t wpb = (W + gridDim.x - 1u) / gridDim.x;
+    const uint32_t wpb = (W + P - 1u) / P;
     const uint32_t w_lo = min(W, blockIdx.x * wpb), w_hi = min(W, w_lo + wpb);
     const int32_t j_lo = static_cast<int32_t>(32u * w_lo); // this block's points: [j_lo, 32 w_hi)
     for (uint32_t t = threadIdx.x; t < 32u * wpb; t += blockDim.x) {
@@ -823,7 +981,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
     __syncthreads();
     const int L0 = s_wtot[nwarp_b - 1];
     // front 0's global writes, spread over the blocks by word
-    for (uint32_t w = blockIdx.x * nwarp_b + warp; w < W; w += gridDim.x * nwarp_b) {
+    for (uint32_t w = blockIdx.x * nwarp_b + warp; w < W; w += P * nwarp_b) {
         const uint32_t z = s_Z[w];
         if ((z >> lane) & 1u) {
             const uint32_t q = w * 32u + lane;
@@ -1026,9 +1184,15 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
             a.list[(k & 1) * n + s_base + t] = s_list[t];
             a.keyv[(k & 1) * n + s_base + t] = s_lkey[t];
         }
-        if (!grid_sync(a.st)) {
+        if (!grid_sync(a.st, kSpinLimit, P)) {
             if (threadIdx.x == 0) atomicExch(&a.st->n_fronts, -1);
             return;
+        }
+        // fronts 0 .. k-1 are complete in global memory (their last writes came
+        // before this barrier): the crowding blocks may take them
+        if (tid == 0) {
+            __threadfence();
+            atomicExch(&a.st->fronts_done, k);
         }
         const int L = *reinterpret_cast<volatile int *>(a.cnt + k);
         if (L == 0) break; // cannot happen while points remain (a dominance cycle would need one); guards the loop
@@ -1093,7 +1257,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
                         s_pos[q] = static_cast<uint16_t>(p);
                         atomicOr(s_pbits + (q >> 5), 1u << (q & 31));
                     }
-                    if (p % static_cast<int>(gridDim.x) == static_cast<int>(blockIdx.x)) {
+                    if (p % static_cast<int>(P) == static_cast<int>(blockIdx.x)) {
                         a.front_indices[off + p] = q;
                         a.rank[q] = k;
                     }
@@ -1109,7 +1273,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
                 const int q = __ldcg(lst + t);
                 atomicAnd(s_rem + (q >> 5), ~(1u << (q & 31)));
             }
-            const int mpb = (L + static_cast<int>(gridDim.x) - 1) / static_cast<int>(gridDim.x);
+            const int mpb = (L + static_cast<int>(P) - 1) / static_cast<int>(P);
             const int m_lo = min(L, static_cast<int>(blockIdx.x) * mpb), m_hi = min(L, m_lo + mpb);
             int32_t *cntm = s_queue; // mpb <= kQueue (checked on the host)
             for (int t = threadIdx.x; t < m_hi - m_lo; t += blockDim.x) cntm[t] = 0;
@@ -1141,7 +1305,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
             }
             prev_global = true;
             pos_ok = false;
-            if (!grid_sync(a.st)) {
+            if (!grid_sync(a.st, kSpinLimit, P)) {
                 if (threadIdx.x == 0) atomicExch(&a.st->n_fronts, -1);
                 return;
             }
@@ -1152,107 +1316,23 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
         off += L;
         __syncthreads();
     }
+    if (P < gridDim.x) {
+        // the last front's writes, then every front to the crowding blocks
+        const bool ok = grid_sync(a.st, kSpinLimit, P);
+        if (tid == 0) {
+            a.st->n_fronts = (!ok || *reinterpret_cast<volatile int *>(&a.st->err)) ? -1 : k;
+            a.front_offsets[0] = 0;
+            __threadfence();
+            atomicExch(&a.st->fronts_done, k);
+            atomicExch(&a.st->peel_done, 1);
+        }
+        return;
+    }
     if (tid == 0) {
         a.st->n_fronts = *reinterpret_cast<volatile int *>(&a.st->err) ? -1 : k;
         a.front_offsets[0] = 0;
     }
 }
-
-// ------------------------------------------------------------ crowding and orders
-
-constexpr int kSortThreads = 1024;
-constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortSmemCap = 4096;                                // (key, value) pairs kept in shared memory
-constexpr int kSortSmemSmall = kSortSmemCap / 16 + 2;             // short ranges per level list
-constexpr int kSortSmemBig = kSortSmemCap / dev::kBlockRange + 2; // block-partitioned ranges per level list
-constexpr size_t kSortSmemBytes = static_cast<size_t>(kSortSmemCap) * (sizeof(dev::key2) + 3u * sizeof(int32_t))
-                                  + 2u * (kSortSmemSmall + kSortSmemBig) * sizeof(int2);
-
-// Where one block sorts L pairs: its shared memory when they fit, else the
-// caller's slices of the global work arrays (L keys, L values, L ranges, 2 L
-// positions).
-template <typename K>
-struct sort_area {
-    K *k;
-    int32_t *v;
-    dev::sort_work w;
-};
-
-template <typename K>
-__device__ sort_area<K> pick_area(unsigned char *smem, int L, K *gk, int32_t *gv, int2 *gl, int32_t *gpos)
-{
-    sort_area<K> a;
-    if (L <= kSortSmemCap) {
-        unsigned char *q = smem;
-        a.k = reinterpret_cast<K *>(q);
-        q += kSortSmemCap * sizeof(dev::key2);
-        a.w.small = reinterpret_cast<int2 *>(q);
-        a.w.small_cap = kSortSmemSmall;
-        q += 2u * kSortSmemSmall * sizeof(int2);
-        a.w.big = reinterpret_cast<int2 *>(q);
-        a.w.big_cap = kSortSmemBig;
-        q += 2u * kSortSmemBig * sizeof(int2);
-        a.v = reinterpret_cast<int32_t *>(q);
-        q += kSortSmemCap * sizeof(int32_t);
-        a.w.pos_l = reinterpret_cast<int *>(q);
-        q += kSortSmemCap * sizeof(int32_t);
-        a.w.pos_r = reinterpret_cast<int *>(q);
-    } else {
-        a.k = gk;
-        a.v = gv;
-        // the small-range list doubles as a ring of int4: start it on a 16-byte boundary
-        int2 *g0 = gl + ((reinterpret_cast<uintptr_t>(gl) & 15u) ? 1 : 0);
-        a.w.big_cap = L / dev::kBlockRange + 2;
-        a.w.small_cap = (L - 1 - 2 * a.w.big_cap) / 2;
-        a.w.small = g0;
-        a.w.big = g0 + 2 * a.w.small_cap;
-        a.w.pos_l = gpos;
-        a.w.pos_r = gpos + L;
-    }
-    return a;
-}
-
-// crowding_distance (multi_objective.cpp:280-315) of one front of L >= 2
-// members (point indices, in front order), by one block, into cd[point]. Per
-// objective: std::sort of the member list by that objective (starting from the
-// previous objective's order), ends := +inf, interior += (f[next] - f[prev]) /
-// (f[last] - f[first]).
-__device__ void front_crowding(const double *__restrict__ pts, uint32_t n, uint32_t m,
-                               const long long *__restrict__ keys, const int32_t *members, int L,
-                               const sort_area<long long> &a, dev::sort_ctl *ctl, int *slots, int *err, double *cd)
-{
-    for (int p = threadIdx.x; p < L; p += blockDim.x) {
-        const int32_t q = members[p];
-        a.v[p] = q;
-        cd[q] = 0.0;
-    }
-    __syncthreads();
-    for (uint32_t k = 0; k < m; ++k) {
-        const long long *kk = keys + static_cast<uint64_t>(k) * n;
-        for (int p = threadIdx.x; p < L; p += blockDim.x) a.k[p] = kk[a.v[p]];
-        __syncthreads();
-        dev::block_std_sort(dev::sort_view<long long>{a.k, a.v}, L, a.w, ctl, slots, err);
-        const int32_t q0 = a.v[0], q1 = a.v[L - 1];
-        const double df = pts[static_cast<uint64_t>(q1) * m + k] - pts[static_cast<uint64_t>(q0) * m + k];
-        for (int p = 1 + static_cast<int>(threadIdx.x); p < L - 1; p += blockDim.x) {
-            const int32_t q = a.v[p];
-            cd[q] += (pts[static_cast<uint64_t>(a.v[p + 1]) * m + k] - pts[static_cast<uint64_t>(a.v[p - 1]) * m + k])
-                     / df;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            cd[q0] = HUGE_VAL;
-            cd[q1] = HUGE_VAL;
-        }
-        __syncthreads();
-    }
-}
-
-// How fronts of one and two points are treated.
-enum : int {
-    kCrowdNsga2 = 0,         // nsga2.cpp:188-193: +inf for fronts of 1 or 2 points
-    kCrowdSortPopulation = 1 // multi_objective.cpp:441-446: 0 for a single point, else crowding_distance
-};
 
 // Crowding distance of every point within its front: blocks take fronts
 // f = blockIdx.x, blockIdx.x + gridDim.x, ... (n_fronts read on the device).
@@ -2007,13 +2087,19 @@ int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n,
         PGX_CUDA(cudaMemsetAsync(sc.Dt, 0, static_cast<size_t>(n) * W8 * sizeof(uint32_t), s));
     }
 
-    // cooperative peel: every block resident at once (the grid barrier needs it)
-    const uint32_t wpb = (W + static_cast<uint32_t>(num_sms) - 1u) / static_cast<uint32_t>(num_sms);
+    // cooperative peel: every block resident at once (the grid barrier needs it);
+    // with crowding, kCrowdBlocks of the blocks compute the crowding distances
+    // of each front as soon as the others have peeled it
+    const bool fused = out.crowding != nullptr && m >= 2u && num_sms > 2 * kCrowdBlocks;
+    const uint32_t npeel = static_cast<uint32_t>(fused ? num_sms - kCrowdBlocks : num_sms);
+    const uint32_t wpb = (W + npeel - 1u) / npeel;
+    bool crowded = false;
     if (W <= static_cast<uint32_t>(kRemWords) && 32u * wpb <= static_cast<uint32_t>(kQueue)
-        && n <= static_cast<uint64_t>(kQueue) * static_cast<uint32_t>(num_sms)) {
-        const size_t smem2 = (3u * static_cast<size_t>(W) + 4u * kTile + kQueue + 64u * wpb) * sizeof(int32_t)
-                             + (n <= kPosPoints ? static_cast<size_t>(W) * 4u + ((static_cast<size_t>(n) * 2u + 3u) & ~size_t(3))
-                                                : 0u);
+        && n <= static_cast<uint64_t>(kQueue) * npeel) {
+        size_t smem2 = (3u * static_cast<size_t>(W) + 4u * kTile + kQueue + 64u * wpb) * sizeof(int32_t)
+                       + (n <= kPosPoints ? static_cast<size_t>(W) * 4u + ((static_cast<size_t>(n) * 2u + 3u) & ~size_t(3))
+                                          : 0u);
+        if (fused) smem2 = std::max(smem2, kSortSmemBytes);
         PGX_CUDA(cudaFuncSetAttribute(peel2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(smem2)));
         int occ2 = 0;
@@ -2033,11 +2119,13 @@ int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n,
         }
         *launches += 2;
         peel2_args pa{sc.Dt, out.dom_count, n, W, W8, sc.wit, sc.widx, sc.list, sc.keyv, sc.cnt,
-                      out.rank, out.front_offsets, out.front_indices, sc.st};
+                      out.rank, out.front_offsets, out.front_indices, sc.st, npeel, d_points, m, sc.keys,
+                      fused ? out.crowding : nullptr, kCrowdNsga2};
         void *args2[] = {&pa};
         PGX_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(peel2_kernel), dim3(num_sms),
                                              dim3(kPeelThreads), args2, smem2, s));
         *launches += 1;
+        crowded = fused;
     } else {
     const size_t smem = 2u * kTile * sizeof(int32_t);
     int occ = 0;
@@ -2059,7 +2147,16 @@ int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n,
     }
     PGX_CUDA(cudaMemcpyAsync(out.n_fronts, &sc.st->n_fronts, sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
 
-    if (out.crowding) {
+    if (crowded) {
+        if (n > static_cast<uint32_t>(kSortSmemCap)) {
+            // fronts longer than the shared-memory sorts: every SM on each of them
+            PGX_TRY(launch_cooperative_sort_kernel(reinterpret_cast<const void *>(big_crowding_kernel), num_sms, s,
+                                                   d_points, n, m, sc.keys, out.front_offsets, out.front_indices,
+                                                   out.n_fronts, sc.wkey, sc.widx, sc.wlist, sc.wpos, out.crowding,
+                                                   sc.st));
+            *launches += 1;
+        }
+    } else if (out.crowding) {
         PGX_TRY(launch_front_crowding(sc, d_points, n, m, out.front_offsets, out.front_indices, out.n_fronts,
                                       kCrowdNsga2, out.crowding, num_sms, s));
         *launches += crowding_launches(n, m);
