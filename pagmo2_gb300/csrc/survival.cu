@@ -348,6 +348,7 @@ struct peel_state {
     int gs[72];   // grid sort: [0] shared-memory ranges, [1 + level] block-partitioned ranges per level
     int fronts_done; // fused crowding: fronts whose members and offsets are complete
     int peel_done;   // fused crowding: the peel has ended (n_fronts final)
+    unsigned peel_arrivals; // peel_sync: arrivals so far (zero at the start of the pass)
 };
 
 constexpr int kStatusNeedTwoObjectives = 1;
@@ -378,6 +379,33 @@ __device__ bool grid_sync(peel_state *st, unsigned long long spin_limit = kSpinL
                 }
                 __nanosleep(64);
             }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *reinterpret_cast<volatile int *>(&st->err) == 0;
+}
+
+// The peel's barrier over its first nb blocks: one counter of arrivals that
+// only grows (it starts at zero for the pass), so the last arrival itself
+// releases the others (round r ends when the count reaches (r + 1) nb); no
+// reset, no second atomic. Gives up like grid_sync.
+__device__ bool peel_sync(peel_state *st, unsigned nb)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned a = atomicAdd(&st->peel_arrivals, 1u);
+        const unsigned target = (a / nb + 1u) * nb;
+        volatile unsigned *vc = &st->peel_arrivals;
+        volatile int *verr = &st->err;
+        for (unsigned long long spins = 0; *vc < target; ++spins) {
+            if (*verr) break;
+            if (spins > kSpinLimit) {
+                atomicExch(&st->err, 1);
+                break;
+            }
+            __nanosleep(16);
         }
         __threadfence();
     }
@@ -921,6 +949,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
     uint32_t *s_pbits = reinterpret_cast<uint32_t *>(s_res + 32u * ((W + P - 1u) / P)); // W
     uint16_t *s_pos = reinterpret_cast<uint16_t *>(s_pbits + W); // n: positions in the previous front
     const bool pos_maps = n <= kPosPoints;
+    uint16_t *s_dc = s_pos + ((n + 1u) & ~1u); // n: domination counts (pos_maps only; n <= kPosPoints < 65536)
     __shared__ int32_t s_list[kLocalMembers], s_lkey[kLocalMembers];
     __shared__ int s_cnt, s_base, s_qn, s_wtot[32];
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -935,6 +964,8 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
         s_wit[t] = j < n ? __ldg(a.wit + j) : -1;
         s_res[t] = j < n ? __ldg(a.res + j) : -1;
     }
+    if (pos_maps)
+        for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) s_dc[t] = static_cast<uint16_t>(__ldg(a.dom_count + t));
 
     // ---- front 0 from dom_count (every block for itself)
     for (uint32_t w = warp; w < W; w += nwarp_b) {
@@ -1093,7 +1124,8 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
                     // the witness: of the lanes' proposals, the dominator with the
                     // most dominators itself (likely in a later front, so j is
                     // rescanned less often)
-                    int best = cand >= 0 ? __ldg(a.dom_count + cand) : -1, bq = cand;
+                    int best = cand >= 0 ? (pos_maps ? static_cast<int>(s_dc[cand]) : __ldg(a.dom_count + cand)) : -1,
+                        bq = cand;
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) {
                         const int ob = __shfl_xor_sync(kFull, best, o), oq = __shfl_xor_sync(kFull, bq, o);
@@ -1184,13 +1216,14 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
             a.list[(k & 1) * n + s_base + t] = s_list[t];
             a.keyv[(k & 1) * n + s_base + t] = s_lkey[t];
         }
-        if (!grid_sync(a.st, kSpinLimit, P)) {
+        if (!peel_sync(a.st, P)) {
             if (threadIdx.x == 0) atomicExch(&a.st->n_fronts, -1);
             return;
         }
         // fronts 0 .. k-1 are complete in global memory (their last writes came
-        // before this barrier): the crowding blocks may take them
-        if (tid == 0) {
+        // before this barrier): the crowding blocks may take them (published by
+        // a warp with no part in the next steps' first loads)
+        if (P < gridDim.x && blockIdx.x == 0 && threadIdx.x == blockDim.x - 32u) {
             __threadfence();
             atomicExch(&a.st->fronts_done, k);
         }
@@ -1305,7 +1338,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
             }
             prev_global = true;
             pos_ok = false;
-            if (!grid_sync(a.st, kSpinLimit, P)) {
+            if (!peel_sync(a.st, P)) {
                 if (threadIdx.x == 0) atomicExch(&a.st->n_fronts, -1);
                 return;
             }
@@ -1318,7 +1351,7 @@ __global__ void __launch_bounds__(kPeelThreads) peel2_kernel(peel2_args a)
     }
     if (P < gridDim.x) {
         // the last front's writes, then every front to the crowding blocks
-        const bool ok = grid_sync(a.st, kSpinLimit, P);
+        const bool ok = peel_sync(a.st, P);
         if (tid == 0) {
             a.st->n_fronts = (!ok || *reinterpret_cast<volatile int *>(&a.st->err)) ? -1 : k;
             a.front_offsets[0] = 0;
@@ -2097,7 +2130,7 @@ int run_survival(const survival_scratch &sc, const double *d_points, uint32_t n,
     if (W <= static_cast<uint32_t>(kRemWords) && 32u * wpb <= static_cast<uint32_t>(kQueue)
         && n <= static_cast<uint64_t>(kQueue) * npeel) {
         size_t smem2 = (3u * static_cast<size_t>(W) + 4u * kTile + kQueue + 64u * wpb) * sizeof(int32_t)
-                       + (n <= kPosPoints ? static_cast<size_t>(W) * 4u + ((static_cast<size_t>(n) * 2u + 3u) & ~size_t(3))
+                       + (n <= kPosPoints ? static_cast<size_t>(W) * 4u + 2u * ((static_cast<size_t>(n) * 2u + 3u) & ~size_t(3))
                                           : 0u);
         if (fused) smem2 = std::max(smem2, kSortSmemBytes);
         PGX_CUDA(cudaFuncSetAttribute(peel2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
