@@ -671,6 +671,35 @@ def run_secondary(ctx, L, N, W, stream, fp64_peak_tflops, cpu_ok=True) -> dict:
                 rec["cpu_ms_2000_points"] = (time.perf_counter() - t) * 1e3
                 rec["cpu_kind"] = "port (long double slabs, O(n^2 log n)), first 2000 points"
         out[name] = rec
+    # hypervolume of 5 objectives (hvwfg) and every point's contribution, on a sphere front of 2000 points
+    wp = W.sphere_front(2000, 5)
+    wr = np.full(5, 1.1)
+    dwp = torch.from_numpy(wp).cuda()
+    dwo = torch.empty(wp.shape[0], dtype=torch.float64, device="cuda")
+
+    def wfg():
+        N.check(L.pgx_hypervolume_device(ctx.handle, dwp.data_ptr(), wp.shape[0], 5, N.ptr(wr), dwo.data_ptr(), sp))
+
+    def wfg_contrib():
+        N.check(L.pgx_hypervolume_contributions_device(ctx.handle, dwp.data_ptr(), wp.shape[0], 5, N.ptr(wr),
+                                                       dwo.data_ptr(), sp))
+    recs = {"hypervolume_wfg_2000x5": {"ms": timed(wfg, reps=5, flush_l2=False)}}
+    recs["hypervolume_wfg_2000x5"]["value"] = float(dwo[0].item())
+    recs["hv_contributions_2000x5"] = {"ms": timed(wfg_contrib, reps=3, flush_l2=False)}
+    if cpu_ok:
+        import oracle
+
+        ref = oracle.reference()
+        if ref is not None:
+            t = time.perf_counter()
+            recs["hypervolume_wfg_2000x5"]["cpu_value"] = ref.hypervolume(wp, wr)
+            recs["hypervolume_wfg_2000x5"]["cpu_ms"] = (time.perf_counter() - t) * 1e3
+            t = time.perf_counter()
+            ref.hv_contributions(wp, wr)
+            recs["hv_contributions_2000x5"]["cpu_ms"] = (time.perf_counter() - t) * 1e3
+            for rec in recs.values():
+                rec["cpu_kind"] = "reference (hvwfg, single-threaded)"
+    out.update(recs)
     out["sort_population_mo_20000x3"] = {"ms": timed(sortpop, reps=10, flush_l2=False)}
     out["archipelago_64_islands"] = run_archipelago(ctx, L, N, W, stream)
     out.update(run_refine(ctx, L, N, W, stream))
