@@ -25,8 +25,8 @@
 // against each other, then the kept points the survivors cover are removed),
 // the counting-rank sorts of a frame and the closed forms; the recursion
 // below the top level runs on an explicit stack, its frames in the warp's
-// slice of a scratch pool (m buffers of n rows); the top level's frames are
-// split into one work item per sub-term (see wfg_args). Every comparison (limit
+// slice of a scratch pool (m buffers of n rows); the frames of the first
+// levels are split into one work item per sub-term (see wfg_args). Every comparison (limit
 // sets, sorts, maxima) runs on 64-bit integer order keys of the coordinates
 // (the IEEE bit pattern with negatives mirrored, -0.0 read as +0.0, which the
 // reference compares equal): the frames hold keys, and only the volumes and
@@ -360,17 +360,32 @@ __device__ double frame_hv(const double *r, frame_pool &pool, int buf, uint32_t 
     }
 }
 
-// The work of one volume or one set of contributions is split in two levels:
-// wfg_top_kernel takes the items (the top-level terms of a volume, or the
-// points of the contributions), builds each item's limit set (its "frame")
-// and finishes the items whose frame has at most two points or two
-// coordinates; every other frame is sorted into a global frame list, one row
-// per sub-term. wfg_sub_kernel takes the rows: row j of an item's frame gives
-// the sub-term |(f_j[d-1] - r_{d-1}) * (vol_{d-1}(f_j) - hv(limit set of f_j
-// over the rows after it))|, with the recursion below it on the warp's own
-// stack. wfg_join_kernel adds each item's sub-terms in order (compute_hv's
-// H += ..., hv_hvwfg.cpp:262-266) and finishes the item. The operations and
-// their order are those of one recursion, split between warps.
+// The work of one volume or one set of contributions is split into levels of
+// rows: wfg_top_kernel takes the items (the top-level terms of a volume, or
+// the points of the contributions), builds each item's limit set (its
+// "frame") and finishes the items whose frame has at most two points or two
+// coordinates; every other frame is sorted into the level-1 row list, one row
+// per sub-term. wfg_rows_kernel(l) takes the rows of level l: row j of a frame
+// gives the sub-term |(f_j[d-1] - r_{d-1}) * (vol_{d-1}(f_j) - hv(limit set
+// of f_j over the rows after it))|; the row's own frame (that limit set) goes
+// to level l + 1 the same way while levels remain, else the recursion below it
+// runs on the warp's own stack. wfg_join_kernel(l) adds each row's sub-terms
+// of level l + 1 in order (compute_hv's H += ..., hv_hvwfg.cpp:262-266) and
+// finishes the row, and wfg_items_kernel finishes the items from level 1. The
+// operations and their order are those of one recursion, split between warps.
+constexpr int kMaxLevels = 4;
+
+struct wfg_level {
+    okey *frames;                  // the frames of this level's rows, rows of d keys
+    uint32_t *row_parent;          // per row: its item (level 1) or its row of the level above
+    double *row_term;              // per row: its sub-term
+    uint32_t *frame_k;             // per parent: rows of its frame here (0: none)
+    unsigned long long *frame_off; // per parent: its first row here
+    unsigned long long *rows_used; // rows handed out (zero at launch)
+    uint64_t row_cap;
+    uint64_t parents;              // entries of frame_k / frame_off
+};
+
 struct wfg_args {
     const okey *pts;    // n rows of m keys; sorted by cmp_points for the terms of a volume
     uint32_t n, m;
@@ -378,16 +393,51 @@ struct wfg_args {
     double *out;        // n
     okey *pool;         // per warp: m buffers of bd keys
     uint64_t bd;
-    unsigned *next;     // work counters (zero at launch): [0] items, [2] rows
+    unsigned *next;     // work counters (zero at launch): [0] items, [2 + l] rows of level l
     unsigned *status;   // set when a warp's pool ran dry
-    unsigned long long *rows_used; // frame rows handed out (zero at launch)
-    uint64_t row_cap;   // rows of the frame list
-    okey *frames;       // the sorted frames, rows of dc keys
-    uint32_t *row_item; // the item of each row
-    double *row_term;   // the sub-term of each row
-    uint32_t *frame_k;  // per item: rows of its frame in the list (0: the item is finished)
-    unsigned long long *frame_off; // per item: its first row
+    int levels;         // row levels in use, 1 .. kMaxLevels
+    wfg_level lv[kMaxLevels + 2]; // lv[1 .. levels]; lv[levels + 1] unused
 };
+
+__device__ __forceinline__ uint32_t first_dims(const wfg_args &a)
+{
+    return a.contributions ? a.m : a.m - 1u; // coordinates of the items' frames
+}
+
+// Row g of level l when it belongs to a frame stored at that level: its frame's
+// rows k, first row off and index j; false for rows of a frame past the
+// list's end (never written: any values).
+__device__ __forceinline__ bool row_of(const wfg_args &a, int l, unsigned long long g, uint32_t *k,
+                                       unsigned long long *off)
+{
+    const wfg_level &L = a.lv[l];
+    const uint32_t parent = L.row_parent[g];
+    if (parent >= L.parents) return false;
+    *k = L.frame_k[parent];
+    *off = L.frame_off[parent];
+    return *k != 0u && g >= *off && g < *off + *k && *off + *k <= L.row_cap;
+}
+
+// The frame `buf` (k points of d coordinates, k > 2, d > 2) into level l's
+// list, one row per point, sorted; the parent's entries set. Returns false
+// when the list is full (the caller recurses instead).
+template <int DM>
+__device__ bool store_frame(const wfg_args &a, int l, uint64_t parent, const okey *buf, uint32_t k, uint32_t d,
+                            unsigned lane)
+{
+    const wfg_level &L = a.lv[l];
+    unsigned long long row0 = 0;
+    if (lane == 0) row0 = atomicAdd(L.rows_used, static_cast<unsigned long long>(k));
+    row0 = __shfl_sync(kMask, row0, 0);
+    if (row0 + k > L.row_cap) return false;
+    sort_rows<DM>(buf, k, d, false, L.frames + row0 * d, lane);
+    for (uint32_t t = lane; t < k; t += 32u) L.row_parent[row0 + t] = static_cast<uint32_t>(parent);
+    if (lane == 0) {
+        L.frame_k[parent] = k;
+        L.frame_off[parent] = row0;
+    }
+    return true;
+}
 
 __device__ __forceinline__ void mark_failed(const wfg_args &a, uint32_t item, unsigned lane)
 {
@@ -406,7 +456,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) wfg_top_kernel(wfg_args a
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t gw = static_cast<uint64_t>(blockIdx.x) * kWarpsPerBlock + (threadIdx.x >> 5);
     const uint32_t m = a.m;
-    const uint32_t dc = a.contributions ? m : m - 1u; // coordinates of the first frame
+    const uint32_t dc = first_dims(a);
     frame_pool pool{a.pool + gw * m * a.bd, a.bd, (1u << m) - 1u};
     for (;;) {
         unsigned item = 0;
@@ -426,38 +476,28 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) wfg_top_kernel(wfg_args a
             ex = __dsub_rn(ex, closed_form<DM>(s_r, pool.at(b0), k0, dc, tb >= 0 ? pool.at(tb) : nullptr, lane));
             if (tb >= 0) pool.give(tb);
             pool.give(b0);
+        } else if (store_frame<DM>(a, 1, item, pool.at(b0), k0, dc, lane)) {
+            pool.give(b0);
+            continue;
         } else {
-            unsigned long long row0 = 0;
-            if (lane == 0) row0 = atomicAdd(a.rows_used, static_cast<unsigned long long>(k0));
-            row0 = __shfl_sync(kMask, row0, 0);
-            if (row0 + k0 <= a.row_cap) {
-                sort_rows<DM>(pool.at(b0), k0, dc, false, a.frames + row0 * dc, lane);
-                for (uint32_t t = lane; t < k0; t += 32u) a.row_item[row0 + t] = item;
-                if (lane == 0) {
-                    a.frame_k[item] = k0;
-                    a.frame_off[item] = row0;
-                }
-                pool.give(b0);
-                continue;
-            }
-            // the frame list is full: this warp finishes the item alone
+            // the level-1 list is full: this warp finishes the item alone
             ex = __dsub_rn(ex, frame_hv<DM>(s_r, pool, b0, k0, dc, lane, &fail));
         }
         if (fail) {
             mark_failed(a, item, lane);
-            if (lane == 0) a.frame_k[item] = 0;
+            if (lane == 0) a.lv[1].frame_k[item] = 0;
             pool.free = (1u << m) - 1u;
             continue;
         }
         if (lane == 0) {
-            a.frame_k[item] = 0;
+            a.lv[1].frame_k[item] = 0;
             a.out[item] = a.contributions ? ex : slice_term(s_r, p, m, ex);
         }
     }
 }
 
 template <int DM>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) wfg_sub_kernel(wfg_args a, wfg_ref ref)
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) wfg_rows_kernel(wfg_args a, wfg_ref ref, int l)
 {
     __shared__ double s_r[DM];
     if (threadIdx.x < DM) s_r[threadIdx.x] = threadIdx.x < a.m ? ref.r[threadIdx.x] : 0.0;
@@ -465,56 +505,89 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) wfg_sub_kernel(wfg_args a
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t gw = static_cast<uint64_t>(blockIdx.x) * kWarpsPerBlock + (threadIdx.x >> 5);
     const uint32_t m = a.m;
-    const uint32_t dc = a.contributions ? m : m - 1u;
-    const unsigned long long used = *a.rows_used;
-    const unsigned long long rows = used < a.row_cap ? used : a.row_cap;
+    const uint32_t d = first_dims(a) - static_cast<uint32_t>(l - 1); // coordinates of this level's rows
+    const wfg_level &L = a.lv[l];
+    const unsigned long long used = *L.rows_used;
+    const unsigned long long rows = used < L.row_cap ? used : L.row_cap;
+    const bool deeper = l < a.levels; // a level below for the rows' own frames
     frame_pool pool{a.pool + gw * m * a.bd, a.bd, (1u << m) - 1u};
     for (;;) {
         unsigned g = 0;
-        if (lane == 0) g = atomicAdd(a.next + 2, 1u);
+        if (lane == 0) g = atomicAdd(a.next + 2 + l, 1u);
         g = __shfl_sync(kMask, g, 0);
         if (g >= rows) break;
-        const uint32_t item = a.row_item[g]; // unwritten (any value) for rows of a frame past the list's end
-        if (item >= a.n) continue;
-        const uint32_t k0 = a.frame_k[item];
-        const unsigned long long off = a.frame_off[item];
-        if (k0 == 0u || g < off || g >= off + k0) continue; // rows of a frame past the list's end
+        uint32_t k = 0;
+        unsigned long long off = 0;
+        if (!row_of(a, l, g, &k, &off)) continue;
         const uint32_t j = static_cast<uint32_t>(g - off);
-        const okey *f = a.frames + off * dc;
-        const okey *p = f + static_cast<uint64_t>(j) * dc;
+        const okey *f = L.frames + off * d;
+        const okey *p = f + static_cast<uint64_t>(j) * d;
         const int cb = pool.take();
-        const uint32_t ck = limit_set<DM>(f, dc, j + 1u, k0, k0, p, dc - 1u, pool.at(cb), lane);
-        double ex = vol(s_r, p, dc - 1u);
+        const uint32_t ck = limit_set<DM>(f, d, j + 1u, k, k, p, d - 1u, pool.at(cb), lane);
+        double ex = vol(s_r, p, d - 1u);
         bool fail = false;
         if (ck == 0u) {
             pool.give(cb);
+        } else if (ck <= 2u || d - 1u == 2u) {
+            const int tb = ck > 2u ? pool.take() : -1;
+            ex = __dsub_rn(ex, closed_form<DM>(s_r, pool.at(cb), ck, d - 1u, tb >= 0 ? pool.at(tb) : nullptr, lane));
+            if (tb >= 0) pool.give(tb);
+            pool.give(cb);
+        } else if (deeper && store_frame<DM>(a, l + 1, g, pool.at(cb), ck, d - 1u, lane)) {
+            pool.give(cb);
+            continue; // wfg_join_kernel(l) finishes the row
         } else {
-            ex = __dsub_rn(ex, frame_hv<DM>(s_r, pool, cb, ck, dc - 1u, lane, &fail));
+            ex = __dsub_rn(ex, frame_hv<DM>(s_r, pool, cb, ck, d - 1u, lane, &fail));
         }
         if (fail) {
             if (lane == 0) {
                 atomicOr(a.status, 1u);
-                a.row_term[g] = __longlong_as_double(0x7ff8000000000000LL);
+                L.row_term[g] = __longlong_as_double(0x7ff8000000000000LL);
             }
             pool.free = (1u << m) - 1u;
-            continue;
+        } else if (lane == 0) {
+            L.row_term[g] = slice_term(s_r, p, d, ex);
         }
-        if (lane == 0) a.row_term[g] = slice_term(s_r, p, dc, ex);
+        if (lane == 0 && deeper) a.lv[l + 1].frame_k[g] = 0;
     }
 }
 
-// The items with a frame in the list: H = the sum of their rows' sub-terms in
+// The rows of level l whose frame went to level l + 1: H = the sum of that
+// frame's sub-terms in order from 0.0, then the row's sub-term.
+__global__ void wfg_join_kernel(wfg_args a, wfg_ref ref, int l)
+{
+    const uint32_t d = first_dims(a) - static_cast<uint32_t>(l - 1);
+    const wfg_level &L = a.lv[l], &C = a.lv[l + 1];
+    const unsigned long long used = *L.rows_used;
+    const unsigned long long rows = used < L.row_cap ? used : L.row_cap;
+    for (unsigned long long g = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; g < rows;
+         g += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+        uint32_t k = 0;
+        unsigned long long off = 0;
+        if (!row_of(a, l, g, &k, &off)) continue;
+        const uint32_t ck = C.frame_k[g];
+        const unsigned long long coff = C.frame_off[g];
+        if (ck == 0u || coff + ck > C.row_cap) continue;
+        double h = 0.0;
+        for (uint32_t t = 0; t < ck; ++t) h = __dadd_rn(h, C.row_term[coff + t]);
+        const okey *p = L.frames + (off + (g - off)) * d;
+        L.row_term[g] = slice_term(ref.r, p, d, __dsub_rn(vol(ref.r, p, d - 1u), h));
+    }
+}
+
+// The items with a frame at level 1: H = the sum of their rows' sub-terms in
 // order from 0.0, then the item's value as wfg_top_kernel would give it.
-__global__ void wfg_join_kernel(wfg_args a, wfg_ref ref)
+__global__ void wfg_items_kernel(wfg_args a, wfg_ref ref)
 {
     const uint32_t m = a.m;
-    const uint32_t dc = a.contributions ? m : m - 1u;
+    const uint32_t dc = first_dims(a);
+    const wfg_level &L = a.lv[1];
     for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < a.n; item += gridDim.x * blockDim.x) {
-        const uint32_t k0 = a.frame_k[item];
+        const uint32_t k0 = L.frame_k[item];
         if (k0 == 0u) continue;
-        const unsigned long long off = a.frame_off[item];
+        const unsigned long long off = L.frame_off[item];
         double h = 0.0;
-        for (uint32_t j = 0; j < k0; ++j) h = __dadd_rn(h, a.row_term[off + j]);
+        for (uint32_t j = 0; j < k0; ++j) h = __dadd_rn(h, L.row_term[off + j]);
         const okey *p = a.pts + static_cast<uint64_t>(item) * m;
         const double ex = __dsub_rn(vol(ref.r, p, dc), h);
         a.out[item] = a.contributions ? ex : slice_term(ref.r, p, m, ex);
@@ -642,12 +715,12 @@ size_t round256(size_t b)
 }
 
 // Scratch of the split kernels over n points of m coordinates: [counters,
-// status | per item: frame rows, first row | per row: item, sub-term, dc keys
-// | pool]; the frame list holds up to kRowCap rows (past it, a frame is
-// finished by the warp that built it), the number of warps fits the pool in
-// kPoolBytes (at least one warp).
+// status, rows handed out | per level: per parent frame rows and first row,
+// per row parent, sub-term and d keys | pool]; each level's list holds up to
+// row_cap rows (past it a frame is finished by the warp that built it), the
+// number of warps fits the pool in kPoolBytes (at least one warp).
 constexpr size_t kPoolBytes = size_t(1) << 30;
-constexpr uint64_t kRowCap = uint64_t(1) << 22;
+constexpr uint64_t kRowCap = uint64_t(1) << 20;
 
 int run_warps(pgx_context *ctx, const okey *d_keys, uint32_t n, uint32_t m, const wfg_ref &ref, int contributions,
               double *d_out, cudaStream_t s)
@@ -658,20 +731,31 @@ int run_warps(pgx_context *ctx, const okey *d_keys, uint32_t n, uint32_t m, cons
               "hypervolume (WFG): " + std::to_string(n) + " points of " + std::to_string(m) +
                   " objectives need more than 4 GiB of frames per warp");
     const uint32_t dc = contributions ? m : m - 1u;
-    const uint64_t row_cap = std::max<uint64_t>(1u, std::min<uint64_t>(static_cast<uint64_t>(n) * (n - 1u) / 2u + n,
-                                                                        kRowCap));
+    // levels 1 .. dc - 2 hold rows of dc .. 3 coordinates (a row of 3 has a frame of 2: closed form)
+    const int levels = static_cast<int>(std::min<uint32_t>(kMaxLevels, dc > 3u ? dc - 2u : 1u));
+    const uint64_t row_cap = std::max<uint64_t>(64u, std::min<uint64_t>(static_cast<uint64_t>(n) * n, kRowCap));
     const uint64_t want = std::min<uint64_t>(std::max<uint64_t>(n, 1024u), static_cast<uint64_t>(ctx->num_sms) * 16u);
     const uint64_t fit = std::max<uint64_t>(1u, kPoolBytes / per_warp);
     uint64_t warps = std::min(want, fit);
     const unsigned blocks = static_cast<unsigned>((warps + kWarpsPerBlock - 1u) / kWarpsPerBlock);
     warps = static_cast<uint64_t>(blocks) * kWarpsPerBlock; // every warp of the grid has its slice
     const size_t b_ctl = 256u;
-    const size_t b_k = round256(static_cast<size_t>(n) * sizeof(uint32_t));
-    const size_t b_off = round256(static_cast<size_t>(n) * sizeof(unsigned long long));
-    const size_t b_ri = round256(row_cap * sizeof(uint32_t));
-    const size_t b_rt = round256(row_cap * sizeof(double));
-    const size_t b_fr = round256(row_cap * dc * sizeof(okey));
-    const size_t head = b_ctl + b_k + b_off + b_ri + b_rt + b_fr;
+    size_t head = b_ctl;
+    size_t lv_off[kMaxLevels + 2][5] = {};
+    for (int l = 1; l <= levels; ++l) {
+        const uint64_t parents = l == 1 ? n : row_cap;
+        const uint32_t d = dc - static_cast<uint32_t>(l - 1);
+        lv_off[l][0] = head; // frame_k
+        head += round256(parents * sizeof(uint32_t));
+        lv_off[l][1] = head; // frame_off
+        head += round256(parents * sizeof(unsigned long long));
+        lv_off[l][2] = head; // row_parent
+        head += round256(row_cap * sizeof(uint32_t));
+        lv_off[l][3] = head; // row_term
+        head += round256(row_cap * sizeof(double));
+        lv_off[l][4] = head; // frames
+        head += round256(row_cap * d * sizeof(okey));
+    }
     PGX_TRY(ctx->h_wfg.ensure(head + warps * per_warp));
     char *base = ctx->h_wfg.as<char>();
     unsigned *ctl = reinterpret_cast<unsigned *>(base);
@@ -686,28 +770,46 @@ int run_warps(pgx_context *ctx, const okey *d_keys, uint32_t n, uint32_t m, cons
     a.bd = bd;
     a.next = ctl;
     a.status = ctl + 1;
-    a.rows_used = reinterpret_cast<unsigned long long *>(ctl + 4);
-    a.row_cap = row_cap;
-    a.frame_k = reinterpret_cast<uint32_t *>(base + b_ctl);
-    a.frame_off = reinterpret_cast<unsigned long long *>(base + b_ctl + b_k);
-    a.row_item = reinterpret_cast<uint32_t *>(base + b_ctl + b_k + b_off);
-    a.row_term = reinterpret_cast<double *>(base + b_ctl + b_k + b_off + b_ri);
-    a.frames = reinterpret_cast<okey *>(base + b_ctl + b_k + b_off + b_ri + b_rt);
-    const int threads = kWarpsPerBlock * 32;
-    if (m <= 4u) {
-        wfg_top_kernel<4><<<blocks, threads, 0, s>>>(a, ref);
-        wfg_sub_kernel<4><<<blocks, threads, 0, s>>>(a, ref);
-    } else if (m <= 8u) {
-        wfg_top_kernel<8><<<blocks, threads, 0, s>>>(a, ref);
-        wfg_sub_kernel<8><<<blocks, threads, 0, s>>>(a, ref);
-    } else {
-        wfg_top_kernel<16><<<blocks, threads, 0, s>>>(a, ref);
-        wfg_sub_kernel<16><<<blocks, threads, 0, s>>>(a, ref);
+    a.levels = levels;
+    for (int l = 1; l <= levels; ++l) {
+        wfg_level &L = a.lv[l];
+        L.frame_k = reinterpret_cast<uint32_t *>(base + lv_off[l][0]);
+        L.frame_off = reinterpret_cast<unsigned long long *>(base + lv_off[l][1]);
+        L.row_parent = reinterpret_cast<uint32_t *>(base + lv_off[l][2]);
+        L.row_term = reinterpret_cast<double *>(base + lv_off[l][3]);
+        L.frames = reinterpret_cast<okey *>(base + lv_off[l][4]);
+        L.rows_used = reinterpret_cast<unsigned long long *>(base + 64u + 8u * static_cast<size_t>(l));
+        L.row_cap = row_cap;
+        L.parents = l == 1 ? n : row_cap;
     }
+    const int threads = kWarpsPerBlock * 32;
+    auto launch_rows = [&](int l) {
+        if (m <= 4u)
+            wfg_rows_kernel<4><<<blocks, threads, 0, s>>>(a, ref, l);
+        else if (m <= 8u)
+            wfg_rows_kernel<8><<<blocks, threads, 0, s>>>(a, ref, l);
+        else
+            wfg_rows_kernel<16><<<blocks, threads, 0, s>>>(a, ref, l);
+    };
+    if (m <= 4u)
+        wfg_top_kernel<4><<<blocks, threads, 0, s>>>(a, ref);
+    else if (m <= 8u)
+        wfg_top_kernel<8><<<blocks, threads, 0, s>>>(a, ref);
+    else
+        wfg_top_kernel<16><<<blocks, threads, 0, s>>>(a, ref);
     PGX_CUDA(cudaGetLastError());
-    wfg_join_kernel<<<(n + 127u) / 128u, 128, 0, s>>>(a, ref);
+    for (int l = 1; l <= levels; ++l) {
+        launch_rows(l);
+        PGX_CUDA(cudaGetLastError());
+    }
+    const unsigned jb = static_cast<unsigned>(std::min<uint64_t>((row_cap + 127u) / 128u, 4096u));
+    for (int l = levels - 1; l >= 1; --l) {
+        wfg_join_kernel<<<jb, 128, 0, s>>>(a, ref, l);
+        PGX_CUDA(cudaGetLastError());
+    }
+    wfg_items_kernel<<<(n + 127u) / 128u, 128, 0, s>>>(a, ref);
     PGX_CUDA(cudaGetLastError());
-    ctx->launches += 3;
+    ctx->launches += 2u + 2u * static_cast<uint64_t>(levels);
     return PGX_OK;
 }
 
