@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(256) dominance_sym_packed_kernel(const uint32_
                                                                    const uint32_t *__restrict__ pb, uint32_t n,
                                                                    uint32_t W8, uint32_t *__restrict__ Dt)
 {
-    __shared__ uint32_t ja[32], jb[32];
+    __shared__ uint4 jw[32]; // per candidate j: its words a, b and a | guard, b | guard
     __shared__ uint32_t tile[32][9];
     const uint32_t bj = blockIdx.y;
     const uint32_t bi0 = blockIdx.x * 8u;
@@ -238,8 +238,8 @@ __global__ void __launch_bounds__(256) dominance_sym_packed_kernel(const uint32_
     const uint32_t J0 = bj * 32u;
     if (threadIdx.x < 32u) {
         const uint32_t j = J0 + threadIdx.x;
-        ja[threadIdx.x] = j < n ? pa[j] : 0u;
-        jb[threadIdx.x] = j < n && NW == 2 ? pb[j] : 0u;
+        const uint32_t a = j < n ? pa[j] : 0u, b = j < n && NW == 2 ? pb[j] : 0u;
+        jw[threadIdx.x] = make_uint4(a, b, a | kRankGuard, b | kRankGuard);
     }
     __syncthreads();
     const uint32_t bi = bi0 + warp;
@@ -248,21 +248,23 @@ __global__ void __launch_bounds__(256) dominance_sym_packed_kernel(const uint32_
     const bool iv = active && i < n;
     const uint32_t ia = iv ? pa[i] : 0u, ib = iv && NW == 2 ? pb[i] : 0u;
     const uint32_t iag = ia | kRankGuard, ibg = ib | kRankGuard;
+    const uint32_t jn = n - J0 < 32u ? n - J0 : 32u; // candidates of this tile
     uint32_t row_i = 0u;
     if (active) {
         for (unsigned jj = 0; jj < 32u; ++jj) {
-            const uint32_t a = ja[jj], b = jb[jj];
-            uint32_t le_ij = (a | kRankGuard) - ia; // i no worse than j in the fields of word a
-            uint32_t le_ji = iag - a;               // j no worse than i
-            bool ne = ia != a;
+            const uint4 w = jw[jj];
+            // no borrow into a guard bit: every field of the first word no smaller
+            uint32_t c_ij = w.z - ia; // i no worse than j in every field
+            uint32_t c_ji = iag - w.x; // j no worse than i
             if (NW == 2) {
-                le_ij &= (b | kRankGuard) - ib;
-                le_ji &= ibg - b;
-                ne |= ib != b;
+                c_ij &= w.w - ib;
+                c_ji &= ibg - w.y;
             }
-            const bool valid = iv && J0 + jj < n && ne;
-            const bool i_dom_j = valid && (le_ij & kRankGuard) == kRankGuard;
-            const bool j_dom_i = valid && (le_ji & kRankGuard) == kRankGuard;
+            const bool le_ij = (c_ij & kRankGuard) == kRankGuard, le_ji = (c_ji & kRankGuard) == kRankGuard;
+            // both ways no worse: every field equal, neither dominates
+            const bool valid = iv && jj < jn;
+            const bool i_dom_j = valid && le_ij && !le_ji;
+            const bool j_dom_i = valid && le_ji && !le_ij;
             const unsigned word = __ballot_sync(kFull, i_dom_j);
             if (lane == 0) tile[jj][warp] = word;
             row_i |= static_cast<uint32_t>(j_dom_i) << jj;
