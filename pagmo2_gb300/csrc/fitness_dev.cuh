@@ -252,40 +252,17 @@ __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uin
     rastrigin_part acc[J];
 #pragma unroll
     for (int j = 0; j < J; ++j) acc[j] = rastrigin_part{isum::make(), 0.0};
-    if constexpr (G == V) {
-        // a short batch (every lane of the row's width): the lane's elements
-        // e = 0, 1, ... (element e V + sub) with their loads kPrefetch ahead,
-        // so a row waits for memory about once
-        constexpr int kPrefetch = 8;
-        double buf[kPrefetch];
+    // chunks of V elements; the next element's load is issued before this
+    // one's arithmetic
+    double xn = sub < nx ? __ldg(xr + sub) : 0.0;
+    for (uint32_t base = 0; base < nx; base += V) {
 #pragma unroll
-        for (int u = 0; u < kPrefetch; ++u) {
-            const uint32_t i = static_cast<uint32_t>(u) * V + sub;
-            buf[u] = i < nx ? __ldg(xr + i) : 0.0;
-        }
-        for (uint32_t e0 = 0; e0 * V < nx; e0 += kPrefetch) {
-#pragma unroll
-            for (int u = 0; u < kPrefetch; ++u) {
-                const uint32_t i = (e0 + static_cast<uint32_t>(u)) * V + sub;
-                const double xi = buf[u];
-                const uint32_t inx = i + kPrefetch * V;
-                buf[u] = inx < nx ? __ldg(xr + inx) : 0.0;
-                if (i < nx) rastrigin_element<GRAD>(xi, acc[0].sx, acc[0].sc, GRAD ? gr + i : nullptr);
-            }
-        }
-    } else {
-        // chunks of V elements; the next element's load is issued before this
-        // one's arithmetic
-        double xn = sub < nx ? __ldg(xr + sub) : 0.0;
-        for (uint32_t base = 0; base < nx; base += V) {
-#pragma unroll
-            for (int j = 0; j < J; ++j) {
-                const uint32_t i = base + sub + static_cast<uint32_t>(G * j);
-                const double xi = xn;
-                const uint32_t inext = j + 1 < J ? i + G : base + V + sub;
-                if (inext < nx) xn = __ldg(xr + inext);
-                if (i < nx) rastrigin_element<GRAD>(xi, acc[j].sx, acc[j].sc, GRAD ? gr + i : nullptr);
-            }
+        for (int j = 0; j < J; ++j) {
+            const uint32_t i = base + sub + static_cast<uint32_t>(G * j);
+            const double xi = xn;
+            const uint32_t inext = j + 1 < J ? i + G : base + V + sub;
+            if (inext < nx) xn = __ldg(xr + inext);
+            if (i < nx) rastrigin_element<GRAD>(xi, acc[j].sx, acc[j].sc, GRAD ? gr + i : nullptr);
         }
     }
     uint32_t flags = 0u;
