@@ -10,6 +10,8 @@
 #ifndef PAGMO_GB300_MULTI_OBJECTIVE_HPP
 #define PAGMO_GB300_MULTI_OBJECTIVE_HPP
 
+#include <algorithm>
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <stdexcept>
@@ -17,6 +19,7 @@
 #include <tuple>
 #include <vector>
 
+#include <pagmo/population.hpp>
 #include <pagmo/types.hpp>
 #include <pagmo/utils/multi_objective.hpp>
 
@@ -234,6 +237,111 @@ inline unsigned long long hypervolume_greatest_contributor(const std::vector<pag
                                               ref.data(), 1, &idx));
     return idx;
 }
+
+// pagmo::hypervolume's interface (include/pagmo/utils/hypervolume.hpp:63-200)
+// with every query on the GPU: the constructors' checks and messages
+// (src/utils/hypervolume.cpp:46-80, 406-432), refpoint, get_points, compute,
+// exclusive, contributions, least_contributor, greatest_contributor. The
+// algorithm overloads (taking an hv_algorithm) are not provided: the GPU picks
+// hv2d / hv3d / hvwfg as the reference's get_best_* do. The queries always
+// check the reference point, whatever the verify flag; copy_points has no
+// effect (the points are always copied to the device).
+class hypervolume
+{
+public:
+    hypervolume() = default;
+    explicit hypervolume(const std::vector<pagmo::vector_double> &points, bool verify = true)
+        : m_points(points), m_verify(verify)
+    {
+        if (m_verify) verify_after_construct();
+    }
+    explicit hypervolume(const pagmo::population &pop, bool verify = false) : m_verify(verify)
+    {
+        if (pop.get_problem().get_nc() > 0u)
+            throw std::invalid_argument("The problem of the population is not unconstrained."
+                                        "Only unconstrained populations can be used to construct hypervolume objects.");
+        if (pop.get_problem().get_nobj() < 2u)
+            throw std::invalid_argument("The problem of the population is not multiobjective."
+                                        "Only multi-objective populations can be used to construct hypervolume "
+                                        "objects.");
+        m_points = pop.get_f();
+        if (m_verify) verify_after_construct();
+    }
+    void set_copy_points(bool c)
+    {
+        m_copy_points = c;
+    }
+    bool get_copy_points() const
+    {
+        return m_copy_points;
+    }
+    void set_verify(bool v)
+    {
+        m_verify = v;
+    }
+    bool get_verify() const
+    {
+        return m_verify;
+    }
+    pagmo::vector_double refpoint(double offset = 0.0) const
+    {
+        if (m_points.empty()) return {};
+        pagmo::vector_double r(m_points[0]);
+        for (std::size_t k = 0; k < r.size(); ++k)
+            for (std::size_t i = 1; i < m_points.size(); ++i) r[k] = std::max(r[k], m_points[i][k]);
+        for (auto &c : r) c += offset;
+        return r;
+    }
+    const std::vector<pagmo::vector_double> &get_points() const
+    {
+        return m_points;
+    }
+    double compute(const pagmo::vector_double &r) const
+    {
+        return hypervolume_compute(m_points, r, m_device);
+    }
+    double exclusive(unsigned p_idx, const pagmo::vector_double &r) const
+    {
+        return hypervolume_exclusive(m_points, p_idx, r, m_device);
+    }
+    std::vector<double> contributions(const pagmo::vector_double &r) const
+    {
+        return hypervolume_contributions(m_points, r, m_device);
+    }
+    unsigned long long least_contributor(const pagmo::vector_double &r) const
+    {
+        return hypervolume_least_contributor(m_points, r, m_device);
+    }
+    unsigned long long greatest_contributor(const pagmo::vector_double &r) const
+    {
+        return hypervolume_greatest_contributor(m_points, r, m_device);
+    }
+    // the GPU the queries run on (default 0)
+    void set_device(int device)
+    {
+        m_device = device;
+    }
+
+private:
+    void verify_after_construct() const
+    {
+        if (m_points.empty()) throw std::invalid_argument("Point set cannot be empty.");
+        const auto m = m_points[0].size();
+        if (m <= 1u) throw std::invalid_argument("Points of dimension > 1 required.");
+        for (const auto &p : m_points)
+            if (p.size() != m) throw std::invalid_argument("All point set dimensions must be equal.");
+        for (const auto &p : m_points)
+            for (double v : p)
+                if (std::isnan(v))
+                    throw std::invalid_argument("A nan value has been encountered in the hypervolume points. Cannot "
+                                                "construct the hypervolume object");
+    }
+
+    std::vector<pagmo::vector_double> m_points;
+    bool m_copy_points = true;
+    bool m_verify = false;
+    int m_device = 0;
+};
 
 } // namespace pagmo_gb300
 

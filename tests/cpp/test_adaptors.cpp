@@ -302,8 +302,30 @@ int main()
             CHECK(hypervolume_greatest_contributor(pts, r) == h.greatest_contributor(r));
             CHECK(throws_with<std::invalid_argument>([&] { hypervolume_exclusive(pts, 40u, r); },
                                                      "Index of the individual is out of bounds."));
+            // the class mirror, from points and from a population
+            pagmo_gb300::hypervolume hg(pts);
+            CHECK(hg.compute(r) == h.compute(r) && hg.contributions(r) == h.contributions(r));
+            CHECK(hg.least_contributor(r) == h.least_contributor(r) && hg.refpoint(0.5) == h.refpoint(0.5));
+            pagmo::population zp{pagmo::problem{pagmo::zdt{1u, 10u}}, 30u, 7u};
+            const pagmo_gb300::hypervolume hz(zp);
+            const pagmo::hypervolume hzr(zp);
+            CHECK(hz.compute(hzr.refpoint(1.0)) == hzr.compute(hzr.refpoint(1.0))
+                  || std::abs(hz.compute(hzr.refpoint(1.0)) - hzr.compute(hzr.refpoint(1.0)))
+                         <= 1e-13 * hzr.compute(hzr.refpoint(1.0)));
         }
     }
+    // the hypervolume class mirror's construction checks (no GPU needed)
+    CHECK(throws_with<std::invalid_argument>([] { pagmo_gb300::hypervolume h{std::vector<pagmo::vector_double>{}}; },
+                                             "Point set cannot be empty."));
+    CHECK(throws_with<std::invalid_argument>(
+        [] { pagmo_gb300::hypervolume h{std::vector<pagmo::vector_double>{{1.0, 2.0}, {1.0}}}; },
+        "All point set dimensions must be equal."));
+    CHECK(throws_with<std::invalid_argument>(
+        [] {
+            pagmo::population p{pagmo::problem{pagmo::rosenbrock{3u}}, 4u, 1u};
+            pagmo_gb300::hypervolume h{p};
+        },
+        "not multiobjective"));
     // gpu_mbh refuses problems it cannot refine (no CPU fallback) and bad perturbations
     CHECK(throws_with<std::invalid_argument>([] { gpu_mbh{10u, 5u, 20u, 0.0}; }, "The perturbation must be in ]0,1]"));
     CHECK(throws_with<std::invalid_argument>(
