@@ -20,24 +20,24 @@
 //
 // GPU layout: one warp per top-level term (compute) or per point
 // (contributions), taken from a work counter in index order (the early terms
-// of the sorted set have the most candidates). The warp's lanes share the
-// limit-set filter (32 candidates at a time against the kept set, then
+// of the sorted set have the most candidates); the frames of the first levels
+// are split into one work item per sub-term, level by level (see wfg_level),
+// and the deepest level recurses on an explicit stack, its frames in the
+// warp's slice of a scratch pool (m buffers of n rows). A warp's lanes share
+// the limit-set filter (32 candidates at a time against the kept set, then
 // against each other, then the kept points the survivors cover are removed),
-// the counting-rank sorts of a frame and the closed forms; the recursion
-// below the top level runs on an explicit stack, its frames in the warp's
-// slice of a scratch pool (m buffers of n rows); the frames of the first
-// levels are split into one work item per sub-term (see wfg_args). Every comparison (limit
-// sets, sorts, maxima) runs on 64-bit integer order keys of the coordinates
-// (the IEEE bit pattern with negatives mirrored, -0.0 read as +0.0, which the
-// reference compares equal): the frames hold keys, and only the volumes and
-// terms turn them back into doubles (GB300's FP64 pipe is far too narrow for
-// the comparisons). A frame's kept set is the unique non-dominated subset of
-// its candidates whatever order they are filtered in, every frame of more than
-// two points is sorted by a strict order before it is used, and the two-point
-// form is symmetric, so the arithmetic is the reference's: every operation is
-// the reference's IEEE double operation in the reference's order (explicit
-// round-to-nearest intrinsics: no contraction into FMA), and the volumes and
-// contributions equal the reference's bit for bit.
+// the counting-rank sorts of a frame and the closed forms. Every comparison
+// (limit sets, sorts, maxima) runs on 64-bit integer order keys of the
+// coordinates (the IEEE bit pattern with negatives mirrored, -0.0 read as
+// +0.0, which the reference compares equal): the frames hold keys, and only
+// the volumes and terms turn them back into doubles (GB300's FP64 pipe is far
+// too narrow for the comparisons). A frame's kept set is the unique
+// non-dominated subset of its candidates whatever order they are filtered in,
+// every frame of more than two points is sorted by a strict order before it is
+// used, and the two-point form is symmetric, so the arithmetic is the
+// reference's: every operation is the reference's IEEE double operation in the
+// reference's order (explicit round-to-nearest intrinsics: no contraction into
+// FMA), and the volumes and contributions equal the reference's bit for bit.
 #include "pgx_internal.cuh"
 
 #include <algorithm>
