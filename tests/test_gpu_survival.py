@@ -97,6 +97,45 @@ def test_config4_nested_fronts_full(ctx, orc):
     check_crowding(cd, orc.nsga2_crowding(p, want["front_offsets"], want["front_indices"]))
 
 
+def layered_points(sizes, m, seed, dup_frac=0.02):
+    """Fronts of exactly the given sizes: layer k lies on the plane where the objectives sum to 2 k, with
+    non-negative offsets summing to at most 1 and the corner (0, ..., 0, 2 k), which dominates every point of
+    layer k + 1; a layer's points are mutually non-dominated, and about dup_frac of them are copies of others of
+    the same layer. The rows are shuffled."""
+    rs = np.random.RandomState(seed)
+    rows = []
+    for k, sz in enumerate(sizes):
+        e = -np.log(1.0 - rs.random_sample((sz, m)))
+        pts = e / e.sum(axis=1, keepdims=True) * rs.random_sample((sz, 1))  # offsets: sum <= 1
+        pts[:, -1] = 2.0 * k - pts[:, :-1].sum(axis=1)
+        pts[0, :-1], pts[0, -1] = 0.0, 2.0 * k
+        nd = int(sz * dup_frac)
+        if nd and sz > 1:
+            pts[sz - nd:] = pts[rs.randint(0, sz - nd, nd)]
+        rows.append(pts)
+    p = np.concatenate(rows)
+    return np.ascontiguousarray(p[rs.permutation(len(p))])
+
+
+@pytest.mark.parametrize("sizes,m", [
+    # up to 32768 points: fronts of up to 2048 members (and keys) sorted while the next front is scanned, larger
+    # ones across the grid, a small front after a large one, single points
+    ([3000, 40, 2049, 2048, 700, 5000, 10, 1, 2100, 300, 1, 1, 2047], 3),
+    # beyond 32768 points (no per-point maps in shared memory)
+    ([6000, 100, 2048, 2049, 5000, 30, 9000, 7000, 1, 4500, 3000, 200], 2),
+])
+def test_front_size_transitions(ctx, orc, sizes, m):
+    p = layered_points(sizes, m, seed=len(sizes) + m)
+    rank, dc, off, idx, cd = MO.nsga2_survival(p, ctx)
+    want = orc.fnds(p, dom_list=False)
+    assert np.array_equal(rank, want["rank"])
+    assert np.array_equal(dc, want["dom_count"])
+    assert np.array_equal(off, want["front_offsets"])
+    assert np.array_equal(idx, want["front_indices"])
+    assert len(off) - 1 == len(sizes)
+    check_crowding(cd, orc.nsga2_crowding(p, want["front_offsets"], want["front_indices"]))
+
+
 @pytest.mark.parametrize("n,m,seed", [(2, 2, 1), (3, 1, 2), (33, 2, 3), (257, 4, 4), (1000, 3, 5), (700, 7, 6)])
 def test_random_sets(ctx, orc, n, m, seed):
     rs = np.random.RandomState(seed)
