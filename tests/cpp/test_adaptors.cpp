@@ -7,6 +7,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
+#include <type_traits>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -61,6 +63,52 @@ bool throws_with(F &&f, const std::string &needle)
         return false;
     }
     return false;
+}
+
+// A byte-stream archive with Boost.Serialization's operator& (save: append the
+// member's bytes; load: read them back in the same order), enough for the
+// plain members the plug-ins' serialize() functions visit: the round trip
+// Boost's archives make of an island's problem, algorithm or bfe.
+struct byte_archive {
+    std::vector<unsigned char> buf;
+    std::size_t pos = 0;
+    bool loading = false;
+    template <typename T>
+    byte_archive &operator&(T &v)
+    {
+        static_assert(std::is_trivially_copyable<T>::value, "plain members only");
+        if (loading) {
+            if (pos + sizeof(T) > buf.size()) throw std::runtime_error("archive exhausted");
+            std::memcpy(&v, buf.data() + pos, sizeof(T));
+            pos += sizeof(T);
+        } else {
+            const auto *q = reinterpret_cast<const unsigned char *>(&v);
+            buf.insert(buf.end(), q, q + sizeof(T));
+        }
+        return *this;
+    }
+};
+
+// src saved and loaded into a default-constructed T; every byte consumed
+template <typename T>
+T round_trip(T src)
+{
+    byte_archive a;
+    src.serialize(a, 0u);
+    T dst{};
+    a.loading = true;
+    dst.serialize(a, 0u);
+    if (a.pos != a.buf.size()) throw std::runtime_error("archive not consumed");
+    return dst;
+}
+
+template <typename T>
+bool same_problem(const T &x, const T &y)
+{
+    const pagmo::problem a{x}, b{y};
+    return a.get_nx() == b.get_nx() && a.get_nobj() == b.get_nobj() && a.get_nix() == b.get_nix()
+           && a.get_bounds() == b.get_bounds() && a.get_name() == b.get_name()
+           && a.get_extra_info() == b.get_extra_info();
 }
 
 static_assert(pagmo::is_udbfe<gpu_bfe>::value, "gpu_bfe must be a UDBFE");
@@ -334,6 +382,24 @@ int main()
             gpu_mbh{}.evolve(pop);
         },
         "Cannot use gpu_mbh"));
+    // serialize(): the members the plug-ins save come back, so a loaded problem,
+    // algorithm or bfe is the saved one (the Boost registration itself is the
+    // export-key / implement macro pair and needs Boost)
+    CHECK(same_problem(round_trip(gpu_rastrigin{13u, 1}), gpu_rastrigin{13u, 1}));
+    CHECK(round_trip(gpu_rastrigin{13u, 1}).param() == 13u);
+    CHECK(same_problem(round_trip(gpu_rosenbrock{21u}), gpu_rosenbrock{21u}));
+    CHECK(same_problem(round_trip(gpu_lennard_jones{9u}), gpu_lennard_jones{9u}));
+    CHECK(same_problem(round_trip(gpu_ackley{5u}), gpu_ackley{5u}));
+    CHECK(same_problem(round_trip(gpu_griewank{6u}), gpu_griewank{6u}));
+    CHECK(same_problem(round_trip(gpu_schwefel{7u}), gpu_schwefel{7u}));
+    CHECK(same_problem(round_trip(gpu_zdt{5u, 12u}), gpu_zdt{5u, 12u}));
+    CHECK(same_problem(round_trip(gpu_dtlz{4u, 9u, 3u, 50u}), gpu_dtlz{4u, 9u, 3u, 50u}));
+    CHECK(same_problem(round_trip(gpu_hock_schittkowski_71{}), gpu_hock_schittkowski_71{}));
+    CHECK(round_trip(gpu_bfe{3}).get_extra_info() == gpu_bfe{3}.get_extra_info());
+    CHECK(round_trip(gpu_mbh{7u, 3u, 11u, 0.2, 0.03, 1e-7, 99u, 2}).get_extra_info()
+          == gpu_mbh(7u, 3u, 11u, 0.2, 0.03, 1e-7, 99u, 2).get_extra_info());
+    CHECK(round_trip(gpu_mbh{7u, 3u, 11u, 0.2, 0.03, 1e-7, 99u, 2}).get_extra_info() != gpu_mbh{}.get_extra_info());
+
     if (failures) {
         std::fprintf(stderr, "%d check(s) failed\n", failures);
         return 1;
