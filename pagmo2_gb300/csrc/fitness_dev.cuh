@@ -170,11 +170,11 @@ __device__ __forceinline__ double cos_2pi(double x, int &neg)
 // accumulated as sum x^2 and sum cos apart; g_i = 2 x_i + 10 omega sin(2 pi x_i)
 // (:98-107). One group of G lanes per row, lanes strided over coordinates.
 // For 2^-60 <= |x| < 2^40 (the usual case) sin and cos come from the integer
-// fixed-point routines of trig_fixed.h, sum x^2 is an exact integer sum
-// (isum.h) and 2x an exponent increment, so the FP64 instructions per element
-// are the cos sum and, with the gradient, its FMA: 2 with the gradient, 1
-// without (21 and 14 with FP64 polynomials). Other x take the FP64
-// polynomials (|x| < 2^-60) or CUDA's sincospi/cospi.
+// fixed-point routines of trig_fixed.h and 2x is an exponent increment. The
+// integer pipe binds these rows, so the FP64 pipe takes the sums: per element
+// the x^2 FMA, the cos add, the gradient's FMA and the two conversions of the
+// fixed-point results (21 FP64 instructions with FP64 polynomials). Other x
+// take the FP64 polynomials (|x| < 2^-60) or CUDA's sincospi/cospi.
 
 // 2x exactly for zero or a normal x whose double 2x is finite
 __device__ __forceinline__ double twice_exact(double x)
@@ -186,17 +186,17 @@ __device__ __forceinline__ double twice_exact(double x)
 // One element's contribution: x^2 into sx, cos(2 pi x) into sc and, with the
 // gradient, g = 2x + 10 omega sin(2 pi x) stored.
 template <bool GRAD>
-__device__ __forceinline__ void rastrigin_element(double xi, isum::sq_acc &sx, double &sc, double *gi)
+__device__ __forceinline__ void rastrigin_element(double xi, double &sx, double &sc, double *gi)
 {
-    isum::add_square(sx, xi);
+    sx = fma(xi, xi, sx);
     if (trigfx::in_range(xi)) {
         if (GRAD) {
             double s, c;
-            trigfx::sincos_2pi(xi, s, c);
+            trigfx::sincos_2pi<true>(xi, s, c);
             sc += c;
             *gi = fma(k10Omega, s, twice_exact(xi));
         } else {
-            sc += trigfx::cos_2pi(xi);
+            sc += trigfx::cos_2pi<true>(xi);
         }
         return;
     }
@@ -230,13 +230,13 @@ __device__ __forceinline__ void rastrigin_element(double xi, isum::sq_acc &sx, d
 // of lanes follows the batch size (more per row for small batches) without
 // changing any value.
 struct rastrigin_part {
-    isum::sq_acc sx; // sum of x^2 (its flags are OR-ed apart: order-free)
-    double sc;       // sum of cos(2 pi x)
+    double sx; // sum of x^2
+    double sc; // sum of cos(2 pi x)
 };
 
 __device__ __forceinline__ void rastrigin_join(rastrigin_part &a, const rastrigin_part &b)
 {
-    isum::add(a.sx, isum::sq_term{b.sx.m, b.sx.e});
+    a.sx = a.sx + b.sx;
     a.sc = a.sc + b.sc;
 }
 
@@ -251,7 +251,7 @@ __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uin
     const unsigned mask = group_mask<G>();
     rastrigin_part acc[J];
 #pragma unroll
-    for (int j = 0; j < J; ++j) acc[j] = rastrigin_part{isum::make(), 0.0};
+    for (int j = 0; j < J; ++j) acc[j] = rastrigin_part{0.0, 0.0};
     // chunks of V elements; the next element's load is issued before this
     // one's arithmetic
     double xn = sub < nx ? __ldg(xr + sub) : 0.0;
@@ -265,16 +265,12 @@ __device__ __forceinline__ void rastrigin_row(const double *__restrict__ xr, uin
             if (i < nx) rastrigin_element<GRAD>(xi, acc[j].sx, acc[j].sc, GRAD ? gr + i : nullptr);
         }
     }
-    uint32_t flags = 0u;
-#pragma unroll
-    for (int j = 0; j < J; ++j) flags |= acc[j].sx.flags;
 #pragma unroll
     for (int h = J / 2; h >= 1; h >>= 1) {
 #pragma unroll
         for (int j = 0; j < h; ++j) rastrigin_join(acc[j], acc[j + h]);
     }
-    acc[0].sx.flags = flags;
-    const double sxv = isum::value(group_isum<G>(acc[0].sx, mask));
+    const double sxv = group_sum<G>(acc[0].sx, mask);
     const double scv = group_sum<G>(acc[0].sc, mask);
     if (sub == 0 && f_out) *f_out = fma(-10.0, scv, sxv) + 10.0 * static_cast<double>(nx);
 }

@@ -1,4 +1,5 @@
-// sin(2 pi x) and cos(2 pi x) with integer arithmetic (no FP64 instruction).
+// sin(2 pi x) and cos(2 pi x) with integer arithmetic (no FP64 instruction,
+// or one conversion per result: to_double).
 //
 // Rastrigin, Ackley and the multi-objective test problems spend most of their
 // FP64 instructions on sin/cos(2 pi x) polynomials; GB300's FP64 pipe retires
@@ -99,15 +100,31 @@ PGX_TRIG_HD bool in_range(double x)
     return (ex - (1023u - 60u) < 100u) || (bits_of(x) << 1) == 0u;
 }
 
-// The double nearest to p 2^e (p > 0, result normal), with the sign bit s.
+// The double nearest to p 2^e (p > 0, result normal), with the sign bit s,
+// in two forms with one rounding each: CVT = false rounds the significand
+// with integer operations (about twenty; ties away from zero), CVT = true
+// converts p with one instruction (ties to even) and scales it through the
+// exponent field. The conversion made the rastrigin rows, where the integer
+// pipe binds, 7 % faster and the ackley and ZDT4 rows, whose FP64 pipe is
+// busier, 5-9 % slower.
+template <bool CVT = false>
 PGX_TRIG_HD double to_double(uint64_t p, int32_t e, uint64_t s)
 {
-    const int lz = clz64(p);
-    const uint64_t n = p << lz;
-    const uint64_t nr = n + 1024u;
-    const uint64_t mant = nr < n ? (1ull << 53) : (nr >> 11);
-    // value n 2^(e - lz): leading bit at 2^(e - lz + 63); the implicit bit adds one to the exponent field
-    return from_bits((s << 63) | ((static_cast<uint64_t>(e - lz + 63 + 1022) << 52) + mant));
+    if constexpr (CVT) {
+#if defined(__CUDA_ARCH__)
+        const double v = __ull2double_rn(p);
+#else
+        const double v = static_cast<double>(p);
+#endif
+        return from_bits((bits_of(v) + (static_cast<uint64_t>(static_cast<int64_t>(e)) << 52)) | (s << 63));
+    } else {
+        const int lz = clz64(p);
+        const uint64_t n = p << lz;
+        const uint64_t nr = n + 1024u;
+        const uint64_t mant = nr < n ? (1ull << 53) : (nr >> 11);
+        // value n 2^(e - lz): leading bit at 2^(e - lz + 63); the implicit bit adds one to the exponent field
+        return from_bits((s << 63) | ((static_cast<uint64_t>(e - lz + 63 + 1022) << 52) + mant));
+    }
 }
 
 struct reduced {
@@ -183,22 +200,24 @@ PGX_TRIG_HD int64_t poly_h(int64_t z)
 }
 
 // cos(2 pi x), x in range
+template <bool CVT = false>
 PGX_TRIG_HD double cos_2pi(double x)
 {
     const reduced r = reduce(x);
     const int64_t z = z_q64(r);
     const int64_t c = (int64_t{1} << 55) + mul_hi_s64(poly_h(z), z); // cos(2 pi r) in Q55, >= 0
     if (c <= 0) return 0.0;
-    return to_double(static_cast<uint64_t>(c), -55, r.odd);
+    return to_double<CVT>(static_cast<uint64_t>(c), -55, r.odd);
 }
 
 // sin(2 pi x) and cos(2 pi x), x in range
+template <bool CVT = false>
 PGX_TRIG_HD void sincos_2pi(double x, double &s, double &c)
 {
     const reduced r = reduce(x);
     const int64_t z = z_q64(r);
     const int64_t cq = (int64_t{1} << 55) + mul_hi_s64(poly_h(z), z);
-    c = cq <= 0 ? 0.0 : to_double(static_cast<uint64_t>(cq), -55, r.odd);
+    c = cq <= 0 ? 0.0 : to_double<CVT>(static_cast<uint64_t>(cq), -55, r.odd);
     const uint64_t sx = bits_of(x) >> 63;
     if (r.rn == 0u) {
         s = from_bits((sx ^ r.odd) << 63); // a zero of the sine, signed as r (+0 for x = +-0: x)
@@ -207,7 +226,7 @@ PGX_TRIG_HD void sincos_2pi(double x, double &s, double &c)
     }
     // |sin(2 pi r)| = rn 2^re S(z), S(z) >= 4 in Q55
     const uint64_t p = mul_hi_u64(r.rn, static_cast<uint64_t>(poly_s(z)));
-    s = to_double(p, r.re + 64 - 55, sx ^ r.odd ^ r.neg);
+    s = to_double<CVT>(p, r.re + 64 - 55, sx ^ r.odd ^ r.neg);
 }
 
 } // namespace trigfx
