@@ -396,12 +396,16 @@ __device__ bool peel_sync(peel_state *st, unsigned nb)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned a = atomicAdd(&st->peel_arrivals, 1u);
+        // the arrival releases the block's writes (ordered before it by the
+        // block barrier), the polls acquire the other blocks'
+        unsigned a;
+        asm volatile("atom.add.release.gpu.u32 %0, [%1], 1;" : "=r"(a) : "l"(&st->peel_arrivals) : "memory");
         const unsigned target = (a / nb + 1u) * nb;
-        volatile unsigned *vc = &st->peel_arrivals;
         volatile int *verr = &st->err;
-        for (unsigned long long spins = 0; *vc < target; ++spins) {
+        for (unsigned long long spins = 0;; ++spins) {
+            unsigned v;
+            asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(v) : "l"(&st->peel_arrivals) : "memory");
+            if (v >= target) break;
             if (*verr) break;
             if (spins > kSpinLimit) {
                 atomicExch(&st->err, 1);
@@ -409,7 +413,6 @@ __device__ bool peel_sync(peel_state *st, unsigned nb)
             }
             __nanosleep(16);
         }
-        __threadfence();
     }
     __syncthreads();
     return *reinterpret_cast<volatile int *>(&st->err) == 0;
