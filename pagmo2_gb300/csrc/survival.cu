@@ -250,24 +250,40 @@ __global__ void __launch_bounds__(256) dominance_sym_packed_kernel(const uint32_
     const uint32_t iag = ia | kRankGuard, ibg = ib | kRankGuard;
     const uint32_t jn = n - J0 < 32u ? n - J0 : 32u; // candidates of this tile
     uint32_t row_i = 0u;
+    // pair (i, jj): i dominates jj / jj dominates i (valid: both points exist)
+    const auto pair = [&](unsigned jj, bool valid, bool &i_dom_j, bool &j_dom_i) {
+        const uint4 w = jw[jj];
+        // no borrow into a guard bit: every field of the first word no smaller
+        uint32_t c_ij = w.z - ia; // i no worse than j in every field
+        uint32_t c_ji = iag - w.x; // j no worse than i
+        if (NW == 2) {
+            c_ij &= w.w - ib;
+            c_ji &= ibg - w.y;
+        }
+        const bool le_ij = (c_ij & kRankGuard) == kRankGuard, le_ji = (c_ji & kRankGuard) == kRankGuard;
+        // both ways no worse: every field equal, neither dominates
+        i_dom_j = valid && le_ij && !le_ji;
+        j_dom_i = valid && le_ji && !le_ij;
+    };
     if (active) {
-        for (unsigned jj = 0; jj < 32u; ++jj) {
-            const uint4 w = jw[jj];
-            // no borrow into a guard bit: every field of the first word no smaller
-            uint32_t c_ij = w.z - ia; // i no worse than j in every field
-            uint32_t c_ji = iag - w.x; // j no worse than i
-            if (NW == 2) {
-                c_ij &= w.w - ib;
-                c_ji &= ibg - w.y;
+        if (jn == 32u && __all_sync(kFull, iv)) {
+            // a full tile (nearly all of them): no validity tests per pair
+#pragma unroll 8
+            for (unsigned jj = 0; jj < 32u; ++jj) {
+                bool idj, jdi;
+                pair(jj, true, idj, jdi);
+                const unsigned word = __ballot_sync(kFull, idj);
+                if (lane == 0) tile[jj][warp] = word;
+                row_i |= static_cast<uint32_t>(jdi) << jj;
             }
-            const bool le_ij = (c_ij & kRankGuard) == kRankGuard, le_ji = (c_ji & kRankGuard) == kRankGuard;
-            // both ways no worse: every field equal, neither dominates
-            const bool valid = iv && jj < jn;
-            const bool i_dom_j = valid && le_ij && !le_ji;
-            const bool j_dom_i = valid && le_ji && !le_ij;
-            const unsigned word = __ballot_sync(kFull, i_dom_j);
-            if (lane == 0) tile[jj][warp] = word;
-            row_i |= static_cast<uint32_t>(j_dom_i) << jj;
+        } else {
+            for (unsigned jj = 0; jj < 32u; ++jj) {
+                bool idj, jdi;
+                pair(jj, iv && jj < jn, idj, jdi);
+                const unsigned word = __ballot_sync(kFull, idj);
+                if (lane == 0) tile[jj][warp] = word;
+                row_i |= static_cast<uint32_t>(jdi) << jj;
+            }
         }
         if (bi != bj && i < n) Dt[static_cast<uint64_t>(i) * W8 + bj] = row_i;
     }
