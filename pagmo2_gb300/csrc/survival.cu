@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(256) dominance_sym_packed_kernel(const uint32_
     if (active) {
         if (jn == 32u && __all_sync(kFull, iv)) {
             // a full tile (nearly all of them): no validity tests per pair
-#pragma unroll 8
+#pragma unroll
             for (unsigned jj = 0; jj < 32u; ++jj) {
                 bool idj, jdi;
                 pair(jj, true, idj, jdi);
