@@ -9,7 +9,8 @@ step = one batch. Prints one JSON line:
          flush between steps)
   e2e    the same metric through the public host-buffer entry point
          (pgx_batch_gradient) from pinned host memory, uploads and downloads
-         inside the timed region
+         inside the timed region; e2e.host_link measures this box's link with
+         the same buffers (upload, download, both at once), the step's floor
   roofline  the rosenbrock kernel against the FP64 peak (measured in-run by a
          DFMA probe; MEASURED_PEAKS.json has no FP64 figure): frac is the FP64
          pipe's load (the kernel's FP64 instructions at 2 flops each), the
@@ -201,6 +202,41 @@ def cpu_reference_step_fn(kind: int, param: int, x: np.ndarray, grad: bool, thre
         g = orc.batch_gradient(kind, param, x, threads) if grad else None
         return f, g
     return step, "port"
+
+
+def host_link_probe(hx, hg, dx, dg, reps: int = 3) -> dict:
+    """The host link of this machine with the e2e step's own pinned buffers: the
+    upload of the decision vectors alone, the download of the gradients alone,
+    and both at once on two streams (the floor of a host-buffer step, whose
+    kernel hides under the transfers). Run after the e2e timing and its parity
+    check (it rewrites the buffers with the same values)."""
+    up_s, down_s = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def up():
+        with torch.cuda.stream(up_s):
+            dx.copy_(hx, non_blocking=True)
+
+    def down():
+        with torch.cuda.stream(down_s):
+            hg.copy_(dg, non_blocking=True)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps
+
+    up()
+    down()
+    t_up, t_down = timed(up), timed(down)
+    t_both = timed(lambda: (up(), down()))
+    b_up, b_down = hx.numel() * 8, hg.numel() * 8
+    return {"h2d_gbs": b_up / t_up / 1e9, "d2h_gbs": b_down / t_down / 1e9,
+            "both_gbs": (b_up + b_down) / t_both / 1e9, "both_ms": t_both * 1e3,
+            "note": "cudaMemcpyAsync of the step's input (up) and gradients (down) between its pinned host buffers "
+                    "and the device, alone and both at once: the floor of ms_per_step"}
 
 
 def time_cpu(step, budget_s: float = 8.0, max_reps: int = 20) -> float:
@@ -421,6 +457,8 @@ def main():
                       "max_scaled_err_gradient": float(np.max(np.abs(go - gl) / gs))}
         except Exception as e:  # the checker is optional; the number is not
             parity = {"error": str(e)}
+    if e2e is not None:
+        e2e["host_link"] = host_link_probe(hx, hg, dx, dg)
 
     secondary = {}
     if rank == 0 and not args.no_secondary:
