@@ -210,6 +210,8 @@ def host_link_probe(hx, hg, dx, dg, reps: int = 3) -> dict:
     and both at once on two streams (the floor of a host-buffer step, whose
     kernel hides under the transfers). Run after the e2e timing and its parity
     check (it rewrites the buffers with the same values)."""
+    import torch
+
     up_s, down_s = torch.cuda.Stream(), torch.cuda.Stream()
 
     def up():
