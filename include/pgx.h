@@ -367,7 +367,7 @@ PGX_API int pgx_nsga2_survival_device(pgx_context *ctx, const double *d_points, 
    n <= 4096 and m <= 8, else PGX_ERR_CAPACITY. The first call on each device
    (and in each CUDA context) does a one-time set-up: it looks up that array's
    device address and loads the library's survival code and data on the device
-   (under lazy module loading, the CUDA default, this is when the ~2.5 MB array
+   (under lazy module loading, the CUDA default, this is when the ~2.6 MB array
    is allocated). Make that first call before another allocator reserves the
    device's memory, and before any stream capture; later calls allocate
    nothing. All calls share the array and it keeps the last call's contents

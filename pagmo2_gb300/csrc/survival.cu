@@ -2504,7 +2504,7 @@ int read_mo_status(pgx_context *ctx, uint64_t n, uint64_t m)
 // (order keys, the dominance bit matrix, peel state, per-objective orders)
 // from one array compiled into the library: g_noalloc_scratch, sized for at
 // most kNoAllocMaxPoints points and kNoAllocMaxObjectives objectives (about
-// 2.5 MB). Larger inputs are rejected with PGX_ERR_CAPACITY. The array is
+// 2.6 MB). Larger inputs are rejected with PGX_ERR_CAPACITY. The array is
 // device memory of the library's survival module: a device holds it from the
 // moment that module is loaded there (at the first call on the device under
 // lazy module loading, the default) until the process exits.
